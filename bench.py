@@ -1,0 +1,293 @@
+#!/usr/bin/env python
+"""Benchmark: LIZARD's LDPC decoder batch on one GB300 (decoded information Gbit/s).
+
+Workload: 65,536 codewords of the four codes in the format's proportions (39% 7/8, 26% 3/4, 15% 2/3, 20% 1/2 by
+count), each a 476-byte block plus its CRC-32C, BPSK over AWGN with Eb/N0 cycling 1.0 to 4.0 dB in 0.5 dB steps,
+quantised to the reference's int8 soft values; layered min-sum, at most 20 iterations, the stall rule (9, 0.95),
+then the CRC-32C check. One step decodes the whole batch (its LLRs, ~354 MB, are larger than L2, so no flush is
+needed between steps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is device-timed with the LLRs resident in HBM; `e2e` is the same metric through the
+C ABI's host-memory entry point (pinned host buffers, copies in and out inside the timed region). The CPU baseline
+times the reference's CPU decoder (compiled from its sources where present, else the oracle's C restatement) on the
+same batch on the host's cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "decoded payload MB/s, frames/s and LDPC Gbit/s on 1 GB300, refined+batched vs plain"
+UNIT = "Gbit/s"
+MAX_ITER, STALL_IT, STALL_RATIO = 20, 9, 0.95
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--count", type=int, default=65536, help="codewords a step (the workload: 65,536)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(count):
+    return {"workload": "LDPC decoder batch: %d codewords, 39/26/15/20%% 7/8,3/4,2/3,1/2, BPSK/AWGN Eb/N0 1.0-4.0 dB "
+                        "(0.5 dB steps, cycled), int8 LLRs, layered min-sum max %d its, stall %d/%.2f, CRC-32C" % (count, MAX_ITER, STALL_IT, STALL_RATIO),
+            "codewords": count, "info_bits_per_codeword": 3840, "max_iter": MAX_ITER, "stall": [STALL_IT, STALL_RATIO],
+            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas (codewords independent)"}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, ws, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.p, self.path = device, None, None
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+            self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.p or not self.path:
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, v in enumerate(flags) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "of measured"
+    except Exception:
+        return 6800.0, "of fallback"
+
+
+def traffic_per_step(count):
+    """DRAM bytes per step from the committed ncu summary (profiles/ldpc_traffic.json), scaled to `count` codewords."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "ldpc_traffic.json")))
+        return float(d["dram_bytes_per_codeword"]) * count
+    except Exception:
+        return None
+
+
+def cpu_decode(batch, threads, sample):
+    """The CPU decoder on the first `sample` codewords: (Gbit/s, seconds, kind)."""
+    import numpy as np
+    import oracle
+    lib, kind = (oracle.ref(), "reference") if oracle.have_ref() else (oracle.port(), "port")
+    n = int(batch["offsets"][sample - 1]) + {6: 4608, 4: 5120, 3: 5760, 2: 7680}[int(batch["rates"][sample - 1])] if sample < batch["rates"].size else batch["llr"].size
+    t0 = time.perf_counter()
+    oracle.ldpc_batch(lib, batch["llr"][:n], batch["offsets"][:sample], batch["rates"][:sample], MAX_ITER, STALL_IT, STALL_RATIO, threads=threads)
+    dt = time.perf_counter() - t0
+    return sample * 3840 / dt / 1e9, dt, kind
+
+
+def run_reference(args, rank, ws):
+    """The reference arm: the reference's CPU decoder on the host cores, same metric and workload."""
+    if rank != 0:
+        return
+    from lizard_gb300 import synth
+    import oracle
+    if not os.path.exists(oracle.PORT_PATH):
+        oracle.build(ref=False)
+    batch = synth.ldpc_batch(args.count, seed=1000)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_decode(batch, threads, min(args.count, 4096))
+    vals, secs = [], []
+    kind = None
+    for _ in range(args.steps):
+        v, dt, kind = cpu_decode(batch, threads, args.count)
+        vals.append(v); secs.append(dt)
+    value = args.count * 3840 * len(secs) / sum(secs) / 1e9
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(secs) / len(secs), 3),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int16",
+                      "data": "synthetic", "config": workload(args.count),
+                      "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": kind,
+                                       "sample": "the whole %d-codeword batch a step" % args.count},
+                      "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    args = parse()
+    rank, ws, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+        return
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    assert torch.cuda.is_available(), "bench.py needs a CUDA device"
+    dev = local
+    torch.cuda.set_device(dev)
+    batch = synth.ldpc_batch(args.count, seed=1000 + rank)
+    plan = lz.LdpcPlan(batch["rates"], MAX_ITER, STALL_IT, STALL_RATIO)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    d_llr = torch.from_numpy(batch["llr"]).to("cuda")
+    d_bits = torch.empty(plan.llr_bytes // 8, dtype=torch.uint8, device="cuda")
+    d_its = torch.empty(plan.count, dtype=torch.int32, device="cuda")
+    d_ok = torch.empty(plan.count, dtype=torch.uint8, device="cuda")
+
+    def step():
+        plan.run_dev(d_llr.data_ptr(), d_bits.data_ptr(), d_its.data_ptr(), d_ok.data_ptr(), sp)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    its = d_its.cpu().numpy()
+    ok = d_ok.cpu().numpy()
+    edges = lz.edge_updates(its, batch["rates"], MAX_ITER, STALL_IT)
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(dev) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+    elapsed_ms = max_over_ranks(t0.elapsed_time(t1), ws)
+    launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    launches = plan.launches * args.steps
+    ms = elapsed_ms / args.steps
+    value = ws * args.count * 3840 / (ms / 1e3) / 1e9
+
+    e2e = None
+    if not args.no_e2e:
+        h_llr = torch.from_numpy(batch["llr"]).pin_memory()
+        h_bits = torch.empty(plan.llr_bytes // 8, dtype=torch.uint8).pin_memory()
+        h_its = torch.empty(plan.count, dtype=torch.int32).pin_memory()
+        h_ok = torch.empty(plan.count, dtype=torch.uint8).pin_memory()
+        nb, ni, no = h_llr.numpy(), h_bits.numpy(), h_its.numpy()
+        nk = h_ok.numpy()
+        for _ in range(max(args.warmup, 3)):
+            plan.run(nb, ni, no, nk, sp)
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.run(nb, ni, no, nk, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e_ms = max_over_ranks(e0.elapsed_time(e1), ws) / args.steps
+        assert np.array_equal(no, its) and np.array_equal(nk, ok)
+        e2e = {"value": round(ws * args.count * 3840 / (e_ms / 1e3) / 1e9, 4), "unit": UNIT,
+               "h2d_bytes_per_step": int(plan.llr_bytes), "d2h_bytes_per_step": int(plan.llr_bytes // 8 + plan.count * 5),
+               "ms_per_step": round(e_ms, 3)}
+
+    if rank != 0:
+        return
+    alg_bytes = plan.llr_bytes + plan.llr_bytes // 8 + plan.count * 5
+    peak, peak_src = peaks()
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    traffic = traffic_per_step(args.count)
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int8/int16", "data": "synthetic (seeded blocks over a simulated AWGN channel)", "config": workload(args.count),
+        "payload_MBps": round(ws * float(ok[its > 0].sum()) * 472 / (ms / 1e3) / 1e6, 2),
+        "codewords_per_s": round(ws * args.count / (ms / 1e3), 1),
+        "ldpc": {"decoded": int((its > 0).sum()), "crc_ok": int(ok[its > 0].sum()), "stalled": int((its == -3).sum()),
+                 "capped": int((its == -1).sum()), "mean_iterations": round(float(lz.iterations_run(its, batch["rates"], MAX_ITER, STALL_IT).mean()), 3),
+                 "edge_updates_per_step": edges, "edge_updates_per_s": round(edges / (launch_ms / 1e3), 1)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
+                     "traffic": None if traffic is None else int(traffic), "peak_source": peak_src,
+                     "kernel": "ldpc_decode_kernel<7/8,3/4,2/3,1/2> (the 4 launches of a step)",
+                     "note": "integer/shared-memory bound, not HBM bound: see ldpc.edge_updates_per_s"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if e2e:
+        out["e2e"] = e2e
+    if ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt, kind = cpu_decode(batch, threads, args.count)
+        out["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": kind,
+                               "sample": "the whole %d-codeword batch once (%.1f s wall on %d threads)" % (args.count, dt, threads)}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

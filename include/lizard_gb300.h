@@ -1,0 +1,81 @@
+// lizard_gb300: the LIZARD receive hot path on one GB300 (sm_103a), behind a plain C ABI.
+//
+// Conventions, as the reference's C API keeps them (liblizard/include/lizard.h:12-18, 50-60):
+//   - every function returns 0 (or a count) on success and a negative LIZG_E_* code on failure; nothing throws
+//     across this boundary; lizg_last_error() is a thread-local message for the last failure on the calling thread;
+//   - buffers are the caller's; handles are opaque; a handle is used from one host thread at a time, different
+//     handles may run concurrently;
+//   - "dev" entry points take device pointers and a cudaStream_t passed as void* (NULL: the legacy default stream)
+//     and return once the work is queued; the other entry points take host pointers and return when done.
+#ifndef LIZARD_GB300_H
+#define LIZARD_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  LIZG_OK = 0,
+  LIZG_E_ARG = -1,      // a NULL pointer, a count or size out of range, a rate with no code
+  LIZG_E_NOMEM = -2,    // a device or host allocation failed
+  LIZG_E_CUDA = -3,     // a CUDA call failed (the message names it)
+  LIZG_E_STATE = -4,    // the handle is in no state for the call
+};
+
+// Thread-local text of the last failure on this thread ("" if none). Replaces liz_last_error
+// (liblizard/include/lizard.h:63).
+const char *lizg_last_error(void);
+// Library version string.
+const char *lizg_version(void);
+
+// ---------------------------------------------------------------- LDPC + CRC-32C (rows d, e of the hot path)
+//
+// Rate indices are the reference's (liblizard/src/ldpc.h:30-33): 6 = 7/8 (n 4608, of which 4480 sent), 4 = 3/4
+// (n 5120), 3 = 2/3 (n 5760), 2 = 1/2 (n 7680). LLRs are int8, codeword order, > 0 meaning bit 0; the 7/8 code's
+// 128 never-sent bits (3840..3967) are fed as the caller knows them (+127, liblizard/src/lizard_phy.c:1823).
+
+// Codeword length n of a rate index, 0 for a rate with no code (liblizard/src/ldpc.h:28 n).
+int lizg_ldpc_n(int rate);
+
+// Replaces ldpc_encode (liblizard/src/ldpc.h:42): k data bits in, n codeword bits out, one bit a byte. Host code.
+int lizg_ldpc_encode(int rate, const uint8_t *data, uint8_t *codeword);
+// The same for count codewords of one rate back to back (k bytes in, n bytes out each). Host code; the synthetic
+// input generator's encoder.
+int lizg_ldpc_encode_many(int rate, const uint8_t *data, int count, uint8_t *codewords);
+
+// Replaces ob_crc32c (liblizard/src/layout.c:44-54): CRC-32C of n bytes. Host code.
+uint32_t lizg_crc32c(const uint8_t *p, size_t n);
+
+// Replaces ldpc_decode_stall (liblizard/src/ldpc.h:48) one codeword at a time, the reference's own signature and
+// meaning, decoded on the GPU: n LLRs in, n hard bits out (one a byte). Returns the iterations used, -1 if the
+// syndrome never cleared within max_iter, -3 if the stall rule gave the block up, or a negative LIZG_E_* - 100.
+int lizg_ldpc_decode_stall(int rate, const int8_t *llr, uint8_t *out, int max_iter, int stall_it, float stall_ratio);
+
+// A batch of codewords of mixed rates, the batched form of the reference's per-block loop
+// (liblizard/src/lizard_phy.c:1775-1871, ldpc_decode_stall + bit pack + CRC-32C compare). The batch is laid out
+// back to back: codeword i's n_i LLR bytes at llr + off_i, off_i = n_0 + ... + n_{i-1}. For each codeword the
+// result is its n hard bits packed most significant bit first at bits + off_i / 8 (the first 476 bytes are the
+// block, the next 4 its CRC as sent), its decoder return in its[i] (as lizg_ldpc_decode_stall), and ok[i] = 1 where
+// the CRC-32C of the first 476 bytes equals the 32 bits after them (0 otherwise, or when its[i] < 0 the CRC is still
+// computed on the hard decisions; the reference skips such blocks: a caller treats ok only where its[i] > 0).
+typedef struct lizg_ldpc_plan lizg_ldpc_plan;
+
+// Plans a batch: `rate` (count entries, host memory) fixes the layout; the plan keeps its own device copy of the
+// work lists. max_iter 1..255; stall_it 0 (off) or 2..max_iter; stall_ratio as the reference's float.
+lizg_ldpc_plan *lizg_ldpc_plan_new(const int32_t *rate, int count, int max_iter, int stall_it, float stall_ratio);
+void lizg_ldpc_plan_free(lizg_ldpc_plan *p);
+// Total LLR bytes of the planned batch (sum of n_i), and the packed output bytes (that over 8).
+int64_t lizg_ldpc_plan_llr_bytes(const lizg_ldpc_plan *p);
+// Decodes the planned batch from device memory into device memory, queued on `stream`.
+int lizg_ldpc_plan_run_dev(lizg_ldpc_plan *p, const int8_t *d_llr, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream);
+// The same from host memory to host memory (pinned or not): copies in, decodes, copies out, waits.
+int lizg_ldpc_plan_run(lizg_ldpc_plan *p, const int8_t *llr, uint8_t *bits, int32_t *its, uint8_t *ok, void *stream);
+// Kernel launches the last run made (for the benchmark's launch count).
+int lizg_ldpc_plan_launches(const lizg_ldpc_plan *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

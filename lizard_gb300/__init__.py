@@ -1,0 +1,154 @@
+"""lizard_gb300: the LIZARD receive hot path on one GB300, behind a C ABI (include/lizard_gb300.h).
+
+This module is the Python face of that ABI, for tests, the benchmark and Python callers. It loads the in-tree
+library lizard_gb300/liblizard_gb300.so (built by lizard_gb300/build.py) and fails loudly when it is missing: there
+is no CPU fallback for any decode here.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblizard_gb300.so")
+
+# The reference's rate indices (liblizard/src/ldpc.h:30-33) and their codes' shapes.
+RATES = (6, 4, 3, 2)
+RATE_NAME = {6: "7/8", 4: "3/4", 3: "2/3", 2: "1/2"}
+CODE_N = {6: 4608, 4: 5120, 3: 5760, 2: 7680}
+CODE_K = {6: 3968, 4: 3840, 3: 3840, 2: 3840}
+CODE_NT = {6: 4480, 4: 5120, 3: 5760, 2: 7680}
+# Entries of H (liblizard/test/ldpc_table.c prints them; the oracle derives them from the tables).
+CODE_EDGES = {6: 14463, 4: 19455, 3: 22527, 2: 26879}
+BLOCK_BYTES = 476
+INFO_BITS = 3840
+
+_lib = None
+
+
+class LizgError(RuntimeError):
+    pass
+
+
+def lib():
+    """The loaded C library. Raises if it has not been built: the decode has no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LizgError("lizard_gb300: %s is not built (run `python lizard_gb300/build.py`)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    L.lizg_last_error.restype = ctypes.c_char_p
+    L.lizg_version.restype = ctypes.c_char_p
+    L.lizg_ldpc_n.argtypes = [I]
+    L.lizg_ldpc_encode.argtypes = [I, P, P]
+    L.lizg_ldpc_encode_many.argtypes = [I, P, I, P]
+    L.lizg_crc32c.argtypes = [P, ctypes.c_size_t]
+    L.lizg_crc32c.restype = ctypes.c_uint32
+    L.lizg_ldpc_decode_stall.argtypes = [I, P, P, I, I, F]
+    L.lizg_ldpc_plan_new.argtypes = [P, I, I, I, F]
+    L.lizg_ldpc_plan_new.restype = P
+    L.lizg_ldpc_plan_free.argtypes = [P]
+    L.lizg_ldpc_plan_llr_bytes.argtypes = [P]
+    L.lizg_ldpc_plan_llr_bytes.restype = ctypes.c_int64
+    L.lizg_ldpc_plan_run_dev.argtypes = [P, P, P, P, P, P]
+    L.lizg_ldpc_plan_run.argtypes = [P, P, P, P, P, P]
+    L.lizg_ldpc_plan_launches.argtypes = [P]
+    _lib = L
+    return L
+
+
+def _check(rc, what):
+    if rc < 0:
+        raise LizgError("%s failed (%d): %s" % (what, rc, lib().lizg_last_error().decode()))
+    return rc
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def crc32c(data):
+    b = np.ascontiguousarray(np.frombuffer(bytes(data), np.uint8))
+    return int(lib().lizg_crc32c(_ptr(b), b.size))
+
+
+def ldpc_encode(rate, data):
+    """k data bits (one a byte) -> n codeword bits, the reference's ldpc_encode."""
+    data = np.ascontiguousarray(data, np.uint8)
+    cw = np.zeros(CODE_N.get(rate, 8), np.uint8)
+    _check(lib().lizg_ldpc_encode(rate, _ptr(data), _ptr(cw)), "lizg_ldpc_encode")
+    return cw
+
+
+def ldpc_encode_many(rate, data):
+    """(count, k) data bits -> (count, n) codewords."""
+    data = np.ascontiguousarray(data, np.uint8)
+    cw = np.zeros((data.shape[0], CODE_N[rate]), np.uint8)
+    _check(lib().lizg_ldpc_encode_many(rate, _ptr(data), data.shape[0], _ptr(cw)), "lizg_ldpc_encode_many")
+    return cw
+
+
+def ldpc_decode_stall(rate, llr, max_iter, stall_it=0, stall_ratio=0.0):
+    """The reference's ldpc_decode_stall on the GPU: (iterations or -1/-3, n hard bits)."""
+    llr = np.ascontiguousarray(llr, np.int8)
+    out = np.zeros(CODE_N[rate], np.uint8)
+    rc = lib().lizg_ldpc_decode_stall(rate, _ptr(llr), _ptr(out), max_iter, stall_it, stall_ratio)
+    if rc <= -100:
+        raise LizgError("lizg_ldpc_decode_stall failed (%d): %s" % (rc + 100, lib().lizg_last_error().decode()))
+    return rc, out
+
+
+class LdpcPlan:
+    """A planned batch of mixed-rate codewords laid back to back (include/lizard_gb300.h lizg_ldpc_plan_*)."""
+
+    def __init__(self, rates, max_iter=30, stall_it=9, stall_ratio=0.95):
+        self.rates = np.ascontiguousarray(rates, np.int32)
+        self.count = int(self.rates.size)
+        h = lib().lizg_ldpc_plan_new(_ptr(self.rates), self.count, max_iter, stall_it, stall_ratio)
+        if not h:
+            raise LizgError("lizg_ldpc_plan_new: " + lib().lizg_last_error().decode())
+        self._h = ctypes.c_void_p(h)
+        self.llr_bytes = int(lib().lizg_ldpc_plan_llr_bytes(self._h))
+        n = np.array([CODE_N[int(r)] for r in self.rates], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lizg_ldpc_plan_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def launches(self):
+        return int(lib().lizg_ldpc_plan_launches(self._h))
+
+    def run(self, llr, bits=None, its=None, ok=None, stream=0):
+        """Host memory in and out: returns (packed bits, its, ok)."""
+        llr = np.ascontiguousarray(llr, np.int8)
+        if llr.size != self.llr_bytes:
+            raise ValueError("llr holds %d bytes, the plan %d" % (llr.size, self.llr_bytes))
+        bits = np.empty(self.llr_bytes // 8, np.uint8) if bits is None else bits
+        its = np.empty(self.count, np.int32) if its is None else its
+        ok = np.empty(self.count, np.uint8) if ok is None else ok
+        _check(lib().lizg_ldpc_plan_run(self._h, _ptr(llr), _ptr(bits), _ptr(its), _ptr(ok), ctypes.c_void_p(stream)), "lizg_ldpc_plan_run")
+        return bits, its, ok
+
+    def run_dev(self, d_llr, d_bits, d_its, d_ok, stream=0):
+        """Device pointers (ints) in and out, queued on `stream` (a cudaStream_t as an int)."""
+        _check(lib().lizg_ldpc_plan_run_dev(self._h, ctypes.c_void_p(d_llr), ctypes.c_void_p(d_bits), ctypes.c_void_p(d_its),
+                                            ctypes.c_void_p(d_ok), ctypes.c_void_p(stream)), "lizg_ldpc_plan_run_dev")
+
+
+def iterations_run(its, rates, max_iter, stall_it):
+    """Iterations each codeword actually ran: its return when positive, max_iter at -1, stall_it at -3."""
+    its = np.asarray(its)
+    return np.where(its > 0, its, np.where(its == -3, stall_it, max_iter))
+
+
+def edge_updates(its, rates, max_iter, stall_it):
+    e = np.array([CODE_EDGES[int(r)] for r in rates], np.int64)
+    return int((iterations_run(its, rates, max_iter, stall_it).astype(np.int64) * e).sum())

@@ -1,0 +1,303 @@
+// Layered normalised min-sum LDPC decoding of the four LIZARD codes plus the block's CRC-32C check, on sm_103a.
+//
+// One warp decodes one codeword. A block row (a layer) has z = 128 checks that share no bit, so lane l takes checks
+// l, l + 32, l + 64 and l + 96 of every layer and keeps their min1 / min2 / sign in registers between the layer's
+// two passes. The codeword's posteriors (int16) and check-to-bit messages (int8) live in the warp's slice of
+// shared memory for the whole decode; global memory is touched once to read the LLRs and once to write the packed
+// hard bits, so the kernel is bound by the integer pipes and shared-memory latency, not by HBM.
+//
+// Persistent grid: one CTA per SM (its shared memory holds as many codewords as fit), warps pull codeword indices
+// from a work counter, so codewords that stop early free their warp for the next one.
+//
+// Arithmetic: the reference's four-times kernel, liblizard/src/ldpc.c:340-423 (and its NEON original, 300-328):
+// the extrinsic L - R saturated to a byte held at [-127, 127]; min1/min2 over byte magnitudes; (x * 13) >> 4 capped
+// at 127; an edge whose magnitude is min1 takes min2; no posterior clamp. Row 0's missing previous parity bit is a
+// certain zero of 8191 (liblizard/src/ldpc.c:655-676). Stop rule: liblizard/src/ldpc.c:1128-1145.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "lizard_codes.h"
+#include "lizg_internal.h"
+
+namespace lizg {
+
+// Per-code compile-time shape: block rows, codeword bits, data bits, data circulants, slots (data circulants plus
+// two staircase slots a row), and the warps a CTA runs (as many codeword states as fit in 227 KB of shared memory).
+template <int C> struct Code;
+template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, WARPS = 9; };
+template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, WARPS = 7; };
+template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, WARPS = 6; };
+template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, WARPS = 5; };
+
+template <int C> __host__ __device__ constexpr int slots() { return Code<C>::NDATA + 2 * Code<C>::MB; }
+// A warp's state: posteriors (N int16) then messages (slots x 128 int8), rounded to 16 bytes.
+template <int C> __host__ __device__ constexpr int warp_bytes() { return (Code<C>::N * 2 + slots<C>() * 128 + 15) & ~15; }
+constexpr int kCrcBytes = (256 + 32 + 1) * 4 + 12;   // table, per-lane shifts, init term; padded to 16
+template <int C> constexpr int cta_smem() { return kCrcBytes + Code<C>::WARPS * warp_bytes<C>(); }
+
+static_assert(cta_smem<0>() <= 227 * 1024, "7/8 state does not fit");
+static_assert(cta_smem<1>() <= 227 * 1024, "3/4 state does not fit");
+static_assert(cta_smem<2>() <= 227 * 1024, "2/3 state does not fit");
+static_assert(cta_smem<3>() <= 227 * 1024, "1/2 state does not fit");
+
+// Block-row tables of the four codes: rowptr and (col << 8 | shift) circulants, read warp-uniformly (broadcast).
+struct DevCode { int rowptr[31]; uint16_t circ[152]; };
+__constant__ DevCode c_codes[4];
+// CRC-32C shift constants: x^(8 (476 - end_l)) mod P for lane l's 15-byte chunk, then the all-ones init's term.
+__constant__ uint32_t c_crc_shift[33];
+
+constexpr uint32_t kCrcPoly = 0x82F63B78u;   // CRC-32C, reflected
+constexpr int kBlockBytes = LIZG_BLOCK_BYTES;
+
+// a * b mod P in the reflected representation (bit 31 is x^0).
+__device__ __forceinline__ uint32_t gf_mul(uint32_t a, uint32_t b) {
+  uint32_t p = 0;
+#pragma unroll
+  for (int i = 0; i < 32; i++) {
+    p ^= b & (0u - ((a >> (31 - i)) & 1u));
+    b = (b >> 1) ^ (kCrcPoly & (0u - (b & 1u)));
+  }
+  return p;
+}
+
+__device__ __forceinline__ int sat127(int v) { return max(-127, min(127, v)); }
+
+template <int C>
+__device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane) {
+  using T = Code<C>;
+  const DevCode &cd = c_codes[C];
+  const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+  int8_t *Rr = R + (p0 + 2 * r) * 128;
+  int16_t *Lp = L + T::K;
+  int m1[4], m2[4], sg[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) { m1[q] = 255; m2[q] = 255; sg[q] = 0; }
+  // Pass 1: the extrinsics' bytes, their signs and two least magnitudes.
+  auto acc = [&](int q, int v) {
+    const int b = sat127(v), a = abs(b);
+    sg[q] ^= b;
+    m2[q] = min(m2[q], max(m1[q], a));
+    m1[q] = min(m1[q], a);
+  };
+  for (int e = 0; e < nd; e++) {
+    const int cs = cd.circ[p0 + e], sh = cs & 255;
+    const int16_t *col = L + (cs >> 8) * 128;
+    const int8_t *Re = Rr + e * 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) { const int i = lane + 32 * q; acc(q, col[(i - sh) & 127] - Re[i]); }
+  }
+  {
+    const int8_t *Re = Rr + nd * 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = lane + 32 * q;
+      int v;
+      if (r > 0) v = Lp[(r - 1) * 128 + i] - Re[i];
+      else v = (i == 0) ? 8191 : Lp[(T::MB - 1) * 128 + i - 1] - Re[i];
+      acc(q, v);
+    }
+    Re += 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) { const int i = lane + 32 * q; acc(q, Lp[r * 128 + i] - Re[i]); }
+  }
+  int s1[4], s2[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) { s1[q] = min(127, (m1[q] * 13) >> 4); s2[q] = min(127, (m2[q] * 13) >> 4); }
+  // Pass 2: new messages and posteriors.
+  auto upd = [&](int q, int v, int8_t *rp, int16_t *lp) {
+    const int b = sat127(v), a = abs(b);
+    const int mag = (a == m1[q]) ? s2[q] : s1[q];
+    const int m = ((sg[q] ^ b) < 0) ? -mag : mag;
+    *rp = (int8_t)m;
+    *lp = (int16_t)(v + m);
+  };
+  for (int e = 0; e < nd; e++) {
+    const int cs = cd.circ[p0 + e], sh = cs & 255;
+    int16_t *col = L + (cs >> 8) * 128;
+    int8_t *Re = Rr + e * 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = lane + 32 * q;
+      int16_t *lp = col + ((i - sh) & 127);
+      upd(q, *lp - Re[i], Re + i, lp);
+    }
+  }
+  {
+    int8_t *Re = Rr + nd * 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = lane + 32 * q;
+      if (r > 0) { int16_t *lp = Lp + (r - 1) * 128 + i; upd(q, *lp - Re[i], Re + i, lp); }
+      else if (i != 0) { int16_t *lp = Lp + (T::MB - 1) * 128 + i - 1; upd(q, *lp - Re[i], Re + i, lp); }
+    }
+    Re += 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) { const int i = lane + 32 * q; int16_t *lp = Lp + r * 128 + i; upd(q, *lp - Re[i], Re + i, lp); }
+  }
+}
+
+// Violated checks over the whole code, summed over the warp.
+template <int C>
+__device__ __forceinline__ int unsat(const int16_t *L, int lane) {
+  using T = Code<C>;
+  const DevCode &cd = c_codes[C];
+  const int16_t *Lp = L + T::K;
+  int bad = 0;
+  for (int r = 0; r < T::MB; r++) {
+    const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+    int x[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = lane + 32 * q;
+      x[q] = Lp[r * 128 + i] ^ (r > 0 ? Lp[(r - 1) * 128 + i] : (i > 0 ? Lp[(T::MB - 1) * 128 + i - 1] : 0));
+    }
+    for (int e = 0; e < nd; e++) {
+      const int cs = cd.circ[p0 + e], sh = cs & 255;
+      const int16_t *col = L + (cs >> 8) * 128;
+#pragma unroll
+      for (int q = 0; q < 4; q++) x[q] ^= col[(lane + 32 * q - sh) & 127];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) bad += x[q] < 0;
+  }
+  return __reduce_add_sync(0xffffffffu, bad);
+}
+
+template <int C>
+__global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(LdpcLaunch a) {
+  using T = Code<C>;
+  extern __shared__ __align__(16) uint8_t smem[];
+  uint32_t *crc_tab = reinterpret_cast<uint32_t *>(smem);
+  uint32_t *crc_k = crc_tab + 256;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int16_t *L = reinterpret_cast<int16_t *>(smem + kCrcBytes + warp * warp_bytes<C>());
+  int8_t *R = reinterpret_cast<int8_t *>(L + T::N);
+  for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+    uint32_t c = (uint32_t)t;
+    for (int k = 0; k < 8; k++) c = (c >> 1) ^ (kCrcPoly & (0u - (c & 1u)));
+    crc_tab[t] = c;
+  }
+  for (int t = threadIdx.x; t < 33; t += blockDim.x) crc_k[t] = c_crc_shift[t];
+  __syncthreads();
+
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(a.counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= a.count) break;
+    const int cw = a.list[item];
+    const int64_t off = a.off[cw];
+
+    // LLRs in: data bits in code order, parity bit k + c (c = i mb + r) at [r][i]; messages cleared.
+    const int4 *src = reinterpret_cast<const int4 *>(a.llr + off);
+    for (int t = lane; t < T::N / 16; t += 32) {
+      const int4 w = __ldg(src + t);
+      const int8_t *b = reinterpret_cast<const int8_t *>(&w);
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const int v = t * 16 + j;
+        if (v < T::K) L[v] = b[j];
+        else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = b[j]; }
+      }
+    }
+    int4 *rz = reinterpret_cast<int4 *>(R);
+    for (int t = lane; t < slots<C>() * 128 / 16; t += 32) rz[t] = make_int4(0, 0, 0, 0);
+    __syncwarp();
+
+    int used = -1, first = 0;
+    for (int it = 0; it < a.max_iter; it++) {
+      for (int step = 0; step < T::MB; step++) {
+        layer<C>(L, R, (it & 1) ? T::MB - 1 - step : step, lane);
+        __syncwarp();
+      }
+      const int bad = unsat<C>(L, lane);
+      if (bad == 0) { used = it + 1; break; }
+      if (a.stall_it > 1 && it == a.stall_it - 1) {
+        if ((float)bad > __fmul_rn(a.stall_ratio, (float)first)) { used = -3; break; }
+      } else if (it == 0 && a.stall_it > 1) first = bad;
+    }
+
+    // Hard bits packed MSB first into the message area (no longer needed), then the CRC over the block's bytes.
+    uint8_t *pk = reinterpret_cast<uint8_t *>(R);
+    for (int j = lane; j < T::N / 8; j += 32) {
+      int byte = 0;
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int v = 8 * j + t;
+        int16_t x;
+        if (v < T::K) x = L[v];
+        else { const int c = v - T::K; x = L[T::K + (c % T::MB) * 128 + c / T::MB]; }
+        byte = (byte << 1) | (x < 0);
+      }
+      pk[j] = (uint8_t)byte;
+    }
+    __syncwarp();
+    const int s0 = 15 * lane, s1 = min(s0 + 15, kBlockBytes);
+    uint32_t c = 0;
+    for (int j = s0; j < s1; j++) c = crc_tab[(c ^ pk[j]) & 255u] ^ (c >> 8);
+    c = gf_mul(c, crc_k[lane]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c ^= __shfl_xor_sync(0xffffffffu, c, o);
+    const uint32_t crc = ~(c ^ crc_k[32]);
+    const uint32_t want = (uint32_t)pk[476] << 24 | (uint32_t)pk[477] << 16 | (uint32_t)pk[478] << 8 | pk[479];
+
+    int4 *dst = reinterpret_cast<int4 *>(a.bits + off / 8);
+    const int4 *pv = reinterpret_cast<const int4 *>(pk);
+    for (int t = lane; t < T::N / 128; t += 32) dst[t] = pv[t];
+    if (lane == 0) { a.its[cw] = used; a.ok[cw] = crc == want; }
+    __syncwarp();
+  }
+}
+
+// x^(8 k) mod P, reflected.
+static uint32_t xpow8(int k) {
+  uint32_t r = 0x80000000u;
+  for (int i = 0; i < 8 * k; i++) r = (r >> 1) ^ (kCrcPoly & (0u - (r & 1u)));
+  return r;
+}
+static uint32_t host_gf_mul(uint32_t a, uint32_t b) {
+  uint32_t p = 0;
+  for (int i = 0; i < 32; i++) { if (a & (0x80000000u >> i)) p ^= b; b = (b >> 1) ^ (kCrcPoly & (0u - (b & 1u))); }
+  return p;
+}
+
+cudaError_t ldpc_upload_tables() {
+  DevCode h[4] = {};
+  for (int c = 0; c < 4; c++) {
+    const lizg_code_def_t &d = LIZG_CODES[c];
+    for (int r = 0; r <= d.mb; r++) h[c].rowptr[r] = d.rowptr[r];
+    for (int e = 0; e < d.rowptr[d.mb]; e++) h[c].circ[e] = d.circ[e];
+  }
+  cudaError_t err = cudaMemcpyToSymbol(c_codes, h, sizeof h);
+  if (err != cudaSuccess) return err;
+  uint32_t k[33];
+  for (int l = 0; l < 32; l++) { const int end = 15 * l + 15 < kBlockBytes ? 15 * l + 15 : kBlockBytes; k[l] = xpow8(kBlockBytes - end); }
+  k[32] = host_gf_mul(0xffffffffu, xpow8(kBlockBytes));
+  return cudaMemcpyToSymbol(c_crc_shift, k, sizeof k);
+}
+
+template <int C>
+static cudaError_t launch_one(const LdpcLaunch &a, int sms, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(ldpc_decode_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, cta_smem<C>());
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int need = (a.count + Code<C>::WARPS - 1) / Code<C>::WARPS;
+  const int grid = need < sms ? need : sms;
+  ldpc_decode_kernel<C><<<grid, Code<C>::WARPS * 32, cta_smem<C>(), st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st) {
+  if (a.count <= 0) return cudaSuccess;
+  switch (code) {
+    case 0: return launch_one<0>(a, sms, st);
+    case 1: return launch_one<1>(a, sms, st);
+    case 2: return launch_one<2>(a, sms, st);
+    case 3: return launch_one<3>(a, sms, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace lizg

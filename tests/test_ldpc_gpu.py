@@ -1,0 +1,125 @@
+"""LDPC + CRC-32C on the GPU, through the C ABI, held bit for bit to the reference (its golden decodes) and to the
+oracle (seeded batches across the Eb/N0 sweep, edge cases), and at the benchmark's full size by properties."""
+import os
+
+import numpy as np
+import pytest
+
+import lizard_gb300 as lz
+import oracle
+from lizard_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def golden():
+    return np.load(os.path.join(GOLD, "ldpc_ref.npz"))
+
+
+@pytest.mark.parametrize("tag,mi,si,ratio", [("stall", 20, 9, 0.95), ("plain", 30, 0, 0.0)])
+def test_batch_matches_reference_golden(tag, mi, si, ratio):
+    g = golden()
+    plan = lz.LdpcPlan(g["rates"], mi, si, ratio)
+    bits, its, ok = plan.run(g["llr"])
+    assert np.array_equal(its, g["its_" + tag])
+    assert np.array_equal(bits, g["bits_" + tag])
+
+
+def test_single_codeword_entry_matches_reference_golden():
+    g = golden()
+    at = 0
+    for i, rate in enumerate(g["rates"][:12]):
+        n = lz.CODE_N[int(rate)]
+        its, out = lz.ldpc_decode_stall(int(rate), g["llr"][at:at + n], 20, 9, 0.95)
+        assert its == g["its_stall"][i]
+        assert np.array_equal(np.packbits(out), g["bits_stall"][at // 8:(at + n) // 8])
+        at += n
+
+
+def check_against_oracle(b, mi=20, si=9, ratio=0.95):
+    plan = lz.LdpcPlan(b["rates"], mi, si, ratio)
+    bits, its, ok = plan.run(b["llr"])
+    ob, oi, oo = oracle.ldpc_batch(oracle.port(), b["llr"], b["offsets"], b["rates"], mi, si, ratio, threads=os.cpu_count() or 4)
+    bad = np.nonzero(oi != its)[0]
+    assert bad.size == 0, "iterations differ at %s: gpu %s oracle %s" % (bad[:8], its[bad[:8]], oi[bad[:8]])
+    assert np.array_equal(bits, ob)
+    assert np.array_equal(ok, oo)
+    return bits, its, ok
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_seeded_sweep_matches_oracle(seed):
+    b = synth.ldpc_batch(3000, seed=seed)
+    bits, its, ok = check_against_oracle(b)
+    # the sweep spans failing and clean codewords
+    assert (its == -1).any() or (its == -3).any()
+    assert (its > 0).any() and ok[its > 0].all()
+
+
+@pytest.mark.parametrize("mi,si,ratio", [(1, 0, 0.0), (2, 2, 0.95), (30, 0, 0.0), (9, 9, 0.5), (255, 9, 0.95)])
+def test_decoder_settings_match_oracle(mi, si, ratio):
+    b = synth.ldpc_batch(400, seed=7)
+    check_against_oracle(b, mi, si, ratio)
+
+
+@pytest.mark.parametrize("count", [1, 2, 5, 9, 10, 31])
+def test_small_and_ragged_batches(count):
+    b = synth.ldpc_batch(count, seed=count, rates=synth.mixed_rates(count, seed=count))
+    check_against_oracle(b)
+
+
+def test_extreme_llrs_match_oracle():
+    rng = np.random.default_rng(9)
+    rates, parts = [], []
+    for r in lz.RATES:
+        n = lz.CODE_N[r]
+        for pat in (np.full(n, -128), np.full(n, 127), np.zeros(n), np.tile([127, -128], n // 2),
+                    rng.integers(-128, 128, n), rng.integers(-2, 3, n)):
+            rates.append(r)
+            parts.append(np.asarray(pat, np.int8))
+    rates = np.array(rates, np.int32)
+    llr = np.concatenate(parts)
+    off = np.concatenate([[0], np.cumsum([lz.CODE_N[int(r)] for r in rates])[:-1]]).astype(np.int64)
+    for mi, si in [(20, 9), (30, 0)]:
+        check_against_oracle({"rates": rates, "llr": llr, "offsets": off}, mi, si, 0.95)
+
+
+def test_device_entry_on_a_side_stream_matches_host_entry():
+    torch = pytest.importorskip("torch")
+    b = synth.ldpc_batch(1000, seed=3)
+    plan = lz.LdpcPlan(b["rates"], 20, 9, 0.95)
+    hb, hi, ho = plan.run(b["llr"])
+    s = torch.cuda.Stream()
+    d_llr = torch.from_numpy(b["llr"]).cuda()
+    d_bits = torch.empty(plan.llr_bytes // 8, dtype=torch.uint8, device="cuda")
+    d_its = torch.empty(plan.count, dtype=torch.int32, device="cuda")
+    d_ok = torch.empty(plan.count, dtype=torch.uint8, device="cuda")
+    s.wait_stream(torch.cuda.current_stream())
+    for _ in range(2):   # the second run reuses the plan's counters
+        plan.run_dev(d_llr.data_ptr(), d_bits.data_ptr(), d_its.data_ptr(), d_ok.data_ptr(), s.cuda_stream)
+    s.synchronize()
+    assert np.array_equal(d_bits.cpu().numpy(), hb)
+    assert np.array_equal(d_its.cpu().numpy(), hi)
+    assert np.array_equal(d_ok.cpu().numpy(), ho)
+    assert plan.launches == 4
+
+
+def test_full_size_batch_properties():
+    """The benchmark's batch (65,536 codewords): every decoded block is its sent codeword and passes its CRC, the
+    CRC flags agree with a host CRC of the output, clean-channel codewords all decode, and a sample matches the oracle."""
+    b = synth.ldpc_batch(65536, seed=0)
+    plan = lz.LdpcPlan(b["rates"], 20, 9, 0.95)
+    bits, its, ok = plan.run(b["llr"])
+    truth = np.packbits(b["codewords"])
+    for i in np.nonzero(its > 0)[0][::97]:
+        o, n = int(b["offsets"][i]) // 8, lz.CODE_N[int(b["rates"][i])] // 8
+        assert np.array_equal(bits[o:o + n], truth[o:o + n])
+    for i in range(0, 65536, 331):
+        o = int(b["offsets"][i]) // 8
+        blk = bits[o:o + 480]
+        assert ok[i] == (lz.crc32c(blk[:476].tobytes()) == int.from_bytes(blk[476:480].tobytes(), "big"))
+    hi = b["ebn0"] >= 4.0
+    assert (its[hi & (b["rates"] != 6)] > 0).mean() > 0.99
+    sub = {k: v for k, v in synth.ldpc_batch(512, seed=0).items()}
+    check_against_oracle(sub)
