@@ -15,6 +15,9 @@ BUILD = os.path.join(HERE, "_build")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
+# Translation units whose float and double arithmetic must round once an operation, in source order (no fused
+# multiply-add): they reproduce the reference's soft values bit for bit.
+EXACT = {"demap.cu": ["-fmad=false"]}
 
 
 def sources():
@@ -28,7 +31,7 @@ def _newest_input():
 
 def _compile(src, extra):
     obj = os.path.join(BUILD, src + ".o")
-    cmd = [NVCC] + COMMON + extra
+    cmd = [NVCC] + COMMON + extra + EXACT.get(src, [])
     if src.endswith(".cu"):
         cmd += ARCH + ["-lineinfo", "-Xptxas", "-v"] if os.environ.get("LIZG_PTXAS_V") else ARCH + ["-lineinfo"]
         cmd += ["-x", "cu"]

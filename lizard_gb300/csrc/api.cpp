@@ -60,6 +60,10 @@ struct lizg_ldpc_plan {
   // staging for the host-memory entry point, made on its first use
   int8_t *s_llr = nullptr; uint8_t *s_bits = nullptr; int32_t *s_its = nullptr; uint8_t *s_ok = nullptr;
   int device = -1;
+  // The four codes' launches run on their own streams, forked from and joined back to the caller's stream, so one
+  // code's persistent CTAs take over the SMs another code's tail frees.
+  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 extern "C" {
@@ -142,10 +146,19 @@ lizg_ldpc_plan *lizg_ldpc_plan_new(const int32_t *rate, int count, int max_iter,
       (e = cudaMalloc(&p->d_off, sizeof(int64_t) * (size_t)count)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_counter, sizeof(int) * 4)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_list, list.data(), sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess) {
+      (e = cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming)) != cudaSuccess) {
     fail_cuda(e, "lizg_ldpc_plan_new");
     lizg_ldpc_plan_free(p);
     return nullptr;
+  }
+  for (int c = 0; c < 4; c++) {
+    if ((e = cudaStreamCreateWithFlags(&p->side[c], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&p->join[c], cudaEventDisableTiming)) != cudaSuccess) {
+      fail_cuda(e, "lizg_ldpc_plan_new: streams");
+      lizg_ldpc_plan_free(p);
+      return nullptr;
+    }
   }
   return p;
 }
@@ -154,6 +167,8 @@ void lizg_ldpc_plan_free(lizg_ldpc_plan *p) {
   if (!p) return;
   cudaFree(p->d_list); cudaFree(p->d_off); cudaFree(p->d_counter);
   cudaFree(p->s_llr); cudaFree(p->s_bits); cudaFree(p->s_its); cudaFree(p->s_ok);
+  for (int c = 0; c < 4; c++) { if (p->side[c]) cudaStreamDestroy(p->side[c]); if (p->join[c]) cudaEventDestroy(p->join[c]); }
+  if (p->fork) cudaEventDestroy(p->fork);
   delete p;
 }
 
@@ -170,12 +185,16 @@ int lizg_ldpc_plan_run_dev(lizg_ldpc_plan *p, const int8_t *d_llr, uint8_t *d_bi
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaMemsetAsync(p->d_counter, 0, sizeof(int) * 4, st);
     if (e != cudaSuccess) return fail_cuda(e, "cudaMemsetAsync");
+    if ((e = cudaEventRecord(p->fork, st)) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
     p->launches = 0;
-    for (int c = 0; c < 4; c++) {
+    for (int c = 0; c < 4; c++) {   // longest code first: 7/8 has the most codewords
       if (!p->counts[c]) continue;
+      if ((e = cudaStreamWaitEvent(p->side[c], p->fork, 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
       lizg::LdpcLaunch a{d_llr, d_bits, d_its, d_ok, p->d_list + p->list_at[c], p->d_off, p->counts[c], p->d_counter + c,
                          p->max_iter, p->stall_it, p->ratio};
-      if ((e = lizg::ldpc_launch(c, a, sms, st)) != cudaSuccess) return fail_cuda(e, "LDPC kernel launch");
+      if ((e = lizg::ldpc_launch(c, a, sms, p->side[c])) != cudaSuccess) return fail_cuda(e, "LDPC kernel launch");
+      if ((e = cudaEventRecord(p->join[c], p->side[c])) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
+      if ((e = cudaStreamWaitEvent(st, p->join[c], 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
       p->launches++;
     }
     return 0;

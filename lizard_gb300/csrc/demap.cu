@@ -1,0 +1,184 @@
+// Row (c) of the hot path on sm_103a: the pilots' grid-shift fit, the soft QPSK demap to int8 LLRs, and the
+// per-block estimate / pilot reading / decline gate. Compiled with -fmad=false: every float and double operation here
+// rounds once, in the reference's order, so from the same spectrum these kernels give the reference's soft values
+// bit for bit (liblizard/src/lizard_phy.c:280-329 pilot_align, :1320-1332 sub_scale, :1411-1451 the x86-64 soft4,
+// :1775-1818 the block estimate, pilots and decline).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include "lizg_internal.h"
+
+namespace lizg {
+
+__device__ __forceinline__ float2 coef_at(const float2 *spec, const int32_t *idx, int i) { return spec[idx ? idx[i] : i]; }
+
+// Coefficient i turned back by the grid shift (dx, dy): the turn's index in float, nearest-even, mod 4096, and the
+// rotation by the table's cos / sin, as liblizard/src/lizard_phy.c:214-218 computes them.
+__device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, const int32_t *idx, int i, float dx, float dy) {
+  const float2 z = coef_at(spec, idx, i);
+  const float uu = (float)fd.uv[2 * i], vv = (float)fd.uv[2 * i + 1];
+  const float t = (uu * dx + vv * dy) * fd.turn_scale;
+  const unsigned k = (unsigned)__float2int_rn(t) & (kTurnsDev - 1);
+  const float2 cs = fd.rot[k];
+  return make_float2(z.x * cs.x + z.y * cs.y, z.y * cs.x - z.x * cs.y);
+}
+
+// One warp a frame. Each lane works out its pilots' six products in parallel; lane 0 adds them in pilot order, so
+// the double sums are the reference's. Writes align[3 f ..] = dx, dy, and 1 where the shift is turned back.
+__global__ void pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align) {
+  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (f >= fd.frames) return;
+  __shared__ double terms[8][32][6];
+  double (*tm)[6] = terms[threadIdx.x >> 5];
+  const float2 *sp = spec + f * spec_stride;
+  const double k = 2.0 * 3.14159265358979323846 / fd.n;
+  double dx = 0, dy = 0, a = 0, b = 0, c = 0, p = 0, q = 0, yy = 0;
+  const int used = fd.npilot;
+  bool give_up = false;
+  for (int it = 0; it < 2 && !give_up; it++) {
+    a = b = c = p = q = yy = 0;
+    for (int c0 = 0; c0 < used; c0 += 32) {
+      const int pi = c0 + lane;
+      if (pi < used) {
+        const int i = fd.pilot_coef[pi], w = fd.pilot_white[pi];
+        const float2 y = turned(fd, sp, idx, i, (float)dx, (float)dy);
+        const double xr = (w & 1) ? -1.0 : 1.0, xi = (w & 2) ? -1.0 : 1.0;
+        const double zr = (double)y.x * xr + (double)y.y * xi, zi = (double)y.y * xr - (double)y.x * xi;
+        const double cu = k * zr * fd.uv[2 * i], cv = k * zr * fd.uv[2 * i + 1];
+        tm[lane][0] = cu * cu; tm[lane][1] = cu * cv; tm[lane][2] = cv * cv; tm[lane][3] = cu * zi; tm[lane][4] = cv * zi; tm[lane][5] = zi * zi;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        const int m = min(32, used - c0);
+        for (int l = 0; l < m; l++) { a += tm[l][0]; b += tm[l][1]; c += tm[l][2]; p += tm[l][3]; q += tm[l][4]; yy += tm[l][5]; }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const double det = a * c - b * b;
+      if (used < 8 || !(det > 0)) give_up = true;
+      else { dx += (p * c - q * b) / det; dy += (a * q - b * p) / det; }
+    }
+    give_up = __shfl_sync(0xffffffffu, give_up, 0);
+    dx = __shfl_sync(0xffffffffu, dx, 0);
+    dy = __shfl_sync(0xffffffffu, dy, 0);
+  }
+  if (lane != 0) return;
+  float d0 = 0, d1 = 0;
+  if (!give_up) {
+    const double det = a * c - b * b, ex = (p * c - q * b) / det, ey = (a * q - b * p) / det;
+    const double s2 = (yy - ex * p - ey * q) / (used - 2);
+    const double chi = s2 > 0 ? (dx * dx * a + 2 * dx * dy * b + dy * dy * c) / s2 : 0;
+    if (chi > 13.8 && dx == dx && dy == dy) { d0 = (float)dx; d1 = (float)dy; }
+  }
+  align[3 * f] = d0; align[3 * f + 1] = d1;
+  align[3 * f + 2] = (used > 0 && (d0 != 0 || d1 != 0)) ? 1.0f : 0.0f;
+}
+
+// ten Brink's J (liblizard/src/lizard_phy.c:73-75)
+__device__ __forceinline__ double axis_info(double g) { return g > 0 ? pow(1 - pow(2.0, -0.3073 * pow(2 * sqrt(g), 1.7870)), 1.1064) : 0; }
+
+// Four lanes a sub-channel, eight sub-channels a warp. Lane q of a group sums the moments of coefficients q, q + 4,
+// ... in order (the reference's four float chains), the chains are added (c0 + c1) + (c2 + c3), the scale is worked
+// out in double, and the soft values are each axis times 8 k, NaN to 0, clamped to +-80, rounded half to even.
+__global__ void demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, const float *align,
+                             int8_t *llrf, double *sub_est, float *sub_rms) {
+  const int gid = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2), qd = threadIdx.x & 3;
+  const int f = gid / fd.subch, j = gid - f * fd.subch;
+  const bool live = f < fd.frames;
+  const float2 *sp = spec + (live ? f : 0) * spec_stride;
+  const bool turn = live && align[3 * f + 2] != 0.0f;
+  const float dx = live ? align[3 * f] : 0, dy = live ? align[3 * f + 1] : 0;
+  float m2 = 0, m4 = 0;
+  if (live) {
+    for (int s = qd; s < kSubDev; s += 4) {
+      const int i = j * kSubDev + s;
+      const float2 y = turn ? turned(fd, sp, idx, i, dx, dy) : coef_at(sp, idx, i);
+      const float e = y.x * y.x + y.y * y.y;
+      m2 = m2 + e; m4 = m4 + e * e;
+    }
+  }
+  // (c0 + c1) + (c2 + c3)
+  const float o2 = __shfl_down_sync(0xffffffffu, m2, 1), o4 = __shfl_down_sync(0xffffffffu, m4, 1);
+  const float p2 = m2 + o2, p4 = m4 + o4;
+  const float r2 = __shfl_down_sync(0xffffffffu, p2, 2), r4 = __shfl_down_sync(0xffffffffu, p4, 2);
+  float k8 = 0;
+  if (qd == 0 && live) {
+    const float fm2 = p2 + r2, fm4 = p4 + r4;
+    const double M2 = (double)fm2 / kSubDev, M4 = (double)fm4 / kSubDev;
+    sub_rms[f * fd.subch + j] = M2 > 0 ? (float)sqrt(M2 / 2) : 0;
+    double a2 = 2 * M2 * M2 - M4;
+    a2 = a2 > 0 ? sqrt(a2) : 0;
+    double nv = M2 - a2;
+    if (nv < 0.02 * M2) nv = 0.02 * M2;
+    sub_est[f * fd.subch + j] = axis_info(a2 / nv);
+    const float kk = (float)(0.7 * 2 * sqrt(2 * a2) / nv);
+    k8 = 8 * kk;
+  }
+  k8 = __shfl_sync(0xffffffffu, k8, threadIdx.x & ~3 & 31);
+  if (!live) return;
+  int8_t *out = llrf + (int64_t)f * fd.subch * 2 * kSubDev + 2 * j * kSubDev;
+  for (int s = qd; s < kSubDev; s += 4) {
+    const int i = j * kSubDev + s;
+    const float2 y = turn ? turned(fd, sp, idx, i, dx, dy) : coef_at(sp, idx, i);
+    float x = k8 * y.x, z = k8 * y.y;
+    x = x != x ? 0.0f : fminf(fmaxf(x, -80.0f), 80.0f);
+    z = z != z ? 0.0f : fminf(fmaxf(z, -80.0f), 80.0f);
+    char2 v;
+    v.x = (signed char)__float2int_rn(x);
+    v.y = (signed char)__float2int_rn(z);
+    *reinterpret_cast<char2 *>(out + 2 * s) = v;
+  }
+}
+
+// One thread a block: its estimate (its sub-channels' information weighted by the slots it holds there, in double, in
+// order), its pilot reading (the tail's axis values against the whitening in units of their sub-channel's rms, in
+// double, in order; NaN where none was read) and the decline gate (est < 0.2 k / nt in float): decl[f blocks + b] = 1.
+__global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, const float *align,
+                              const double *sub_est, const float *sub_rms, float *est, float *pilot, uint8_t *decl) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= fd.frames * fd.blocks) return;
+  const int f = g / fd.blocks, b = g - f * fd.blocks;
+  const int t = fd.block_tier[b], nb = fd.tier_slots[t], s0 = fd.block_slot[b], nt = fd.tier_nt[t];
+  const double *se = sub_est + f * fd.subch;
+  const float *sr = sub_rms + f * fd.subch;
+  double info = 0;
+  for (int j = s0 / (2 * kSubDev); j * 2 * kSubDev < s0 + nb; j++) {
+    const int lo = max(s0, 2 * kSubDev * j), hi = min(s0 + nb, 2 * kSubDev * (j + 1));
+    info += se[j] * (hi - lo);
+  }
+  const float e = (float)(info / nb);
+  est[g] = e;
+  float pv = __int_as_float(0x7fc00000);   // NaN: no pilot read
+  if (nt < nb) {
+    const float2 *sp = spec + f * spec_stride;
+    const bool turn = align[3 * f + 2] != 0.0f;
+    const float dx = align[3 * f], dy = align[3 * f + 1];
+    double cs = 0;
+    int got = 0;
+    for (int i = nt; i < nb; i++) {
+      const int gs = s0 + i, ci = gs / 2;
+      const float rms = sr[gs / (2 * kSubDev)];
+      if (!(rms > 0)) continue;
+      const float2 y = turn ? turned(fd, sp, idx, ci, dx, dy) : coef_at(sp, idx, ci);
+      const float yv = (i & 1) ? y.y : y.x;
+      cs += (fd.white[gs] ? -1.0 : 1.0) * yv / rms;
+      got++;
+    }
+    if (got) pv = (float)(cs / (nb - nt));
+  }
+  pilot[g] = pv;
+  decl[g] = e < 0.2f * (float)fd.tier_k[t] / (float)nt;
+}
+
+cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
+                         double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st) {
+  pilot_align_kernel<<<(fd.frames + 7) / 8, 256, 0, st>>>(fd, spec, spec_stride, idx, align);
+  const int groups = fd.frames * fd.subch;
+  demap_kernel<<<(groups + 63) / 64, 256, 0, st>>>(fd, spec, spec_stride, idx, align, llrf, sub_est, sub_rms);
+  const int nbk = fd.frames * fd.blocks;
+  blocks_kernel<<<(nbk + 127) / 128, 128, 0, st>>>(fd, spec, spec_stride, idx, align, sub_est, sub_rms, est, pilot, decl);
+  return cudaGetLastError();
+}
+
+}  // namespace lizg

@@ -23,10 +23,11 @@ namespace lizg {
 // Per-code compile-time shape: block rows, codeword bits, data bits, data circulants, slots (data circulants plus
 // two staircase slots a row), and the warps a CTA runs (as many codeword states as fit in 227 KB of shared memory).
 template <int C> struct Code;
-template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, WARPS = 9; };
-template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, WARPS = 7; };
-template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, WARPS = 6; };
-template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, WARPS = 5; };
+// NDMAX: the most data circulants any block row has.
+template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, NDMAX = 21, WARPS = 9; };
+template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, NDMAX = 14, WARPS = 7; };
+template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, NDMAX = 10, WARPS = 6; };
+template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5; };
 
 template <int C> __host__ __device__ constexpr int slots() { return Code<C>::NDATA + 2 * Code<C>::MB; }
 // A warp's state: posteriors (N int16) then messages (slots x 128 int8), rounded to 16 bytes.
@@ -61,8 +62,96 @@ __device__ __forceinline__ uint32_t gf_mul(uint32_t a, uint32_t b) {
 
 __device__ __forceinline__ int sat127(int v) { return max(-127, min(127, v)); }
 
+// One layer (block row r). Lane l takes checks i = l + 32 t, t = 0..3. Pass 1 loads every slot's extrinsic
+// q = L - R into registers (the row's circulants are unrolled to the code's widest row, so the register arrays are
+// statically indexed) and folds them into two interleaved min1/min2 chains a check, merged at the end; pass 2 makes
+// the messages and posteriors from the registers without reading shared memory again.
 template <int C>
 __device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane) {
+  using T = Code<C>;
+  constexpr int NDM = T::NDMAX;
+  const DevCode &cd = c_codes[C];
+  const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+  int8_t *Rr = R + (p0 + 2 * r) * 128 + lane;
+  int16_t *Lp = L + T::K;
+  int q[NDM + 2][4];
+  int colb[NDM], sh[NDM];
+#pragma unroll
+  for (int e = 0; e < NDM; e++) {
+    if (e < nd) {
+      const int cs = cd.circ[p0 + e];
+      colb[e] = (cs >> 8) * 128; sh[e] = cs & 255;
+#pragma unroll
+      for (int t = 0; t < 4; t++) q[e][t] = L[colb[e] + ((lane + 32 * t - sh[e]) & 127)] - Rr[e * 128 + 32 * t];
+    }
+  }
+  const int prev = r > 0 ? (r - 1) * 128 + lane : (T::MB - 1) * 128 + lane - 1;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    q[NDM][t] = (r == 0 && lane + 32 * t == 0) ? 8191 : Lp[prev + 32 * t] - Rr[nd * 128 + 32 * t];
+    q[NDM + 1][t] = Lp[r * 128 + lane + 32 * t] - Rr[(nd + 1) * 128 + 32 * t];
+  }
+  int m1[4], m2[4], sg[4];
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    int a1 = 255, a2 = 255, b1 = 255, b2 = 255, s = q[NDM][t] ^ q[NDM + 1][t];
+    {
+      const int a = min(abs(q[NDM][t]), 127), b = min(abs(q[NDM + 1][t]), 127);
+      a1 = a; b1 = b;
+    }
+#pragma unroll
+    for (int e = 0; e < NDM; e++) {
+      if (e < nd) {
+        const int a = min(abs(q[e][t]), 127);
+        s ^= q[e][t];
+        if (e & 1) { b2 = min(b2, max(b1, a)); b1 = min(b1, a); }
+        else { a2 = min(a2, max(a1, a)); a1 = min(a1, a); }
+      }
+    }
+    m1[t] = min(a1, b1);
+    m2[t] = min(max(a1, b1), min(a2, b2));
+    sg[t] = s;
+  }
+  int s1[4], s2[4];
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    const int x1 = min(127, (m1[t] * 13) >> 4), x2 = min(127, (m2[t] * 13) >> 4);
+    s1[t] = sg[t] < 0 ? -x1 : x1;     // the check's sign folded in
+    s2[t] = sg[t] < 0 ? -x2 : x2;
+  }
+  auto msg = [&](int v, int t) {
+    const int a = min(abs(v), 127);
+    const int m = (a == m1[t]) ? s2[t] : s1[t];
+    return v < 0 ? -m : m;
+  };
+#pragma unroll
+  for (int e = 0; e < NDM; e++) {
+    if (e < nd) {
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int m = msg(q[e][t], t);
+        Rr[e * 128 + 32 * t] = (int8_t)m;
+        L[colb[e] + ((lane + 32 * t - sh[e]) & 127)] = (int16_t)(q[e][t] + m);
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    if (!(r == 0 && lane + 32 * t == 0)) {
+      const int m = msg(q[NDM][t], t);
+      Rr[nd * 128 + 32 * t] = (int8_t)m;
+      Lp[prev + 32 * t] = (int16_t)(q[NDM][t] + m);
+    }
+    const int m = msg(q[NDM + 1][t], t);
+    Rr[(nd + 1) * 128 + 32 * t] = (int8_t)m;
+    Lp[r * 128 + lane + 32 * t] = (int16_t)(q[NDM + 1][t] + m);
+  }
+}
+
+// The same layer with the row's slots in a loop, the extrinsics recomputed in pass 2: fewer registers, which the
+// 7/8 code's 21-circulant rows need.
+template <int C>
+__device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lane) {
   using T = Code<C>;
   const DevCode &cd = c_codes[C];
   const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
@@ -139,25 +228,26 @@ __device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane) {
 template <int C>
 __device__ __forceinline__ int unsat(const int16_t *L, int lane) {
   using T = Code<C>;
+  constexpr int NDM = T::NDMAX;
   const DevCode &cd = c_codes[C];
   const int16_t *Lp = L + T::K;
   int bad = 0;
   for (int r = 0; r < T::MB; r++) {
     const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+    const int prev = r > 0 ? (r - 1) * 128 + lane : (T::MB - 1) * 128 + lane - 1;
     int x[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int i = lane + 32 * q;
-      x[q] = Lp[r * 128 + i] ^ (r > 0 ? Lp[(r - 1) * 128 + i] : (i > 0 ? Lp[(T::MB - 1) * 128 + i - 1] : 0));
-    }
-    for (int e = 0; e < nd; e++) {
-      const int cs = cd.circ[p0 + e], sh = cs & 255;
-      const int16_t *col = L + (cs >> 8) * 128;
+    for (int t = 0; t < 4; t++) x[t] = Lp[r * 128 + lane + 32 * t] ^ ((r == 0 && lane + 32 * t == 0) ? 0 : Lp[prev + 32 * t]);
 #pragma unroll
-      for (int q = 0; q < 4; q++) x[q] ^= col[(lane + 32 * q - sh) & 127];
+    for (int e = 0; e < NDM; e++) {
+      if (e < nd) {
+        const int cs = cd.circ[p0 + e], cb = (cs >> 8) * 128, sh = cs & 255;
+#pragma unroll
+        for (int t = 0; t < 4; t++) x[t] ^= L[cb + ((lane + 32 * t - sh) & 127)];
+      }
     }
 #pragma unroll
-    for (int q = 0; q < 4; q++) bad += x[q] < 0;
+    for (int t = 0; t < 4; t++) bad += x[t] < 0;
   }
   return __reduce_add_sync(0xffffffffu, bad);
 }
@@ -184,21 +274,49 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
     if (lane == 0) item = atomicAdd(a.counter, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= a.count) break;
-    const int cw = a.list[item];
-    const int64_t off = a.off[cw];
-
-    // LLRs in: data bits in code order, parity bit k + c (c = i mb + r) at [r][i]; messages cleared.
-    const int4 *src = reinterpret_cast<const int4 *>(a.llr + off);
-    for (int t = lane; t < T::N / 16; t += 32) {
-      const int4 w = __ldg(src + t);
-      const int8_t *b = reinterpret_cast<const int8_t *>(&w);
+    int cw, g = 0;
+    int64_t off = 0;
+    if (a.rx.llrf) {
+      // Receiver mode: item -> (frame, block) of this tier. A declined block is not tried (its -2). Otherwise its
+      // slots' soft values go through the bit map into codeword order, whitening taken off by sign, the never-sent
+      // bits at 0 and the 7/8 code's known zeros past the block's 3840 bits at 127
+      // (liblizard/src/lizard_phy.c:156-192, 1818-1823).
+      const int f = item / a.fd.tier_blocks[a.tier], b = a.fd.tier_first[a.tier] + item % a.fd.tier_blocks[a.tier];
+      g = f * a.fd.blocks + b;
+      cw = g;
+      if (a.rx.decl[g]) {
+        if (lane == 0) { a.its[g] = -2; a.ok[g] = 0; }
+        continue;
+      }
+      const int s0 = a.fd.block_slot[b], nt = a.fd.tier_nt[a.tier];
+      const int8_t *sl = a.rx.llrf + f * a.rx.llr_stride + s0;
+      const uint8_t *wh = a.fd.white + s0;
+      const int16_t *perm = a.fd.perm[a.tier];
+      for (int i = lane; i < nt; i += 32) {
+        const int v = perm[i];
+        const int8_t x = sl[i];
+        const int8_t y = wh[i] ? (int8_t)(-x) : x;
+        if (v < T::K) L[v] = y;
+        else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = y; }
+      }
+      for (int v = LIZG_INFO_BITS + lane; v < T::K; v += 32) L[v] = 127;
+    } else {
+      cw = a.list[item];
+      off = a.off[cw];
+      // LLRs in: data bits in code order, parity bit k + c (c = i mb + r) at [r][i].
+      const int4 *src = reinterpret_cast<const int4 *>(a.llr + off);
+      for (int t = lane; t < T::N / 16; t += 32) {
+        const int4 w = __ldg(src + t);
+        const int8_t *b = reinterpret_cast<const int8_t *>(&w);
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int v = t * 16 + j;
-        if (v < T::K) L[v] = b[j];
-        else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = b[j]; }
+        for (int j = 0; j < 16; j++) {
+          const int v = t * 16 + j;
+          if (v < T::K) L[v] = b[j];
+          else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = b[j]; }
+        }
       }
     }
+    // messages cleared
     int4 *rz = reinterpret_cast<int4 *>(R);
     for (int t = lane; t < slots<C>() * 128 / 16; t += 32) rz[t] = make_int4(0, 0, 0, 0);
     __syncwarp();
@@ -206,7 +324,9 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
     int used = -1, first = 0;
     for (int it = 0; it < a.max_iter; it++) {
       for (int step = 0; step < T::MB; step++) {
-        layer<C>(L, R, (it & 1) ? T::MB - 1 - step : step, lane);
+        const int r = (it & 1) ? T::MB - 1 - step : step;
+        if (T::NDMAX > 16) layer_loop<C>(L, R, r, lane);
+        else layer<C>(L, R, r, lane);
         __syncwarp();
       }
       const int bad = unsat<C>(L, lane);
@@ -240,10 +360,17 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
     const uint32_t crc = ~(c ^ crc_k[32]);
     const uint32_t want = (uint32_t)pk[476] << 24 | (uint32_t)pk[477] << 16 | (uint32_t)pk[478] << 8 | pk[479];
 
-    int4 *dst = reinterpret_cast<int4 *>(a.bits + off / 8);
-    const int4 *pv = reinterpret_cast<const int4 *>(pk);
-    for (int t = lane; t < T::N / 128; t += 32) dst[t] = pv[t];
-    if (lane == 0) { a.its[cw] = used; a.ok[cw] = crc == want; }
+    if (a.rx.llrf) {
+      // the block's 476 bytes, verified or not (ok says which)
+      uint8_t *dst = a.rx.blocks + (int64_t)g * kBlockBytes;
+      for (int t = lane; t < kBlockBytes; t += 32) dst[t] = pk[t];
+    } else {
+      int4 *dst = reinterpret_cast<int4 *>(a.bits + off / 8);
+      const int4 *pv = reinterpret_cast<const int4 *>(pk);
+      for (int t = lane; t < T::N / 128; t += 32) dst[t] = pv[t];
+    }
+    // the batch reports the CRC of whatever was decided; the receiver verifies only decoded blocks (its > 0)
+    if (lane == 0) { a.its[cw] = used; a.ok[cw] = (a.rx.llrf ? used > 0 : true) && crc == want; }
     __syncwarp();
   }
 }

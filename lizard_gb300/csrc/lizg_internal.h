@@ -6,6 +6,31 @@
 
 namespace lizg {
 
+constexpr int kSubDev = 320, kTurnsDev = 4096;
+
+// A format's tables on the device plus the batch's frame count, passed by value to the receive kernels.
+struct FmtDev {
+  int n, subch, blocks, frames, npilot, V;
+  float turn_scale;                  // (float)4096 / (float)n
+  int tier_first[4], tier_blocks[4], tier_slots[4], tier_nt[4], tier_k[4];
+  const int16_t *uv;                 // (u, v) a coefficient, pos order
+  const int32_t *tix;                // its index in the spectrum array [v][u mod n]
+  const uint8_t *white;              // whitening bit a frame slot
+  const int16_t *perm[4];            // per tier: block slot -> codeword bit
+  const int32_t *block_tier, *block_slot;
+  const int32_t *pilot_coef;         // the block tails' coefficients in block order
+  const uint8_t *pilot_white;        // their whitening (bit 0 real, bit 1 imaginary)
+  const float2 *rot;                 // cos, sin of 2 pi k / 4096
+};
+
+// The receiver's per-batch soft-value and block state, in device memory.
+struct RxState {
+  const int8_t *llrf;     // frames x subch x 640 soft values, slot order
+  const uint8_t *decl;    // frames x blocks: 1 where the decline gate skipped the block
+  uint8_t *blocks;        // frames x blocks x 476 decoded bytes
+  int64_t llr_stride;     // bytes a frame of llrf
+};
+
 // One launch of the LDPC kernel over the codewords of one code.
 struct LdpcLaunch {
   const int8_t *llr;      // the batch's LLRs, codeword i at llr + off[i]
@@ -18,9 +43,15 @@ struct LdpcLaunch {
   int *counter;           // work counter, zero at launch
   int max_iter, stall_it;
   float stall_ratio;
+  // receiver mode (rx.llrf set): items are (frame, block) of one tier; its/ok indexed frame x blocks + block
+  RxState rx;
+  FmtDev fd;
+  int tier;
 };
 
 cudaError_t ldpc_upload_tables();
+cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
+                         double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
 

@@ -120,3 +120,221 @@ def ldpc_batch(lib, llr, offsets, rates, max_iter, stall_it, stall_ratio, thread
     if rc:
         raise RuntimeError("oracle batch failed")
     return bits, its, ok
+
+
+# ------------------------------------------------------------------ the receiver
+
+SUB = 320
+
+
+def _phy_sigs(L):
+    P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    L.orc_fmt_new.argtypes = [I, I, I]
+    L.orc_fmt_new.restype = P
+    L.orc_fmt_free.argtypes = [P]
+    L.orc_tiers_for.argtypes = [I, P, P, P]
+    L.orc_fmt_info.argtypes = [P, P]
+    L.orc_fmt_tables.argtypes = [P, P, P, P, P, P, P, P]
+    L.orc_fmt_perm.argtypes = [P, I, P]
+    L.orc_spectrum.argtypes = [P, P, P, P]
+    L.orc_pilot_align.argtypes = [P, P, P]
+    L.orc_demap.argtypes = [P, P, P, P, P, P]
+    L.orc_blocks.argtypes = [P, P, P, P, P, P, I, P, P, P, P, P]
+
+
+class Fmt:
+    """The oracle's restatement of one format (n, subch, span)."""
+
+    def __init__(self, n, subch, span=128):
+        L = port()
+        if not hasattr(L, "_phy"):
+            _phy_sigs(L)
+            L._phy = True
+        self.L = L
+        self.h = L.orc_fmt_new(n, subch, span)
+        if not self.h:
+            raise ValueError("no format at n=%d subch=%d span=%d" % (n, subch, span))
+        info = np.zeros(20, np.int32)
+        L.orc_fmt_info(self.h, _p(info))
+        self.n, self.subch, self.span, self.blocks, self.used, self.bw, self.vblocks, self.tiers = (int(x) for x in info[:8])
+        self.tier = [(int(info[8 + 3 * t]), int(info[9 + 3 * t]), int(info[10 + 3 * t])) for t in range(self.tiers)]
+        need = self.subch * SUB
+        self.pos = np.zeros(need, np.int32)
+        self.uv = np.zeros(2 * need, np.int16)
+        self.white = np.zeros(2 * need, np.uint8)
+        self.block_tier = np.zeros(self.blocks, np.int32)
+        self.block_slot = np.zeros(self.blocks, np.int32)
+        self.erase = np.zeros(14, np.int32)
+        self.hole_inv = np.zeros(36, np.float64)
+        L.orc_fmt_tables(self.h, _p(self.pos), _p(self.uv), _p(self.white), _p(self.block_tier), _p(self.block_slot), _p(self.erase), _p(self.hole_inv))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_fmt_free(self.h)
+            self.h = None
+
+    def perm(self, t):
+        out = np.zeros(7680, np.int32)
+        nt = self.L.orc_fmt_perm(self.h, t, _p(out))
+        return out[:nt]
+
+    def spectrum(self, grid):
+        """FP64 detrended spectrum (complex128, pos order) of a row-major n x n grid (grey / 255); also the erased grid
+        and the 5 projections."""
+        g = np.ascontiguousarray(grid, np.float32).copy()
+        coef = np.zeros(2 * self.subch * SUB, np.float64)
+        proj = np.zeros(5, np.float64)
+        self.L.orc_spectrum(self.h, _p(g), _p(coef), _p(proj))
+        return coef[0::2] + 1j * coef[1::2], g, proj
+
+    def pilot_align(self, coef):
+        c = np.ascontiguousarray(coef, np.float32)
+        d = np.zeros(2, np.float32)
+        used = self.L.orc_pilot_align(self.h, _p(c), _p(d))
+        return d, used
+
+    def demap(self, coef, turn=None):
+        """coef: float32 pairs (2 a coefficient, pos order). Returns (llrf int8, sub_est float64, sub_rms float32)."""
+        c = np.ascontiguousarray(coef, np.float32)
+        llrf = np.zeros(2 * self.subch * SUB, np.int8)
+        est = np.zeros(self.subch, np.float64)
+        rms = np.zeros(self.subch, np.float32)
+        t = None if turn is None else np.ascontiguousarray(turn, np.float32)
+        self.L.orc_demap(self.h, _p(c), None if t is None else _p(t), _p(llrf), _p(est), _p(rms))
+        return llrf, est, rms
+
+    def blocks_stage(self, llrf, est, rms, coef, turn=None, max_iter=30):
+        c = np.ascontiguousarray(coef, np.float32)
+        blocks = np.zeros((self.blocks, 476), np.uint8)
+        ok = np.zeros(self.blocks, np.uint8)
+        its = np.zeros(self.blocks, np.int8)
+        best = np.zeros(self.blocks, np.float32)
+        pil = np.zeros(self.blocks, np.float32)
+        t = None if turn is None else np.ascontiguousarray(turn, np.float32)
+        self.L.orc_blocks(self.h, _p(np.ascontiguousarray(llrf, np.int8)), _p(np.ascontiguousarray(est, np.float64)),
+                          _p(np.ascontiguousarray(rms, np.float32)), _p(c), None if t is None else _p(t), max_iter,
+                          _p(blocks), _p(ok), _p(its), _p(best), _p(pil))
+        return {"blocks": blocks, "ok": ok, "its": its, "est": best, "pilot": pil}
+
+    def receive(self, grid, fp64_spectrum=True):
+        """The whole finish on a grid: spectrum (FP64, narrowed to float), pilots, soft values, blocks."""
+        spec, _, _ = self.spectrum(grid)
+        coef = np.empty(2 * spec.size, np.float32)
+        coef[0::2] = spec.real
+        coef[1::2] = spec.imag
+        d, used = self.pilot_align(coef)
+        turn = d if (used and (d[0] != 0 or d[1] != 0)) else None
+        llrf, est, rms = self.demap(coef, turn)
+        out = self.blocks_stage(llrf, est, rms, coef, turn)
+        out.update({"coef": coef, "llrf": llrf, "sub_est": est, "sub_rms": rms, "align": d if turn is not None else np.zeros(2, np.float32)})
+        return out
+
+
+class RefFmt:
+    """The reference codec at one format (only where oracle/_ref was built)."""
+
+    def __init__(self, n, subch, span=128):
+        L = ref()
+        if L is None:
+            raise RuntimeError("the reference is not built here")
+        if not hasattr(L, "_phy"):
+            P, I = ctypes.c_void_p, ctypes.c_int
+            L.ref_fmt_new.argtypes = [I, I, I]
+            L.ref_fmt_new.restype = P
+            L.ref_fmt_free.argtypes = [P]
+            L.ref_fmt_info.argtypes = [P, P]
+            L.ref_fmt_tables.argtypes = [P, P, P, P, P, P, P]
+            L.ref_fmt_perm.argtypes = [P, I, P]
+            L.ref_encode.argtypes = [P, P, I, P, P]
+            L.ref_finish_grid.argtypes = [P] + [P] * 11
+            L.ref_decode_frame.argtypes = [P, P, I, I, P, P, P, P, P, P]
+            L.ref_sample_grid.argtypes = [P, P, I, I, P, I, P]
+            L._phy = True
+        self.L = L
+        self.h = L.ref_fmt_new(n, subch, span)
+        if not self.h:
+            raise ValueError("no format")
+        info = np.zeros(21, np.int32)
+        L.ref_fmt_info(self.h, _p(info))
+        self.n, self.subch, self.blocks, self.used, self.bw, self.vblocks, self.tiers, self.pxm, self.px = (int(x) for x in info[:9])
+        self.tier = [(int(info[9 + 3 * t]), int(info[10 + 3 * t]), int(info[11 + 3 * t])) for t in range(self.tiers)]
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.ref_fmt_free(self.h)
+            self.h = None
+
+    def tables(self):
+        need = self.subch * SUB
+        pos = np.zeros(need, np.int32)
+        white = np.zeros(2 * need, np.uint8)
+        bt = np.zeros(self.blocks, np.int32)
+        bs = np.zeros(self.blocks, np.int32)
+        er = np.zeros(14, np.int32)
+        hi = np.zeros(36, np.float64)
+        self.L.ref_fmt_tables(self.h, _p(pos), _p(white), _p(bt), _p(bs), _p(er), _p(hi))
+        return {"pos": pos, "white": white, "block_tier": bt, "block_slot": bs, "erase": er, "hole_inv": hi}
+
+    def perm(self, t):
+        out = np.zeros(7680, np.int32)
+        nt = self.L.ref_fmt_perm(self.h, t, _p(out))
+        return out[:nt]
+
+    def encode(self, blocks, c=0):
+        """(drive px x px float32, grey W x W uint8)."""
+        blocks = np.ascontiguousarray(blocks, np.uint8)
+        drive = np.zeros(self.px * self.px, np.float32)
+        W = self.px + 4 * self.pxm
+        grey = np.zeros(W * W, np.uint8)
+        self.L.ref_encode(self.h, _p(blocks), c, _p(drive), _p(grey))
+        return drive.reshape(self.px, self.px), grey.reshape(W, W)
+
+    def finish_grid(self, grid):
+        g = np.ascontiguousarray(grid, np.float32)
+        need = self.subch * SUB
+        out = {"coef": np.zeros(2 * need, np.float32), "llrf": np.zeros(2 * need, np.int8), "sub_est": np.zeros(self.subch, np.float64),
+               "sub_rms": np.zeros(self.subch, np.float32), "align": np.zeros(2, np.float32), "its": np.zeros(self.blocks, np.int8),
+               "est": np.zeros(self.blocks, np.float32), "pilot": np.zeros(self.blocks, np.float32),
+               "blocks": np.zeros((self.blocks, 476), np.uint8), "ok": np.zeros(self.blocks, np.uint8)}
+        good = self.L.ref_finish_grid(self.h, _p(g), *[_p(out[k]) for k in ("coef", "llrf", "sub_est", "sub_rms", "align", "its", "est", "pilot", "blocks", "ok")])
+        out["good"] = good
+        return out
+
+    def decode_frame(self, luma):
+        luma = np.ascontiguousarray(luma, np.uint8)
+        ih, iw = luma.shape
+        blocks = np.zeros((self.blocks, 476), np.uint8)
+        ok = np.zeros(self.blocks, np.uint8)
+        its = np.zeros(self.blocks, np.int8)
+        reg = np.zeros(9 + 2 * 40 * 40, np.float32)
+        nxy = np.zeros(80, np.float32)
+        nn = np.zeros(2, np.int32)
+        good = self.L.ref_decode_frame(self.h, _p(luma), iw, ih, _p(blocks), _p(ok), _p(its), _p(reg), _p(nxy), _p(nn))
+        nx, ny = int(nn[0]), int(nn[1])
+        return {"good": good, "blocks": blocks, "ok": ok, "its": its, "H": reg[:9].copy(),
+                "nodes": reg[9:9 + 2 * nx * ny].reshape(ny, nx, 2).copy(), "node_x": nxy[:nx].copy(), "node_y": nxy[nx:nx + ny].copy()}
+
+    def sample_grid(self, luma, H, nodes, fast):
+        luma = np.ascontiguousarray(luma, np.uint8)
+        ih, iw = luma.shape
+        reg = np.concatenate([np.asarray(H, np.float32).ravel(), np.asarray(nodes, np.float32).ravel()]).astype(np.float32)
+        g = np.zeros(self.n * self.n, np.float32)
+        self.L.ref_sample_grid(self.h, _p(luma), iw, ih, _p(reg), int(fast), _p(g))
+        return g.reshape(self.n, self.n)
+
+
+def spec_blocks(count, seed=None):
+    """Blocks as the spec's test vector makes them (id LE, byte j = j mod 256), or seeded random payloads."""
+    b = np.zeros((count, 476), np.uint8)
+    b[:, :4] = np.arange(count, dtype="<u4").view(np.uint8).reshape(count, 4)
+    if seed is None:
+        b[:, 4:] = np.arange(472, dtype=np.int64) & 255
+    else:
+        b[:, 4:] = np.random.default_rng(seed).integers(0, 256, (count, 472), dtype=np.uint8)
+    return b
+
+
+def picture_grid(grey, n, pxm, quiet_modules=2, margin=15):
+    """The n x n picture grid (grey / 255) out of a painted grey square at an exact-copy scale (pxm = n / span)."""
+    o = (quiet_modules + margin) * pxm
+    return grey[o:o + n, o:o + n].astype(np.float32) / 255.0

@@ -39,6 +39,26 @@ uint32_t orc_crc32c(const uint8_t *p, int n);
 int orc_ldpc_batch(const int8_t *llr, const int64_t *off, const int32_t *rate, int count, int max_iter, int stall_it,
                    float stall_ratio, uint8_t *out, int32_t *its, uint8_t *ok, int threads);
 
+// ------------------------------------------------------------------ the receiver (oracle_phy.c)
+typedef struct orc_fmt orc_fmt_t;
+// The format at (n, subch, span) (liblizard/src/lizard_phy.c:485-562), NULL for none.
+orc_fmt_t *orc_fmt_new(int n, int subch, int span);
+void orc_fmt_free(orc_fmt_t *f);
+// The rate profile (liblizard/src/lizard_phy.c:578-621): tiers' rate, blocks and slots; returns the tier count.
+int orc_tiers_for(int subch, int32_t *rate, int32_t *blocks, int32_t *slots);
+int orc_fmt_info(const orc_fmt_t *f, int32_t *info);
+int orc_fmt_tables(const orc_fmt_t *f, int32_t *pos, int16_t *uv, uint8_t *white, int32_t *btier, int32_t *bslot, int32_t *erase, double *hole_inv);
+int orc_fmt_perm(const orc_fmt_t *f, int tier, int32_t *perm);
+// The detrended spectrum of a row-major grid in FP64 at the used coefficients, pos order (erases grid in place).
+int orc_spectrum(const orc_fmt_t *f, float *grid, double *coef, double *proj_out);
+// The pilots' grid shift (liblizard/src/lizard_phy.c:280-329).
+int orc_pilot_align(const orc_fmt_t *f, const float *coef, float d[2]);
+// Soft values of every slot (x86-64 arithmetic), each sub-channel's estimate and rms.
+int orc_demap(const orc_fmt_t *f, const float *coef, const float *turn, int8_t *llrf, double *sub_est, float *sub_rms);
+// The block stage: decline, bit map, LDPC (max_iter, stall 9 / 0.95), CRC, pilots.
+int orc_blocks(const orc_fmt_t *f, const int8_t *llrf, const double *sub_est, const float *sub_rms, const float *coef,
+               const float *turn, int max_iter, uint8_t *blocks, uint8_t *ok, int8_t *its, float *est, float *pilot);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,8 +7,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include "ldpc.h"
-#include "lizard_phy.h"
-#include "internal.h"
+// The receiver's workspace is private to lizard_phy.c, so the harness compiles it in (the pattern of the reference's
+// own liblizard/test/phy_x86.c:9) to read the spectrum, soft values and per-block results a finish leaves there.
+#include "lizard_phy.c"
 
 uint32_t ob_debug_hash;
 
@@ -91,5 +92,115 @@ int ref_ldpc_batch(const int8_t *llr, const int64_t *off, const int32_t *rate, i
   for (int t = 1; t < threads; t++) pthread_create(&th[t], 0, ref_worker, &b);
   ref_worker(&b);
   for (int t = 1; t < threads; t++) pthread_join(th[t], 0);
+  return 0;
+}
+
+
+// ------------------------------------------------------------------ the receiver
+
+lizard_t *ref_fmt_new(int n, int subch, int span) {
+  lizard_t *f = calloc(1, sizeof *f);
+  if (!f) return 0;
+  if (lizard_init(f, n, subch, span)) { free(f); return 0; }
+  return f;
+}
+void ref_fmt_free(lizard_t *f) { if (f) { lizard_free(f); free(f); } }
+
+// n, subch, blocks, used, bw, vblocks, tiers, pxm, px, then per tier rate, blocks, slots.
+void ref_fmt_info(const lizard_t *f, int32_t *o) {
+  o[0] = f->n; o[1] = f->subch; o[2] = f->blocks; o[3] = f->used; o[4] = f->bw; o[5] = f->vblocks; o[6] = f->tiers; o[7] = f->pxm; o[8] = f->px;
+  for (int t = 0; t < 4; t++) { o[9 + 3 * t] = t < f->tiers ? f->tier[t].rate : 0; o[10 + 3 * t] = t < f->tiers ? f->tier[t].blocks : 0; o[11 + 3 * t] = t < f->tiers ? f->tier[t].slots : 0; }
+}
+void ref_fmt_tables(const lizard_t *f, int32_t *pos, uint8_t *white, int32_t *btier, int32_t *bslot, int32_t *erase, double *hole_inv) {
+  const struct lizard_ws *w = f->ws;
+  memcpy(pos, f->pos, (size_t)f->subch * LIZARD_SUB * sizeof(int));
+  memcpy(white, w->white, (size_t)f->subch * LIZARD_SUB * 2);
+  memcpy(btier, f->block_tier, (size_t)f->blocks * sizeof(int));
+  memcpy(bslot, f->block_slot, (size_t)f->blocks * sizeof(int));
+  for (int i = 0; i < OB_ANCH_K; i++) { erase[i] = w->elo[i]; erase[OB_ANCH_K + i] = w->ehi[i]; }
+  memcpy(hole_inv, w->hole_inv, sizeof w->hole_inv);
+}
+int ref_fmt_perm(const lizard_t *f, int t, int32_t *perm) {
+  if (t < 0 || t >= f->tiers) return -1;
+  memcpy(perm, f->ws->perm[t], (size_t)f->code[t].nt * sizeof(int));
+  return f->code[t].nt;
+}
+
+// The sender: blocks (blocks x 476) encoded with pilot count c, the drive (px^2 floats) and its grey square with the
+// quiet margin (W^2 bytes, W = px + 2 LIZARD_QUIET pxm). Returns W.
+int ref_encode(lizard_t *f, const uint8_t *blocks, int c, float *drive, uint8_t *grey) {
+  lizard_parity(f, c);
+  lizard_encode(f, blocks, drive);
+  if (grey) lizard_paint_grey(f, drive, grey);
+  return f->px + 2 * LIZARD_QUIET * f->pxm;
+}
+
+// The finish on a supplied picture grid (row-major n x n, grey / 255), as lizard_finish(f, grid, ...) runs it with a
+// registration held: the transform and detrend in FP32, the pilots, the soft values, the blocks. Out (any NULL):
+// coef (2 floats a coefficient, pos order), llrf (subch x 640), sub_est (subch doubles), sub_rms, align (2), and per
+// block its, est, pilot; blocks and ok as lizard_finish gives them. Returns the blocks verified.
+int ref_finish_grid(lizard_t *f, const float *grid, float *coef, int8_t *llrf, double *sub_est, float *sub_rms, float *align,
+                    int8_t *its, float *est, float *pilot, uint8_t *blocks, uint8_t *ok) {
+  struct lizard_ws *w = f->ws;
+  const int n = f->n, sw = LIZARD_STRIP;
+  float *strips = malloc((size_t)n * n * sizeof(float));
+  for (int y = 0; y < n; y++) for (int x = 0; x < n; x++) strips[(size_t)(x / sw) * n * sw + (size_t)y * sw + x % sw] = grid[(size_t)y * n + x];
+  lizard_debug(f, 1, 0, 0);
+  memset(&w->hold_reg, 0, sizeof w->hold_reg);
+  w->hold_valid = 1;
+  ob_result_t res;
+  uint8_t *bl = blocks ? blocks : malloc((size_t)f->blocks * LIZARD_BLOCK);
+  uint8_t *okk = ok ? ok : malloc((size_t)f->blocks);
+  const int good = lizard_finish(f, strips, bl, okk, &res);
+  if (coef) memcpy(coef, w->dbg_coef, (size_t)f->subch * LIZARD_SUB * 2 * sizeof(float));
+  if (llrf) memcpy(llrf, w->llrf, (size_t)f->subch * LIZARD_SUB * 2);
+  if (sub_est) memcpy(sub_est, w->sub_est, (size_t)f->subch * sizeof(double));
+  if (sub_rms) memcpy(sub_rms, w->sub_rms, (size_t)f->subch * sizeof(float));
+  if (align) { align[0] = w->align[0]; align[1] = w->align[1]; }
+  if (its) memcpy(its, w->blk_its, (size_t)f->blocks);
+  if (est) memcpy(est, w->blk_est, (size_t)f->blocks * sizeof(float));
+  if (pilot) memcpy(pilot, w->blk_pilot, (size_t)f->blocks * sizeof(float));
+  if (!blocks) free(bl);
+  if (!ok) free(okk);
+  free(strips);
+  return good;
+}
+
+// The whole decode of a luma frame (registration, then the finish), for the end-to-end comparisons. reg_out (any
+// NULL): the registration found, H (9 floats) then the node mesh's (dx, dy) for nx x ny nodes; node_xy: the mesh
+// nodes' module coordinates (nx then ny floats), nn: {nx, ny}.
+int ref_decode_frame(lizard_t *f, const uint8_t *luma, int iw, int ih, uint8_t *blocks, uint8_t *ok, int8_t *its,
+                     float *reg_out, float *node_xy, int32_t *nn) {
+  ob_result_t res;
+  if (!lizard_acquire(f, luma, iw, ih, 1.0f, &res)) { memset(ok, 0, (size_t)f->blocks); return -1; }
+  const struct lizard_ws *w = f->ws;
+  const ob_layout_t *L = &f->frame;
+  if (nn) { nn[0] = L->nx; nn[1] = L->ny; }
+  if (node_xy) { memcpy(node_xy, L->node_x, (size_t)L->nx * sizeof(float)); memcpy(node_xy + L->nx, L->node_y, (size_t)L->ny * sizeof(float)); }
+  if (reg_out) {
+    memcpy(reg_out, w->hold_reg.H.h, 9 * sizeof(float));
+    for (int k = 0; k < L->nx * L->ny; k++) { reg_out[9 + 2 * k] = w->hold_reg.nodes[k].dx; reg_out[10 + 2 * k] = w->hold_reg.nodes[k].dy; }
+  }
+  const int good = lizard_finish(f, 0, blocks, ok, &res);
+  if (its) memcpy(its, w->blk_its, (size_t)f->blocks);
+  return good;
+}
+
+// The picture sampler on a given registration (H, nodes as ref_decode_frame reports them): the exact walk
+// (ob_sample_grid) when fast = 0, the decode's own integer read (ob_sample_grid_pic) when 1; the n x n grid
+// row-major.
+int ref_sample_grid(lizard_t *f, const uint8_t *luma, int iw, int ih, const float *reg, int fast, float *grid) {
+  image_t im;
+  ob_image_init(&im, luma, iw, ih, 1.0f);
+  const ob_layout_t *L = &f->frame;
+  ob_reg_t r;
+  memcpy(r.H.h, reg, 9 * sizeof(float));
+  r.nodes = calloc((size_t)L->nx * L->ny, sizeof(node_t));
+  for (int k = 0; k < L->nx * L->ny; k++) { r.nodes[k].dx = reg[9 + 2 * k]; r.nodes[k].dy = reg[10 + 2 * k]; }
+  const float g0 = f->margin + 0.5f / f->scale, step = 1.0f / f->scale;
+  const int n = f->n;
+  if (fast) ob_sample_grid_pic(L, &im, &r, g0, g0, step, 0, n, 0, n, grid, n);
+  else ob_sample_grid(L, &im, &r, g0, g0, step, 0, n, 0, n, grid, n);
+  free(r.nodes);
   return 0;
 }
