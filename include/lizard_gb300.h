@@ -75,6 +75,19 @@ int lizg_ldpc_plan_run(lizg_ldpc_plan *p, const int8_t *llr, uint8_t *bits, int3
 // Kernel launches the last run made (for the benchmark's launch count).
 int lizg_ldpc_plan_launches(const lizg_ldpc_plan *p);
 
+// No counterpart in the reference: the batch decode for callers that cannot allocate device memory (a plug-in inside
+// a host application that owns the device allocator, a pipeline whose memory is reserved up front). It allocates
+// nothing: its scratch (work lists, offsets, counters) is a fixed array inside the library's device image, sized for
+// LIZG_NOALLOC_MAX_CODEWORDS codewords, held on every GPU that loads the library until the process exits. Inputs
+// and outputs are the caller's device buffers, laid out as the plan's (codewords back to back, offsets from the
+// rates); d_rate holds the count rate indices in device memory; a codeword whose rate has no code gets its = -4.
+// Queued on `stream`. The first call on a device looks up the array's address there; make that first call before
+// any stream capture. Every call shares the one array, so calls whose work overlaps on the GPU (other streams, other
+// host threads) race; serialise them. count above the maximum is refused with LIZG_E_ARG.
+enum { LIZG_NOALLOC_MAX_CODEWORDS = 8192 };
+int lizg_ldpc_decode_noalloc(const int8_t *d_llr, const int32_t *d_rate, int count, int max_iter, int stall_it,
+                             float stall_ratio, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

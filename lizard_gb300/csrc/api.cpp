@@ -48,6 +48,11 @@ int code_k(int code) { return LIZG_CODES[code].kb * LIZG_Z; }
 
 }  // namespace
 
+namespace lizg {
+int device_ready(int *sms) { return device_setup(sms); }
+int record_error(int code, const char *what) { return fail(code, what); }
+}  // namespace lizg
+
 struct lizg_ldpc_plan {
   int count = 0, max_iter = 0, stall_it = 0, launches = 0;
   float ratio = 0;
@@ -190,8 +195,9 @@ int lizg_ldpc_plan_run_dev(lizg_ldpc_plan *p, const int8_t *d_llr, uint8_t *d_bi
     for (int c = 0; c < 4; c++) {   // longest code first: 7/8 has the most codewords
       if (!p->counts[c]) continue;
       if ((e = cudaStreamWaitEvent(p->side[c], p->fork, 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
-      lizg::LdpcLaunch a{d_llr, d_bits, d_its, d_ok, p->d_list + p->list_at[c], p->d_off, p->counts[c], p->d_counter + c,
-                         p->max_iter, p->stall_it, p->ratio};
+      lizg::LdpcLaunch a{};
+      a.llr = d_llr; a.bits = d_bits; a.its = d_its; a.ok = d_ok; a.list = p->d_list + p->list_at[c]; a.off = p->d_off;
+      a.count = p->counts[c]; a.counter = p->d_counter + c; a.max_iter = p->max_iter; a.stall_it = p->stall_it; a.stall_ratio = p->ratio;
       if ((e = lizg::ldpc_launch(c, a, sms, p->side[c])) != cudaSuccess) return fail_cuda(e, "LDPC kernel launch");
       if ((e = cudaEventRecord(p->join[c], p->side[c])) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
       if ((e = cudaStreamWaitEvent(st, p->join[c], 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");

@@ -17,6 +17,8 @@
 #include <stdint.h>
 #include "lizard_codes.h"
 #include "lizg_internal.h"
+#include "lizard_gb300.h"
+#include <mutex>
 
 namespace lizg {
 
@@ -268,12 +270,13 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
   }
   for (int t = threadIdx.x; t < 33; t += blockDim.x) crc_k[t] = c_crc_shift[t];
   __syncthreads();
+  const int count = a.count_dev ? *a.count_dev : a.count;
 
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(a.counter, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= a.count) break;
+    if (item >= count) break;
     int cw, g = 0;
     int64_t off = 0;
     if (a.rx.llrf) {
@@ -427,4 +430,124 @@ cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st)
   return cudaErrorInvalidValue;
 }
 
+// ---------------------------------------------------------------- the decode without allocation
+//
+// For callers that cannot allocate device memory themselves: a driver or plug-in running inside a host that owns
+// the allocator (a capture pipeline that hands out frame buffers from its own pool, a runtime whose device memory is
+// fully reserved up front) may not call cudaMalloc, yet the plan API needs a few device words of scratch (per-code
+// work lists, offsets and counters). Here that scratch is a fixed array in the library's own device image, sized for
+// LIZG_NOALLOC_MAX_CODEWORDS codewords; every GPU that loads the library holds it until the process exits.
+
+constexpr int kNoAllocMax = LIZG_NOALLOC_MAX_CODEWORDS;
+// Layout: counts[4], counters[4], then (from byte 256) the four codes' work lists (kNoAllocMax entries each), then
+// the codewords' LLR offsets.
+constexpr size_t kNaLists = 256, kNaOffs = kNaLists + 4 * sizeof(int32_t) * kNoAllocMax, kNaBytes = kNaOffs + sizeof(int64_t) * kNoAllocMax;
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNaBytes];
+
+__device__ __forceinline__ int code_n_dev(int c) { return c == 0 ? 4608 : c == 1 ? 5120 : c == 2 ? 5760 : c == 3 ? 7680 : 0; }
+
+// One CTA of 1024 threads builds the batch's layout in the scratch: codeword i's LLR offset (the n of every valid
+// codeword before it), the per-code work lists in codeword order, their counts, the work counters at zero. A
+// codeword whose rate index has no code gets its = -4, ok = 0 and no offset share.
+__global__ void __launch_bounds__(1024) ldpc_noalloc_prepare(const int32_t *rate, int count, uint8_t *scr, int32_t *its, uint8_t *ok) {
+  int *counts = reinterpret_cast<int *>(scr);
+  int32_t *lists = reinterpret_cast<int32_t *>(scr + kNaLists);
+  int64_t *offs = reinterpret_cast<int64_t *>(scr + kNaOffs);
+  constexpr int PER = kNoAllocMax / 1024;
+  __shared__ int64_t s_bits[1024];
+  __shared__ int s_cnt[4][1024];
+  const int tid = threadIdx.x, i0 = tid * PER;
+  int code[PER];
+  int64_t bits = 0;
+  int cnt[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const int i = i0 + k;
+    int c = -1;
+    if (i < count) {
+      const int r = rate[i];
+      c = r == 6 ? 0 : r == 4 ? 1 : r == 3 ? 2 : r == 2 ? 3 : -1;
+      if (c < 0) { its[i] = -4; ok[i] = 0; }
+      else { bits += code_n_dev(c); cnt[c]++; }
+    }
+    code[k] = c;
+  }
+  s_bits[tid] = bits;
+  for (int c = 0; c < 4; c++) s_cnt[c][tid] = cnt[c];
+  __syncthreads();
+  // inclusive scans over the threads (Hillis-Steele)
+  for (int d = 1; d < 1024; d <<= 1) {
+    const int64_t vb = tid >= d ? s_bits[tid - d] : 0;
+    int vc[4];
+    for (int c = 0; c < 4; c++) vc[c] = tid >= d ? s_cnt[c][tid - d] : 0;
+    __syncthreads();
+    s_bits[tid] += vb;
+    for (int c = 0; c < 4; c++) s_cnt[c][tid] += vc[c];
+    __syncthreads();
+  }
+  int64_t at = s_bits[tid] - bits;
+  int pos[4];
+  for (int c = 0; c < 4; c++) pos[c] = s_cnt[c][tid] - cnt[c];
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const int i = i0 + k, c = code[k];
+    if (c < 0) continue;
+    offs[i] = at;
+    at += code_n_dev(c);
+    lists[c * kNoAllocMax + pos[c]++] = i;
+  }
+  if (tid == 0) for (int c = 0; c < 4; c++) { counts[c] = s_cnt[c][1023]; counts[4 + c] = 0; }
+}
+
+namespace {
+std::mutex g_na_mu;
+uint8_t *g_na_ptr[64];   // the scratch's device address, per device
+}  // namespace
+
 }  // namespace lizg
+
+extern "C" int lizg_ldpc_decode_noalloc(const int8_t *d_llr, const int32_t *d_rate, int count, int max_iter, int stall_it,
+                                        float stall_ratio, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream) {
+  using namespace lizg;
+  if (!d_llr || !d_rate || !d_bits || !d_its || !d_ok) return record_error(LIZG_E_ARG, "lizg_ldpc_decode_noalloc: NULL argument");
+  if (count < 1 || count > kNoAllocMax)
+    return record_error(LIZG_E_ARG, "lizg_ldpc_decode_noalloc: count must be 1..LIZG_NOALLOC_MAX_CODEWORDS (8192)");
+  if (max_iter < 1 || max_iter > 255 || stall_it < 0 || stall_it == 1 || stall_it > max_iter)
+    return record_error(LIZG_E_ARG, "lizg_ldpc_decode_noalloc: bad max_iter or stall_it");
+  if ((reinterpret_cast<uintptr_t>(d_llr) | reinterpret_cast<uintptr_t>(d_bits)) & 15)
+    return record_error(LIZG_E_ARG, "lizg_ldpc_decode_noalloc: llr and bits must be 16-byte aligned");
+  int sms = 0;
+  if (int rc = device_ready(&sms)) return rc;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) return record_error(LIZG_E_CUDA, "lizg_ldpc_decode_noalloc: cudaGetDevice");
+  uint8_t *scr = nullptr;
+  {
+    // Set-up, once a device with that device current: the scratch array's device address. In host code the
+    // array's name is only a stand-in for it.
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_ptr[dev]) {
+      void *ptr = nullptr;
+      if ((e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch)) != cudaSuccess)
+        return record_error(LIZG_E_CUDA, "lizg_ldpc_decode_noalloc: cudaGetSymbolAddress failed");
+      g_na_ptr[dev] = static_cast<uint8_t *>(ptr);
+    }
+    scr = g_na_ptr[dev];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ldpc_noalloc_prepare<<<1, 1024, 0, st>>>(d_rate, count, scr, d_its, d_ok);
+  if ((e = cudaGetLastError()) != cudaSuccess) return record_error(LIZG_E_CUDA, "lizg_ldpc_decode_noalloc: prepare launch");
+  int *counts = reinterpret_cast<int *>(scr);
+  for (int c = 0; c < 4; c++) {
+    LdpcLaunch a{};
+    a.llr = d_llr; a.bits = d_bits; a.its = d_its; a.ok = d_ok;
+    a.list = reinterpret_cast<const int32_t *>(scr + kNaLists) + c * kNoAllocMax;
+    a.off = reinterpret_cast<const int64_t *>(scr + kNaOffs);
+    a.count = count;                 // bounds the grid; the kernel reads the code's own count from the scratch
+    a.count_dev = counts + c;
+    a.counter = counts + 4 + c;
+    a.max_iter = max_iter; a.stall_it = stall_it; a.stall_ratio = stall_ratio;
+    if ((e = ldpc_launch(c, a, sms, st)) != cudaSuccess) return record_error(LIZG_E_CUDA, "lizg_ldpc_decode_noalloc: decode launch");
+  }
+  return 0;
+}

@@ -40,6 +40,7 @@ struct LdpcLaunch {
   const int32_t *list;    // the codeword indices of this code
   const int64_t *off;     // per codeword LLR offset
   int count;              // entries of list
+  const int *count_dev;   // or, when set, the entries of list as a device word written by an earlier kernel
   int *counter;           // work counter, zero at launch
   int max_iter, stall_it;
   float stall_ratio;
@@ -50,6 +51,11 @@ struct LdpcLaunch {
 };
 
 cudaError_t ldpc_upload_tables();
+// The calling thread's current device made ready (tables uploaded once); its SM count. 0, or a LIZG_E_* code with
+// the message recorded.
+int device_ready(int *sms);
+// Records a failure message for lizg_last_error(); returns code.
+int record_error(int code, const char *what);
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
