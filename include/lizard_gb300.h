@@ -88,6 +88,55 @@ enum { LIZG_NOALLOC_MAX_CODEWORDS = 8192 };
 int lizg_ldpc_decode_noalloc(const int8_t *d_llr, const int32_t *d_rate, int count, int max_iter, int stall_it,
                              float stall_ratio, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream);
 
+// ---------------------------------------------------------------- the receiver (rows a-e)
+//
+// A receiver handle for one format: the picture size n (384, 512, 768, 1024, 1152, 1280, 1536), the sub-channels
+// (a multiple of 16 from 64 to 1024: LIZARD-subch) and the ring's span in modules (128, 256, 512; 0 for 256), with the
+// format's tables on the device and working buffers for up to max_frames frames a call. It is the batched, GPU
+// form of the reference's per-frame codec (lizard_init and lizard_finish / lizard_finish_ext,
+// liblizard/src/lizard_phy.h:177, 230-240).
+typedef struct lizg_rx lizg_rx;
+
+// The format's tables, host code, no device needed (any pointer NULL to skip). info (22 ints): n, subch, span,
+// blocks, used slots, bw, vblocks, tiers, V (spectrum rows kept), pilots, then per tier (up to 4) its rate index,
+// blocks and slots a block. uv: (u, v) of every used coefficient in the reference's pos order (2 x subch x 320);
+// white: the whitening bit of every slot (subch x 640); each block's tier and first slot; erase: the anchors' erase
+// ranges (7 lo then 7 hi); hole_inv: the shading fit's inverse normal matrix (36); detrend: the reference's
+// lizard_tables layout, cx, qx, x1r, x1i, x2r, x2i (n each) then sx2, sq2 (liblizard/src/lizard_phy.h:249,
+// lizard_phy.c:1928-1934); perm: every tier's bit map back to back (block slot -> codeword bit, nt each). Replaces
+// the tables of lizard_init / ws_init (liblizard/src/lizard_phy.c:348-562). Returns 0, or LIZG_E_ARG for no format.
+int lizg_format_tables(int n, int subch, int span, int32_t *info, int16_t *uv, uint8_t *white, int32_t *block_tier,
+                       int32_t *block_slot, int32_t *erase, double *hole_inv, float *detrend, int16_t *perm);
+lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames);
+void lizg_rx_free(lizg_rx *r);
+// info (22 ints): n, subch, span, blocks, used slots, bw, vblocks, tiers, V (spectrum rows kept), pilots, then per
+// tier (up to 4) its rate index, blocks and slots a block.
+int lizg_rx_info(const lizg_rx *r, int32_t *info);
+// Tier t's bit map: block slot i -> codeword bit (nt entries); returns nt.
+int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm);
+// Kernel launches the last finish made.
+int lizg_rx_launches(const lizg_rx *r);
+
+// Per-frame outputs, device pointers, frames x blocks entries each unless noted. Required: blocks (476 bytes a block,
+// the decoded bytes whether or not verified), ok (1 where the CRC-32C verified a decoded block), its (LDPC
+// iterations; -1 never converged, -2 declined, -3 stalled: liblizard/src/lizard_phy.h:186-188). Optional (NULL: kept
+// inside the handle): est (the block's information estimate), pilot (its pilot reading, NaN where none), align
+// (frames x 3: the pilots' grid shift dx, dy and 1 where it was turned back), llrf (frames x subch x 640 soft values,
+// slot order), sub_est (frames x subch doubles), sub_rms (frames x subch).
+typedef struct {
+  uint8_t *blocks, *ok;
+  int32_t *its;
+  float *est, *pilot, *align;
+  int8_t *llrf;
+  double *sub_est;
+  float *sub_rms;
+} lizg_rx_out;
+
+// Rows c-e from spectra: d_coef holds frames x subch x 320 complex floats (re, im), each frame's detrended spectrum at
+// the used coefficients in pos order (what the reference's lizard_debug reads back, liblizard/src/lizard_phy.c:1719).
+// The replacement for lizard_finish_ext's path after the transform (liblizard/src/lizard_phy.c:1720-1871).
+int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const lizg_rx_out *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -152,3 +152,112 @@ def iterations_run(its, rates, max_iter, stall_it):
 def edge_updates(its, rates, max_iter, stall_it):
     e = np.array([CODE_EDGES[int(r)] for r in rates], np.int64)
     return int((iterations_run(its, rates, max_iter, stall_it).astype(np.int64) * e).sum())
+
+
+# ---------------------------------------------------------------- the receiver
+
+SUB = 320
+PICTURES = (384, 512, 768, 1024, 1152, 1280, 1536)
+
+
+def _rx_sigs(L):
+    P, I = ctypes.c_void_p, ctypes.c_int
+    L.lizg_format_tables.argtypes = [I, I, I, P, P, P, P, P, P, P, P, P]
+    L.lizg_rx_new.argtypes = [I, I, I, I]
+    L.lizg_rx_new.restype = P
+    L.lizg_rx_free.argtypes = [P]
+    L.lizg_rx_info.argtypes = [P, P]
+    L.lizg_rx_perm.argtypes = [P, I, P]
+    L.lizg_rx_launches.argtypes = [P]
+    L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
+
+
+class RxOut(ctypes.Structure):
+    """lizg_rx_out: device pointers."""
+    _fields_ = [("blocks", ctypes.c_void_p), ("ok", ctypes.c_void_p), ("its", ctypes.c_void_p), ("est", ctypes.c_void_p),
+                ("pilot", ctypes.c_void_p), ("align", ctypes.c_void_p), ("llrf", ctypes.c_void_p), ("sub_est", ctypes.c_void_p),
+                ("sub_rms", ctypes.c_void_p)]
+
+
+class Format:
+    """A format's host-side tables (lizg_format_tables): no device needed."""
+
+    def __init__(self, n, subch, span=128):
+        L = lib()
+        if not hasattr(L, "_rx"):
+            _rx_sigs(L)
+            L._rx = True
+        info = np.zeros(22, np.int32)
+        _check(L.lizg_format_tables(n, subch, span, _ptr(info), None, None, None, None, None, None, None, None), "lizg_format_tables")
+        self.n, self.subch, self.span, self.blocks, self.used, self.bw, self.vblocks, self.tiers, self.V, self.npilot = (int(x) for x in info[:10])
+        self.tier = [(int(info[10 + 3 * t]), int(info[11 + 3 * t]), int(info[12 + 3 * t])) for t in range(self.tiers)]
+        need = self.subch * SUB
+        self.uv = np.zeros(2 * need, np.int16)
+        self.white = np.zeros(2 * need, np.uint8)
+        self.block_tier = np.zeros(self.blocks, np.int32)
+        self.block_slot = np.zeros(self.blocks, np.int32)
+        self.erase = np.zeros(14, np.int32)
+        self.hole_inv = np.zeros(36, np.float64)
+        self.detrend = np.zeros(6 * self.n + 2, np.float32)
+        nts = [CODE_NT[r] for r, _, _ in self.tier]
+        perm = np.zeros(sum(nts), np.int16)
+        _check(L.lizg_format_tables(n, subch, span, None, _ptr(self.uv), _ptr(self.white), _ptr(self.block_tier), _ptr(self.block_slot),
+                                    _ptr(self.erase), _ptr(self.hole_inv), _ptr(self.detrend), _ptr(perm)), "lizg_format_tables")
+        self.perm = np.split(perm, np.cumsum(nts)[:-1])
+        self.scale = np.float32(n) / np.float32(span)
+
+    def tix(self):
+        u, v = self.uv[0::2].astype(np.int64), self.uv[1::2].astype(np.int64)
+        return v * self.n + (u + self.n) % self.n
+
+
+class Receiver:
+    """A receiver handle (lizg_rx_*) for one format and up to max_frames frames a call."""
+
+    def __init__(self, n, subch, span=128, max_frames=1):
+        self.fmt = Format(n, subch, span)
+        L = lib()
+        h = L.lizg_rx_new(n, subch, span, max_frames)
+        if not h:
+            raise LizgError("lizg_rx_new: " + L.lizg_last_error().decode())
+        self._h = ctypes.c_void_p(h)
+        self.max_frames = max_frames
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lizg_rx_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def launches(self):
+        return int(lib().lizg_rx_launches(self._h))
+
+    def _outputs(self, frames, torch, keep):
+        f = self.fmt
+        o = {"blocks": torch.zeros((frames, f.blocks, BLOCK_BYTES), dtype=torch.uint8, device="cuda"),
+             "ok": torch.zeros((frames, f.blocks), dtype=torch.uint8, device="cuda"),
+             "its": torch.zeros((frames, f.blocks), dtype=torch.int32, device="cuda"),
+             "est": torch.zeros((frames, f.blocks), dtype=torch.float32, device="cuda"),
+             "pilot": torch.zeros((frames, f.blocks), dtype=torch.float32, device="cuda"),
+             "align": torch.zeros((frames, 3), dtype=torch.float32, device="cuda")}
+        if keep:
+            o["llrf"] = torch.zeros((frames, 2 * f.subch * SUB), dtype=torch.int8, device="cuda")
+            o["sub_est"] = torch.zeros((frames, f.subch), dtype=torch.float64, device="cuda")
+            o["sub_rms"] = torch.zeros((frames, f.subch), dtype=torch.float32, device="cuda")
+        s = RxOut(*[o[k].data_ptr() if k in o else None for k in ("blocks", "ok", "its", "est", "pilot", "align", "llrf", "sub_est", "sub_rms")])
+        return o, s
+
+    def finish_coef(self, coef, keep=True, stream=None):
+        """coef: frames x subch x 320 complex64 (or float32 pairs). Returns a dict of numpy arrays."""
+        import torch
+        c = np.ascontiguousarray(np.asarray(coef).view(np.float32) if np.iscomplexobj(coef) else coef, np.float32)
+        frames = c.size // (2 * self.fmt.subch * SUB)
+        d = torch.from_numpy(c.reshape(frames, -1)).cuda()
+        o, s = self._outputs(frames, torch, keep)
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_rx_finish_coef_dev(self._h, ctypes.c_void_p(d.data_ptr()), frames, ctypes.byref(s), ctypes.c_void_p(st)), "lizg_rx_finish_coef_dev")
+        torch.cuda.synchronize()
+        return {k: v.cpu().numpy() for k, v in o.items()}

@@ -1,0 +1,219 @@
+// The receiver plan (include/lizard_gb300.h lizg_rx_*): one format's device tables and a batch's working buffers,
+// and the order the receive kernels run in. Host C++.
+#include "lizard_gb300.h"
+#include "format.h"
+#include "lizg_internal.h"
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+struct lizg_rx {
+  lizg::Format f;
+  int max_frames = 0, device = -1;
+  // device tables
+  int16_t *uv = nullptr, *perm[4] = {nullptr, nullptr, nullptr, nullptr};
+  int32_t *tix = nullptr, *block_tier = nullptr, *block_slot = nullptr, *pilot_coef = nullptr;
+  uint8_t *white = nullptr, *pilot_white = nullptr;
+  float2 *rot = nullptr;
+  // working buffers for max_frames frames
+  int8_t *llrf = nullptr;
+  double *sub_est = nullptr;
+  float *sub_rms = nullptr, *est = nullptr, *pilot = nullptr, *align = nullptr;
+  uint8_t *decl = nullptr;
+  int *counters = nullptr;
+  // per-tier streams, forked from and joined to the caller's
+  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
+  int launches = 0;
+  std::vector<void *> owned;
+};
+
+namespace {
+
+template <class T>
+cudaError_t dev_copy(lizg_rx *r, T **dst, const T *src, size_t count) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * (count ? count : 1));
+  if (e != cudaSuccess) return e;
+  r->owned.push_back(*dst);
+  if (count) e = cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+  return e;
+}
+
+template <class T>
+cudaError_t dev_alloc(lizg_rx *r, T **dst, size_t count) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * (count ? count : 1));
+  if (e == cudaSuccess) r->owned.push_back(*dst);
+  return e;
+}
+
+lizg::FmtDev fmt_dev(const lizg_rx *r, int frames) {
+  lizg::FmtDev d{};
+  const lizg::Format &f = r->f;
+  d.n = f.n; d.subch = f.subch; d.blocks = f.blocks; d.frames = frames; d.npilot = (int)f.pilot_coef.size();
+  d.V = f.vblocks * f.bw;
+  d.turn_scale = (float)lizg::kTurns / (float)f.n;
+  for (int t = 0; t < f.tiers; t++) {
+    d.tier_first[t] = f.tier_first[t]; d.tier_blocks[t] = f.tier[t].blocks; d.tier_slots[t] = f.tier[t].slots;
+    d.tier_nt[t] = f.tier[t].nt; d.tier_k[t] = f.tier[t].k; d.perm[t] = r->perm[t];
+  }
+  d.uv = r->uv; d.tix = r->tix; d.white = r->white; d.block_tier = r->block_tier; d.block_slot = r->block_slot;
+  d.pilot_coef = r->pilot_coef; d.pilot_white = r->pilot_white; d.rot = r->rot;
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
+  if (max_frames < 1 || max_frames > 4096) { lizg::record_error(LIZG_E_ARG, "lizg_rx_new: max_frames must be 1..4096"); return nullptr; }
+  int sms = 0;
+  if (lizg::device_ready(&sms)) return nullptr;
+  lizg_rx *r = new (std::nothrow) lizg_rx;
+  if (!r) { lizg::record_error(LIZG_E_NOMEM, "lizg_rx_new: out of host memory"); return nullptr; }
+  if (lizg::format_build(n, subch, span, r->f)) {
+    lizg::record_error(LIZG_E_ARG, "lizg_rx_new: no format at this (n, subch, span)");
+    delete r;
+    return nullptr;
+  }
+  r->max_frames = max_frames;
+  cudaGetDevice(&r->device);
+  const lizg::Format &f = r->f;
+  const size_t need = (size_t)f.subch * lizg::kSub;
+  std::vector<float2> rot(lizg::kTurns);
+  for (int i = 0; i < lizg::kTurns; i++) {
+    const double th = 2.0 * 3.14159265358979323846 * i / lizg::kTurns;
+    rot[i] = make_float2((float)std::cos(th), (float)std::sin(th));
+  }
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t x) { if (e == cudaSuccess) e = x; return e == cudaSuccess; };
+  ok(dev_copy(r, &r->uv, f.uv.data(), f.uv.size()));
+  ok(dev_copy(r, &r->tix, f.tix.data(), f.tix.size()));
+  ok(dev_copy(r, &r->white, f.white.data(), f.white.size()));
+  for (int t = 0; t < f.tiers; t++) ok(dev_copy(r, &r->perm[t], f.perm[t].data(), f.perm[t].size()));
+  ok(dev_copy(r, &r->block_tier, f.block_tier.data(), f.block_tier.size()));
+  ok(dev_copy(r, &r->block_slot, f.block_slot.data(), f.block_slot.size()));
+  ok(dev_copy(r, &r->pilot_coef, f.pilot_coef.data(), f.pilot_coef.size()));
+  ok(dev_copy(r, &r->pilot_white, f.pilot_white.data(), f.pilot_white.size()));
+  ok(dev_copy(r, &r->rot, rot.data(), rot.size()));
+  const size_t F = (size_t)max_frames;
+  ok(dev_alloc(r, &r->llrf, F * 2 * need));
+  ok(dev_alloc(r, &r->sub_est, F * f.subch));
+  ok(dev_alloc(r, &r->sub_rms, F * f.subch));
+  ok(dev_alloc(r, &r->est, F * f.blocks));
+  ok(dev_alloc(r, &r->pilot, F * f.blocks));
+  ok(dev_alloc(r, &r->align, F * 3));
+  ok(dev_alloc(r, &r->decl, F * f.blocks));
+  ok(dev_alloc(r, &r->counters, 4));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming);
+  for (int t = 0; t < 4 && e == cudaSuccess; t++) {
+    if ((e = cudaStreamCreateWithFlags(&r->side[t], cudaStreamNonBlocking)) == cudaSuccess)
+      e = cudaEventCreateWithFlags(&r->join[t], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_new: ") + cudaGetErrorString(e)).c_str());
+    lizg_rx_free(r);
+    return nullptr;
+  }
+  return r;
+}
+
+void lizg_rx_free(lizg_rx *r) {
+  if (!r) return;
+  for (void *p : r->owned) cudaFree(p);
+  for (int t = 0; t < 4; t++) { if (r->side[t]) cudaStreamDestroy(r->side[t]); if (r->join[t]) cudaEventDestroy(r->join[t]); }
+  if (r->fork) cudaEventDestroy(r->fork);
+  delete r;
+}
+
+int lizg_rx_info(const lizg_rx *r, int32_t *info) {
+  if (!r || !info) return lizg::record_error(LIZG_E_ARG, "lizg_rx_info: NULL argument");
+  const lizg::Format &f = r->f;
+  const int32_t head[10] = {f.n, f.subch, f.span, f.blocks, f.used, f.bw, f.vblocks, f.tiers, f.vblocks * f.bw, (int32_t)f.pilot_coef.size()};
+  std::memcpy(info, head, sizeof head);
+  for (int t = 0; t < 4; t++) {
+    info[10 + 3 * t] = t < f.tiers ? f.tier[t].rate : 0;
+    info[11 + 3 * t] = t < f.tiers ? f.tier[t].blocks : 0;
+    info[12 + 3 * t] = t < f.tiers ? f.tier[t].slots : 0;
+  }
+  return 0;
+}
+
+int lizg_format_tables(int n, int subch, int span, int32_t *info, int16_t *uv, uint8_t *white, int32_t *block_tier,
+                       int32_t *block_slot, int32_t *erase, double *hole_inv, float *detrend, int16_t *perm) {
+  lizg::Format f;
+  if (lizg::format_build(n, subch, span, f)) return lizg::record_error(LIZG_E_ARG, "lizg_format_tables: no format at this (n, subch, span)");
+  if (info) {
+    const int32_t head[10] = {f.n, f.subch, f.span, f.blocks, f.used, f.bw, f.vblocks, f.tiers, f.vblocks * f.bw, (int32_t)f.pilot_coef.size()};
+    std::memcpy(info, head, sizeof head);
+    for (int t = 0; t < 4; t++) {
+      info[10 + 3 * t] = t < f.tiers ? f.tier[t].rate : 0;
+      info[11 + 3 * t] = t < f.tiers ? f.tier[t].blocks : 0;
+      info[12 + 3 * t] = t < f.tiers ? f.tier[t].slots : 0;
+    }
+  }
+  if (uv) std::memcpy(uv, f.uv.data(), f.uv.size() * sizeof(int16_t));
+  if (white) std::memcpy(white, f.white.data(), f.white.size());
+  if (block_tier) std::memcpy(block_tier, f.block_tier.data(), f.block_tier.size() * sizeof(int32_t));
+  if (block_slot) std::memcpy(block_slot, f.block_slot.data(), f.block_slot.size() * sizeof(int32_t));
+  if (erase) for (int i = 0; i < lizg::kAnchK; i++) { erase[i] = f.elo[i]; erase[lizg::kAnchK + i] = f.ehi[i]; }
+  if (hole_inv) std::memcpy(hole_inv, f.hole_inv, sizeof f.hole_inv);
+  if (detrend) {
+    const std::vector<float> *parts[6] = {&f.cx, &f.qx, &f.x1r, &f.x1i, &f.x2r, &f.x2i};
+    for (int k = 0; k < 6; k++) std::memcpy(detrend + (size_t)k * f.n, parts[k]->data(), (size_t)f.n * sizeof(float));
+    detrend[6 * f.n] = (float)f.sx2; detrend[6 * f.n + 1] = (float)f.sq2;
+  }
+  if (perm) for (int t = 0, at = 0; t < f.tiers; at += (int)f.perm[t].size(), t++) std::memcpy(perm + at, f.perm[t].data(), f.perm[t].size() * sizeof(int16_t));
+  return 0;
+}
+
+int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm) {
+  if (!r || !perm || tier < 0 || tier >= r->f.tiers) return lizg::record_error(LIZG_E_ARG, "lizg_rx_perm: bad tier");
+  std::memcpy(perm, r->f.perm[tier].data(), r->f.perm[tier].size() * sizeof(int16_t));
+  return (int)r->f.perm[tier].size();
+}
+
+int lizg_rx_launches(const lizg_rx *r) { return r ? r->launches : LIZG_E_ARG; }
+
+// Rows (c), (d), (e) on a batch of spectra: the pilots' fit, the soft values, the block stage, then the LDPC and
+// CRC of every block not declined, the four codes on their own streams.
+int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const lizg_rx_out *out, void *stream) {
+  if (!r || !d_coef || !out || !out->blocks || !out->ok || !out->its) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_coef_dev: NULL argument");
+  if (frames < 1 || frames > r->max_frames) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_coef_dev: frames out of 1..max_frames");
+  int sms = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  const lizg::Format &f = r->f;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  lizg::FmtDev fd = fmt_dev(r, frames);
+  const int64_t need = (int64_t)f.subch * lizg::kSub;
+  int8_t *llrf = out->llrf ? out->llrf : r->llrf;
+  double *sub_est = out->sub_est ? out->sub_est : r->sub_est;
+  float *sub_rms = out->sub_rms ? out->sub_rms : r->sub_rms;
+  float *est = out->est ? out->est : r->est;
+  float *pilot = out->pilot ? out->pilot : r->pilot;
+  float *align = out->align ? out->align : r->align;
+  cudaError_t e = lizg::demap_launch(fd, reinterpret_cast<const float2 *>(d_coef), need, nullptr, align, llrf, sub_est, sub_rms, est, pilot, r->decl, st);
+  if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("demap: ") + cudaGetErrorString(e)).c_str());
+  r->launches = 3;
+  if ((e = cudaMemsetAsync(r->counters, 0, 4 * sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(r->fork, st)) != cudaSuccess)
+    return lizg::record_error(LIZG_E_CUDA, (std::string("rx fork: ") + cudaGetErrorString(e)).c_str());
+  for (int t = 0; t < f.tiers; t++) {
+    lizg::LdpcLaunch a{};
+    a.its = out->its; a.ok = out->ok;
+    a.count = frames * f.tier[t].blocks; a.counter = r->counters + t;
+    a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // the receiver's (liblizard/src/lizard_phy.c:80-82, 1824)
+    a.rx.llrf = llrf; a.rx.decl = r->decl; a.rx.blocks = out->blocks; a.rx.llr_stride = 2 * need;
+    a.fd = fd; a.tier = t;
+    if ((e = cudaStreamWaitEvent(r->side[t], r->fork, 0)) != cudaSuccess ||
+        (e = lizg::ldpc_launch(f.tier[t].code, a, sms, r->side[t])) != cudaSuccess ||
+        (e = cudaEventRecord(r->join[t], r->side[t])) != cudaSuccess || (e = cudaStreamWaitEvent(st, r->join[t], 0)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_CUDA, (std::string("rx LDPC: ") + cudaGetErrorString(e)).c_str());
+    r->launches++;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -8,7 +8,7 @@ the 7/8 code's never-sent bits fed as known zeros, +127 (liblizard/src/lizard_ph
 """
 import numpy as np
 
-from . import BLOCK_BYTES, CODE_K, CODE_N, CODE_NT, INFO_BITS, crc32c, ldpc_encode_many
+from . import BLOCK_BYTES, CODE_K, CODE_N, CODE_NT, INFO_BITS, SUB, crc32c, ldpc_encode_many
 
 # Rate mix of the batch by count (the format's profile: 39% 7/8, 26% 3/4, 15% 2/3, 20% 1/2) and the Eb/N0 sweep.
 MIX = ((6, 0.39), (4, 0.26), (3, 0.15), (2, 0.20))
@@ -67,3 +67,101 @@ def ldpc_batch(count, seed=0, ebn0_db=EBN0_SWEEP_DB, rates=None):
             llr[off[i]:off[i] + nn] = q[j]
             cws[off[i]:off[i] + nn] = cw[j]
     return {"rates": rates, "offsets": off, "llr": llr, "codewords": cws, "blocks": blk, "ebn0": ebn0}
+
+
+# ---------------------------------------------------------------- pictures and captures
+
+def _block_bits(block_rows):
+    """count x 476 bytes -> count x 3840 bits: the bytes MSB first, then the CRC-32C MSB first."""
+    count = block_rows.shape[0]
+    crc = np.array([crc32c(block_rows[i].tobytes()) for i in range(count)], np.uint32)
+    cb = np.stack([(crc >> 24) & 255, (crc >> 16) & 255, (crc >> 8) & 255, crc & 255], axis=1).astype(np.uint8)
+    return np.unpackbits(np.concatenate([block_rows, cb], axis=1), axis=1)
+
+
+def slots(fmt, block_rows, parity=0):
+    """The frame's subch x 640 slot bits (liblizard/src/lizard_phy.c:1096-1150): each block's codeword through the bit
+    map and the whitening, its tail the pilot bit (bit 0 of the count on an even block, bit 1 on an odd one), the
+    padding the whitening alone."""
+    out = fmt.white.copy()
+    bits = _block_bits(np.asarray(block_rows, np.uint8))
+    for t in range(fmt.tiers):
+        rate = fmt.tier[t][0]
+        idx = np.nonzero(fmt.block_tier == t)[0]
+        data = np.zeros((idx.size, CODE_K[rate]), np.uint8)
+        data[:, :INFO_BITS] = bits[idx]
+        cw = ldpc_encode_many(rate, data)
+        nt, nb = CODE_NT[rate], fmt.tier[t][2]
+        for j, b in enumerate(idx):
+            s0 = int(fmt.block_slot[b])
+            seg = np.empty(nb, np.uint8)
+            seg[:nt] = cw[j][fmt.perm[t]]
+            seg[nt:] = (parity >> (b & 1)) & 1
+            out[s0:s0 + nb] = seg ^ fmt.white[s0:s0 + nb]
+    return out
+
+
+def picture(fmt, block_rows, parity=0, anchors=True):
+    """The n x n picture as grey levels (uint8): Gray QPSK of unit magnitude on the used coefficients, the Hermitian
+    inverse transform, clipped at 2 sqrt(640 subch) and mapped to 0..1 (liblizard/src/lizard_phy.c:1134-1187), the
+    anchors' squares painted over it (liblizard/src/lizard_phy.c:1218-1234), rounded to 8 bits (:700-716). Computed
+    in double; a sender's own rounding differs in the last bits, not in what a receiver reads."""
+    n = fmt.n
+    sb = slots(fmt, block_rows, parity)
+    a = np.float32(0.70710678)
+    sym = np.where(sb[0::2], -a, a).astype(np.float64) + 1j * np.where(sb[1::2], -a, a).astype(np.float64)
+    S = np.zeros((n, n), np.complex128)
+    u, v = fmt.uv[0::2].astype(np.int64), fmt.uv[1::2].astype(np.int64)
+    S[v, (u + n) % n] = sym
+    z = 2.0 * np.real(np.fft.ifft2(S)) * (n * n)      # z[y, x]
+    lim = np.float32(2.0 * 2.0 * np.sqrt(np.float32(0.5 * fmt.subch * SUB)))
+    sc = np.float32(0.5) / lim
+    d = (np.float32(0.5) + np.clip(z.astype(np.float32), -lim, lim) * sc).astype(np.float32)
+    if anchors:
+        span = fmt.span
+        aside = span // 64
+        pxm = n / span
+        for j in range(7):
+            for i in range(7):
+                m0x = int(np.floor(15 + span * (i + 0.5) / 7 - aside / 2.0 + 0.5)) - 15
+                m0y = int(np.floor(15 + span * (j + 0.5) / 7 - aside / 2.0 + 0.5)) - 15
+                side = aside * pxm
+                half = 0.5 * side
+                ys = np.arange(int(m0y * pxm), int(m0y * pxm + side))
+                xs = np.arange(int(m0x * pxm), int(m0x * pxm + side))
+                yy, xx = np.meshgrid(ys - m0y * pxm + 0.5 - half, xs - m0x * pxm + 0.5 - half, indexing="ij")
+                dd = np.maximum(np.abs(xx), np.abs(yy)) / half
+                d[np.ix_(ys, xs)] = np.where((dd < 0.25) | (dd >= 0.6), 1.0, 0.0)
+    return np.clip((d.astype(np.float64) * 255.0 + 0.5).astype(np.int64), 0, 255).astype(np.uint8)
+
+
+def noisy(grey, sigma, rng):
+    """AWGN of sigma grey levels, rounded and clipped to 8 bits."""
+    return np.clip(np.rint(grey.astype(np.float64) + sigma * rng.standard_normal(grey.shape)), 0, 255).astype(np.uint8)
+
+
+def random_blocks(count, seed):
+    b = np.zeros((count, BLOCK_BYTES), np.uint8)
+    b[:, :4] = np.arange(count, dtype="<u4").view(np.uint8).reshape(count, 4)
+    b[:, 4:] = np.random.default_rng(seed).integers(0, 256, (count, BLOCK_BYTES - 4), dtype=np.uint8)
+    return b
+
+
+def grids(fmt, frames, seed=0, sigma=3.0, shift=None):
+    """Config-3-style picture grids: frames x n x n float32 (grey / 255), each a seeded random frame of blocks painted,
+    AWGN of sigma grey levels added. shift=(dx, dy) samples moves every picture by a sub-sample amount (a phase ramp on
+    its spectrum) before quantisation, which the pilots' fit then has to find. Also returns the blocks."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((frames, fmt.n, fmt.n), np.float32)
+    blocks = []
+    for f in range(frames):
+        b = random_blocks(fmt.blocks, seed * 1000 + f)
+        g = picture(fmt, b, parity=f & 3).astype(np.float64)
+        if shift is not None:
+            n = fmt.n
+            k = np.fft.fftfreq(n) * n
+            ramp = np.exp(-2j * np.pi * (k[None, :] * shift[0] + k[:, None] * shift[1]) / n)
+            g = np.real(np.fft.ifft2(np.fft.fft2(g) * ramp))
+        out[f] = noisy(g, sigma, rng).astype(np.float32) / np.float32(255.0)
+        blocks.append(b)
+    return out, blocks

@@ -1,0 +1,60 @@
+"""Rows c-e on the GPU (pilot fit, soft demap, block stage, LDPC, CRC) through the C ABI: held bit for bit to the
+reference's own outputs (tests/golden/rx_ref.npz) and to the oracle on synthetic frames of every picture size."""
+import os
+
+import numpy as np
+import pytest
+
+import lizard_gb300 as lz
+import oracle
+from lizard_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def check(out, want, frame=0):
+    assert np.array_equal(out["align"][frame][:2], want["align"])
+    assert np.array_equal(out["llrf"][frame], want["llrf"])
+    assert np.array_equal(out["sub_rms"][frame], want["sub_rms"])
+    np.testing.assert_allclose(out["sub_est"][frame], want["sub_est"], rtol=1e-13)
+    assert np.array_equal(out["its"][frame], want["its"].astype(np.int32))
+    assert np.array_equal(out["ok"][frame], want["ok"])
+    np.testing.assert_allclose(out["est"][frame], want["est"], rtol=1e-6)
+    assert np.array_equal(out["pilot"][frame], want["pilot"], equal_nan=True)
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_finish_coef_matches_reference_golden(tag):
+    g = np.load(os.path.join(GOLD, "rx_ref.npz"))
+    n, subch, span = (int(x) for x in g[tag + "_fmt"])
+    rx = lz.Receiver(n, subch, span, max_frames=1)
+    out = rx.finish_coef(g[tag + "_coef"][None])
+    check(out, {k: g[tag + "_" + k] for k in ("align", "llrf", "sub_rms", "sub_est", "its", "ok", "est", "pilot")})
+    ok = out["ok"][0].astype(bool)
+    assert ok.all()
+    assert np.array_equal(out["blocks"][0], g[tag + "_blocks"])
+
+
+def oracle_frames(fmt, frames, seed, shift=None, sigma=3.0):
+    o = oracle.Fmt(fmt.n, fmt.subch, fmt.span)
+    grids, blocks = synth.grids(fmt, frames, seed=seed, sigma=sigma, shift=shift)
+    res = [o.receive(grids[f]) for f in range(frames)]
+    return grids, blocks, res
+
+
+@pytest.mark.parametrize("n,subch,frames,shift,sigma", [(384, 64, 3, None, 3.0), (512, 256, 2, (0.2, 0.1), 3.0),
+                                                        (768, 320, 2, None, 12.0), (1024, 1024, 1, (-0.15, 0.3), 3.0),
+                                                        (1152, 720, 1, None, 3.0), (1280, 880, 1, None, 3.0),
+                                                        (1536, 1024, 2, (0.3, -0.25), 3.0)])
+def test_finish_coef_matches_oracle(n, subch, frames, shift, sigma):
+    fmt = lz.Format(n, subch, 128)
+    _, blocks, res = oracle_frames(fmt, frames, seed=n + frames, shift=shift, sigma=sigma)
+    rx = lz.Receiver(n, subch, 128, max_frames=frames)
+    out = rx.finish_coef(np.stack([r["coef"] for r in res]))
+    for f in range(frames):
+        check(out, {"align": res[f]["align"], "llrf": res[f]["llrf"], "sub_rms": res[f]["sub_rms"], "sub_est": res[f]["sub_est"],
+                    "its": res[f]["its"], "ok": res[f]["ok"], "est": res[f]["est"], "pilot": res[f]["pilot"]}, f)
+        ok = out["ok"][f].astype(bool)
+        assert np.array_equal(out["blocks"][f][ok], blocks[f][ok])
+    assert rx.launches == 3 + fmt.tiers
