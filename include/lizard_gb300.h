@@ -109,9 +109,12 @@ int lizg_format_tables(int n, int subch, int span, int32_t *info, int16_t *uv, u
                        int32_t *block_slot, int32_t *erase, double *hole_inv, float *detrend, int16_t *perm);
 lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames);
 void lizg_rx_free(lizg_rx *r);
-// info (22 ints): n, subch, span, blocks, used slots, bw, vblocks, tiers, V (spectrum rows kept), pilots, then per
-// tier (up to 4) its rate index, blocks and slots a block.
+// info (24 ints): n, subch, span, blocks, used slots, bw, vblocks, tiers, V (spectrum rows kept), pilots, then per
+// tier (up to 4) its rate index, blocks and slots a block, then the registration mesh's nx, ny.
 int lizg_rx_info(const lizg_rx *r, int32_t *info);
+// The registration mesh's node centres in module coordinates for a ring of span modules (the layout is span + 30
+// modules square, liblizard/src/layout.c:110-117): nn = {nx, ny}; returns nx. Host code.
+int lizg_layout_nodes(int span, float *node_x, float *node_y, int32_t *nn);
 // Tier t's bit map: block slot i -> codeword bit (nt entries); returns nt.
 int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm);
 // Kernel launches the last finish made.
@@ -136,6 +139,22 @@ typedef struct {
 // the used coefficients in pos order (what the reference's lizard_debug reads back, liblizard/src/lizard_phy.c:1719).
 // The replacement for lizard_finish_ext's path after the transform (liblizard/src/lizard_phy.c:1720-1871).
 int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const lizg_rx_out *out, void *stream);
+// Rows b-e from picture grids: d_grid holds frames x n x n floats (row y, column x; grey / 255), each frame's picture
+// sampled at its n x n grid. The anchors' squares are erased to the shading surface, the detrend projections taken,
+// the 2D FFT made and the surface's spectrum subtracted (liblizard/src/lizard_phy.c:1596-1716), then as
+// lizg_rx_finish_coef_dev. d_coef (optional, NULL to skip) receives each frame's spectrum at the used coefficients
+// (frames x subch x 320 complex floats, pos order). The replacement for lizard_finish(f, grid, ...)
+// (liblizard/src/lizard_phy.h:236). d_grid is not modified.
+int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const lizg_rx_out *out, float *d_coef, void *stream);
+// Rows a-e from captured frames: d_luma holds frames 8-bit luma images (w x h, rows pitch bytes apart, frames
+// frame_stride bytes apart); d_reg holds each frame's registration, 9 + 2 nx ny floats: the homography H (module
+// coordinates to image pixels, h[8] = 1, liblizard/src/internal.h:105-112) then the node mesh's (dx, dy) pixel
+// displacements row by row (liblizard/src/internal.h:123-124, what the reference's acquisition leaves held). Each
+// frame's picture is sampled on its n x n grid (liblizard/src/acquire.c:5121-5196), then as lizg_rx_finish_grid_dev.
+// d_grid (optional) receives the sampled grids (frames x n x n). The replacement for lizard_finish(f, NULL, ...) on
+// a held registration (liblizard/src/lizard_phy.c:1566-1871).
+int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
+                            int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
 
 #ifdef __cplusplus
 }

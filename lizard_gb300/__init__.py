@@ -170,6 +170,8 @@ def _rx_sigs(L):
     L.lizg_rx_perm.argtypes = [P, I, P]
     L.lizg_rx_launches.argtypes = [P]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
+    L.lizg_rx_finish_grid_dev.argtypes = [P, P, I, P, P, P]
+    L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
 
 
 class RxOut(ctypes.Structure):
@@ -261,3 +263,42 @@ class Receiver:
         _check(lib().lizg_rx_finish_coef_dev(self._h, ctypes.c_void_p(d.data_ptr()), frames, ctypes.byref(s), ctypes.c_void_p(st)), "lizg_rx_finish_coef_dev")
         torch.cuda.synchronize()
         return {k: v.cpu().numpy() for k, v in o.items()}
+
+    def finish_grid(self, grids, keep=True, coef=True, stream=None):
+        """grids: frames x n x n float32 (grey / 255). Returns a dict of numpy arrays (coef: frames x subch*320 complex64)."""
+        import torch
+        g = np.ascontiguousarray(grids, np.float32)
+        frames = g.shape[0]
+        d = torch.from_numpy(g).cuda()
+        o, s = self._outputs(frames, torch, keep)
+        c = torch.zeros((frames, 2 * self.fmt.subch * SUB), dtype=torch.float32, device="cuda") if coef else None
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_rx_finish_grid_dev(self._h, ctypes.c_void_p(d.data_ptr()), frames, ctypes.byref(s),
+                                              ctypes.c_void_p(c.data_ptr()) if coef else None, ctypes.c_void_p(st)), "lizg_rx_finish_grid_dev")
+        torch.cuda.synchronize()
+        out = {k: v.cpu().numpy() for k, v in o.items()}
+        if coef:
+            out["coef"] = c.cpu().numpy()
+        return out
+
+    def finish_luma(self, luma, reg, keep=True, stream=None):
+        """luma: frames x h x w uint8; reg: frames x (9 + 2 nx ny) float32 (H then the node mesh). Returns a dict of
+        numpy arrays including the sampled grids and the spectra."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        frames, h, w = lu.shape
+        d = torch.from_numpy(lu).cuda()
+        dr = torch.from_numpy(np.ascontiguousarray(reg, np.float32)).cuda()
+        o, s = self._outputs(frames, torch, keep)
+        n = self.fmt.n
+        grid = torch.zeros((frames, n, n), dtype=torch.float32, device="cuda")
+        c = torch.zeros((frames, 2 * self.fmt.subch * SUB), dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_rx_finish_luma_dev(self._h, ctypes.c_void_p(d.data_ptr()), w, h, w, h * w, ctypes.c_void_p(dr.data_ptr()), frames,
+                                              ctypes.byref(s), ctypes.c_void_p(grid.data_ptr()), ctypes.c_void_p(c.data_ptr()), ctypes.c_void_p(st)),
+               "lizg_rx_finish_luma_dev")
+        torch.cuda.synchronize()
+        out = {k: v.cpu().numpy() for k, v in o.items()}
+        out["grid"] = grid.cpu().numpy()
+        out["coef"] = c.cpu().numpy()
+        return out

@@ -102,6 +102,7 @@ int format_build(int n, int subch, int span, Format &f) {
   int vmax = 0;
   for (int i = 0; i < need; i++) vmax = std::max(vmax, all[i].v);
   f.vblocks = vmax / f.bw + 1;
+  f.vmax = vmax;
   f.uv.resize(2 * (size_t)need);
   f.tix.resize(need);
   for (int i = 0; i < need; i++) {
@@ -195,6 +196,16 @@ int format_build(int n, int subch, int span, Format &f) {
   }
   for (int r = 0; r < 6; r++) for (int c = 0; c < 6; c++) f.hole_inv[r][c] = g[r][6 + c];
   return 0;
+}
+
+// The registration mesh's node centres along one axis of a square layout of `side` modules (liblizard/src/layout.c:
+// 110-117): every 16 modules from the border's centre line at 3.5, the last one 3.5 from the far edge, at most 40.
+int layout_nodes(int side, float *pos) {
+  const float line = 3.5f;
+  int cnt = 0;
+  for (float c = line; c < side - line - 16 / 2 && cnt < 40 - 1; c += 16) pos[cnt++] = c;
+  pos[cnt++] = side - line;
+  return cnt;
 }
 
 }  // namespace lizg

@@ -12,7 +12,7 @@ enum { kSub = 320, kStrip = 64, kAnchK = 7, kAnchMargin = 2, kMargin = 15, kTurn
 struct Tier { int rate, blocks, slots, code, nt, k, np; };
 
 struct Format {
-  int n = 0, subch = 0, span = 0, blocks = 0, used = 0, bw = 0, vblocks = 0, tiers = 0;
+  int n = 0, subch = 0, span = 0, blocks = 0, used = 0, bw = 0, vblocks = 0, tiers = 0, vmax = 0;
   float scale = 0;                // picture samples a module, n / span
   Tier tier[kMaxTiers] = {};
   int tier_first[kMaxTiers] = {};  // first block of each tier (blocks of a tier are contiguous)
@@ -36,6 +36,8 @@ int tiers_for(int subch, Tier *out);
 int format_build(int n, int subch, int span, Format &f);
 // The slots a block of a rate index takes (its code's sent bits, then 16 pilots at 7/8, 32 at 3/4).
 int block_slots(int rate);
+// The registration mesh's node centres along an axis of a layout of `side` modules; returns their count.
+int layout_nodes(int side, float *pos);
 
 }  // namespace lizg
 #endif

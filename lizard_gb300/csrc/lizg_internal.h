@@ -23,6 +23,24 @@ struct FmtDev {
   const float2 *rot;                 // cos, sin of 2 pi k / 4096
 };
 
+// A format's transform tables (row b), passed by value to the transform kernels.
+struct FftDev {
+  int n, nstages, radix[8], vrows;   // the Stockham passes' radices; rows v kept (the used coefficients' v <= vrows - 1)
+  const float2 *tw;                  // e^{-2 pi i t / n}, t < n
+  const float *cx, *qx;              // detrend basis
+  const float2 *x1, *x2;             // their DFTs
+  double sx2, sq2;
+  int elo[7], ehi[7];                // anchors' erase ranges
+  double hole_inv[36];
+};
+
+// The sampler's format-side inputs (row a): picture size, grid origin and step in modules, the node lattice.
+struct SampleDev {
+  int n, nx, ny;
+  float g0, step;                    // margin + 0.5 / scale, 1 / scale (floats, as the reference computes them)
+  const float *node_x, *node_y;      // node centres' module coordinates
+};
+
 // The receiver's per-batch soft-value and block state, in device memory.
 struct RxState {
   const int8_t *llrf;     // frames x subch x 640 soft values, slot order
@@ -58,6 +76,13 @@ int device_ready(int *sms);
 int record_error(int code, const char *what);
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
+cudaError_t fft_launch(const FftDev &xd, int frames, const float *grid, int64_t stride, double *beta, double *colsum,
+                       float2 *Y, float2 *T, cudaStream_t st);
+cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, int w, int h, int pitch, int64_t fstride,
+                          const float *reg, int regstride, float *grid, cudaStream_t st);
+// The node lattice of a layout of side modules (liblizard/src/layout.c:110-117): returns nx (= ny).
+int layout_nodes(int side, float *pos);
+cudaError_t gather_coef_launch(const float2 *T, int64_t tstride, const int32_t *tix, int need, int frames, float2 *coef, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
 

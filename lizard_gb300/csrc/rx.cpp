@@ -18,12 +18,21 @@ struct lizg_rx {
   int32_t *tix = nullptr, *block_tier = nullptr, *block_slot = nullptr, *pilot_coef = nullptr;
   uint8_t *white = nullptr, *pilot_white = nullptr;
   float2 *rot = nullptr;
+  // transform tables
+  lizg::FftDev xd{};
+  float2 *tw = nullptr, *x1 = nullptr, *x2 = nullptr;
+  float *cx = nullptr, *qx = nullptr;
   // working buffers for max_frames frames
   int8_t *llrf = nullptr;
   double *sub_est = nullptr;
   float *sub_rms = nullptr, *est = nullptr, *pilot = nullptr, *align = nullptr;
   uint8_t *decl = nullptr;
   int *counters = nullptr;
+  double *beta = nullptr, *colsum = nullptr;
+  float *grid = nullptr;              // sampled pictures (luma input)
+  lizg::SampleDev sd{};
+  float *node_xy = nullptr;
+  float2 *Y = nullptr, *T = nullptr;
   // per-tier streams, forked from and joined to the caller's
   cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -99,7 +108,46 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   ok(dev_copy(r, &r->pilot_coef, f.pilot_coef.data(), f.pilot_coef.size()));
   ok(dev_copy(r, &r->pilot_white, f.pilot_white.data(), f.pilot_white.size()));
   ok(dev_copy(r, &r->rot, rot.data(), rot.size()));
+  // the transform's plan and tables: radix-4 passes, then 2, 3 and 5; twiddles and the detrend's DFTs in double
+  {
+    lizg::FftDev &xd = r->xd;
+    xd.n = n; xd.vrows = f.vmax + 1; xd.nstages = 0;
+    int m = n;
+    while (m % 4 == 0) { xd.radix[xd.nstages++] = 4; m /= 4; }
+    while (m % 2 == 0) { xd.radix[xd.nstages++] = 2; m /= 2; }
+    while (m % 3 == 0) { xd.radix[xd.nstages++] = 3; m /= 3; }
+    while (m % 5 == 0) { xd.radix[xd.nstages++] = 5; m /= 5; }
+    std::vector<float2> tw(n), x1(n), x2(n);
+    for (int t = 0; t < n; t++) {
+      const double th = -2.0 * 3.14159265358979323846 * t / n;
+      tw[t] = make_float2((float)std::cos(th), (float)std::sin(th));
+      x1[t] = make_float2(f.x1r[t], f.x1i[t]); x2[t] = make_float2(f.x2r[t], f.x2i[t]);
+    }
+    ok(dev_copy(r, &r->tw, tw.data(), tw.size()));
+    ok(dev_copy(r, &r->x1, x1.data(), x1.size()));
+    ok(dev_copy(r, &r->x2, x2.data(), x2.size()));
+    ok(dev_copy(r, &r->cx, f.cx.data(), f.cx.size()));
+    ok(dev_copy(r, &r->qx, f.qx.data(), f.qx.size()));
+    xd.tw = r->tw; xd.x1 = r->x1; xd.x2 = r->x2; xd.cx = r->cx; xd.qx = r->qx; xd.sx2 = f.sx2; xd.sq2 = f.sq2;
+    for (int i = 0; i < lizg::kAnchK; i++) { xd.elo[i] = f.elo[i]; xd.ehi[i] = f.ehi[i]; }
+    for (int i = 0; i < 36; i++) xd.hole_inv[i] = f.hole_inv[i / 6][i % 6];
+  }
+  {
+    float nodes[40];
+    const int nn = lizg::layout_nodes(f.span + 2 * lizg::kMargin, nodes);
+    std::vector<float> nxy(nodes, nodes + nn);
+    nxy.insert(nxy.end(), nodes, nodes + nn);
+    ok(dev_copy(r, &r->node_xy, nxy.data(), nxy.size()));
+    r->sd.n = n; r->sd.nx = nn; r->sd.ny = nn;
+    r->sd.g0 = lizg::kMargin + 0.5f / f.scale; r->sd.step = 1.0f / f.scale;
+    r->sd.node_x = r->node_xy; r->sd.node_y = r->node_xy + nn;
+  }
   const size_t F = (size_t)max_frames;
+  ok(dev_alloc(r, &r->grid, F * n * n));
+  ok(dev_alloc(r, &r->beta, F * 6));
+  ok(dev_alloc(r, &r->colsum, F * n * 3));
+  ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
+  ok(dev_alloc(r, &r->T, F * (size_t)r->xd.vrows * n));
   ok(dev_alloc(r, &r->llrf, F * 2 * need));
   ok(dev_alloc(r, &r->sub_est, F * f.subch));
   ok(dev_alloc(r, &r->sub_rms, F * f.subch));
@@ -139,7 +187,18 @@ int lizg_rx_info(const lizg_rx *r, int32_t *info) {
     info[11 + 3 * t] = t < f.tiers ? f.tier[t].blocks : 0;
     info[12 + 3 * t] = t < f.tiers ? f.tier[t].slots : 0;
   }
+  info[22] = r->sd.nx; info[23] = r->sd.ny;
   return 0;
+}
+
+int lizg_layout_nodes(int span, float *node_x, float *node_y, int32_t *nn) {
+  if (span != 128 && span != 256 && span != 512) return lizg::record_error(LIZG_E_ARG, "lizg_layout_nodes: span must be 128, 256 or 512");
+  float p[40];
+  const int k = lizg::layout_nodes(span + 2 * lizg::kMargin, p);
+  if (node_x) std::memcpy(node_x, p, (size_t)k * sizeof(float));
+  if (node_y) std::memcpy(node_y, p, (size_t)k * sizeof(float));
+  if (nn) { nn[0] = k; nn[1] = k; }
+  return k;
 }
 
 int lizg_format_tables(int n, int subch, int span, int32_t *info, int16_t *uv, uint8_t *white, int32_t *block_tier,
@@ -178,15 +237,11 @@ int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm) {
 
 int lizg_rx_launches(const lizg_rx *r) { return r ? r->launches : LIZG_E_ARG; }
 
-// Rows (c), (d), (e) on a batch of spectra: the pilots' fit, the soft values, the block stage, then the LDPC and
-// CRC of every block not declined, the four codes on their own streams.
-int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const lizg_rx_out *out, void *stream) {
-  if (!r || !d_coef || !out || !out->blocks || !out->ok || !out->its) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_coef_dev: NULL argument");
-  if (frames < 1 || frames > r->max_frames) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_coef_dev: frames out of 1..max_frames");
-  int sms = 0;
-  if (int rc = lizg::device_ready(&sms)) return rc;
+// Rows (c), (d), (e) on a batch of spectra (spec: frame f's coefficient i at spec[f stride + (idx ? idx[i] : i)]):
+// the pilots' fit, the soft values, the block stage, then the LDPC and CRC of every block not declined, the four
+// codes on their own streams.
+static int finish_spec(lizg_rx *r, const float2 *spec, int64_t stride, const int32_t *idx, int frames, const lizg_rx_out *out, cudaStream_t st, int sms) {
   const lizg::Format &f = r->f;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   lizg::FmtDev fd = fmt_dev(r, frames);
   const int64_t need = (int64_t)f.subch * lizg::kSub;
   int8_t *llrf = out->llrf ? out->llrf : r->llrf;
@@ -195,9 +250,9 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
   float *est = out->est ? out->est : r->est;
   float *pilot = out->pilot ? out->pilot : r->pilot;
   float *align = out->align ? out->align : r->align;
-  cudaError_t e = lizg::demap_launch(fd, reinterpret_cast<const float2 *>(d_coef), need, nullptr, align, llrf, sub_est, sub_rms, est, pilot, r->decl, st);
+  cudaError_t e = lizg::demap_launch(fd, spec, stride, idx, align, llrf, sub_est, sub_rms, est, pilot, r->decl, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("demap: ") + cudaGetErrorString(e)).c_str());
-  r->launches = 3;
+  r->launches += 3;
   if ((e = cudaMemsetAsync(r->counters, 0, 4 * sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(r->fork, st)) != cudaSuccess)
     return lizg::record_error(LIZG_E_CUDA, (std::string("rx fork: ") + cudaGetErrorString(e)).c_str());
   for (int t = 0; t < f.tiers; t++) {
@@ -214,6 +269,53 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
     r->launches++;
   }
   return 0;
+}
+
+static int check_call(lizg_rx *r, const void *in, int frames, const lizg_rx_out *out, const char *who, int *sms) {
+  if (!r || !in || !out || !out->blocks || !out->ok || !out->its) return lizg::record_error(LIZG_E_ARG, (std::string(who) + ": NULL argument").c_str());
+  if (frames < 1 || frames > r->max_frames) return lizg::record_error(LIZG_E_ARG, (std::string(who) + ": frames out of 1..max_frames").c_str());
+  return lizg::device_ready(sms);
+}
+
+int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const lizg_rx_out *out, void *stream) {
+  int sms = 0;
+  if (int rc = check_call(r, d_coef, frames, out, "lizg_rx_finish_coef_dev", &sms)) return rc;
+  r->launches = 0;
+  return finish_spec(r, reinterpret_cast<const float2 *>(d_coef), (int64_t)r->f.subch * lizg::kSub, nullptr, frames, out, static_cast<cudaStream_t>(stream), sms);
+}
+
+// Rows (b) to (e) on a batch of picture grids: the anchors' erase and the detrended 2D transform, then as above.
+int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const lizg_rx_out *out, float *d_coef, void *stream) {
+  int sms = 0;
+  if (int rc = check_call(r, d_grid, frames, out, "lizg_rx_finish_grid_dev", &sms)) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int n = r->f.n;
+  const int64_t tstride = (int64_t)r->xd.vrows * n;
+  cudaError_t e = lizg::fft_launch(r->xd, frames, d_grid, (int64_t)n * n, r->beta, r->colsum, r->Y, r->T, st);
+  if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
+  r->launches = 3;
+  if (d_coef) {
+    if ((e = lizg::gather_coef_launch(r->T, tstride, r->tix, r->f.subch * lizg::kSub, frames, reinterpret_cast<float2 *>(d_coef), st)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_CUDA, (std::string("gather: ") + cudaGetErrorString(e)).c_str());
+    r->launches++;
+  }
+  return finish_spec(r, r->T, tstride, r->tix, frames, out, st, sms);
+}
+
+// Rows (a) to (e) on a batch of captured luma frames, each with its registration (H, then the node mesh).
+int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
+                            int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream) {
+  int sms = 0;
+  if (int rc = check_call(r, d_luma, frames, out, "lizg_rx_finish_luma_dev", &sms)) return rc;
+  if (!d_reg || w < 2 || h < 2 || pitch < w || frame_stride < (int64_t)pitch * h)
+    return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_luma_dev: bad frame geometry or NULL registration");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  float *grid = d_grid ? d_grid : r->grid;
+  cudaError_t e = lizg::sample_launch(r->sd, frames, d_luma, w, h, pitch, frame_stride, d_reg, 9 + 2 * r->sd.nx * r->sd.ny, grid, st);
+  if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("sampler: ") + cudaGetErrorString(e)).c_str());
+  const int rc = lizg_rx_finish_grid_dev(r, grid, frames, out, d_coef, stream);
+  r->launches += 1;
+  return rc;
 }
 
 }  // extern "C"

@@ -165,3 +165,67 @@ def grids(fmt, frames, seed=0, sigma=3.0, shift=None):
         out[f] = noisy(g, sigma, rng).astype(np.float32) / np.float32(255.0)
         blocks.append(b)
     return out, blocks
+
+
+def layout_nodes(span):
+    """The registration mesh's node centres (module coordinates) of a ring of span modules."""
+    from . import lib, _ptr
+    import ctypes
+    nx = np.zeros(40, np.float32)
+    nn = np.zeros(2, np.int32)
+    lib().lizg_layout_nodes.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    k = lib().lizg_layout_nodes(span, _ptr(nx), None, _ptr(nn))
+    return nx[:k].copy()
+
+
+def capture(fmt, grey, width=1280, height=720, H=None, sigma=2.0, rng=None, mid=128):
+    """A captured luma frame holding the picture: the n x n grey picture at exact-copy scale (one pixel a sample;
+    pxm = n / span pixels a module) inside its layout (light border, not read by the receiver), mapped into a
+    width x height frame of mid-grey by the homography H (module coordinates to image pixels; None: axis-aligned and
+    centred), bilinear in the picture's pixels, AWGN of sigma grey levels. Returns (luma uint8, registration floats:
+    H then a zero node mesh)."""
+    n, span = fmt.n, fmt.span
+    pxm = n / span
+    side = span + 30
+    px = int(round(side * pxm))
+    drive = np.full((px, px), 255.0)
+    o = int(round(15 * pxm))
+    drive[o:o + n, o:o + n] = grey
+    if H is None:
+        ox, oy = (width - px) // 2, (height - px) // 2
+        H = np.array([pxm, 0, ox, 0, pxm, oy, 0, 0, 1], np.float64)
+    Hm = np.asarray(H, np.float64).reshape(3, 3)
+    Hi = np.linalg.inv(Hm)
+    V, U = np.mgrid[0:height, 0:width].astype(np.float64)
+    q = Hi @ np.stack([U.ravel() + 0.5, V.ravel() + 0.5, np.ones(U.size)])
+    mx, my = q[0] / q[2], q[1] / q[2]
+    # drive pixel coordinates, centres at half-integers
+    sx, sy = mx * pxm - 0.5, my * pxm - 0.5
+    inside = (sx >= 0) & (sy >= 0) & (sx <= px - 1.001) & (sy <= px - 1.001)
+    x0 = np.clip(np.floor(sx).astype(np.int64), 0, px - 2)
+    y0 = np.clip(np.floor(sy).astype(np.int64), 0, px - 2)
+    fx, fy = np.clip(sx - x0, 0, 1), np.clip(sy - y0, 0, 1)
+    val = (drive[y0, x0] * (1 - fx) + drive[y0, x0 + 1] * fx) * (1 - fy) + (drive[y0 + 1, x0] * (1 - fx) + drive[y0 + 1, x0 + 1] * fx) * fy
+    img = np.where(inside, val, float(mid)).reshape(height, width)
+    rng = np.random.default_rng(0) if rng is None else rng
+    luma = np.clip(np.rint(img + sigma * rng.standard_normal(img.shape)), 0, 255).astype(np.uint8)
+    nn = layout_nodes(span).size
+    reg = np.concatenate([np.asarray(H, np.float32).ravel() / np.float32(np.asarray(H).ravel()[8]), np.zeros(2 * nn * nn, np.float32)])
+    return luma, reg
+
+
+def warp(fmt, width, height, rng, rot_deg=15.0, tilt=0.0002, scale=(0.9, 1.05)):
+    """A random homography (module -> image): rotation, a little perspective and scale about the frame centre, the
+    picture at exact-copy pixels a module times the scale."""
+    pxm = fmt.n / fmt.span
+    side = fmt.span + 30
+    th = np.deg2rad(rng.uniform(-rot_deg, rot_deg))
+    s = pxm * rng.uniform(*scale)
+    c, si = np.cos(th), np.sin(th)
+    # centre the layout's middle on the frame centre
+    A = np.array([[s * c, -s * si, 0], [s * si, s * c, 0], [0, 0, 1]])
+    T0 = np.array([[1, 0, -side / 2], [0, 1, -side / 2], [0, 0, 1]])
+    P = np.array([[1, 0, 0], [0, 1, 0], [rng.uniform(-tilt, tilt), rng.uniform(-tilt, tilt), 1]])
+    T1 = np.array([[1, 0, width / 2], [0, 1, height / 2], [0, 0, 1]])
+    H = T1 @ P @ A @ T0
+    return (H / H[2, 2]).ravel()

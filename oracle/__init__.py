@@ -140,6 +140,8 @@ def _phy_sigs(L):
     L.orc_pilot_align.argtypes = [P, P, P]
     L.orc_demap.argtypes = [P, P, P, P, P, P]
     L.orc_blocks.argtypes = [P, P, P, P, P, P, I, P, P, P, P, P]
+    L.orc_layout_nodes.argtypes = [I, P]
+    L.orc_sample_grid.argtypes = [I, I, P, I, I, I, P, P]
 
 
 class Fmt:
@@ -215,6 +217,14 @@ class Fmt:
                           _p(np.ascontiguousarray(rms, np.float32)), _p(c), None if t is None else _p(t), max_iter,
                           _p(blocks), _p(ok), _p(its), _p(best), _p(pil))
         return {"blocks": blocks, "ok": ok, "its": its, "est": best, "pilot": pil}
+
+    def sample(self, luma, reg):
+        """The picture grid (n x n float32) of a luma frame through a registration (H then the mesh)."""
+        luma = np.ascontiguousarray(luma, np.uint8)
+        h, w = luma.shape
+        g = np.zeros(self.n * self.n, np.float32)
+        self.L.orc_sample_grid(self.n, self.span, _p(luma), w, h, w, _p(np.ascontiguousarray(reg, np.float32)), _p(g))
+        return g.reshape(self.n, self.n)
 
     def receive(self, grid, fp64_spectrum=True):
         """The whole finish on a grid: spectrum (FP64, narrowed to float), pilots, soft values, blocks."""

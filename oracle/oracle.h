@@ -59,6 +59,10 @@ int orc_demap(const orc_fmt_t *f, const float *coef, const float *turn, int8_t *
 int orc_blocks(const orc_fmt_t *f, const int8_t *llrf, const double *sub_est, const float *sub_rms, const float *coef,
                const float *turn, int max_iter, uint8_t *blocks, uint8_t *ok, int8_t *its, float *est, float *pilot);
 
+// The sampler's exact walk (liblizard/src/acquire.c:5121-5196): reg = H (9) then the node mesh's (dx, dy).
+int orc_layout_nodes(int side, float *pos);
+int orc_sample_grid(int n, int span, const uint8_t *luma, int w, int h, int pitch, const float *reg, float *grid);
+
 #ifdef __cplusplus
 }
 #endif

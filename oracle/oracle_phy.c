@@ -474,3 +474,55 @@ int orc_blocks(const orc_fmt_t *f, const int8_t *llrf, const double *sub_est, co
   free(cl); free(bits);
   return good;
 }
+
+// ------------------------------------------------------------------ the sampler (row a)
+
+// The node lattice of a square layout of `side` modules (liblizard/src/layout.c:110-117).
+int orc_layout_nodes(int side, float *pos) {
+  int cnt = 0;
+  for (float c = 3.5f; c < side - 3.5f - 8 && cnt < 39; c += 16) pos[cnt++] = c;
+  pos[cnt++] = side - 3.5f;
+  return cnt;
+}
+
+static int cell_of(const float *node, int nn, float m) {
+  int k = 0;
+  for (int q = 1; q <= nn - 2; q++) if (m >= node[q]) k = q;
+  return k;
+}
+
+// The picture grid of a luma frame through a registration (H: 9 floats, then the nx x ny mesh's (dx, dy)), by the
+// reference's exact walk: liblizard/src/acquire.c:5121-5196 (the scalar branch) and internal.h:11-23 sample(), float
+// operations in the same order, one rounding each.
+int orc_sample_grid(int n, int span, const uint8_t *luma, int w, int h, int pitch, const float *reg, float *grid) {
+  float node[40];
+  const int nn = orc_layout_nodes(span + 2 * MARGIN, node);
+  const float scale = (float)n / span, g0 = MARGIN + 0.5f / scale, step = 1.0f / scale;
+  const float *H = reg, *nodes = reg + 9;
+  for (int y = 0; y < n; y++) {
+    const float my = g0 + (float)y * step;
+    const int j = cell_of(node, nn, my);
+    const float v = (my - node[j]) / (node[j + 1] - node[j]);
+    const float kw = H[7] * my + 1, ku = H[1] * my + H[2], kv = H[4] * my + H[5];
+    for (int x = 0; x < n; x++) {
+      const float mx = g0 + (float)x * step;
+      const int i = cell_of(node, nn, mx);
+      const float *n00 = nodes + 2 * (j * nn + i), *n10 = n00 + 2, *n01 = n00 + 2 * nn, *n11 = n01 + 2;
+      const float inv = 1.0f / (node[i + 1] - node[i]);
+      const float ex = ((n10[0] - n00[0]) * (1 - v) + (n11[0] - n01[0]) * v) * inv, cx = n00[0] * (1 - v) + n01[0] * v - ex * node[i];
+      const float ey = ((n10[1] - n00[1]) * (1 - v) + (n11[1] - n01[1]) * v) * inv, cy = n00[1] * (1 - v) + n01[1] * v - ey * node[i];
+      const float rw = 1 / (H[6] * mx + kw);
+      const float pu = (H[0] * mx + ku) * rw, pv = (H[3] * mx + kv) * rw;
+      const float dx = cx + ex * mx, dy = cy + ey * mx;
+      float sx = pu + dx - 0.5f, sy = pv + dy - 0.5f;
+      if (sx < 0) sx = 0; else if (sx > w - 1.001f) sx = w - 1.001f;
+      if (sy < 0) sy = 0; else if (sy > h - 1.001f) sy = h - 1.001f;
+      const int xi = sx >= 0 ? (int)sx : 0, yi = sy >= 0 ? (int)sy : 0;
+      const float fx = sx - xi, fy = sy - yi;
+      const uint8_t *p = luma + (size_t)yi * pitch + xi;
+      const float a = p[0] / 255.0f, b = p[1] / 255.0f, c = p[pitch] / 255.0f, d = p[pitch + 1] / 255.0f;
+      grid[(size_t)y * n + x] = (a + (b - a) * fx) * (1 - fy) + (c + (d - c) * fx) * fy;
+    }
+  }
+  return nn;
+}

@@ -1,0 +1,63 @@
+"""Row a, the picture sampler: the oracle's exact walk held to the reference's (where built here) and, on the GPU,
+the sampler kernel held to the oracle bit for bit, then rows a-e end to end from captured luma frames."""
+import numpy as np
+import pytest
+
+import lizard_gb300 as lz
+import oracle
+from lizard_gb300 import synth
+
+CASES = [(384, 64, 1280, 720, False), (384, 64, 1280, 720, True), (768, 320, 1920, 1080, True), (1536, 1024, 3840, 2160, True)]
+
+
+def frame(n, subch, W, H, warped, seed=1, mesh=0.0):
+    f = lz.Format(n, subch, 128)
+    rng = np.random.default_rng(seed)
+    blocks = synth.random_blocks(f.blocks, seed)
+    grey = synth.picture(f, blocks)
+    Hm = synth.warp(f, W, H, rng) if warped else None
+    luma, reg = synth.capture(f, grey, W, H, H=Hm, sigma=2.0, rng=rng)
+    if mesh:
+        reg[9:] = rng.uniform(-mesh, mesh, reg[9:].size).astype(np.float32)
+    return f, luma, reg, blocks
+
+
+@pytest.mark.skipif(not oracle.have_ref(), reason="the reference is not built here")
+@pytest.mark.parametrize("n,subch,W,H,warped", CASES[:3])
+def test_oracle_walk_matches_reference(n, subch, W, H, warped):
+    f, luma, reg, _ = frame(n, subch, W, H, warped, mesh=0.6)
+    o, r = oracle.Fmt(n, subch, 128), oracle.RefFmt(n, subch, 128)
+    go = o.sample(luma, reg)
+    assert np.array_equal(go, r.sample_grid(luma, reg[:9], reg[9:], fast=False))
+    # the reference decoder's own integer read, within its test's 1/200 of grey of the walk
+    assert np.abs(r.sample_grid(luma, reg[:9], reg[9:], fast=True) - go).max() < 1 / 200
+
+
+@pytest.mark.parametrize("n,subch,W,H,warped", CASES)
+def test_captures_decode_in_the_oracle(n, subch, W, H, warped):
+    f, luma, reg, blocks = frame(n, subch, W, H, warped)
+    o = oracle.Fmt(n, subch, 128)
+    res = o.receive(o.sample(luma, reg))
+    assert res["ok"].all() and np.array_equal(res["blocks"], blocks)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,subch,W,H,warped", CASES)
+def test_gpu_luma_path_matches_oracle(n, subch, W, H, warped):
+    import torch
+    f, luma, reg, blocks = frame(n, subch, W, H, warped, mesh=0.3 if warped else 0.0)
+    o = oracle.Fmt(n, subch, 128)
+    go = o.sample(luma, reg)
+    rx = lz.Receiver(n, subch, 128, max_frames=2)
+    out = rx.finish_luma(np.stack([luma, luma]), np.stack([reg, reg]))
+    for k in range(2):
+        assert np.array_equal(out["grid"][k], go)
+    res = o.receive(go.copy())
+    c = out["coef"][0]
+    d, used = o.pilot_align(c)
+    turn = d if (used and (d[0] != 0 or d[1] != 0)) else None
+    llrf, est, rms = o.demap(c, turn)
+    assert np.array_equal(out["llrf"][0], llrf)
+    assert np.array_equal(out["ok"][0], res["ok"]) and out["ok"][0].all()
+    assert np.array_equal(out["blocks"][0], blocks)
+    assert rx.launches == 1 + 3 + 1 + 3 + f.tiers
