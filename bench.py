@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--count", type=int, default=65536, help="codewords a step (the workload: 65,536)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-receiver", action="store_true", help="skip the frame receiver's workloads")
+    ap.add_argument("--receiver-only", action="store_true", help="time only the frame receiver (profiling)")
     return ap.parse_args()
 
 
@@ -155,6 +157,96 @@ def cpu_decode(batch, threads, sample):
     return sample * 3840 / dt / 1e9, dt, kind
 
 
+def picture_frames(fmt, unique, copies, seed, sigma):
+    """unique painted pictures (n x n, AWGN of sigma grey levels) each repeated `copies` times, as luma frames of
+    the picture alone (w = h = n), with the registration that samples them one pixel a sample."""
+    import numpy as np
+    from lizard_gb300 import synth
+    rng = np.random.default_rng(seed)
+    n, scale = fmt.n, fmt.n / fmt.span
+    nn = synth.layout_nodes(fmt.span).size
+    reg = np.concatenate([np.array([scale, 0, -15 * scale, 0, scale, -15 * scale, 0, 0, 1], np.float32), np.zeros(2 * nn * nn, np.float32)])
+    pics = [synth.noisy(synth.picture(fmt, synth.random_blocks(fmt.blocks, seed * 100 + u), parity=u & 3), sigma, rng) for u in range(unique)]
+    luma = np.stack([pics[i % unique] for i in range(unique * copies)])
+    return luma, np.tile(reg, (unique * copies, 1))
+
+
+def bench_receiver(args, stream):
+    """The frame receiver, rows a-e (sampler, erase, detrend, 2D FFT, pilots, demap, LDPC, CRC), on two workloads:
+    the FFT demod batch (256 pictures: 64 each at n = 384, 768, 1152, 1536 at their top versions, 64 ring, AWGN 3
+    grey levels, one call per picture size) and the plain receiver one frame a call (LIZARD-64, n = 384, 1280 x 720,
+    AWGN 2). Device-timed with CUDA events; frames/s and payload MB/s (472 bytes a verified block)."""
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    res = {}
+    sp = stream.cuda_stream
+    # --- FFT demod batch
+    sizes = [(384, 80), (768, 320), (1152, 720), (1536, 1024)]
+    per = 64
+    rxs, bufs, blocks_total = [], [], 0
+    for n, subch in sizes:
+        rx = lz.Receiver(n, subch, 128, max_frames=per)
+        luma, reg = picture_frames(rx.fmt, 8, per // 8, seed=n, sigma=3.0)
+        d_l = torch.from_numpy(luma).cuda()
+        d_r = torch.from_numpy(reg).cuda()
+        o, s = rx._outputs(per, torch, keep=False)
+        rxs.append(rx)
+        bufs.append((d_l, d_r, o, s, n))
+        blocks_total += per * rx.fmt.blocks
+
+    def step():
+        for rx, (d_l, d_r, o, s, n) in zip(rxs, bufs):
+            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), n, n, n, n * n, lz.ctypes.c_void_p(d_r.data_ptr()),
+                                                         per, lz.ctypes.byref(s), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    ok = sum(int(b[2]["ok"].sum().item()) for b in bufs)
+    K = max(1, args.steps // 3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    res["fft_demod_batch"] = {"workload": "256 pictures, 64 each at n=384/768/1152/1536 (LIZARD-80/320/720/1024), 64 ring, AWGN 3 DN, rows a-e, one call per size",
+                              "frames_per_s": round(256 / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
+                              "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
+                              "gpu_launches_per_step": sum(rx.launches for rx in rxs)}
+    # --- plain receiver, one frame a call
+    rx = lz.Receiver(384, 64, 128, max_frames=1)
+    rng = np.random.default_rng(5)
+    grey = synth.picture(rx.fmt, synth.random_blocks(rx.fmt.blocks, 5))
+    luma, reg = synth.capture(rx.fmt, grey, 1280, 720, sigma=2.0, rng=rng)
+    d_l = torch.from_numpy(luma).cuda()
+    d_r = torch.from_numpy(reg).cuda()
+    o, s = rx._outputs(1, torch, keep=False)
+
+    def one():
+        lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1280, 720, 1280, 1280 * 720, lz.ctypes.c_void_p(d_r.data_ptr()),
+                                                     1, lz.ctypes.byref(s), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
+
+    for _ in range(10):
+        one()
+    torch.cuda.synchronize()
+    K1 = 200
+    e0.record(stream)
+    for _ in range(K1):
+        one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms1 = e0.elapsed_time(e1) / K1
+    ok1 = int(o["ok"].sum().item())
+    res["plain_one_frame"] = {"workload": "LIZARD-64, n=384, 64 ring, 1280x720 luma, AWGN 2 DN, axis-aligned, one frame a call",
+                              "frames_per_s": round(1e3 / ms1, 1), "payload_MBps": round(ok1 * 472 / (ms1 / 1e3) / 1e6, 3),
+                              "ms_per_frame": round(ms1, 4), "blocks_verified": ok1, "blocks": rx.fmt.blocks, "gpu_launches_per_frame": rx.launches}
+    return res
+
+
 def run_reference(args, rank, ws):
     """The reference arm: the reference's CPU decoder on the host cores, same metric and workload."""
     if rank != 0:
@@ -195,6 +287,9 @@ def main():
     assert torch.cuda.is_available(), "bench.py needs a CUDA device"
     dev = local
     torch.cuda.set_device(dev)
+    if args.receiver_only:
+        print(json.dumps(bench_receiver(args, torch.cuda.current_stream())))
+        return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
     plan = lz.LdpcPlan(batch["rates"], MAX_ITER, STALL_IT, STALL_RATIO)
     stream = torch.cuda.current_stream()
@@ -281,6 +376,8 @@ def main():
     }
     if e2e:
         out["e2e"] = e2e
+    if not args.no_receiver:
+        out["receiver"] = bench_receiver(args, stream)
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt, kind = cpu_decode(batch, threads, args.count)
