@@ -217,33 +217,50 @@ def bench_receiver(args, stream):
                               "frames_per_s": round(256 / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
                               "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
                               "gpu_launches_per_step": sum(rx.launches for rx in rxs)}
-    # --- plain receiver, one frame a call
-    rx = lz.Receiver(384, 64, 128, max_frames=1)
-    rng = np.random.default_rng(5)
-    grey = synth.picture(rx.fmt, synth.random_blocks(rx.fmt.blocks, 5))
-    luma, reg = synth.capture(rx.fmt, grey, 1280, 720, sigma=2.0, rng=rng)
-    d_l = torch.from_numpy(luma).cuda()
-    d_r = torch.from_numpy(reg).cuda()
-    o, s = rx._outputs(1, torch, keep=False)
+    # --- one frame a call (direct and captured), and a batch of frames a call, at n = 384 and n = 1536
+    def capture_frames(n, subch, W, Hh, count, seed):
+        rx = lz.Receiver(n, subch, 128, max_frames=count)
+        rng = np.random.default_rng(seed)
+        lumas, regs = [], []
+        for u in range(min(count, 4)):
+            grey = synth.picture(rx.fmt, synth.random_blocks(rx.fmt.blocks, seed + u), parity=u & 3)
+            luma, reg = synth.capture(rx.fmt, grey, W, Hh, sigma=2.0, rng=rng)
+            lumas.append(luma)
+            regs.append(reg)
+        luma = np.stack([lumas[i % len(lumas)] for i in range(count)])
+        reg = np.stack([regs[i % len(regs)] for i in range(count)])
+        return rx, torch.from_numpy(luma).cuda(), torch.from_numpy(reg).cuda()
 
-    def one():
-        lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1280, 720, 1280, 1280 * 720, lz.ctypes.c_void_p(d_r.data_ptr()),
-                                                     1, lz.ctypes.byref(s), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
+    def timed(call, K):
+        for _ in range(10):
+            call()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(K):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
 
-    for _ in range(10):
-        one()
-    torch.cuda.synchronize()
-    K1 = 200
-    e0.record(stream)
-    for _ in range(K1):
-        one()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms1 = e0.elapsed_time(e1) / K1
-    ok1 = int(o["ok"].sum().item())
-    res["plain_one_frame"] = {"workload": "LIZARD-64, n=384, 64 ring, 1280x720 luma, AWGN 2 DN, axis-aligned, one frame a call",
-                              "frames_per_s": round(1e3 / ms1, 1), "payload_MBps": round(ok1 * 472 / (ms1 / 1e3) / 1e6, 3),
-                              "ms_per_frame": round(ms1, 4), "blocks_verified": ok1, "blocks": rx.fmt.blocks, "gpu_launches_per_frame": rx.launches}
+    def receiver_line(n, subch, W, Hh, frames, graph, K, label):
+        rx, d_l, d_r = capture_frames(n, subch, W, Hh, frames, seed=n)
+        o, s = rx._outputs(frames, torch, keep=False)
+        fn = lz.lib().lizg_rx_finish_luma_graph if graph else lz.lib().lizg_rx_finish_luma_dev
+
+        def call():
+            lz._check(fn(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W, W * Hh, lz.ctypes.c_void_p(d_r.data_ptr()), frames,
+                         lz.ctypes.byref(s), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
+        ms = timed(call, K)
+        okb = int(o["ok"].sum().item())
+        return {"workload": label, "frames_per_call": frames, "graph": graph, "frames_per_s": round(frames / (ms / 1e3), 1),
+                "payload_MBps": round(okb * 472 / (ms / 1e3) / 1e6, 3), "ms_per_call": round(ms, 4),
+                "blocks_verified": okb, "blocks": frames * rx.fmt.blocks, "gpu_launches_per_call": rx.launches}
+
+    res["plain_one_frame"] = receiver_line(384, 64, 1280, 720, 1, False, 200, "LIZARD-64, n=384, 64 ring, 1280x720 luma, AWGN 2 DN, axis-aligned, one frame a call")
+    res["plain_one_frame_graph"] = receiver_line(384, 64, 1280, 720, 1, True, 400, "the same, the call replayed from a CUDA graph")
+    res["n1536_one_frame"] = receiver_line(1536, 1024, 3840, 2160, 1, False, 50, "LIZARD-1024, n=1536, 64 ring, 3840x2160 luma, AWGN 2 DN, one frame a call")
+    res["n1536_batched_graph"] = receiver_line(1536, 1024, 3840, 2160, 32, True, 5, "the same, 32 frames a call replayed from a CUDA graph")
+    res["n1536_batched_vs_one_frame"] = round(res["n1536_batched_graph"]["frames_per_s"] / res["n1536_one_frame"]["frames_per_s"], 2)
     return res
 
 

@@ -155,6 +155,12 @@ int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const l
 // a held registration (liblizard/src/lizard_phy.c:1566-1871).
 int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
                             int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
+// lizg_rx_finish_luma_dev replayed from a CUDA graph: the first call with a given set of buffers and sizes captures
+// the whole per-frame pipeline on the handle's own stream; later calls with the same arguments launch the captured
+// graph on `stream` in one call (different arguments capture again). For a caller that decodes frame after frame
+// into the same buffers, where the launches would otherwise cost more than the work.
+int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
+                              int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
 
 #ifdef __cplusplus
 }

@@ -172,6 +172,7 @@ def _rx_sigs(L):
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
     L.lizg_rx_finish_grid_dev.argtypes = [P, P, I, P, P, P]
     L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
+    L.lizg_rx_finish_luma_graph.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
 
 
 class RxOut(ctypes.Structure):
@@ -281,7 +282,7 @@ class Receiver:
             out["coef"] = c.cpu().numpy()
         return out
 
-    def finish_luma(self, luma, reg, keep=True, stream=None):
+    def finish_luma(self, luma, reg, keep=True, grid=True, stream=None):
         """luma: frames x h x w uint8; reg: frames x (9 + 2 nx ny) float32 (H then the node mesh). Returns a dict of
         numpy arrays including the sampled grids and the spectra."""
         import torch
@@ -291,14 +292,15 @@ class Receiver:
         dr = torch.from_numpy(np.ascontiguousarray(reg, np.float32)).cuda()
         o, s = self._outputs(frames, torch, keep)
         n = self.fmt.n
-        grid = torch.zeros((frames, n, n), dtype=torch.float32, device="cuda")
+        g = torch.zeros((frames, n, n), dtype=torch.float32, device="cuda") if grid else None
         c = torch.zeros((frames, 2 * self.fmt.subch * SUB), dtype=torch.float32, device="cuda")
         st = torch.cuda.current_stream().cuda_stream if stream is None else stream
         _check(lib().lizg_rx_finish_luma_dev(self._h, ctypes.c_void_p(d.data_ptr()), w, h, w, h * w, ctypes.c_void_p(dr.data_ptr()), frames,
-                                              ctypes.byref(s), ctypes.c_void_p(grid.data_ptr()), ctypes.c_void_p(c.data_ptr()), ctypes.c_void_p(st)),
-               "lizg_rx_finish_luma_dev")
+                                              ctypes.byref(s), ctypes.c_void_p(g.data_ptr()) if grid else None, ctypes.c_void_p(c.data_ptr()),
+                                              ctypes.c_void_p(st)), "lizg_rx_finish_luma_dev")
         torch.cuda.synchronize()
         out = {k: v.cpu().numpy() for k, v in o.items()}
-        out["grid"] = grid.cpu().numpy()
+        if grid:
+            out["grid"] = g.cpu().numpy()
         out["coef"] = c.cpu().numpy()
         return out

@@ -23,49 +23,49 @@ __device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, c
   return make_float2(z.x * cs.x + z.y * cs.y, z.y * cs.x - z.x * cs.y);
 }
 
-// One warp a frame. Each lane works out its pilots' six products in parallel; lane 0 adds them in pilot order, so
-// the double sums are the reference's. Writes align[3 f ..] = dx, dy, and 1 where the shift is turned back.
-__global__ void pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align) {
-  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (f >= fd.frames) return;
-  __shared__ double terms[8][32][6];
-  double (*tm)[6] = terms[threadIdx.x >> 5];
+// One CTA a frame. Its threads work out every pilot's six products in parallel into shared memory; six threads
+// then add one sum each in pilot order, so the double sums are the reference's (liblizard/src/lizard_phy.c:283-317).
+// Writes align[3 f ..] = dx, dy, and 1 where the shift is turned back.
+__global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align) {
+  extern __shared__ double tm[];              // npilot x 6
+  __shared__ double sums[6], dxy[2];
+  __shared__ int give_up;
+  const int f = blockIdx.x, used = fd.npilot;
   const float2 *sp = spec + f * spec_stride;
   const double k = 2.0 * 3.14159265358979323846 / fd.n;
-  double dx = 0, dy = 0, a = 0, b = 0, c = 0, p = 0, q = 0, yy = 0;
-  const int used = fd.npilot;
-  bool give_up = false;
-  for (int it = 0; it < 2 && !give_up; it++) {
-    a = b = c = p = q = yy = 0;
-    for (int c0 = 0; c0 < used; c0 += 32) {
-      const int pi = c0 + lane;
-      if (pi < used) {
-        const int i = fd.pilot_coef[pi], w = fd.pilot_white[pi];
-        const float2 y = turned(fd, sp, idx, i, (float)dx, (float)dy);
-        const double xr = (w & 1) ? -1.0 : 1.0, xi = (w & 2) ? -1.0 : 1.0;
-        const double zr = (double)y.x * xr + (double)y.y * xi, zi = (double)y.y * xr - (double)y.x * xi;
-        const double cu = k * zr * fd.uv[2 * i], cv = k * zr * fd.uv[2 * i + 1];
-        tm[lane][0] = cu * cu; tm[lane][1] = cu * cv; tm[lane][2] = cv * cv; tm[lane][3] = cu * zi; tm[lane][4] = cv * zi; tm[lane][5] = zi * zi;
-      }
-      __syncwarp();
-      if (lane == 0) {
-        const int m = min(32, used - c0);
-        for (int l = 0; l < m; l++) { a += tm[l][0]; b += tm[l][1]; c += tm[l][2]; p += tm[l][3]; q += tm[l][4]; yy += tm[l][5]; }
-      }
-      __syncwarp();
+  if (threadIdx.x == 0) { dxy[0] = dxy[1] = 0; give_up = 0; }
+  __syncthreads();
+  for (int it = 0; it < 2; it++) {
+    const double dx = dxy[0], dy = dxy[1];
+    for (int pi = threadIdx.x; pi < used; pi += blockDim.x) {
+      const int i = fd.pilot_coef[pi], w = fd.pilot_white[pi];
+      const float2 y = turned(fd, sp, idx, i, (float)dx, (float)dy);
+      const double xr = (w & 1) ? -1.0 : 1.0, xi = (w & 2) ? -1.0 : 1.0;
+      const double zr = (double)y.x * xr + (double)y.y * xi, zi = (double)y.y * xr - (double)y.x * xi;
+      const double cu = k * zr * fd.uv[2 * i], cv = k * zr * fd.uv[2 * i + 1];
+      double *t = tm + 6 * pi;
+      t[0] = cu * cu; t[1] = cu * cv; t[2] = cv * cv; t[3] = cu * zi; t[4] = cv * zi; t[5] = zi * zi;
     }
-    if (lane == 0) {
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      double acc = 0;
+      for (int pi = 0; pi < used; pi++) acc += tm[6 * pi + threadIdx.x];
+      sums[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double a = sums[0], b = sums[1], c = sums[2], p = sums[3], q = sums[4];
       const double det = a * c - b * b;
-      if (used < 8 || !(det > 0)) give_up = true;
-      else { dx += (p * c - q * b) / det; dy += (a * q - b * p) / det; }
+      if (used < 8 || !(det > 0)) give_up = 1;
+      else { dxy[0] = dx + (p * c - q * b) / det; dxy[1] = dy + (a * q - b * p) / det; }
     }
-    give_up = __shfl_sync(0xffffffffu, give_up, 0);
-    dx = __shfl_sync(0xffffffffu, dx, 0);
-    dy = __shfl_sync(0xffffffffu, dy, 0);
+    __syncthreads();
+    if (give_up) break;
   }
-  if (lane != 0) return;
+  if (threadIdx.x != 0) return;
   float d0 = 0, d1 = 0;
   if (!give_up) {
+    const double a = sums[0], b = sums[1], c = sums[2], p = sums[3], q = sums[4], yy = sums[5], dx = dxy[0], dy = dxy[1];
     const double det = a * c - b * b, ex = (p * c - q * b) / det, ey = (a * q - b * p) / det;
     const double s2 = (yy - ex * p - ey * q) / (used - 2);
     const double chi = s2 > 0 ? (dx * dx * a + 2 * dx * dy * b + dy * dy * c) / s2 : 0;
@@ -173,7 +173,15 @@ __global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride
 
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st) {
-  pilot_align_kernel<<<(fd.frames + 7) / 8, 256, 0, st>>>(fd, spec, spec_stride, idx, align);
+  static bool attr = false;
+  const int psm = 6 * (fd.npilot > 0 ? fd.npilot : 1) * (int)sizeof(double);
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(pilot_align_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * 1024 * (int)sizeof(double));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (fd.npilot > 1024) return cudaErrorInvalidValue;
+  pilot_align_kernel<<<fd.frames, 256, psm, st>>>(fd, spec, spec_stride, idx, align);
   const int groups = fd.frames * fd.subch;
   demap_kernel<<<(groups + 63) / 64, 256, 0, st>>>(fd, spec, spec_stride, idx, align, llrf, sub_est, sub_rms);
   const int nbk = fd.frames * fd.blocks;

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "lizg_internal.h"
+#include "sample_dev.cuh"
 
 namespace lizg {
 
@@ -79,6 +80,14 @@ __device__ float2 *fft_lines(float2 *a, float2 *b, int L, const FftDev &xd) {
   return a;
 }
 
+// A frame's picture sample (x, y): read from a supplied grid, or sampled straight from the captured frame through
+// its registration (the sampler fused into the pass that reads it).
+__device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y) {
+  if (s.grid) return s.grid[f * s.gstride + (int64_t)y * s.sd.n + x];
+  const float *H = s.reg + (int64_t)f * s.regstride;
+  return sample_at(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, x, y);
+}
+
 __device__ __forceinline__ bool in_square(const FftDev &xd, int t) {
   bool in = false;
 #pragma unroll
@@ -92,14 +101,13 @@ __device__ __forceinline__ void hole_basis(const FftDev &xd, int x, int y, doubl
   b[0] = 1; b[1] = cx; b[2] = xd.qx[x]; b[3] = cy; b[4] = xd.qx[y]; b[5] = cx * cy;
 }
 
-__global__ void __launch_bounds__(256) hole_fit_kernel(FftDev xd, const float *grid, int64_t stride, double *beta) {
+__global__ void __launch_bounds__(256) hole_fit_kernel(FftDev xd, SrcDev src, double *beta) {
   const int f = blockIdx.x, n = xd.n, c = n / 8;
-  const float *g = grid + f * stride;
   double rhs[6] = {0, 0, 0, 0, 0, 0};
   for (int k = threadIdx.x; k < c * c; k += blockDim.x) {
     const int x = 8 * (k % c), y = 8 * (k / c);
     if (in_square(xd, x) && in_square(xd, y)) continue;
-    const double v = g[(int64_t)y * n + x];
+    const double v = src_at(src, f, x, y);
     double b[6];
     hole_basis(xd, x, y, b);
     for (int r = 0; r < 6; r++) rhs[r] += b[r] * v;
@@ -121,13 +129,11 @@ __global__ void __launch_bounds__(256) hole_fit_kernel(FftDev xd, const float *g
 constexpr int kColTile = 8;          // picture columns a column-pass CTA takes (kColTile / 2 complex lines)
 constexpr int kRowTile = 4;          // kept rows a row-pass CTA takes
 
-__global__ void __launch_bounds__(256) fft_cols_kernel(FftDev xd, const float *grid, int64_t stride, const double *beta,
-                                                       double *colsum, float2 *Y) {
+__global__ void __launch_bounds__(256) fft_cols_kernel(FftDev xd, SrcDev src, const double *beta, double *colsum, float2 *Y) {
   extern __shared__ float2 sm[];
   const int n = xd.n, tiles = n / kColTile, f = blockIdx.x / tiles, x0 = (blockIdx.x % tiles) * kColTile;
   constexpr int L = kColTile / 2;
   float2 *a = sm, *b = sm + L * n;
-  const float *g = grid + f * stride;
   double bt[6];
   for (int r = 0; r < 6; r++) bt[r] = beta[f * 6 + r];
   // load: thread t takes column j = t % 8 at rows y = t / 8, t / 8 + 32, ...; the anchors' squares are erased to
@@ -136,12 +142,14 @@ __global__ void __launch_bounds__(256) fft_cols_kernel(FftDev xd, const float *g
   const bool xin = in_square(xd, x);
   float s0 = 0, s1 = 0, s2 = 0;
   for (int y = threadIdx.x / kColTile; y < n; y += blockDim.x / kColTile) {
-    float v = g[(int64_t)y * n + x];
+    float v;
     if (xin && in_square(xd, y)) {
       double bb[6], h = 0;
       hole_basis(xd, x, y, bb);
       for (int r = 0; r < 6; r++) h += bt[r] * bb[r];
       v = (float)h;
+    } else {
+      v = src_at(src, f, x, y);
     }
     s0 += v; s1 += v * xd.cx[y]; s2 += v * xd.qx[y];
     float2 *dst = a + (j % L) * n + y;
@@ -169,14 +177,10 @@ __global__ void __launch_bounds__(256) fft_cols_kernel(FftDev xd, const float *g
   }
 }
 
-__global__ void __launch_bounds__(256) fft_rows_kernel(FftDev xd, const double *colsum, const float2 *Y, float2 *T) {
-  extern __shared__ float2 sm[];
-  const int n = xd.n, tiles = (xd.vrows + kRowTile - 1) / kRowTile, f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * kRowTile;
-  const int L = min(kRowTile, xd.vrows - v0);
-  float2 *a = sm, *b = sm + kRowTile * n;
-  const float2 *Yf = Y + (int64_t)f * xd.vrows * n;
-  for (int t = threadIdx.x; t < L * n; t += blockDim.x) a[t] = Yf[(int64_t)v0 * n + t];
-  // the five projections from the columns' moments (liblizard/src/lizard_phy.c:1584-1591, 1718)
+// The five projections of each frame from its columns' moments, normalised (liblizard/src/lizard_phy.c:1584-1591,
+// 1718): px, py, pxy, pxx, pyy.
+__global__ void __launch_bounds__(256) proj_kernel(FftDev xd, const double *colsum, double *proj) {
+  const int f = blockIdx.x, n = xd.n;
   const double *cs = colsum + (int64_t)f * n * 3;
   double p[5] = {0, 0, 0, 0, 0};
   for (int xx = threadIdx.x; xx < n; xx += blockDim.x) {
@@ -184,7 +188,6 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(FftDev xd, const double *
     p[0] += c * S0; p[1] += S1; p[2] += c * S1; p[3] += q * S0; p[4] += S2;
   }
   __shared__ double red[5][256];
-  __shared__ double proj[5];
   for (int r = 0; r < 5; r++) red[r][threadIdx.x] = p[r];
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -192,31 +195,48 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(FftDev xd, const double *
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    proj[0] = red[0][0] / (n * xd.sx2); proj[1] = red[1][0] / (n * xd.sx2); proj[2] = red[2][0] / (xd.sx2 * xd.sx2);
-    proj[3] = red[3][0] / (n * xd.sq2); proj[4] = red[4][0] / (n * xd.sq2);
+    double *o = proj + 5 * f;
+    o[0] = red[0][0] / (n * xd.sx2); o[1] = red[1][0] / (n * xd.sx2); o[2] = red[2][0] / (xd.sx2 * xd.sx2);
+    o[3] = red[3][0] / (n * xd.sq2); o[4] = red[4][0] / (n * xd.sq2);
   }
+}
+
+__global__ void __launch_bounds__(256) fft_rows_kernel(FftDev xd, const double *proj, const float2 *Y, float2 *T) {
+  extern __shared__ float2 sm[];
+  const int n = xd.n, tiles = (xd.vrows + kRowTile - 1) / kRowTile, f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * kRowTile;
+  const int L = min(kRowTile, xd.vrows - v0);
+  float2 *a = sm, *b = sm + kRowTile * n;
+  const float2 *Yf = Y + (int64_t)f * xd.vrows * n;
+  for (int t = threadIdx.x; t < L * n; t += blockDim.x) a[t] = Yf[(int64_t)v0 * n + t];
   __syncthreads();
   float2 *z = fft_lines(a, b, L, xd);
   float2 *Tf = T + (int64_t)f * xd.vrows * n;
-  const double px = proj[0], py = proj[1], pxy = proj[2], pxx = proj[3], pyy = proj[4];
-  for (int t = threadIdx.x; t < L * n; t += blockDim.x) {
-    const int l = t / n, u = t - l * n, v = v0 + l;
-    float2 o = z[t];
-    const float2 x1u = xd.x1[u], x1v = xd.x1[v];
+  const double *pj = proj + 5 * f;
+  const double px = pj[0], py = pj[1], pxy = pj[2], pxx = pj[3], pyy = pj[4];
+  // the surface's spectrum off (liblizard/src/lizard_phy.c:1697-1716): the xy term's column factor pxy X1[u] worked
+  // out once a u for the CTA's rows, then the x terms on v = 0 and the y terms on u = 0
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {
+    const float2 x1u = xd.x1[u];
     const float ar = (float)(pxy * x1u.x), ai = (float)(pxy * x1u.y);
-    o.x -= ar * x1v.x - ai * x1v.y;
-    o.y -= ar * x1v.y + ai * x1v.x;
-    if (v == 0) {
+    float2 c0 = make_float2(0, 0);
+    if (v0 == 0) {
       const float2 x2u = xd.x2[u];
-      o.x -= (float)(n * (px * x1u.x + pxx * x2u.x));
-      o.y -= (float)(n * (px * x1u.y + pxx * x2u.y));
+      c0 = make_float2((float)(n * (px * x1u.x + pxx * x2u.x)), (float)(n * (px * x1u.y + pxx * x2u.y)));
     }
-    if (u == 0) {
-      const float2 x2v = xd.x2[v];
-      o.x -= (float)(n * (py * x1v.x + pyy * x2v.x));
-      o.y -= (float)(n * (py * x1v.y + pyy * x2v.y));
+    for (int l = 0; l < L; l++) {
+      const int v = v0 + l;
+      float2 o = z[l * n + u];
+      const float2 x1v = xd.x1[v];
+      o.x -= ar * x1v.x - ai * x1v.y;
+      o.y -= ar * x1v.y + ai * x1v.x;
+      if (v == 0) { o.x -= c0.x; o.y -= c0.y; }
+      if (u == 0) {
+        const float2 x2v = xd.x2[v];
+        o.x -= (float)(n * (py * x1v.x + pyy * x2v.x));
+        o.y -= (float)(n * (py * x1v.y + pyy * x2v.y));
+      }
+      Tf[(int64_t)v * n + u] = o;
     }
-    Tf[(int64_t)v * n + u] = o;
   }
 }
 
@@ -230,7 +250,7 @@ __global__ void gather_coef_kernel(const float2 *T, int64_t tstride, const int32
 
 static bool g_attr[2] = {false, false};
 
-cudaError_t fft_launch(const FftDev &xd, int frames, const float *grid, int64_t stride, double *beta, double *colsum,
+cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, double *beta, double *colsum, double *proj,
                        float2 *Y, float2 *T, cudaStream_t st) {
   const int smc = 2 * (kColTile / 2) * xd.n * (int)sizeof(float2), smr = 2 * kRowTile * xd.n * (int)sizeof(float2);
   cudaError_t e;
@@ -239,9 +259,10 @@ cudaError_t fft_launch(const FftDev &xd, int frames, const float *grid, int64_t 
     if ((e = cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * kRowTile * 1536 * 8)) != cudaSuccess) return e;
     g_attr[0] = true;
   }
-  hole_fit_kernel<<<frames, 256, 0, st>>>(xd, grid, stride, beta);
-  fft_cols_kernel<<<frames * (xd.n / kColTile), 256, smc, st>>>(xd, grid, stride, beta, colsum, Y);
-  fft_rows_kernel<<<frames * ((xd.vrows + kRowTile - 1) / kRowTile), 256, smr, st>>>(xd, colsum, Y, T);
+  hole_fit_kernel<<<frames, 256, 0, st>>>(xd, src, beta);
+  fft_cols_kernel<<<frames * (xd.n / kColTile), 256, smc, st>>>(xd, src, beta, colsum, Y);
+  proj_kernel<<<frames, 256, 0, st>>>(xd, colsum, proj);
+  fft_rows_kernel<<<frames * ((xd.vrows + kRowTile - 1) / kRowTile), 256, smr, st>>>(xd, proj, Y, T);
   return cudaGetLastError();
 }
 

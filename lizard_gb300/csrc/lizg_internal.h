@@ -41,6 +41,19 @@ struct SampleDev {
   const float *node_x, *node_y;      // node centres' module coordinates
 };
 
+// Where the transform reads a frame's picture samples from: a grid (grid set; frame f at grid + f gstride, row-major
+// n x n) or the captured frames through their registrations (the sampler fused in).
+struct SrcDev {
+  const float *grid;
+  int64_t gstride;
+  const uint8_t *luma;
+  int w, h, pitch;
+  int64_t fstride;
+  const float *reg;
+  int regstride;
+  SampleDev sd;
+};
+
 // The receiver's per-batch soft-value and block state, in device memory.
 struct RxState {
   const int8_t *llrf;     // frames x subch x 640 soft values, slot order
@@ -76,7 +89,7 @@ int device_ready(int *sms);
 int record_error(int code, const char *what);
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
-cudaError_t fft_launch(const FftDev &xd, int frames, const float *grid, int64_t stride, double *beta, double *colsum,
+cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, double *beta, double *colsum, double *proj,
                        float2 *Y, float2 *T, cudaStream_t st);
 cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, int w, int h, int pitch, int64_t fstride,
                           const float *reg, int regstride, float *grid, cudaStream_t st);

@@ -28,7 +28,7 @@ struct lizg_rx {
   float *sub_rms = nullptr, *est = nullptr, *pilot = nullptr, *align = nullptr;
   uint8_t *decl = nullptr;
   int *counters = nullptr;
-  double *beta = nullptr, *colsum = nullptr;
+  double *beta = nullptr, *colsum = nullptr, *proj = nullptr;
   float *grid = nullptr;              // sampled pictures (luma input)
   lizg::SampleDev sd{};
   float *node_xy = nullptr;
@@ -38,6 +38,11 @@ struct lizg_rx {
   cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
   int launches = 0;
   std::vector<void *> owned;
+  // the captured pipeline of lizg_rx_finish_luma_graph and the call it was captured for
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<uintptr_t> graph_key;
+  int graph_launches = 0;
 };
 
 namespace {
@@ -145,6 +150,7 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   const size_t F = (size_t)max_frames;
   ok(dev_alloc(r, &r->grid, F * n * n));
   ok(dev_alloc(r, &r->beta, F * 6));
+  ok(dev_alloc(r, &r->proj, F * 5));
   ok(dev_alloc(r, &r->colsum, F * n * 3));
   ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
   ok(dev_alloc(r, &r->T, F * (size_t)r->xd.vrows * n));
@@ -174,6 +180,8 @@ void lizg_rx_free(lizg_rx *r) {
   for (void *p : r->owned) cudaFree(p);
   for (int t = 0; t < 4; t++) { if (r->side[t]) cudaStreamDestroy(r->side[t]); if (r->join[t]) cudaEventDestroy(r->join[t]); }
   if (r->fork) cudaEventDestroy(r->fork);
+  if (r->graph) cudaGraphExecDestroy(r->graph);
+  if (r->cap) cudaStreamDestroy(r->cap);
   delete r;
 }
 
@@ -284,16 +292,13 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
   return finish_spec(r, reinterpret_cast<const float2 *>(d_coef), (int64_t)r->f.subch * lizg::kSub, nullptr, frames, out, static_cast<cudaStream_t>(stream), sms);
 }
 
-// Rows (b) to (e) on a batch of picture grids: the anchors' erase and the detrended 2D transform, then as above.
-int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const lizg_rx_out *out, float *d_coef, void *stream) {
-  int sms = 0;
-  if (int rc = check_call(r, d_grid, frames, out, "lizg_rx_finish_grid_dev", &sms)) return rc;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
+// Rows (b) to (e) from a picture source: the anchors' erase and the detrended 2D transform, then as above.
+static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const lizg_rx_out *out, float *d_coef, cudaStream_t st, int sms) {
   const int n = r->f.n;
   const int64_t tstride = (int64_t)r->xd.vrows * n;
-  cudaError_t e = lizg::fft_launch(r->xd, frames, d_grid, (int64_t)n * n, r->beta, r->colsum, r->Y, r->T, st);
+  cudaError_t e = lizg::fft_launch(r->xd, frames, src, r->beta, r->colsum, r->proj, r->Y, r->T, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
-  r->launches = 3;
+  r->launches += 4;
   if (d_coef) {
     if ((e = lizg::gather_coef_launch(r->T, tstride, r->tix, r->f.subch * lizg::kSub, frames, reinterpret_cast<float2 *>(d_coef), st)) != cudaSuccess)
       return lizg::record_error(LIZG_E_CUDA, (std::string("gather: ") + cudaGetErrorString(e)).c_str());
@@ -302,7 +307,17 @@ int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const l
   return finish_spec(r, r->T, tstride, r->tix, frames, out, st, sms);
 }
 
-// Rows (a) to (e) on a batch of captured luma frames, each with its registration (H, then the node mesh).
+int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const lizg_rx_out *out, float *d_coef, void *stream) {
+  int sms = 0;
+  if (int rc = check_call(r, d_grid, frames, out, "lizg_rx_finish_grid_dev", &sms)) return rc;
+  lizg::SrcDev src{};
+  src.grid = d_grid; src.gstride = (int64_t)r->f.n * r->f.n; src.sd = r->sd;
+  r->launches = 0;
+  return finish_src(r, src, frames, out, d_coef, static_cast<cudaStream_t>(stream), sms);
+}
+
+// Rows (a) to (e) on a batch of captured luma frames, each with its registration (H, then the node mesh). The
+// sampler runs inside the transform's passes (no grid in HBM) unless the caller asks for the grid.
 int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
                             int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream) {
   int sms = 0;
@@ -310,12 +325,55 @@ int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int
   if (!d_reg || w < 2 || h < 2 || pitch < w || frame_stride < (int64_t)pitch * h)
     return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_luma_dev: bad frame geometry or NULL registration");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  float *grid = d_grid ? d_grid : r->grid;
-  cudaError_t e = lizg::sample_launch(r->sd, frames, d_luma, w, h, pitch, frame_stride, d_reg, 9 + 2 * r->sd.nx * r->sd.ny, grid, st);
-  if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("sampler: ") + cudaGetErrorString(e)).c_str());
-  const int rc = lizg_rx_finish_grid_dev(r, grid, frames, out, d_coef, stream);
-  r->launches += 1;
-  return rc;
+  const int regstride = 9 + 2 * r->sd.nx * r->sd.ny;
+  r->launches = 0;
+  lizg::SrcDev src{};
+  src.sd = r->sd;
+  if (d_grid) {
+    cudaError_t e = lizg::sample_launch(r->sd, frames, d_luma, w, h, pitch, frame_stride, d_reg, regstride, d_grid, st);
+    if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("sampler: ") + cudaGetErrorString(e)).c_str());
+    r->launches = 1;
+    src.grid = d_grid; src.gstride = (int64_t)r->f.n * r->f.n;
+  } else {
+    src.luma = d_luma; src.w = w; src.h = h; src.pitch = pitch; src.fstride = frame_stride; src.reg = d_reg; src.regstride = regstride;
+  }
+  return finish_src(r, src, frames, out, d_coef, st, sms);
+}
+
+// The same call as lizg_rx_finish_luma_dev, replayed from a CUDA graph: the first call with a given set of buffers
+// and sizes captures the whole per-frame pipeline (its 10 to 12 kernels, the per-code fork and join) on the handle's
+// own stream; later calls with the same arguments launch the captured graph on `stream` in one call. Different
+// arguments capture again. The graph reads the buffers the call names, so their contents may change between calls.
+int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
+                              int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream) {
+  int sms = 0;
+  if (int rc = check_call(r, d_luma, frames, out, "lizg_rx_finish_luma_graph", &sms)) return rc;
+  const std::vector<uintptr_t> key = {(uintptr_t)d_luma, (uintptr_t)w, (uintptr_t)h, (uintptr_t)pitch, (uintptr_t)frame_stride,
+                                      (uintptr_t)d_reg, (uintptr_t)frames, (uintptr_t)out->blocks, (uintptr_t)out->ok, (uintptr_t)out->its,
+                                      (uintptr_t)out->est, (uintptr_t)out->pilot, (uintptr_t)out->align, (uintptr_t)out->llrf,
+                                      (uintptr_t)out->sub_est, (uintptr_t)out->sub_rms, (uintptr_t)d_grid, (uintptr_t)d_coef};
+  cudaError_t e;
+  if (!r->graph || key != r->graph_key) {
+    if (r->graph) { cudaGraphExecDestroy(r->graph); r->graph = nullptr; }
+    if (!r->cap && (e = cudaStreamCreateWithFlags(&r->cap, cudaStreamNonBlocking)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_CUDA, (std::string("graph stream: ") + cudaGetErrorString(e)).c_str());
+    if ((e = cudaStreamBeginCapture(r->cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_CUDA, (std::string("begin capture: ") + cudaGetErrorString(e)).c_str());
+    const int rc = lizg_rx_finish_luma_dev(r, d_luma, w, h, pitch, frame_stride, d_reg, frames, out, d_grid, d_coef, r->cap);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(r->cap, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("end capture: ") + cudaGetErrorString(e)).c_str());
+    e = cudaGraphInstantiate(&r->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { r->graph = nullptr; return lizg::record_error(LIZG_E_CUDA, (std::string("instantiate: ") + cudaGetErrorString(e)).c_str()); }
+    r->graph_key = key;
+    r->graph_launches = r->launches;
+  }
+  if ((e = cudaGraphLaunch(r->graph, static_cast<cudaStream_t>(stream))) != cudaSuccess)
+    return lizg::record_error(LIZG_E_CUDA, (std::string("graph launch: ") + cudaGetErrorString(e)).c_str());
+  r->launches = r->graph_launches;
+  return 0;
 }
 
 }  // extern "C"

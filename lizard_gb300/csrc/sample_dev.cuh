@@ -1,0 +1,48 @@
+// The picture sampler's arithmetic for one sample (row a), shared by the standalone sampler and the column pass that
+// reads samples straight from the captured frame. Every float operation is an explicit round-to-nearest intrinsic
+// in the reference's order (liblizard/src/acquire.c:5121-5196 and internal.h:11-23), so no compiler contraction can
+// change a value: the result is the reference's exact walk bit for bit, whatever the file's -fmad setting.
+#ifndef LIZG_SAMPLE_DEV_CUH
+#define LIZG_SAMPLE_DEV_CUH
+#include "lizg_internal.h"
+
+namespace lizg {
+
+// The mesh cell along one axis: the last k in [0, nn - 2] with m >= node[k], else 0 (liblizard/src/acquire.c:5089).
+__device__ __forceinline__ int node_cell(const float *node, int nn, float m) {
+  int k = 0;
+  for (int q = 1; q <= nn - 2; q++) if (m >= node[q]) k = q;
+  return k;
+}
+
+// Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh.
+__device__ __forceinline__ float sample_at(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
+                                           const float *nodes, int x, int y) {
+  const float mx = __fadd_rn(sd.g0, __fmul_rn((float)x, sd.step)), my = __fadd_rn(sd.g0, __fmul_rn((float)y, sd.step));
+  const int j = node_cell(sd.node_y, sd.ny, my), i = node_cell(sd.node_x, sd.nx, mx);
+  const float v = __fdiv_rn(__fsub_rn(my, sd.node_y[j]), __fsub_rn(sd.node_y[j + 1], sd.node_y[j])), omv = __fsub_rn(1.0f, v);
+  const float *n00 = nodes + 2 * (j * sd.nx + i), *n10 = n00 + 2, *n01 = n00 + 2 * sd.nx, *n11 = n01 + 2;
+  const float inv = __fdiv_rn(1.0f, __fsub_rn(sd.node_x[i + 1], sd.node_x[i]));
+  const float ex = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[0], n00[0]), omv), __fmul_rn(__fsub_rn(n11[0], n01[0]), v)), inv);
+  const float cx = __fsub_rn(__fadd_rn(__fmul_rn(n00[0], omv), __fmul_rn(n01[0], v)), __fmul_rn(ex, sd.node_x[i]));
+  const float ey = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[1], n00[1]), omv), __fmul_rn(__fsub_rn(n11[1], n01[1]), v)), inv);
+  const float cy = __fsub_rn(__fadd_rn(__fmul_rn(n00[1], omv), __fmul_rn(n01[1], v)), __fmul_rn(ey, sd.node_x[i]));
+  const float kw = __fadd_rn(__fmul_rn(H[7], my), 1.0f), ku = __fadd_rn(__fmul_rn(H[1], my), H[2]), kv = __fadd_rn(__fmul_rn(H[4], my), H[5]);
+  const float rw = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(H[6], mx), kw));
+  const float pu = __fmul_rn(__fadd_rn(__fmul_rn(H[0], mx), ku), rw), pv = __fmul_rn(__fadd_rn(__fmul_rn(H[3], mx), kv), rw);
+  const float dx = __fadd_rn(cx, __fmul_rn(ex, mx)), dy = __fadd_rn(cy, __fmul_rn(ey, mx));
+  float sx = __fsub_rn(__fadd_rn(pu, dx), 0.5f), sy = __fsub_rn(__fadd_rn(pv, dy), 0.5f);
+  const float xm = __fsub_rn((float)w, 1.001f), ym = __fsub_rn((float)h, 1.001f);
+  if (sx < 0) sx = 0; else if (sx > xm) sx = xm;
+  if (sy < 0) sy = 0; else if (sy > ym) sy = ym;
+  const int xi = sx >= 0 ? (int)sx : 0, yi = sy >= 0 ? (int)sy : 0;   // a NaN coordinate reads pixel 0
+  const float fx = __fsub_rn(sx, (float)xi), fy = __fsub_rn(sy, (float)yi);
+  const uint8_t *p = px + (int64_t)yi * pitch + xi;
+  const float a = __fdiv_rn((float)p[0], 255.0f), b = __fdiv_rn((float)p[1], 255.0f);
+  const float c = __fdiv_rn((float)p[pitch], 255.0f), d = __fdiv_rn((float)p[pitch + 1], 255.0f);
+  return __fadd_rn(__fmul_rn(__fadd_rn(a, __fmul_rn(__fsub_rn(b, a), fx)), __fsub_rn(1.0f, fy)),
+                   __fmul_rn(__fadd_rn(c, __fmul_rn(__fsub_rn(d, c), fx)), fy));
+}
+
+}  // namespace lizg
+#endif
