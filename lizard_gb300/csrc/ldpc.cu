@@ -25,17 +25,19 @@ namespace lizg {
 // Per-code compile-time shape: block rows, codeword bits, data bits, data circulants, slots (data circulants plus
 // two staircase slots a row), and the warps a CTA runs (as many codeword states as fit in 227 KB of shared memory).
 template <int C> struct Code;
-// NDMAX: the most data circulants any block row has.
-template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, NDMAX = 21, WARPS = 9; };
-template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, NDMAX = 14, WARPS = 7; };
-template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, NDMAX = 10, WARPS = 6; };
-template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5; };
+// NDMAX: the most data circulants any block row has. WARPS: codewords a CTA holds; WPC: warps a codeword (lane l of
+// warp w of a codeword takes checks l + 32 t, t = w (4 / WPC) .. (w + 1) (4 / WPC) - 1, of every layer).
+template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, NDMAX = 21, WARPS = 9, WPC = 2; };
+template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, NDMAX = 14, WARPS = 7, WPC = 2; };
+template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, NDMAX = 10, WARPS = 6, WPC = 2; };
+template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5, WPC = 2; };
 
 template <int C> __host__ __device__ constexpr int slots() { return Code<C>::NDATA + 2 * Code<C>::MB; }
 // A warp's state: posteriors (N int16) then messages (slots x 128 int8), rounded to 16 bytes.
 template <int C> __host__ __device__ constexpr int warp_bytes() { return (Code<C>::N * 2 + slots<C>() * 128 + 15) & ~15; }
 constexpr int kCrcBytes = (256 + 32 + 1) * 4 + 12;   // table, per-lane shifts, init term; padded to 16
 template <int C> constexpr int cta_smem() { return kCrcBytes + Code<C>::WARPS * warp_bytes<C>(); }
+template <int C> constexpr int cta_threads() { return Code<C>::WARPS * Code<C>::WPC * 32; }
 
 static_assert(cta_smem<0>() <= 227 * 1024, "7/8 state does not fit");
 static_assert(cta_smem<1>() <= 227 * 1024, "3/4 state does not fit");
@@ -64,43 +66,35 @@ __device__ __forceinline__ uint32_t gf_mul(uint32_t a, uint32_t b) {
 
 __device__ __forceinline__ int sat127(int v) { return max(-127, min(127, v)); }
 
-// One layer (block row r). Lane l takes checks i = l + 32 t, t = 0..3. Pass 1 loads every slot's extrinsic
-// q = L - R into registers (the row's circulants are unrolled to the code's widest row, so the register arrays are
-// statically indexed) and folds them into two interleaved min1/min2 chains a check, merged at the end; pass 2 makes
-// the messages and posteriors from the registers without reading shared memory again.
-template <int C>
-__device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane) {
+// One layer (block row r). Lane l takes checks i = l + 32 t, t = 0..3 (TW of them from T0 at a time). Pass 1 loads every slot's
+// extrinsic q = L - R into registers (the row's circulants unrolled to the code's widest row, so the register arrays
+// are statically indexed) and folds them into two interleaved min1/min2 chains a check, merged at the end; pass 2
+// makes the messages and posteriors from the registers without reading shared memory again.
+template <int C, int TW>
+__device__ __forceinline__ void layer_part(int16_t *L, int8_t *R, int r, int lane, int T0, int p0, int nd, const int *colb, const int *sh) {
   using T = Code<C>;
   constexpr int NDM = T::NDMAX;
-  const DevCode &cd = c_codes[C];
-  const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
   int8_t *Rr = R + (p0 + 2 * r) * 128 + lane;
   int16_t *Lp = L + T::K;
-  int q[NDM + 2][4];
-  int colb[NDM], sh[NDM];
+  int q[NDM + 2][TW];
 #pragma unroll
   for (int e = 0; e < NDM; e++) {
     if (e < nd) {
-      const int cs = cd.circ[p0 + e];
-      colb[e] = (cs >> 8) * 128; sh[e] = cs & 255;
 #pragma unroll
-      for (int t = 0; t < 4; t++) q[e][t] = L[colb[e] + ((lane + 32 * t - sh[e]) & 127)] - Rr[e * 128 + 32 * t];
+      for (int t = 0; t < TW; t++) q[e][t] = L[colb[e] + ((lane + 32 * (T0 + t) - sh[e]) & 127)] - Rr[e * 128 + 32 * (T0 + t)];
     }
   }
   const int prev = r > 0 ? (r - 1) * 128 + lane : (T::MB - 1) * 128 + lane - 1;
 #pragma unroll
-  for (int t = 0; t < 4; t++) {
-    q[NDM][t] = (r == 0 && lane + 32 * t == 0) ? 8191 : Lp[prev + 32 * t] - Rr[nd * 128 + 32 * t];
-    q[NDM + 1][t] = Lp[r * 128 + lane + 32 * t] - Rr[(nd + 1) * 128 + 32 * t];
+  for (int t = 0; t < TW; t++) {
+    const int tt = T0 + t;
+    q[NDM][t] = (r == 0 && lane + 32 * tt == 0) ? 8191 : Lp[prev + 32 * tt] - Rr[nd * 128 + 32 * tt];
+    q[NDM + 1][t] = Lp[r * 128 + lane + 32 * tt] - Rr[(nd + 1) * 128 + 32 * tt];
   }
-  int m1[4], m2[4], sg[4];
+  int m1[TW], m2[TW], sg[TW];
 #pragma unroll
-  for (int t = 0; t < 4; t++) {
-    int a1 = 255, a2 = 255, b1 = 255, b2 = 255, s = q[NDM][t] ^ q[NDM + 1][t];
-    {
-      const int a = min(abs(q[NDM][t]), 127), b = min(abs(q[NDM + 1][t]), 127);
-      a1 = a; b1 = b;
-    }
+  for (int t = 0; t < TW; t++) {
+    int a1 = min(abs(q[NDM][t]), 127), a2 = 255, b1 = min(abs(q[NDM + 1][t]), 127), b2 = 255, s = q[NDM][t] ^ q[NDM + 1][t];
 #pragma unroll
     for (int e = 0; e < NDM; e++) {
       if (e < nd) {
@@ -114,9 +108,9 @@ __device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane) {
     m2[t] = min(max(a1, b1), min(a2, b2));
     sg[t] = s;
   }
-  int s1[4], s2[4];
+  int s1[TW], s2[TW];
 #pragma unroll
-  for (int t = 0; t < 4; t++) {
+  for (int t = 0; t < TW; t++) {
     const int x1 = min(127, (m1[t] * 13) >> 4), x2 = min(127, (m2[t] * 13) >> 4);
     s1[t] = sg[t] < 0 ? -x1 : x1;     // the check's sign folded in
     s2[t] = sg[t] < 0 ? -x2 : x2;
@@ -130,38 +124,52 @@ __device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane) {
   for (int e = 0; e < NDM; e++) {
     if (e < nd) {
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
+      for (int t = 0; t < TW; t++) {
         const int m = msg(q[e][t], t);
-        Rr[e * 128 + 32 * t] = (int8_t)m;
-        L[colb[e] + ((lane + 32 * t - sh[e]) & 127)] = (int16_t)(q[e][t] + m);
+        Rr[e * 128 + 32 * (T0 + t)] = (int8_t)m;
+        L[colb[e] + ((lane + 32 * (T0 + t) - sh[e]) & 127)] = (int16_t)(q[e][t] + m);
       }
     }
   }
 #pragma unroll
-  for (int t = 0; t < 4; t++) {
-    if (!(r == 0 && lane + 32 * t == 0)) {
+  for (int t = 0; t < TW; t++) {
+    const int tt = T0 + t;
+    if (!(r == 0 && lane + 32 * tt == 0)) {
       const int m = msg(q[NDM][t], t);
-      Rr[nd * 128 + 32 * t] = (int8_t)m;
-      Lp[prev + 32 * t] = (int16_t)(q[NDM][t] + m);
+      Rr[nd * 128 + 32 * tt] = (int8_t)m;
+      Lp[prev + 32 * tt] = (int16_t)(q[NDM][t] + m);
     }
     const int m = msg(q[NDM + 1][t], t);
-    Rr[(nd + 1) * 128 + 32 * t] = (int8_t)m;
-    Lp[r * 128 + lane + 32 * t] = (int16_t)(q[NDM + 1][t] + m);
+    Rr[(nd + 1) * 128 + 32 * tt] = (int8_t)m;
+    Lp[r * 128 + lane + 32 * tt] = (int16_t)(q[NDM + 1][t] + m);
   }
+}
+
+template <int C, int TW>
+__device__ __forceinline__ void layer(int16_t *L, int8_t *R, int r, int lane, int T0) {
+  constexpr int NDM = Code<C>::NDMAX;
+  const DevCode &cd = c_codes[C];
+  const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+  int colb[NDM], sh[NDM];
+#pragma unroll
+  for (int e = 0; e < NDM; e++) {
+    if (e < nd) { const int cs = cd.circ[p0 + e]; colb[e] = (cs >> 8) * 128; sh[e] = cs & 255; }
+  }
+  layer_part<C, TW>(L, R, r, lane, T0, p0, nd, colb, sh);
 }
 
 // The same layer with the row's slots in a loop, the extrinsics recomputed in pass 2: fewer registers, which the
 // 7/8 code's 21-circulant rows need.
-template <int C>
-__device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lane) {
+template <int C, int TW>
+__device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lane, int T0) {
   using T = Code<C>;
   const DevCode &cd = c_codes[C];
   const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
   int8_t *Rr = R + (p0 + 2 * r) * 128;
   int16_t *Lp = L + T::K;
-  int m1[4], m2[4], sg[4];
+  int m1[TW], m2[TW], sg[TW];
 #pragma unroll
-  for (int q = 0; q < 4; q++) { m1[q] = 255; m2[q] = 255; sg[q] = 0; }
+  for (int q = 0; q < TW; q++) { m1[q] = 255; m2[q] = 255; sg[q] = 0; }
   // Pass 1: the extrinsics' bytes, their signs and two least magnitudes.
   auto acc = [&](int q, int v) {
     const int b = sat127(v), a = abs(b);
@@ -174,13 +182,13 @@ __device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lan
     const int16_t *col = L + (cs >> 8) * 128;
     const int8_t *Re = Rr + e * 128;
 #pragma unroll
-    for (int q = 0; q < 4; q++) { const int i = lane + 32 * q; acc(q, col[(i - sh) & 127] - Re[i]); }
+    for (int q = 0; q < TW; q++) { const int i = lane + 32 * (T0 + q); acc(q, col[(i - sh) & 127] - Re[i]); }
   }
   {
     const int8_t *Re = Rr + nd * 128;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int i = lane + 32 * q;
+    for (int q = 0; q < TW; q++) {
+      const int i = lane + 32 * (T0 + q);
       int v;
       if (r > 0) v = Lp[(r - 1) * 128 + i] - Re[i];
       else v = (i == 0) ? 8191 : Lp[(T::MB - 1) * 128 + i - 1] - Re[i];
@@ -188,11 +196,11 @@ __device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lan
     }
     Re += 128;
 #pragma unroll
-    for (int q = 0; q < 4; q++) { const int i = lane + 32 * q; acc(q, Lp[r * 128 + i] - Re[i]); }
+    for (int q = 0; q < TW; q++) { const int i = lane + 32 * (T0 + q); acc(q, Lp[r * 128 + i] - Re[i]); }
   }
-  int s1[4], s2[4];
+  int s1[TW], s2[TW];
 #pragma unroll
-  for (int q = 0; q < 4; q++) { s1[q] = min(127, (m1[q] * 13) >> 4); s2[q] = min(127, (m2[q] * 13) >> 4); }
+  for (int q = 0; q < TW; q++) { s1[q] = min(127, (m1[q] * 13) >> 4); s2[q] = min(127, (m2[q] * 13) >> 4); }
   // Pass 2: new messages and posteriors.
   auto upd = [&](int q, int v, int8_t *rp, int16_t *lp) {
     const int b = sat127(v), a = abs(b);
@@ -206,8 +214,8 @@ __device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lan
     int16_t *col = L + (cs >> 8) * 128;
     int8_t *Re = Rr + e * 128;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int i = lane + 32 * q;
+    for (int q = 0; q < TW; q++) {
+      const int i = lane + 32 * (T0 + q);
       int16_t *lp = col + ((i - sh) & 127);
       upd(q, *lp - Re[i], Re + i, lp);
     }
@@ -215,53 +223,67 @@ __device__ __forceinline__ void layer_loop(int16_t *L, int8_t *R, int r, int lan
   {
     int8_t *Re = Rr + nd * 128;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int i = lane + 32 * q;
+    for (int q = 0; q < TW; q++) {
+      const int i = lane + 32 * (T0 + q);
       if (r > 0) { int16_t *lp = Lp + (r - 1) * 128 + i; upd(q, *lp - Re[i], Re + i, lp); }
       else if (i != 0) { int16_t *lp = Lp + (T::MB - 1) * 128 + i - 1; upd(q, *lp - Re[i], Re + i, lp); }
     }
     Re += 128;
 #pragma unroll
-    for (int q = 0; q < 4; q++) { const int i = lane + 32 * q; int16_t *lp = Lp + r * 128 + i; upd(q, *lp - Re[i], Re + i, lp); }
+    for (int q = 0; q < TW; q++) { const int i = lane + 32 * (T0 + q); int16_t *lp = Lp + r * 128 + i; upd(q, *lp - Re[i], Re + i, lp); }
   }
 }
 
-// Violated checks over the whole code, summed over the warp.
-template <int C>
-__device__ __forceinline__ int unsat(const int16_t *L, int lane) {
+// Violated checks over the whole code, summed over the warp (count = 1); or, with count = 0, 1 as soon as a block
+// row holds a violated check and 0 if none does (the reference's layers_clear, liblizard/src/ldpc.c:930-949), the
+// rows tested in the order the iteration updated them (rev: last row first), which finds a violated one soonest.
+template <int C, int TW>
+__device__ __forceinline__ int unsat(const int16_t *L, int lane, int T0, int count, int rev) {
   using T = Code<C>;
   constexpr int NDM = T::NDMAX;
   const DevCode &cd = c_codes[C];
   const int16_t *Lp = L + T::K;
   int bad = 0;
-  for (int r = 0; r < T::MB; r++) {
+  for (int k = 0; k < T::MB; k++) {
+    const int r = rev ? T::MB - 1 - k : k;
     const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
     const int prev = r > 0 ? (r - 1) * 128 + lane : (T::MB - 1) * 128 + lane - 1;
-    int x[4];
+    int x[TW];
 #pragma unroll
-    for (int t = 0; t < 4; t++) x[t] = Lp[r * 128 + lane + 32 * t] ^ ((r == 0 && lane + 32 * t == 0) ? 0 : Lp[prev + 32 * t]);
+    for (int t = 0; t < TW; t++) { const int tt = T0 + t; x[t] = Lp[r * 128 + lane + 32 * tt] ^ ((r == 0 && lane + 32 * tt == 0) ? 0 : Lp[prev + 32 * tt]); }
 #pragma unroll
     for (int e = 0; e < NDM; e++) {
       if (e < nd) {
         const int cs = cd.circ[p0 + e], cb = (cs >> 8) * 128, sh = cs & 255;
 #pragma unroll
-        for (int t = 0; t < 4; t++) x[t] ^= L[cb + ((lane + 32 * t - sh) & 127)];
+        for (int t = 0; t < TW; t++) x[t] ^= L[cb + ((lane + 32 * (T0 + t) - sh) & 127)];
       }
     }
 #pragma unroll
-    for (int t = 0; t < 4; t++) bad += x[t] < 0;
+    for (int t = 0; t < TW; t++) bad += x[t] < 0;
+    if (!count && __any_sync(0xffffffffu, bad)) return 1;
   }
-  return __reduce_add_sync(0xffffffffu, bad);
+  return count ? __reduce_add_sync(0xffffffffu, bad) : 0;
+}
+
+// The WPC warps of one codeword meet here between layers (a named barrier a codeword; 0 is __syncthreads').
+template <int WPC>
+__device__ __forceinline__ void group_sync(int g) {
+  if (WPC == 1) __syncwarp();
+  else asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(WPC * 32) : "memory");
 }
 
 template <int C>
-__global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(LdpcLaunch a) {
+__global__ void __launch_bounds__(cta_threads<C>(), 1) ldpc_decode_kernel(LdpcLaunch a) {
   using T = Code<C>;
+  constexpr int WPC = T::WPC, CPL = 4 / WPC, GT = WPC * 32;
+  static_assert(T::WARPS <= 15, "one named barrier a codeword");
   extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int s_item[T::WARPS], s_red[T::WARPS][WPC];
   uint32_t *crc_tab = reinterpret_cast<uint32_t *>(smem);
   uint32_t *crc_k = crc_tab + 256;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int16_t *L = reinterpret_cast<int16_t *>(smem + kCrcBytes + warp * warp_bytes<C>());
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = warp / WPC, sub = warp % WPC, tg = sub * 32 + lane, t0 = sub * CPL;
+  int16_t *L = reinterpret_cast<int16_t *>(smem + kCrcBytes + g * warp_bytes<C>());
   int8_t *R = reinterpret_cast<int8_t *>(L + T::N);
   for (int t = threadIdx.x; t < 256; t += blockDim.x) {
     uint32_t c = (uint32_t)t;
@@ -273,11 +295,12 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
   const int count = a.count_dev ? *a.count_dev : a.count;
 
   for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(a.counter, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
+    if (tg == 0) s_item[g] = atomicAdd(a.counter, 1);
+    group_sync<WPC>(g);
+    const int item = s_item[g];
+    group_sync<WPC>(g);   // every warp of the codeword has read it before its next write
     if (item >= count) break;
-    int cw, g = 0;
+    int cw, gi = 0;
     int64_t off = 0;
     if (a.rx.llrf) {
       // Receiver mode: item -> (frame, block) of this tier. A declined block is not tried (its -2). Otherwise its
@@ -285,54 +308,65 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
       // bits at 0 and the 7/8 code's known zeros past the block's 3840 bits at 127
       // (liblizard/src/lizard_phy.c:156-192, 1818-1823).
       const int f = item / a.fd.tier_blocks[a.tier], b = a.fd.tier_first[a.tier] + item % a.fd.tier_blocks[a.tier];
-      g = f * a.fd.blocks + b;
-      cw = g;
-      if (a.rx.decl[g]) {
-        if (lane == 0) { a.its[g] = -2; a.ok[g] = 0; }
+      gi = f * a.fd.blocks + b;
+      cw = gi;
+      if (a.rx.decl[gi]) {
+        if (tg == 0) { a.its[gi] = -2; a.ok[gi] = 0; }
         continue;
       }
       const int s0 = a.fd.block_slot[b], nt = a.fd.tier_nt[a.tier];
       const int8_t *sl = a.rx.llrf + f * a.rx.llr_stride + s0;
       const uint8_t *wh = a.fd.white + s0;
       const int16_t *perm = a.fd.perm[a.tier];
-      for (int i = lane; i < nt; i += 32) {
+      for (int i = tg; i < nt; i += GT) {
         const int v = perm[i];
         const int8_t x = sl[i];
         const int8_t y = wh[i] ? (int8_t)(-x) : x;
         if (v < T::K) L[v] = y;
         else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = y; }
       }
-      for (int v = LIZG_INFO_BITS + lane; v < T::K; v += 32) L[v] = 127;
+      for (int v = LIZG_INFO_BITS + tg; v < T::K; v += GT) L[v] = 127;
     } else {
       cw = a.list[item];
       off = a.off[cw];
       // LLRs in: data bits in code order, parity bit k + c (c = i mb + r) at [r][i].
       const int4 *src = reinterpret_cast<const int4 *>(a.llr + off);
-      for (int t = lane; t < T::N / 16; t += 32) {
+      for (int t = tg; t < T::N / 16; t += GT) {
         const int4 w = __ldg(src + t);
-        const int8_t *b = reinterpret_cast<const int8_t *>(&w);
+        const int8_t *bb = reinterpret_cast<const int8_t *>(&w);
 #pragma unroll
         for (int j = 0; j < 16; j++) {
           const int v = t * 16 + j;
-          if (v < T::K) L[v] = b[j];
-          else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = b[j]; }
+          if (v < T::K) L[v] = bb[j];
+          else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = bb[j]; }
         }
       }
     }
     // messages cleared
     int4 *rz = reinterpret_cast<int4 *>(R);
-    for (int t = lane; t < slots<C>() * 128 / 16; t += 32) rz[t] = make_int4(0, 0, 0, 0);
-    __syncwarp();
+    for (int t = tg; t < slots<C>() * 128 / 16; t += GT) rz[t] = make_int4(0, 0, 0, 0);
+    group_sync<WPC>(g);
 
     int used = -1, first = 0;
     for (int it = 0; it < a.max_iter; it++) {
       for (int step = 0; step < T::MB; step++) {
         const int r = (it & 1) ? T::MB - 1 - step : step;
-        if (T::NDMAX > 16) layer_loop<C>(L, R, r, lane);
-        else layer<C>(L, R, r, lane);
-        __syncwarp();
+        // the 7/8 code's 21-circulant rows run faster in the loop form
+        if (T::NDMAX > 16) layer_loop<C, CPL>(L, R, r, lane, t0);
+        else layer<C, CPL>(L, R, r, lane, t0);
+        group_sync<WPC>(g);
       }
-      const int bad = unsat<C>(L, lane);
+      // the count only where the stall rule reads it (after the first iteration and at stall_it), else a clear test
+      const bool counted = a.stall_it > 1 && (it == 0 || it == a.stall_it - 1);
+      int bad = unsat<C, CPL>(L, lane, t0, counted, it & 1);
+      if (WPC > 1) {
+        if (lane == 0) s_red[g][sub] = bad;
+        group_sync<WPC>(g);
+        bad = 0;
+#pragma unroll
+        for (int w = 0; w < WPC; w++) bad += s_red[g][w];
+        group_sync<WPC>(g);
+      }
       if (bad == 0) { used = it + 1; break; }
       if (a.stall_it > 1 && it == a.stall_it - 1) {
         if ((float)bad > __fmul_rn(a.stall_ratio, (float)first)) { used = -3; break; }
@@ -341,7 +375,7 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
 
     // Hard bits packed MSB first into the message area (no longer needed), then the CRC over the block's bytes.
     uint8_t *pk = reinterpret_cast<uint8_t *>(R);
-    for (int j = lane; j < T::N / 8; j += 32) {
+    for (int j = tg; j < T::N / 8; j += GT) {
       int byte = 0;
 #pragma unroll
       for (int t = 0; t < 8; t++) {
@@ -353,28 +387,29 @@ __global__ void __launch_bounds__(Code<C>::WARPS * 32, 1) ldpc_decode_kernel(Ldp
       }
       pk[j] = (uint8_t)byte;
     }
-    __syncwarp();
-    const int s0 = 15 * lane, s1 = min(s0 + 15, kBlockBytes);
-    uint32_t c = 0;
-    for (int j = s0; j < s1; j++) c = crc_tab[(c ^ pk[j]) & 255u] ^ (c >> 8);
-    c = gf_mul(c, crc_k[lane]);
+    group_sync<WPC>(g);
+    if (sub == 0) {
+      const int s0 = 15 * lane, s1 = min(s0 + 15, kBlockBytes);
+      uint32_t c = 0;
+      for (int j = s0; j < s1; j++) c = crc_tab[(c ^ pk[j]) & 255u] ^ (c >> 8);
+      c = gf_mul(c, crc_k[lane]);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) c ^= __shfl_xor_sync(0xffffffffu, c, o);
-    const uint32_t crc = ~(c ^ crc_k[32]);
-    const uint32_t want = (uint32_t)pk[476] << 24 | (uint32_t)pk[477] << 16 | (uint32_t)pk[478] << 8 | pk[479];
-
+      for (int o = 16; o > 0; o >>= 1) c ^= __shfl_xor_sync(0xffffffffu, c, o);
+      const uint32_t crc = ~(c ^ crc_k[32]);
+      const uint32_t want = (uint32_t)pk[476] << 24 | (uint32_t)pk[477] << 16 | (uint32_t)pk[478] << 8 | pk[479];
+      // the batch reports the CRC of whatever was decided; the receiver verifies only decoded blocks (its > 0)
+      if (lane == 0) { a.its[cw] = used; a.ok[cw] = (a.rx.llrf ? used > 0 : true) && crc == want; }
+    }
     if (a.rx.llrf) {
       // the block's 476 bytes, verified or not (ok says which)
-      uint8_t *dst = a.rx.blocks + (int64_t)g * kBlockBytes;
-      for (int t = lane; t < kBlockBytes; t += 32) dst[t] = pk[t];
+      uint8_t *dst = a.rx.blocks + (int64_t)gi * kBlockBytes;
+      for (int t = tg; t < kBlockBytes; t += GT) dst[t] = pk[t];
     } else {
       int4 *dst = reinterpret_cast<int4 *>(a.bits + off / 8);
       const int4 *pv = reinterpret_cast<const int4 *>(pk);
-      for (int t = lane; t < T::N / 128; t += 32) dst[t] = pv[t];
+      for (int t = tg; t < T::N / 128; t += GT) dst[t] = pv[t];
     }
-    // the batch reports the CRC of whatever was decided; the receiver verifies only decoded blocks (its > 0)
-    if (lane == 0) { a.its[cw] = used; a.ok[cw] = (a.rx.llrf ? used > 0 : true) && crc == want; }
-    __syncwarp();
+    group_sync<WPC>(g);
   }
 }
 
@@ -415,7 +450,7 @@ static cudaError_t launch_one(const LdpcLaunch &a, int sms, cudaStream_t st) {
   }
   const int need = (a.count + Code<C>::WARPS - 1) / Code<C>::WARPS;
   const int grid = need < sms ? need : sms;
-  ldpc_decode_kernel<C><<<grid, Code<C>::WARPS * 32, cta_smem<C>(), st>>>(a);
+  ldpc_decode_kernel<C><<<grid, cta_threads<C>(), cta_smem<C>(), st>>>(a);
   return cudaGetLastError();
 }
 
