@@ -30,7 +30,7 @@ template <int C> struct Code;
 template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, NDMAX = 21, WARPS = 9, WPC = 2; };
 template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, NDMAX = 14, WARPS = 7, WPC = 2; };
 template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, NDMAX = 10, WARPS = 6, WPC = 2; };
-template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5, WPC = 2; };
+template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5, WPC = 4; };
 
 template <int C> __host__ __device__ constexpr int slots() { return Code<C>::NDATA + 2 * Code<C>::MB; }
 // A warp's state: posteriors (N int16) then messages (slots x 128 int8), rounded to 16 bytes.
