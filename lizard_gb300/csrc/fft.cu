@@ -57,25 +57,27 @@ __device__ __forceinline__ void dft5(float2 *v) {
 
 // L lines of n points (line l at a + l n) transformed along their length; b is as large as a. The passes alternate
 // between the two; the result's buffer is returned. Every thread of the CTA takes part.
+// n / d for n < 2^16 by the pass's precomputed reciprocal m = ceil(2^32 / d) (m = 0: d = 1).
+__device__ __forceinline__ int fdiv(int n, uint32_t m) { return m ? (int)__umulhi((uint32_t)n, m) : n; }
+
 __device__ float2 *fft_lines(float2 *a, float2 *b, int L, const FftDev &xd) {
   const int N = xd.n, tid = threadIdx.x, nth = blockDim.x;
-  int Ns = 1;
   for (int s = 0; s < xd.nstages; s++) {
-    const int R = xd.radix[s], NR = N / R, step = N / (Ns * R);
+    const int R = xd.radix[s], NR = xd.nr[s], Ns = xd.ns[s], step = N / (Ns * R);
+    const uint32_t mnr = xd.mnr[s], mns = xd.mns[s];
     for (int t = tid; t < L * NR; t += nth) {
-      const int l = t / NR, j = t - l * NR, k = j % Ns;
+      const int l = fdiv(t, mnr), j = t - l * NR, jq = fdiv(j, mns), k = j - jq * Ns;
       const float2 *in = a + l * N;
       float2 *out = b + l * N;
       float2 v[5];
       v[0] = in[j];
       for (int r = 1; r < R; r++) v[r] = cmul(in[j + r * NR], xd.tw[r * k * step]);
       if (R == 4) dft4(v); else if (R == 2) dft2(v); else if (R == 3) dft3(v); else dft5(v);
-      const int base = (j / Ns) * Ns * R + k;
+      const int base = jq * Ns * R + k;
       for (int r = 0; r < R; r++) out[base + r * Ns] = v[r];
     }
     __syncthreads();
     float2 *x = a; a = b; b = x;
-    Ns *= R;
   }
   return a;
 }
@@ -85,7 +87,7 @@ __device__ float2 *fft_lines(float2 *a, float2 *b, int L, const FftDev &xd) {
 __device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y) {
   if (s.grid) return s.grid[f * s.gstride + (int64_t)y * s.sd.n + x];
   const float *H = s.reg + (int64_t)f * s.regstride;
-  return sample_at(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, x, y);
+  return sample_xy(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, s.sd.colt[x], s.sd.rowt[y]);
 }
 
 __device__ __forceinline__ bool in_square(const FftDev &xd, int t) {

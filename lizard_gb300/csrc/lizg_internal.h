@@ -26,6 +26,10 @@ struct FmtDev {
 // A format's transform tables (row b), passed by value to the transform kernels.
 struct FftDev {
   int n, nstages, radix[8], vrows;   // the Stockham passes' radices; rows v kept (the used coefficients' v <= vrows - 1)
+  // per pass: NR = n / radix, Ns = the product of the passes before, and their reciprocals ceil(2^32 / d) for exact
+  // division of numerators below 2^16 by one multiply-high (0 stands for a divisor of 1)
+  int nr[8], ns[8];
+  uint32_t mnr[8], mns[8];
   const float2 *tw;                  // e^{-2 pi i t / n}, t < n
   const float *cx, *qx;              // detrend basis
   const float2 *x1, *x2;             // their DFTs
@@ -39,6 +43,11 @@ struct SampleDev {
   int n, nx, ny;
   float g0, step;                    // margin + 0.5 / scale, 1 / scale (floats, as the reference computes them)
   const float *node_x, *node_y;      // node centres' module coordinates
+  // per picture column x: its module coordinate mx, mesh cell i and 1 / (node_x[i + 1] - node_x[i]); per row y: my,
+  // mesh cell j and the row's place v in it. Built once a format by sample_tables_kernel with the walk's own float
+  // operations, so reading them gives the walk's values.
+  const float4 *colt;                // (mx, i as float bits, inv, 0)
+  const float4 *rowt;                // (my, j as float bits, v, 0)
 };
 
 // Where the transform reads a frame's picture samples from: a grid (grid set; frame f at grid + f gstride, row-major
@@ -93,6 +102,7 @@ cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, double *
                        float2 *Y, float2 *T, cudaStream_t st);
 cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, int w, int h, int pitch, int64_t fstride,
                           const float *reg, int regstride, float *grid, cudaStream_t st);
+cudaError_t sample_tables_launch(SampleDev sd, float4 *colt, float4 *rowt, cudaStream_t st);
 // The node lattice of a layout of side modules (liblizard/src/layout.c:110-117): returns nx (= ny).
 int layout_nodes(int side, float *pos);
 cudaError_t gather_coef_launch(const float2 *T, int64_t tstride, const int32_t *tix, int need, int frames, float2 *coef, cudaStream_t st);

@@ -32,6 +32,7 @@ struct lizg_rx {
   float *grid = nullptr;              // sampled pictures (luma input)
   lizg::SampleDev sd{};
   float *node_xy = nullptr;
+  float4 *sample_t = nullptr;
   float2 *Y = nullptr, *T = nullptr;
   // per-tier streams, forked from and joined to the caller's
   cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -122,6 +123,11 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
     while (m % 2 == 0) { xd.radix[xd.nstages++] = 2; m /= 2; }
     while (m % 3 == 0) { xd.radix[xd.nstages++] = 3; m /= 3; }
     while (m % 5 == 0) { xd.radix[xd.nstages++] = 5; m /= 5; }
+    auto recip = [](int d) { return d == 1 ? 0u : (uint32_t)((((uint64_t)1 << 32) + (uint64_t)d - 1) / (uint64_t)d); };
+    for (int st = 0, ns = 1; st < xd.nstages; ns *= xd.radix[st], st++) {
+      xd.nr[st] = n / xd.radix[st]; xd.ns[st] = ns;
+      xd.mnr[st] = recip(xd.nr[st]); xd.mns[st] = recip(ns);
+    }
     std::vector<float2> tw(n), x1(n), x2(n);
     for (int t = 0; t < n; t++) {
       const double th = -2.0 * 3.14159265358979323846 * t / n;
@@ -146,6 +152,12 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
     r->sd.n = n; r->sd.nx = nn; r->sd.ny = nn;
     r->sd.g0 = lizg::kMargin + 0.5f / f.scale; r->sd.step = 1.0f / f.scale;
     r->sd.node_x = r->node_xy; r->sd.node_y = r->node_xy + nn;
+    ok(dev_alloc(r, &r->sample_t, 2 * (size_t)n));
+    if (e == cudaSuccess) {
+      r->sd.colt = r->sample_t; r->sd.rowt = r->sample_t + n;
+      ok(lizg::sample_tables_launch(r->sd, r->sample_t, r->sample_t + n, nullptr));
+      ok(cudaDeviceSynchronize());
+    }
   }
   const size_t F = (size_t)max_frames;
   ok(dev_alloc(r, &r->grid, F * n * n));

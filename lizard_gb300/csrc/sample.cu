@@ -21,7 +21,17 @@ __global__ void __launch_bounds__(256) sample_kernel(SampleDev sd, const uint8_t
   const int n = sd.n;
   if (x >= n || y >= n) return;
   const float *H = reg + (int64_t)f * regstride;
-  grid[(int64_t)f * n * n + (int64_t)y * n + x] = sample_at(sd, luma + f * fstride, w, h, pitch, H, H + 9, x, y);
+  grid[(int64_t)f * n * n + (int64_t)y * n + x] = sample_xy(sd, luma + f * fstride, w, h, pitch, H, H + 9, sd.colt[x], sd.rowt[y]);
+}
+
+__global__ void sample_tables_kernel(SampleDev sd, float4 *colt, float4 *rowt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < sd.n) { colt[t] = sample_col(sd, t); rowt[t] = sample_row(sd, t); }
+}
+
+cudaError_t sample_tables_launch(SampleDev sd, float4 *colt, float4 *rowt, cudaStream_t st) {
+  sample_tables_kernel<<<(sd.n + 255) / 256, 256, 0, st>>>(sd, colt, rowt);
+  return cudaGetLastError();
 }
 
 cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, int w, int h, int pitch, int64_t fstride,

@@ -15,18 +15,30 @@ __device__ __forceinline__ int node_cell(const float *node, int nn, float m) {
   return k;
 }
 
-// Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh.
-__device__ __forceinline__ float sample_at(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
-                                           const float *nodes, int x, int y) {
-  const float mx = __fadd_rn(sd.g0, __fmul_rn((float)x, sd.step)), my = __fadd_rn(sd.g0, __fmul_rn((float)y, sd.step));
-  const int j = node_cell(sd.node_y, sd.ny, my), i = node_cell(sd.node_x, sd.nx, mx);
-  const float v = __fdiv_rn(__fsub_rn(my, sd.node_y[j]), __fsub_rn(sd.node_y[j + 1], sd.node_y[j])), omv = __fsub_rn(1.0f, v);
+// The format's per-column and per-row quantities of the walk (liblizard/src/acquire.c:5131-5140, 5160-5166).
+__device__ __forceinline__ float4 sample_col(const SampleDev &sd, int x) {
+  const float mx = __fadd_rn(sd.g0, __fmul_rn((float)x, sd.step));
+  const int i = node_cell(sd.node_x, sd.nx, mx);
+  return make_float4(mx, __int_as_float(i), __fdiv_rn(1.0f, __fsub_rn(sd.node_x[i + 1], sd.node_x[i])), 0.0f);
+}
+__device__ __forceinline__ float4 sample_row(const SampleDev &sd, int y) {
+  const float my = __fadd_rn(sd.g0, __fmul_rn((float)y, sd.step));
+  const int j = node_cell(sd.node_y, sd.ny, my);
+  return make_float4(my, __int_as_float(j), __fdiv_rn(__fsub_rn(my, sd.node_y[j]), __fsub_rn(sd.node_y[j + 1], sd.node_y[j])), 0.0f);
+}
+
+// Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh,
+// given the column's and the row's table entries.
+__device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
+                                           const float *nodes, float4 ct, float4 rt) {
+  const float mx = ct.x, inv = ct.z, my = rt.x, v = rt.z, omv = __fsub_rn(1.0f, v);
+  const int i = __float_as_int(ct.y), j = __float_as_int(rt.y);
   const float *n00 = nodes + 2 * (j * sd.nx + i), *n10 = n00 + 2, *n01 = n00 + 2 * sd.nx, *n11 = n01 + 2;
-  const float inv = __fdiv_rn(1.0f, __fsub_rn(sd.node_x[i + 1], sd.node_x[i]));
+  const float nxi = sd.node_x[i];
   const float ex = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[0], n00[0]), omv), __fmul_rn(__fsub_rn(n11[0], n01[0]), v)), inv);
-  const float cx = __fsub_rn(__fadd_rn(__fmul_rn(n00[0], omv), __fmul_rn(n01[0], v)), __fmul_rn(ex, sd.node_x[i]));
+  const float cx = __fsub_rn(__fadd_rn(__fmul_rn(n00[0], omv), __fmul_rn(n01[0], v)), __fmul_rn(ex, nxi));
   const float ey = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[1], n00[1]), omv), __fmul_rn(__fsub_rn(n11[1], n01[1]), v)), inv);
-  const float cy = __fsub_rn(__fadd_rn(__fmul_rn(n00[1], omv), __fmul_rn(n01[1], v)), __fmul_rn(ey, sd.node_x[i]));
+  const float cy = __fsub_rn(__fadd_rn(__fmul_rn(n00[1], omv), __fmul_rn(n01[1], v)), __fmul_rn(ey, nxi));
   const float kw = __fadd_rn(__fmul_rn(H[7], my), 1.0f), ku = __fadd_rn(__fmul_rn(H[1], my), H[2]), kv = __fadd_rn(__fmul_rn(H[4], my), H[5]);
   const float rw = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(H[6], mx), kw));
   const float pu = __fmul_rn(__fadd_rn(__fmul_rn(H[0], mx), ku), rw), pv = __fmul_rn(__fadd_rn(__fmul_rn(H[3], mx), kv), rw);
