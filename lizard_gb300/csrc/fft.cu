@@ -1,18 +1,25 @@
 // Row (b) of the hot path on sm_103a: the anchors' erase, the detrend projections and the 2D mixed-radix FFT of the
 // n x n picture grid, restated from the reference's decode (liblizard/src/lizard_phy.c:1596-1716) for the GPU.
 //
-// Three kernels a batch:
-//   hole_fit_kernel   one CTA a frame: the shading surface's right-hand side over every eighth sample outside the
-//                     anchors' squares, times the inverse normal matrix: beta (6 doubles a frame);
-//   fft_cols_kernel   a CTA takes 8 picture columns of a frame (4 complex lines: column x0 + j real, x0 + 4 + j
-//                     imaginary), erases the anchors' squares as it loads them (beta's surface), sums each column's
-//                     detrend moments, transforms the 4 lines along y in shared memory and separates the two real
-//                     columns of each, writing Y[v][x] for the kept rows v (the used coefficients' v < vrows);
-//   fft_rows_kernel   a CTA takes 4 kept rows v of a frame, reduces the columns' moments to the five projections,
-//                     transforms along x and subtracts the surface's spectrum (the xy term everywhere, the x terms
-//                     on v = 0, the y terms on u = 0), writing T[v][u].
-// The transforms are Stockham autosort passes of radix 4, 2, 3 and 5 (every ladder size is 2^a 3^b 5^c) over
-// shared-memory ping-pong buffers, twiddles from a table computed in double. FP32 throughout, as the reference's.
+// Four kernels a batch:
+//   hole_rhs_kernel   a CTA takes a band of the frame's every-eighth-sample rows: the shading fit's right-hand side
+//                     over the samples outside the anchors' squares, one partial sum a band (6 doubles);
+//   fft_cols_kernel   a CTA takes 2L picture columns of a frame (L complex lines: column x0 + l real, x0 + L + l
+//                     imaginary), forms the shading surface beta from the bands' partials, erases the anchors' squares
+//                     as it loads them, sums each column's detrend moments, transforms the L lines along y in shared
+//                     memory and separates the two real columns of each, writing Y[v][x] for the kept rows v;
+//   fac_kernel        one CTA a frame: the five projections from the columns' moments, then the surface spectrum's
+//                     per-column and per-row factors (the double products the reference rounds to float);
+//   fft_rows_kernel   a CTA takes L kept rows v of a frame, transforms along x and subtracts the surface's spectrum
+//                     (the xy term everywhere, the x terms on v = 0, the y terms on u = 0), writing T[v][u].
+// L is the most lines of n points that fit 6144 complex points (so every CTA holds about the same 48 KB of samples).
+//
+// The transforms are Stockham autosort passes of radix 16, 9, 8, 6, 5, 4, 3 or 2 (every ladder size takes three),
+// each pass in place: every thread reads its butterflies' points into registers, the CTA waits, every thread writes
+// its outputs. Shared memory holds a line with one spare slot after every 16 points (so the passes' 16-point runs,
+// read or written, fall on distinct banks within a half-warp) and lines 4 (mod 16) slots apart; the passes'
+// twiddles sit beside the lines, per pass [r - 1][k], so a warp reads consecutive entries. FP32 throughout, as the
+// reference's; the twiddles and the surface factors are worked out in double.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "lizg_internal.h"
@@ -20,19 +27,27 @@
 
 namespace lizg {
 
+constexpr int kThreads = 384;   // threads of a transform CTA
+constexpr int kHoleBand = 16;   // every-eighth-sample rows a hole_rhs CTA takes
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 
-// Forward DFTs (e^{-i}) of 2, 3, 4 and 5 points in place.
-__device__ __forceinline__ void dft2(float2 *v) { const float2 a = v[0], b = v[1]; v[0] = cadd(a, b); v[1] = csub(a, b); }
-__device__ __forceinline__ void dft4(float2 *v) {
+// A point's slot in its line: one spare slot after every 16.
+__device__ __forceinline__ int pad(int p) { return p + (p >> 4); }
+
+// Forward DFTs (e^{-i}) of R points in place.
+template <int R> __device__ __forceinline__ void dft(float2 *v);
+
+template <> __device__ __forceinline__ void dft<2>(float2 *v) { const float2 a = v[0], b = v[1]; v[0] = cadd(a, b); v[1] = csub(a, b); }
+template <> __device__ __forceinline__ void dft<4>(float2 *v) {
   const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]), s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
   v[0] = cadd(s02, s13); v[2] = csub(s02, s13);
   v[1] = make_float2(d02.x + d13.y, d02.y - d13.x);   // d02 - i d13
   v[3] = make_float2(d02.x - d13.y, d02.y + d13.x);   // d02 + i d13
 }
-__device__ __forceinline__ void dft3(float2 *v) {
+template <> __device__ __forceinline__ void dft<3>(float2 *v) {
   const float s3 = 0.86602540378443864676f;
   const float2 a = v[0], t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
   const float2 m = make_float2(a.x - 0.5f * t.x, a.y - 0.5f * t.y);
@@ -40,7 +55,7 @@ __device__ __forceinline__ void dft3(float2 *v) {
   v[1] = make_float2(m.x + s3 * d.y, m.y - s3 * d.x);   // m - i s3 d
   v[2] = make_float2(m.x - s3 * d.y, m.y + s3 * d.x);   // m + i s3 d
 }
-__device__ __forceinline__ void dft5(float2 *v) {
+template <> __device__ __forceinline__ void dft<5>(float2 *v) {
   const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;   // cos 2pi/5, cos 4pi/5
   const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;    // sin 2pi/5, sin 4pi/5
   const float2 a = v[0], p1 = cadd(v[1], v[4]), m1 = csub(v[1], v[4]), p2 = cadd(v[2], v[3]), m2 = csub(v[2], v[3]);
@@ -55,39 +70,137 @@ __device__ __forceinline__ void dft5(float2 *v) {
   v[3] = make_float2(r2.x - q2.y, r2.y + q2.x);
 }
 
-// L lines of n points (line l at a + l n) transformed along their length; b is as large as a. The passes alternate
-// between the two; the result's buffer is returned. Every thread of the CTA takes part.
-// n / d for n < 2^16 by the pass's precomputed reciprocal m = ceil(2^32 / d) (m = 0: d = 1).
-__device__ __forceinline__ int fdiv(int n, uint32_t m) { return m ? (int)__umulhi((uint32_t)n, m) : n; }
+// e^{-2 pi i m / R} for the m a composite DFT turns by that are not eighth turns.
+template <int R> __device__ __forceinline__ float2 wconst(int m);
+template <> __device__ __forceinline__ float2 wconst<16>(int m) {
+  return m == 1 ? make_float2(0.92387953251128673848f, -0.38268343236508978178f)
+       : m == 3 ? make_float2(0.38268343236508983729f, -0.92387953251128673848f)
+                : make_float2(-0.92387953251128684951f, 0.38268343236508967076f);   // m = 9
+}
+template <> __device__ __forceinline__ float2 wconst<8>(int) { return make_float2(1.0f, 0.0f); }   // every turn of 8 is an eighth
+template <> __device__ __forceinline__ float2 wconst<6>(int m) {
+  return m == 1 ? make_float2(0.5f, -0.86602540378443864676f) : make_float2(-0.5f, -0.86602540378443864676f);   // m = 2
+}
+template <> __device__ __forceinline__ float2 wconst<9>(int m) {
+  return m == 1 ? make_float2(0.76604444311897801345f, -0.64278760968653925190f)
+       : m == 2 ? make_float2(0.17364817766693041445f, -0.98480775301220802032f)
+                : make_float2(-0.93969262078590831688f, -0.34202014332566887944f);   // m = 4
+}
+// a e^{-2 pi i m / R} for a constant m (after unrolling): quarter and eighth turns by adds, the rest by cos/sin.
+template <int R> __device__ __forceinline__ float2 twc(float2 a, int m) {
+  m %= R;
+  const float c = 0.70710678118654757274f;
+  if (m == 0) return a;
+  if (4 * m == R) return make_float2(a.y, -a.x);
+  if (2 * m == R) return make_float2(-a.x, -a.y);
+  if (4 * m == 3 * R) return make_float2(-a.y, a.x);
+  if (8 * m == R) return make_float2(c * (a.x + a.y), c * (a.y - a.x));
+  if (8 * m == 3 * R) return make_float2(c * (a.y - a.x), -c * (a.x + a.y));
+  return cmul(a, wconst<R>(m));
+}
 
-__device__ float2 *fft_lines(float2 *a, float2 *b, int L, const FftDev &xd) {
-  const int N = xd.n, tid = threadIdx.x, nth = blockDim.x;
-  for (int s = 0; s < xd.nstages; s++) {
-    const int R = xd.radix[s], NR = xd.nr[s], Ns = xd.ns[s], step = N / (Ns * R);
-    const uint32_t mnr = xd.mnr[s], mns = xd.mns[s];
-    for (int t = tid; t < L * NR; t += nth) {
-      const int l = fdiv(t, mnr), j = t - l * NR, jq = fdiv(j, mns), k = j - jq * Ns;
-      const float2 *in = a + l * N;
-      float2 *out = b + l * N;
-      float2 v[5];
-      v[0] = in[j];
-      for (int r = 1; r < R; r++) v[r] = cmul(in[j + r * NR], xd.tw[r * k * step]);
-      if (R == 4) dft4(v); else if (R == 2) dft2(v); else if (R == 3) dft3(v); else dft5(v);
-      const int base = jq * Ns * R + k;
-      for (int r = 0; r < R; r++) out[base + r * Ns] = v[r];
-    }
-    __syncthreads();
-    float2 *x = a; a = b; b = x;
+// R = P Q points by P-point DFTs over the Q interleaved subsequences, twiddles, then Q-point DFTs:
+// X[k1 + P k2] = sum_n2 W_Q^{n2 k2} W_R^{n2 k1} sum_n1 x[Q n1 + n2] W_P^{n1 k1}.
+template <int P, int Q> __device__ __forceinline__ void dft_pq(float2 *x) {
+  constexpr int R = P * Q;
+  float2 a[Q][P];
+#pragma unroll
+  for (int n2 = 0; n2 < Q; n2++) {
+#pragma unroll
+    for (int n1 = 0; n1 < P; n1++) a[n2][n1] = x[Q * n1 + n2];
+    dft<P>(a[n2]);
+#pragma unroll
+    for (int k1 = 1; k1 < P; k1++) a[n2][k1] = twc<R>(a[n2][k1], n2 * k1);
   }
-  return a;
+#pragma unroll
+  for (int k1 = 0; k1 < P; k1++) {
+    float2 b[Q];
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) b[n2] = a[n2][k1];
+    dft<Q>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) x[k1 + P * k2] = b[k2];
+  }
+}
+template <> __device__ __forceinline__ void dft<8>(float2 *v) { dft_pq<4, 2>(v); }
+template <> __device__ __forceinline__ void dft<16>(float2 *v) { dft_pq<4, 4>(v); }
+template <> __device__ __forceinline__ void dft<6>(float2 *v) { dft_pq<3, 2>(v); }
+template <> __device__ __forceinline__ void dft<9>(float2 *v) { dft_pq<3, 3>(v); }
+
+// The transform plan of each ladder size: three passes' radices and the lines a CTA holds (the most lines of n
+// points within kFftPoints, n a multiple of twice that). Host and device read the same table.
+struct Plan {
+  int r0, r1, r2, lines;
+};
+__host__ __device__ constexpr Plan plan_of(int n) {
+  return n == 384    ? Plan{16, 8, 3, 16}
+         : n == 512  ? Plan{16, 16, 2, 8}
+         : n == 768  ? Plan{16, 16, 3, 8}
+         : n == 1024 ? Plan{16, 16, 4, 4}
+         : n == 1152 ? Plan{16, 8, 9, 4}
+         : n == 1280 ? Plan{16, 16, 5, 4}
+         : n == 1536 ? Plan{16, 16, 6, 4}
+                     : Plan{0, 0, 0, 0};
+}
+// Slots from one line to the next: the padded line rounded up to 16 slots, plus 4.
+__host__ __device__ constexpr int lstride_of(int n) { return (n + n / 16 + 15) / 16 * 16 + 4; }
+
+// One Stockham pass of radix R over the CTA's lines (Lr <= L of them) in place, n = N points a line. Butterfly j of
+// a line (j < NR = N / R, k = j mod NS) reads points j + r NR, turns point r by e^{-2 pi i r k / (NS R)}
+// (tw[(r - 1) NS + k]) and writes its DFT's output r to (j / NS) NS R + k + r NS. A thread takes butterflies tid,
+// tid + kThreads, ... (at most B = ceil(L NR / kThreads) of them).
+template <int N, int R, int NS, int L>
+__device__ __forceinline__ void pass(float2 *buf, const float2 *tw, int Lr) {
+  constexpr int NR = N / R, LSTR = lstride_of(N), B = (L * NR + kThreads - 1) / kThreads;
+  const int total = Lr * NR;
+  float2 v[B][R];
+#pragma unroll
+  for (int b = 0; b < B; b++) {
+    const int t = threadIdx.x + b * kThreads;
+    if (t < total) {
+      const int l = t / NR, j = t - l * NR, k = j % NS;
+      const float2 *in = buf + l * LSTR;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[b][r] = in[pad(j + r * NR)];
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; r++) v[b][r] = cmul(v[b][r], tw[NS - 1 + (r - 1) * NS + k]);
+      }
+      dft<R>(v[b]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < B; b++) {
+    const int t = threadIdx.x + b * kThreads;
+    if (t < total) {
+      const int l = t / NR, j = t - l * NR, jq = j / NS, k = j - jq * NS;
+      float2 *out = buf + l * LSTR;
+      const int base = jq * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) out[pad(base + r * NS)] = v[b][r];
+    }
+  }
+  __syncthreads();
+}
+
+// The Lr lines at buf (line l at buf + l lstride_of(N), point p at slot pad(p)) transformed along their N points in
+// place by the size's three passes. tw: the passes' twiddles, pass s's at NS - 1. Every thread of the CTA takes part.
+template <int N>
+__device__ __forceinline__ void fft_lines(float2 *buf, const float2 *tw, int Lr) {
+  constexpr Plan P = plan_of(N);
+  pass<N, P.r0, 1, P.lines>(buf, tw, Lr);
+  pass<N, P.r1, P.r0, P.lines>(buf, tw, Lr);
+  pass<N, P.r2, P.r0 * P.r1, P.lines>(buf, tw, Lr);
 }
 
 // A frame's picture sample (x, y): read from a supplied grid, or sampled straight from the captured frame through
-// its registration (the sampler fused into the pass that reads it).
-__device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y) {
+// its registration (the sampler fused into the pass that reads it). lut, when given, holds k / 255 for the grey
+// levels (the sampler's own divisions, made once a CTA).
+__device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y, const float *lut) {
   if (s.grid) return s.grid[f * s.gstride + (int64_t)y * s.sd.n + x];
   const float *H = s.reg + (int64_t)f * s.regstride;
-  return sample_xy(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, s.sd.colt[x], s.sd.rowt[y]);
+  return sample_xy(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, s.sd.colt[x], s.sd.rowt[y], lut);
 }
 
 __device__ __forceinline__ bool in_square(const FftDev &xd, int t) {
@@ -103,13 +216,16 @@ __device__ __forceinline__ void hole_basis(const FftDev &xd, int x, int y, doubl
   b[0] = 1; b[1] = cx; b[2] = xd.qx[x]; b[3] = cy; b[4] = xd.qx[y]; b[5] = cx * cy;
 }
 
-__global__ void __launch_bounds__(256) hole_fit_kernel(FftDev xd, SrcDev src, double *beta) {
-  const int f = blockIdx.x, n = xd.n, c = n / 8;
+// The shading fit's right-hand side (liblizard/src/lizard_phy.c:1609-1623) over kHoleBand of the frame's
+// every-eighth rows: hole[f][band][0..5].
+__global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, int bands, double *hole) {
+  const int f = blockIdx.x / bands, band = blockIdx.x % bands, n = xd.n, c = n / 8;
+  const int ky0 = band * kHoleBand, ky1 = min(c, ky0 + kHoleBand);
   double rhs[6] = {0, 0, 0, 0, 0, 0};
-  for (int k = threadIdx.x; k < c * c; k += blockDim.x) {
-    const int x = 8 * (k % c), y = 8 * (k / c);
+  for (int k = threadIdx.x; k < (ky1 - ky0) * c; k += blockDim.x) {
+    const int x = 8 * (k % c), y = 8 * (ky0 + k / c);
     if (in_square(xd, x) && in_square(xd, y)) continue;
-    const double v = src_at(src, f, x, y);
+    const double v = src_at(src, f, x, y, nullptr);
     double b[6];
     hole_basis(xd, x, y, b);
     for (int r = 0; r < 6; r++) rhs[r] += b[r] * v;
@@ -121,67 +237,117 @@ __global__ void __launch_bounds__(256) hole_fit_kernel(FftDev xd, SrcDev src, do
     if ((int)threadIdx.x < s) for (int r = 0; r < 6; r++) red[r][threadIdx.x] += red[r][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x < 6) {
-    double acc = 0;
-    for (int k = 0; k < 6; k++) acc += xd.hole_inv[threadIdx.x * 6 + k] * red[k][0];
-    beta[f * 6 + threadIdx.x] = acc;
-  }
+  if (threadIdx.x < 6) hole[((int64_t)f * bands + band) * 6 + threadIdx.x] = red[threadIdx.x][0];
 }
 
-constexpr int kColTile = 8;          // picture columns a column-pass CTA takes (kColTile / 2 complex lines)
-constexpr int kRowTile = 4;          // kept rows a row-pass CTA takes
+// The transform CTA's shared memory: the lines, the twiddles, the moments' reduction, the grey table.
+struct SmemMap {
+  float2 *buf, *tw;
+  double *red;
+  float *lut;
+};
+__host__ __device__ constexpr int smem_bytes_of(int n) {
+  return (plan_of(n).lines * lstride_of(n) + n) * (int)sizeof(float2) + (kThreads / 32) * 6 * plan_of(n).lines * (int)sizeof(double) +
+         256 * (int)sizeof(float);
+}
+template <int N>
+__device__ __forceinline__ SmemMap smem_map(unsigned char *raw) {
+  SmemMap m;
+  m.buf = reinterpret_cast<float2 *>(raw);
+  m.tw = m.buf + plan_of(N).lines * lstride_of(N);
+  m.red = reinterpret_cast<double *>(m.tw + N);
+  m.lut = reinterpret_cast<float *>(m.red + (kThreads / 32) * 6 * plan_of(N).lines);
+  return m;
+}
 
-__global__ void __launch_bounds__(256) fft_cols_kernel(FftDev xd, SrcDev src, const double *beta, double *colsum, float2 *Y) {
-  extern __shared__ float2 sm[];
-  const int n = xd.n, tiles = n / kColTile, f = blockIdx.x / tiles, x0 = (blockIdx.x % tiles) * kColTile;
-  constexpr int L = kColTile / 2;
-  float2 *a = sm, *b = sm + L * n;
-  double bt[6];
-  for (int r = 0; r < 6; r++) bt[r] = beta[f * 6 + r];
-  // load: thread t takes column j = t % 8 at rows y = t / 8, t / 8 + 32, ...; the anchors' squares are erased to
-  // the shading surface as they are read; each column's z, z c(y), z q(y) summed on the way.
-  const int j = threadIdx.x % kColTile, x = x0 + j;
-  const bool xin = in_square(xd, x);
-  float s0 = 0, s1 = 0, s2 = 0;
-  for (int y = threadIdx.x / kColTile; y < n; y += blockDim.x / kColTile) {
-    float v;
-    if (xin && in_square(xd, y)) {
-      double bb[6], h = 0;
-      hole_basis(xd, x, y, bb);
-      for (int r = 0; r < 6; r++) h += bt[r] * bb[r];
-      v = (float)h;
-    } else {
-      v = src_at(src, f, x, y);
-    }
-    s0 += v; s1 += v * xd.cx[y]; s2 += v * xd.qx[y];
-    float2 *dst = a + (j % L) * n + y;
-    if (j < L) dst->x = v; else dst->y = v;
+// The surface's value at (x, y) inside an anchor's square (liblizard/src/lizard_phy.c:341-346).
+__device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta, int x, int y) {
+  double bb[6], h = 0;
+  hole_basis(xd, x, y, bb);
+  for (int r = 0; r < 6; r++) h += beta[r] * bb[r];
+  return (float)h;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev src, int bands, const double *hole, double *colsum, float2 *Y) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
+  const SmemMap sm = smem_map<N>(smraw);
+  const int f = blockIdx.x / tiles, x0 = (blockIdx.x % tiles) * 2 * L;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
+  if (!src.grid) for (int i = tid; i < 256; i += kThreads) sm.lut[i] = __fdiv_rn((float)i, 255.0f);
+  // the shading surface: beta = hole_inv rhs, rhs the bands' partial sums in band order
+  __shared__ double s_rhs[6], s_beta[6];
+  if (tid < 6) {
+    double acc = 0;
+    for (int b = 0; b < bands; b++) acc += hole[((int64_t)f * bands + b) * 6 + tid];
+    s_rhs[tid] = acc;
   }
-  __shared__ double red[3][256];
-  red[0][threadIdx.x] = s0; red[1][threadIdx.x] = s1; red[2][threadIdx.x] = s2;
   __syncthreads();
-  if (threadIdx.x < kColTile) {
-    double t0 = 0, t1 = 0, t2 = 0;
-    for (int k = threadIdx.x; k < (int)blockDim.x; k += kColTile) { t0 += red[0][k]; t1 += red[1][k]; t2 += red[2][k]; }
-    double *cs = colsum + ((int64_t)f * n + x0 + threadIdx.x) * 3;
-    cs[0] = t0; cs[1] = t1; cs[2] = t2;
+  if (tid == 0) {
+#pragma unroll
+    for (int r = 0; r < 6; r++) {
+      double acc = 0;
+#pragma unroll
+      for (int k = 0; k < 6; k++) acc += xd.hole_inv[r * 6 + k] * s_rhs[k];
+      s_beta[r] = acc;
+    }
   }
-  float2 *z = fft_lines(a, b, L, xd);
+  __syncthreads();
+  // load: thread t takes line l = t mod L (columns xa = x0 + l, xb = x0 + L + l) at rows y = t / L, t / L + kThreads / L,
+  // ...; the anchors' squares are erased to the shading surface as they are read; each column's z, z c(y), z q(y)
+  // summed on the way.
+  const int l = tid % L, xa = x0 + l, xb = x0 + L + l;
+  const bool ina = in_square(xd, xa), inb = in_square(xd, xb);
+  float s[6] = {0, 0, 0, 0, 0, 0};
+  float2 *line = sm.buf + l * LSTR;
+  const float *lut = src.grid ? nullptr : sm.lut;
+#pragma unroll 2
+  for (int y = tid / L; y < n; y += ystep) {
+    const bool ysq = (ina || inb) && in_square(xd, y);
+    const float va = ina && ysq ? hole_value(xd, s_beta, xa, y) : src_at(src, f, xa, y, lut);
+    const float vb = inb && ysq ? hole_value(xd, s_beta, xb, y) : src_at(src, f, xb, y, lut);
+    const float cy = __ldg(xd.cx + y), qy = __ldg(xd.qx + y);
+    s[0] += va; s[1] += va * cy; s[2] += va * qy;
+    s[3] += vb; s[4] += vb * cy; s[5] += vb * qy;
+    line[pad(y)] = make_float2(va, vb);
+  }
+  // the moments: the lanes of a line summed by shuffles, then the warps' sums in warp order
+  double d[6];
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    d[q] = s[q];
+    for (int o = L; o < 32; o <<= 1) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
+  }
+  const int warp = tid >> 5, lane = tid & 31;
+  if (lane < L) {
+#pragma unroll
+    for (int q = 0; q < 6; q++) sm.red[(warp * L + lane) * 6 + q] = d[q];
+  }
+  __syncthreads();
+  if (tid < 6 * L) {
+    const int ll = tid / 6, q = tid % 6;
+    double acc = 0;
+    for (int w = 0; w < kThreads / 32; w++) acc += sm.red[(w * L + ll) * 6 + q];
+    const int x = q < 3 ? x0 + ll : x0 + L + ll;
+    colsum[((int64_t)f * n + x) * 3 + q % 3] = acc;
+  }
+  fft_lines<N>(sm.buf, sm.tw, L);
   // separate the two real columns of each line: A(v) = (Z(v) + conj Z(n - v)) / 2, B(v) = -i (Z(v) - conj Z(n - v)) / 2
   float2 *Yf = Y + (int64_t)f * xd.vrows * n;
-  for (int t = threadIdx.x; t < xd.vrows * kColTile; t += blockDim.x) {
-    const int v = t / kColTile, jj = t % kColTile, l = jj % L;
-    const float2 zv = z[l * n + v], zm = z[l * n + (n - v) % n];
-    float2 o;
-    if (jj < L) o = make_float2(0.5f * (zv.x + zm.x), 0.5f * (zv.y - zm.y));
-    else o = make_float2(0.5f * (zv.y + zm.y), -0.5f * (zv.x - zm.x));
-    Yf[(int64_t)v * n + x0 + jj] = o;
+  for (int v = tid / L; v < xd.vrows; v += ystep) {
+    const float2 zv = line[pad(v)], zm = line[pad(v ? n - v : 0)];
+    Yf[(int64_t)v * n + xa] = make_float2(0.5f * (zv.x + zm.x), 0.5f * (zv.y - zm.y));
+    Yf[(int64_t)v * n + xb] = make_float2(0.5f * (zv.y + zm.y), -0.5f * (zv.x - zm.x));
   }
 }
 
 // The five projections of each frame from its columns' moments, normalised (liblizard/src/lizard_phy.c:1584-1591,
-// 1718): px, py, pxy, pxx, pyy.
-__global__ void __launch_bounds__(256) proj_kernel(FftDev xd, const double *colsum, double *proj) {
+// 1697), then the surface spectrum's factors (liblizard/src/lizard_phy.c:1702-1716), rounded to float as there:
+// fac[f] = xy[u] (pxy X1[u]) for u < n, x0[u] (n (px X1[u] + pxx X2[u])) for u < n, y0[v] (n (py X1[v] + pyy X2[v]))
+// for v < vrows.
+__global__ void __launch_bounds__(256) fac_kernel(FftDev xd, const double *colsum, float2 *fac) {
   const int f = blockIdx.x, n = xd.n;
   const double *cs = colsum + (int64_t)f * n * 3;
   double p[5] = {0, 0, 0, 0, 0};
@@ -196,48 +362,47 @@ __global__ void __launch_bounds__(256) proj_kernel(FftDev xd, const double *cols
     if ((int)threadIdx.x < s) for (int r = 0; r < 5; r++) red[r][threadIdx.x] += red[r][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    double *o = proj + 5 * f;
-    o[0] = red[0][0] / (n * xd.sx2); o[1] = red[1][0] / (n * xd.sx2); o[2] = red[2][0] / (xd.sx2 * xd.sx2);
-    o[3] = red[3][0] / (n * xd.sq2); o[4] = red[4][0] / (n * xd.sq2);
+  const double px = red[0][0] / (n * xd.sx2), py = red[1][0] / (n * xd.sx2), pxy = red[2][0] / (xd.sx2 * xd.sx2);
+  const double pxx = red[3][0] / (n * xd.sq2), pyy = red[4][0] / (n * xd.sq2);
+  float2 *o = fac + (int64_t)f * (2 * n + xd.vrows);
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {
+    const float2 x1 = xd.x1[u], x2 = xd.x2[u];
+    o[u] = make_float2((float)(pxy * x1.x), (float)(pxy * x1.y));
+    o[n + u] = make_float2((float)(n * (px * x1.x + pxx * x2.x)), (float)(n * (px * x1.y + pxx * x2.y)));
+  }
+  for (int v = threadIdx.x; v < xd.vrows; v += blockDim.x) {
+    const float2 x1 = xd.x1[v], x2 = xd.x2[v];
+    o[2 * n + v] = make_float2((float)(n * (py * x1.x + pyy * x2.x)), (float)(n * (py * x1.y + pyy * x2.y)));
   }
 }
 
-__global__ void __launch_bounds__(256) fft_rows_kernel(FftDev xd, const double *proj, const float2 *Y, float2 *T) {
-  extern __shared__ float2 sm[];
-  const int n = xd.n, tiles = (xd.vrows + kRowTile - 1) / kRowTile, f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * kRowTile;
-  const int L = min(kRowTile, xd.vrows - v0);
-  float2 *a = sm, *b = sm + kRowTile * n;
-  const float2 *Yf = Y + (int64_t)f * xd.vrows * n;
-  for (int t = threadIdx.x; t < L * n; t += blockDim.x) a[t] = Yf[(int64_t)v0 * n + t];
+template <int N>
+__global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, float2 *T) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N);
+  const SmemMap sm = smem_map<N>(smraw);
+  const int tiles = (xd.vrows + L - 1) / L, f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L;
+  const int Lr = min(L, xd.vrows - v0), tid = threadIdx.x;
+  for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
+  const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
+  for (int l = 0; l < Lr; l++)
+    for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
   __syncthreads();
-  float2 *z = fft_lines(a, b, L, xd);
-  float2 *Tf = T + (int64_t)f * xd.vrows * n;
-  const double *pj = proj + 5 * f;
-  const double px = pj[0], py = pj[1], pxy = pj[2], pxx = pj[3], pyy = pj[4];
-  // the surface's spectrum off (liblizard/src/lizard_phy.c:1697-1716): the xy term's column factor pxy X1[u] worked
-  // out once a u for the CTA's rows, then the x terms on v = 0 and the y terms on u = 0
-  for (int u = threadIdx.x; u < n; u += blockDim.x) {
-    const float2 x1u = xd.x1[u];
-    const float ar = (float)(pxy * x1u.x), ai = (float)(pxy * x1u.y);
-    float2 c0 = make_float2(0, 0);
-    if (v0 == 0) {
-      const float2 x2u = xd.x2[u];
-      c0 = make_float2((float)(n * (px * x1u.x + pxx * x2u.x)), (float)(n * (px * x1u.y + pxx * x2u.y)));
-    }
-    for (int l = 0; l < L; l++) {
+  fft_lines<N>(sm.buf, sm.tw, Lr);
+  float2 *Tf = T + ((int64_t)f * xd.vrows + v0) * n;
+  const float2 *fx = fac + (int64_t)f * (2 * n + xd.vrows), *fx0 = fx + n, *fy0 = fx + 2 * n;
+  // the surface's spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0
+  for (int u = tid; u < n; u += kThreads) {
+    const float2 a = fx[u];
+    for (int l = 0; l < Lr; l++) {
       const int v = v0 + l;
-      float2 o = z[l * n + u];
+      float2 o = sm.buf[l * LSTR + pad(u)];
       const float2 x1v = xd.x1[v];
-      o.x -= ar * x1v.x - ai * x1v.y;
-      o.y -= ar * x1v.y + ai * x1v.x;
-      if (v == 0) { o.x -= c0.x; o.y -= c0.y; }
-      if (u == 0) {
-        const float2 x2v = xd.x2[v];
-        o.x -= (float)(n * (py * x1v.x + pyy * x2v.x));
-        o.y -= (float)(n * (py * x1v.y + pyy * x2v.y));
-      }
-      Tf[(int64_t)v * n + u] = o;
+      o.x -= a.x * x1v.x - a.y * x1v.y;
+      o.y -= a.x * x1v.y + a.y * x1v.x;
+      if (v == 0) { const float2 c = fx0[u]; o.x -= c.x; o.y -= c.y; }
+      if (u == 0) { const float2 c = fy0[v]; o.x -= c.x; o.y -= c.y; }
+      Tf[(int64_t)l * n + u] = o;
     }
   }
 }
@@ -250,22 +415,47 @@ __global__ void gather_coef_kernel(const float2 *T, int64_t tstride, const int32
   coef[g] = T[f * tstride + tix[i]];
 }
 
-static bool g_attr[2] = {false, false};
+int fft_plan(int n, int radix[3], int *lines) {
+  const Plan p = plan_of(n);
+  if (!p.lines) return -1;
+  radix[0] = p.r0; radix[1] = p.r1; radix[2] = p.r2;
+  *lines = p.lines;
+  return 0;
+}
 
-cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, double *beta, double *colsum, double *proj,
-                       float2 *Y, float2 *T, cudaStream_t st) {
-  const int smc = 2 * (kColTile / 2) * xd.n * (int)sizeof(float2), smr = 2 * kRowTile * xd.n * (int)sizeof(float2);
+int fft_hole_bands(int n) { return (n / 8 + kHoleBand - 1) / kHoleBand; }
+
+template <int N>
+static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, cudaStream_t st) {
+  constexpr int L = plan_of(N).lines, smem = smem_bytes_of(N);
+  static_assert(smem <= kFftSmemMax, "transform CTA's shared memory");
+  static_assert(N % (2 * L) == 0 && L * N <= kFftPoints && kThreads % L == 0 && L <= 32, "transform plan");
+  static bool attr = false;
   cudaError_t e;
-  if (!g_attr[0]) {
-    if ((e = cudaFuncSetAttribute(fft_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 4 * 1536 * 8)) != cudaSuccess) return e;
-    if ((e = cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * kRowTile * 1536 * 8)) != cudaSuccess) return e;
-    g_attr[0] = true;
+  if (!attr) {
+    if ((e = cudaFuncSetAttribute(fft_cols_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(fft_rows_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+    attr = true;
   }
-  hole_fit_kernel<<<frames, 256, 0, st>>>(xd, src, beta);
-  fft_cols_kernel<<<frames * (xd.n / kColTile), 256, smc, st>>>(xd, src, beta, colsum, Y);
-  proj_kernel<<<frames, 256, 0, st>>>(xd, colsum, proj);
-  fft_rows_kernel<<<frames * ((xd.vrows + kRowTile - 1) / kRowTile), 256, smr, st>>>(xd, proj, Y, T);
+  const int bands = fft_hole_bands(N);
+  hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
+  fft_cols_kernel<N><<<frames * (N / (2 * L)), kThreads, smem, st>>>(xd, src, bands, b.hole, b.colsum, b.Y);
+  fac_kernel<<<frames, 256, 0, st>>>(xd, b.colsum, b.fac);
+  fft_rows_kernel<N><<<frames * ((xd.vrows + L - 1) / L), kThreads, smem, st>>>(xd, b.fac, b.Y, b.T);
   return cudaGetLastError();
+}
+
+cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, cudaStream_t st) {
+  switch (xd.n) {
+    case 384: return fft_launch_n<384>(xd, frames, src, b, st);
+    case 512: return fft_launch_n<512>(xd, frames, src, b, st);
+    case 768: return fft_launch_n<768>(xd, frames, src, b, st);
+    case 1024: return fft_launch_n<1024>(xd, frames, src, b, st);
+    case 1152: return fft_launch_n<1152>(xd, frames, src, b, st);
+    case 1280: return fft_launch_n<1280>(xd, frames, src, b, st);
+    case 1536: return fft_launch_n<1536>(xd, frames, src, b, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t gather_coef_launch(const float2 *T, int64_t tstride, const int32_t *tix, int need, int frames, float2 *coef, cudaStream_t st) {

@@ -25,18 +25,27 @@ struct FmtDev {
 
 // A format's transform tables (row b), passed by value to the transform kernels.
 struct FftDev {
-  int n, nstages, radix[8], vrows;   // the Stockham passes' radices; rows v kept (the used coefficients' v <= vrows - 1)
-  // per pass: NR = n / radix, Ns = the product of the passes before, and their reciprocals ceil(2^32 / d) for exact
-  // division of numerators below 2^16 by one multiply-high (0 stands for a divisor of 1)
-  int nr[8], ns[8];
-  uint32_t mnr[8], mns[8];
-  const float2 *tw;                  // e^{-2 pi i t / n}, t < n
+  int n, vrows;                      // picture size; rows v kept (the used coefficients' v <= vrows - 1)
+  const float2 *tws;                 // the passes' twiddles: pass s at Ns - 1, [r - 1][k] = e^{-2 pi i r k / (Ns R)}
   const float *cx, *qx;              // detrend basis
   const float2 *x1, *x2;             // their DFTs
   double sx2, sq2;
   int elo[7], ehi[7];                // anchors' erase ranges
   double hole_inv[36];
 };
+
+// The transform's per-batch device buffers.
+struct FftBufs {
+  double *hole;                      // frames x bands x 6: the shading fit's partial right-hand sides
+  double *colsum;                    // frames x n x 3: each column's z, z c(y), z q(y)
+  float2 *fac;                       // frames x (2 n + vrows): the surface spectrum's factors
+  float2 *Y;                         // frames x vrows x n: the column transforms' kept rows
+  float2 *T;                         // frames x vrows x n: the detrended spectrum
+};
+
+// The transform CTA's dynamic shared memory bound and the complex points its lines hold at most.
+constexpr int kFftSmemMax = 96 * 1024;
+constexpr int kFftPoints = 6144;
 
 // The sampler's format-side inputs (row a): picture size, grid origin and step in modules, the node lattice.
 struct SampleDev {
@@ -98,8 +107,11 @@ int device_ready(int *sms);
 int record_error(int code, const char *what);
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
-cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, double *beta, double *colsum, double *proj,
-                       float2 *Y, float2 *T, cudaStream_t st);
+cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, cudaStream_t st);
+// The transform plan of picture size n (three passes' radices, lines a CTA): 0, or -1 for a size off the ladder.
+int fft_plan(int n, int radix[3], int *lines);
+// The shading fit's bands a frame.
+int fft_hole_bands(int n);
 cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, int w, int h, int pitch, int64_t fstride,
                           const float *reg, int regstride, float *grid, cudaStream_t st);
 cudaError_t sample_tables_launch(SampleDev sd, float4 *colt, float4 *rowt, cudaStream_t st);

@@ -28,7 +28,8 @@ struct lizg_rx {
   float *sub_rms = nullptr, *est = nullptr, *pilot = nullptr, *align = nullptr;
   uint8_t *decl = nullptr;
   int *counters = nullptr;
-  double *beta = nullptr, *colsum = nullptr, *proj = nullptr;
+  double *hole = nullptr, *colsum = nullptr;
+  float2 *fac = nullptr;
   float *grid = nullptr;              // sampled pictures (luma input)
   lizg::SampleDev sd{};
   float *node_xy = nullptr;
@@ -114,32 +115,30 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   ok(dev_copy(r, &r->pilot_coef, f.pilot_coef.data(), f.pilot_coef.size()));
   ok(dev_copy(r, &r->pilot_white, f.pilot_white.data(), f.pilot_white.size()));
   ok(dev_copy(r, &r->rot, rot.data(), rot.size()));
-  // the transform's plan and tables: radix-4 passes, then 2, 3 and 5; twiddles and the detrend's DFTs in double
+  // the transform's plan (three passes a ladder size) and tables: the passes' twiddles and the detrend's DFTs in double
   {
     lizg::FftDev &xd = r->xd;
-    xd.n = n; xd.vrows = f.vmax + 1; xd.nstages = 0;
-    int m = n;
-    while (m % 4 == 0) { xd.radix[xd.nstages++] = 4; m /= 4; }
-    while (m % 2 == 0) { xd.radix[xd.nstages++] = 2; m /= 2; }
-    while (m % 3 == 0) { xd.radix[xd.nstages++] = 3; m /= 3; }
-    while (m % 5 == 0) { xd.radix[xd.nstages++] = 5; m /= 5; }
-    auto recip = [](int d) { return d == 1 ? 0u : (uint32_t)((((uint64_t)1 << 32) + (uint64_t)d - 1) / (uint64_t)d); };
-    for (int st = 0, ns = 1; st < xd.nstages; ns *= xd.radix[st], st++) {
-      xd.nr[st] = n / xd.radix[st]; xd.ns[st] = ns;
-      xd.mnr[st] = recip(xd.nr[st]); xd.mns[st] = recip(ns);
+    xd.n = n; xd.vrows = f.vmax + 1;
+    int rad[3], lines = 0;
+    if (lizg::fft_plan(n, rad, &lines)) {
+      lizg::record_error(LIZG_E_ARG, "lizg_rx_new: no transform plan for this n");
+      lizg_rx_free(r);
+      return nullptr;
     }
-    std::vector<float2> tw(n), x1(n), x2(n);
-    for (int t = 0; t < n; t++) {
-      const double th = -2.0 * 3.14159265358979323846 * t / n;
-      tw[t] = make_float2((float)std::cos(th), (float)std::sin(th));
-      x1[t] = make_float2(f.x1r[t], f.x1i[t]); x2[t] = make_float2(f.x2r[t], f.x2i[t]);
-    }
-    ok(dev_copy(r, &r->tw, tw.data(), tw.size()));
+    std::vector<float2> tws(n), x1(n), x2(n);
+    for (int st = 0, ns = 1; st < 3; ns *= rad[st], st++)
+      for (int q = 1; q < rad[st]; q++)
+        for (int k = 0; k < ns; k++) {
+          const double th = -2.0 * 3.14159265358979323846 * q * k / ((double)ns * rad[st]);
+          tws[ns - 1 + (q - 1) * ns + k] = make_float2((float)std::cos(th), (float)std::sin(th));
+        }
+    for (int t = 0; t < n; t++) { x1[t] = make_float2(f.x1r[t], f.x1i[t]); x2[t] = make_float2(f.x2r[t], f.x2i[t]); }
+    ok(dev_copy(r, &r->tw, tws.data(), tws.size()));
     ok(dev_copy(r, &r->x1, x1.data(), x1.size()));
     ok(dev_copy(r, &r->x2, x2.data(), x2.size()));
     ok(dev_copy(r, &r->cx, f.cx.data(), f.cx.size()));
     ok(dev_copy(r, &r->qx, f.qx.data(), f.qx.size()));
-    xd.tw = r->tw; xd.x1 = r->x1; xd.x2 = r->x2; xd.cx = r->cx; xd.qx = r->qx; xd.sx2 = f.sx2; xd.sq2 = f.sq2;
+    xd.tws = r->tw; xd.x1 = r->x1; xd.x2 = r->x2; xd.cx = r->cx; xd.qx = r->qx; xd.sx2 = f.sx2; xd.sq2 = f.sq2;
     for (int i = 0; i < lizg::kAnchK; i++) { xd.elo[i] = f.elo[i]; xd.ehi[i] = f.ehi[i]; }
     for (int i = 0; i < 36; i++) xd.hole_inv[i] = f.hole_inv[i / 6][i % 6];
   }
@@ -161,8 +160,8 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   }
   const size_t F = (size_t)max_frames;
   ok(dev_alloc(r, &r->grid, F * n * n));
-  ok(dev_alloc(r, &r->beta, F * 6));
-  ok(dev_alloc(r, &r->proj, F * 5));
+  ok(dev_alloc(r, &r->hole, F * lizg::fft_hole_bands(n) * 6));
+  ok(dev_alloc(r, &r->fac, F * (2 * (size_t)n + r->xd.vrows)));
   ok(dev_alloc(r, &r->colsum, F * n * 3));
   ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
   ok(dev_alloc(r, &r->T, F * (size_t)r->xd.vrows * n));
@@ -308,7 +307,8 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
 static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const lizg_rx_out *out, float *d_coef, cudaStream_t st, int sms) {
   const int n = r->f.n;
   const int64_t tstride = (int64_t)r->xd.vrows * n;
-  cudaError_t e = lizg::fft_launch(r->xd, frames, src, r->beta, r->colsum, r->proj, r->Y, r->T, st);
+  const lizg::FftBufs b{r->hole, r->colsum, r->fac, r->Y, r->T};
+  cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
   r->launches += 4;
   if (d_coef) {

@@ -28,9 +28,10 @@ __device__ __forceinline__ float4 sample_row(const SampleDev &sd, int y) {
 }
 
 // Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh,
-// given the column's and the row's table entries.
+// given the column's and the row's table entries. lut, when given, holds k / 255 for k < 256 made by the same
+// division, read in place of dividing.
 __device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
-                                           const float *nodes, float4 ct, float4 rt) {
+                                           const float *nodes, float4 ct, float4 rt, const float *lut = nullptr) {
   const float mx = ct.x, inv = ct.z, my = rt.x, v = rt.z, omv = __fsub_rn(1.0f, v);
   const int i = __float_as_int(ct.y), j = __float_as_int(rt.y);
   const float *n00 = nodes + 2 * (j * sd.nx + i), *n10 = n00 + 2, *n01 = n00 + 2 * sd.nx, *n11 = n01 + 2;
@@ -50,8 +51,13 @@ __device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *p
   const int xi = sx >= 0 ? (int)sx : 0, yi = sy >= 0 ? (int)sy : 0;   // a NaN coordinate reads pixel 0
   const float fx = __fsub_rn(sx, (float)xi), fy = __fsub_rn(sy, (float)yi);
   const uint8_t *p = px + (int64_t)yi * pitch + xi;
-  const float a = __fdiv_rn((float)p[0], 255.0f), b = __fdiv_rn((float)p[1], 255.0f);
-  const float c = __fdiv_rn((float)p[pitch], 255.0f), d = __fdiv_rn((float)p[pitch + 1], 255.0f);
+  float a, b, c, d;
+  if (lut) {
+    a = lut[p[0]]; b = lut[p[1]]; c = lut[p[pitch]]; d = lut[p[pitch + 1]];
+  } else {
+    a = __fdiv_rn((float)p[0], 255.0f); b = __fdiv_rn((float)p[1], 255.0f);
+    c = __fdiv_rn((float)p[pitch], 255.0f); d = __fdiv_rn((float)p[pitch + 1], 255.0f);
+  }
   return __fadd_rn(__fmul_rn(__fadd_rn(a, __fmul_rn(__fsub_rn(b, a), fx)), __fsub_rn(1.0f, fy)),
                    __fmul_rn(__fadd_rn(c, __fmul_rn(__fsub_rn(d, c), fx)), fy));
 }
