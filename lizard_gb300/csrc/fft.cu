@@ -149,14 +149,22 @@ __host__ __device__ constexpr int lstride_of(int n) { return (n + n / 16 + 15) /
 // a line (j < NR = N / R, k = j mod NS) reads points j + r NR, turns point r by e^{-2 pi i r k / (NS R)}
 // (tw[(r - 1) NS + k]) and writes its DFT's output r to (j / NS) NS R + k + r NS. A thread takes butterflies tid,
 // tid + kThreads, ... (at most B = ceil(L NR / kThreads) of them).
+// The thread's index, read afresh: the passes' offsets hang on it, so a loop round the passes recomputes them pass by
+// pass instead of holding every pass's offsets live across the loop.
+__device__ __forceinline__ int tid_fresh() {
+  int t;
+  asm volatile("mov.u32 %0, %%tid.x;" : "=r"(t));
+  return t;
+}
+
 template <int N, int R, int NS, int L>
 __device__ __forceinline__ void pass(float2 *buf, const float2 *tw, int Lr) {
   constexpr int NR = N / R, LSTR = lstride_of(N), B = (L * NR + kThreads - 1) / kThreads;
-  const int total = Lr * NR;
+  const int total = Lr * NR, tid = tid_fresh();
   float2 v[B][R];
 #pragma unroll
   for (int b = 0; b < B; b++) {
-    const int t = threadIdx.x + b * kThreads;
+    const int t = tid + b * kThreads;
     if (t < total) {
       const int l = t / NR, j = t - l * NR, k = j % NS;
       const float2 *in = buf + l * LSTR;
@@ -172,7 +180,7 @@ __device__ __forceinline__ void pass(float2 *buf, const float2 *tw, int Lr) {
   __syncthreads();
 #pragma unroll
   for (int b = 0; b < B; b++) {
-    const int t = threadIdx.x + b * kThreads;
+    const int t = tid + b * kThreads;
     if (t < total) {
       const int l = t / NR, j = t - l * NR, jq = j / NS, k = j - jq * NS;
       float2 *out = buf + l * LSTR;
@@ -268,102 +276,129 @@ __device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta
   return (float)h;
 }
 
-template <int N>
-__global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev src, int bands, const double *hole, double *colsum, float2 *Y) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
-  const SmemMap sm = smem_map<N>(smraw);
-  const int f = blockIdx.x / tiles, x0 = (blockIdx.x % tiles) * 2 * L;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
-  if (!src.grid) for (int i = tid; i < 256; i += kThreads) sm.lut[i] = __fdiv_rn((float)i, 255.0f);
-  // the shading surface: beta = hole_inv rhs, rhs the bands' partial sums in band order
-  __shared__ double s_rhs[6], s_beta[6];
-  if (tid < 6) {
-    double acc = 0;
-    for (int b = 0; b < bands; b++) acc += hole[((int64_t)f * bands + b) * 6 + tid];
-    s_rhs[tid] = acc;
-  }
-  __syncthreads();
-  if (tid == 0) {
-#pragma unroll
-    for (int r = 0; r < 6; r++) {
-      double acc = 0;
-#pragma unroll
-      for (int k = 0; k < 6; k++) acc += xd.hole_inv[r * 6 + k] * s_rhs[k];
-      s_beta[r] = acc;
-    }
-  }
-  __syncthreads();
-  // load: thread t takes line l = t mod L (columns xa = x0 + l, xb = x0 + L + l) at rows y = t / L, t / L + kThreads / L,
-  // ...; the anchors' squares are erased to the shading surface as they are read; each column's z, z c(y), z q(y)
-  // summed on the way.
-  const int l = tid % L, xa = x0 + l, xb = x0 + L + l;
+// One column tile's samples: thread t takes line l = t mod L (columns xa = x0 + l as the real part, xb = x0 + L + l as
+// the imaginary part) at rows y = t / L, t / L + kThreads / L, ...; the anchors' squares erased to the shading
+// surface as they are read. Each row's two samples are summed into the five detrend projections' raw sums, z c(x),
+// z c(y), z c(x) c(y), z q(x), z q(y) (liblizard/src/lizard_phy.c:1584-1591, 1657-1667), in p.
+template <int N, bool GRID>
+__device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, int f, int x0, const double *beta, const float *lut,
+                                          float2 *line, float p[5]) {
+  constexpr int L = plan_of(N).lines, ystep = kThreads / L;
+  const int l = threadIdx.x % L, xa = x0 + l, xb = x0 + L + l;
   const bool ina = in_square(xd, xa), inb = in_square(xd, xb);
-  float s[6] = {0, 0, 0, 0, 0, 0};
-  float2 *line = sm.buf + l * LSTR;
-  const float *lut = src.grid ? nullptr : sm.lut;
+  const float cxa = __ldg(xd.cx + xa), qxa = __ldg(xd.qx + xa), cxb = __ldg(xd.cx + xb), qxb = __ldg(xd.qx + xb);
+  float Hr[9], mxa = 0, mxb = 0, h6a = 0, h0a = 0, h3a = 0, h6b = 0, h0b = 0, h3b = 0, inva = 0, invb = 0;
+  int ia = 0, ib = 0;
+  const float *nodes = nullptr;
+  const uint8_t *px = nullptr;
+  if (!GRID) {
+    const float *H = src.reg + (int64_t)f * src.regstride;
+#pragma unroll
+    for (int k = 0; k < 9; k++) Hr[k] = H[k];
+    nodes = H + 9;
+    px = src.luma + f * src.fstride;
+    const float4 ca = src.sd.colt[xa], cb = src.sd.colt[xb];
+    mxa = ca.x; ia = __float_as_int(ca.y); inva = ca.z;
+    mxb = cb.x; ib = __float_as_int(cb.y); invb = cb.z;
+    h6a = __fmul_rn(Hr[6], mxa); h0a = __fmul_rn(Hr[0], mxa); h3a = __fmul_rn(Hr[3], mxa);
+    h6b = __fmul_rn(Hr[6], mxb); h0b = __fmul_rn(Hr[0], mxb); h3b = __fmul_rn(Hr[3], mxb);
+  }
 #pragma unroll 2
-  for (int y = tid / L; y < n; y += ystep) {
+  for (int y = threadIdx.x / L; y < N; y += ystep) {
     const bool ysq = (ina || inb) && in_square(xd, y);
-    const float va = ina && ysq ? hole_value(xd, s_beta, xa, y) : src_at(src, f, xa, y, lut);
-    const float vb = inb && ysq ? hole_value(xd, s_beta, xb, y) : src_at(src, f, xb, y, lut);
+    float va, vb;
+    if (GRID) {
+      const float *g = src.grid + f * src.gstride + (int64_t)y * N;
+      va = g[xa]; vb = g[xb];
+    } else {
+      const RowTerms r = row_terms(Hr, src.sd.rowt[y]);
+      const CellTerms ca = cell_terms(src.sd, nodes, ia, inva, r);
+      const CellTerms cb = ib == ia ? ca : cell_terms(src.sd, nodes, ib, invb, r);
+      va = sample_at(px, src.w, src.h, src.pitch, mxa, h6a, h0a, h3a, r, ca, lut);
+      vb = sample_at(px, src.w, src.h, src.pitch, mxb, h6b, h0b, h3b, r, cb, lut);
+    }
+    if (ina && ysq) va = hole_value(xd, beta, xa, y);
+    if (inb && ysq) vb = hole_value(xd, beta, xb, y);
     const float cy = __ldg(xd.cx + y), qy = __ldg(xd.qx + y);
-    s[0] += va; s[1] += va * cy; s[2] += va * qy;
-    s[3] += vb; s[4] += vb * cy; s[5] += vb * qy;
+    const float t0 = va + vb, t1 = cxa * va + cxb * vb, t2 = qxa * va + qxb * vb;
+    p[0] += t1; p[1] += cy * t0; p[2] += cy * t1; p[3] += t2; p[4] += qy * t0;
     line[pad(y)] = make_float2(va, vb);
-  }
-  // the moments: the lanes of a line summed by shuffles, then the warps' sums in warp order
-  double d[6];
-#pragma unroll
-  for (int q = 0; q < 6; q++) {
-    d[q] = s[q];
-    for (int o = L; o < 32; o <<= 1) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
-  }
-  const int warp = tid >> 5, lane = tid & 31;
-  if (lane < L) {
-#pragma unroll
-    for (int q = 0; q < 6; q++) sm.red[(warp * L + lane) * 6 + q] = d[q];
-  }
-  __syncthreads();
-  if (tid < 6 * L) {
-    const int ll = tid / 6, q = tid % 6;
-    double acc = 0;
-    for (int w = 0; w < kThreads / 32; w++) acc += sm.red[(w * L + ll) * 6 + q];
-    const int x = q < 3 ? x0 + ll : x0 + L + ll;
-    colsum[((int64_t)f * n + x) * 3 + q % 3] = acc;
-  }
-  fft_lines<N>(sm.buf, sm.tw, L);
-  // separate the two real columns of each line: A(v) = (Z(v) + conj Z(n - v)) / 2, B(v) = -i (Z(v) - conj Z(n - v)) / 2
-  float2 *Yf = Y + (int64_t)f * xd.vrows * n;
-  for (int v = tid / L; v < xd.vrows; v += ystep) {
-    const float2 zv = line[pad(v)], zm = line[pad(v ? n - v : 0)];
-    Yf[(int64_t)v * n + xa] = make_float2(0.5f * (zv.x + zm.x), 0.5f * (zv.y - zm.y));
-    Yf[(int64_t)v * n + xb] = make_float2(0.5f * (zv.y + zm.y), -0.5f * (zv.x - zm.x));
   }
 }
 
-// The five projections of each frame from its columns' moments, normalised (liblizard/src/lizard_phy.c:1584-1591,
-// 1697), then the surface spectrum's factors (liblizard/src/lizard_phy.c:1702-1716), rounded to float as there:
-// fac[f] = xy[u] (pxy X1[u]) for u < n, x0[u] (n (px X1[u] + pxx X2[u])) for u < n, y0[v] (n (py X1[v] + pyy X2[v]))
-// for v < vrows.
-__global__ void __launch_bounds__(256) fac_kernel(FftDev xd, const double *colsum, float2 *fac) {
-  const int f = blockIdx.x, n = xd.n;
-  const double *cs = colsum + (int64_t)f * n * 3;
-  double p[5] = {0, 0, 0, 0, 0};
-  for (int xx = threadIdx.x; xx < n; xx += blockDim.x) {
-    const double c = xd.cx[xx], q = xd.qx[xx], S0 = cs[3 * xx], S1 = cs[3 * xx + 1], S2 = cs[3 * xx + 2];
-    p[0] += c * S0; p[1] += S1; p[2] += c * S1; p[3] += q * S0; p[4] += S2;
-  }
-  __shared__ double red[5][256];
-  for (int r = 0; r < 5; r++) red[r][threadIdx.x] = p[r];
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s) for (int r = 0; r < 5; r++) red[r][threadIdx.x] += red[r][threadIdx.x + s];
+// The column pass: a CTA takes a column tile (frame f, columns x0 .. x0 + 2L - 1): the shading surface beta from the
+// frame's bands, the tile's samples (erased, projections summed: part[f][tile][0..4]), the L lines' transforms along
+// y, and the two real columns of each line separated: A(v) = (Z(v) + conj Z(n - v)) / 2, B(v) = -i (Z(v) - conj
+// Z(n - v)) / 2, written to Y[f][v][x] for the kept rows v.
+template <int N>
+__global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev src, int bands, const double *hole, double *part, float2 *Y) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
+  const SmemMap sm = smem_map<N>(smraw);
+  const int tid = threadIdx.x, l = tid % L, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
+  if (!src.grid) for (int i = tid; i < 256; i += kThreads) sm.lut[i] = __fdiv_rn((float)i, 255.0f);
+  __shared__ double s_rhs[6], s_beta[6];
+  __shared__ float s_part[kThreads / 32][5];
+  float2 *line = sm.buf + l * LSTR;
+  {
+    const int f = blockIdx.x / tiles, tile = blockIdx.x % tiles, x0 = tile * 2 * L;
+    if (tid < 6) {
+      double acc = 0;
+      for (int b = 0; b < bands; b++) acc += hole[((int64_t)f * bands + b) * 6 + tid];
+      s_rhs[tid] = acc;
+    }
     __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int r = 0; r < 6; r++) {
+        double acc = 0;
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc += xd.hole_inv[r * 6 + k] * s_rhs[k];
+        s_beta[r] = acc;
+      }
+    }
+    __syncthreads();
+    float p[5] = {0, 0, 0, 0, 0};
+    if (src.grid) load_tile<N, true>(xd, src, f, x0, s_beta, nullptr, line, p);
+    else load_tile<N, false>(xd, src, f, x0, s_beta, sm.lut, line, p);
+#pragma unroll
+    for (int q = 0; q < 5; q++)
+      for (int o = 16; o > 0; o >>= 1) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
+    if (lane == 0)
+      for (int q = 0; q < 5; q++) s_part[warp][q] = p[q];
+    __syncthreads();
+    if (tid < 5) {
+      double acc = 0;
+      for (int w = 0; w < kThreads / 32; w++) acc += s_part[w][tid];
+      part[((int64_t)f * tiles + tile) * 5 + tid] = acc;
+    }
+    fft_lines<N>(sm.buf, sm.tw, L);
+    float2 *Yf = Y + (int64_t)f * xd.vrows * n;
+    const int xa = x0 + l, xb = x0 + L + l;
+    for (int v = tid / L; v < xd.vrows; v += ystep) {
+      const float2 zv = line[pad(v)], zm = line[pad(v ? n - v : 0)];
+      Yf[(int64_t)v * n + xa] = make_float2(0.5f * (zv.x + zm.x), 0.5f * (zv.y - zm.y));
+      Yf[(int64_t)v * n + xb] = make_float2(0.5f * (zv.y + zm.y), -0.5f * (zv.x - zm.x));
+    }
   }
-  const double px = red[0][0] / (n * xd.sx2), py = red[1][0] / (n * xd.sx2), pxy = red[2][0] / (xd.sx2 * xd.sx2);
-  const double pxx = red[3][0] / (n * xd.sq2), pyy = red[4][0] / (n * xd.sq2);
+}
+
+// The five projections of each frame from its column tiles' sums, in tile order, normalised
+// (liblizard/src/lizard_phy.c:1697), then the surface spectrum's factors (liblizard/src/lizard_phy.c:1702-1716),
+// rounded to float as there: fac[f] = xy[u] (pxy X1[u]) for u < n, x0[u] (n (px X1[u] + pxx X2[u])) for u < n,
+// y0[v] (n (py X1[v] + pyy X2[v])) for v < vrows.
+__global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const double *part, float2 *fac) {
+  const int f = blockIdx.x, n = xd.n;
+  __shared__ double s_p[5];
+  if (threadIdx.x < 5) {
+    double acc = 0;
+    for (int t = 0; t < tiles; t++) acc += part[((int64_t)f * tiles + t) * 5 + threadIdx.x];
+    s_p[threadIdx.x] = acc;
+  }
+  __syncthreads();
+  const double px = s_p[0] / (n * xd.sx2), py = s_p[1] / (n * xd.sx2), pxy = s_p[2] / (xd.sx2 * xd.sx2);
+  const double pxx = s_p[3] / (n * xd.sq2), pyy = s_p[4] / (n * xd.sq2);
   float2 *o = fac + (int64_t)f * (2 * n + xd.vrows);
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
     const float2 x1 = xd.x1[u], x2 = xd.x2[u];
@@ -376,33 +411,36 @@ __global__ void __launch_bounds__(256) fac_kernel(FftDev xd, const double *colsu
   }
 }
 
+// The row pass: a CTA takes (frame f, rows v0 .. v0 + L - 1), transforms them along x and takes the surface's
+// spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0.
 template <int N>
 __global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, float2 *T) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N);
   const SmemMap sm = smem_map<N>(smraw);
-  const int tiles = (xd.vrows + L - 1) / L, f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L;
-  const int Lr = min(L, xd.vrows - v0), tid = threadIdx.x;
+  const int tid = threadIdx.x, tiles = (xd.vrows + L - 1) / L;
   for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
-  const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
-  for (int l = 0; l < Lr; l++)
-    for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
-  __syncthreads();
-  fft_lines<N>(sm.buf, sm.tw, Lr);
-  float2 *Tf = T + ((int64_t)f * xd.vrows + v0) * n;
-  const float2 *fx = fac + (int64_t)f * (2 * n + xd.vrows), *fx0 = fx + n, *fy0 = fx + 2 * n;
-  // the surface's spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0
-  for (int u = tid; u < n; u += kThreads) {
-    const float2 a = fx[u];
-    for (int l = 0; l < Lr; l++) {
-      const int v = v0 + l;
-      float2 o = sm.buf[l * LSTR + pad(u)];
-      const float2 x1v = xd.x1[v];
-      o.x -= a.x * x1v.x - a.y * x1v.y;
-      o.y -= a.x * x1v.y + a.y * x1v.x;
-      if (v == 0) { const float2 c = fx0[u]; o.x -= c.x; o.y -= c.y; }
-      if (u == 0) { const float2 c = fy0[v]; o.x -= c.x; o.y -= c.y; }
-      Tf[(int64_t)l * n + u] = o;
+  {
+    const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
+    const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
+    for (int l = 0; l < Lr; l++)
+      for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
+    __syncthreads();
+    fft_lines<N>(sm.buf, sm.tw, Lr);
+    float2 *Tf = T + ((int64_t)f * xd.vrows + v0) * n;
+    const float2 *fx = fac + (int64_t)f * (2 * n + xd.vrows), *fx0 = fx + n, *fy0 = fx + 2 * n;
+    for (int u = tid; u < n; u += kThreads) {
+      const float2 a = fx[u];
+      for (int l = 0; l < Lr; l++) {
+        const int v = v0 + l;
+        float2 o = sm.buf[l * LSTR + pad(u)];
+        const float2 x1v = xd.x1[v];
+        o.x -= a.x * x1v.x - a.y * x1v.y;
+        o.y -= a.x * x1v.y + a.y * x1v.x;
+        if (v == 0) { const float2 c = fx0[u]; o.x -= c.x; o.y -= c.y; }
+        if (u == 0) { const float2 c = fy0[v]; o.x -= c.x; o.y -= c.y; }
+        Tf[(int64_t)l * n + u] = o;
+      }
     }
   }
 }
@@ -426,8 +464,8 @@ int fft_plan(int n, int radix[3], int *lines) {
 int fft_hole_bands(int n) { return (n / 8 + kHoleBand - 1) / kHoleBand; }
 
 template <int N>
-static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, cudaStream_t st) {
-  constexpr int L = plan_of(N).lines, smem = smem_bytes_of(N);
+static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st) {
+  constexpr int L = plan_of(N).lines, smem = smem_bytes_of(N), tiles = N / (2 * L);
   static_assert(smem <= kFftSmemMax, "transform CTA's shared memory");
   static_assert(N % (2 * L) == 0 && L * N <= kFftPoints && kThreads % L == 0 && L <= 32, "transform plan");
   static bool attr = false;
@@ -437,23 +475,24 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
     if ((e = cudaFuncSetAttribute(fft_rows_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
     attr = true;
   }
-  const int bands = fft_hole_bands(N);
+  (void)sms;
+  const int bands = fft_hole_bands(N), rtiles = (xd.vrows + L - 1) / L;
   hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
-  fft_cols_kernel<N><<<frames * (N / (2 * L)), kThreads, smem, st>>>(xd, src, bands, b.hole, b.colsum, b.Y);
-  fac_kernel<<<frames, 256, 0, st>>>(xd, b.colsum, b.fac);
-  fft_rows_kernel<N><<<frames * ((xd.vrows + L - 1) / L), kThreads, smem, st>>>(xd, b.fac, b.Y, b.T);
+  fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, bands, b.hole, b.part, b.Y);
+  fac_kernel<<<frames, 256, 0, st>>>(xd, tiles, b.part, b.fac);
+  fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, b.Y, b.T);
   return cudaGetLastError();
 }
 
-cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, cudaStream_t st) {
+cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st) {
   switch (xd.n) {
-    case 384: return fft_launch_n<384>(xd, frames, src, b, st);
-    case 512: return fft_launch_n<512>(xd, frames, src, b, st);
-    case 768: return fft_launch_n<768>(xd, frames, src, b, st);
-    case 1024: return fft_launch_n<1024>(xd, frames, src, b, st);
-    case 1152: return fft_launch_n<1152>(xd, frames, src, b, st);
-    case 1280: return fft_launch_n<1280>(xd, frames, src, b, st);
-    case 1536: return fft_launch_n<1536>(xd, frames, src, b, st);
+    case 384: return fft_launch_n<384>(xd, frames, src, b, sms, st);
+    case 512: return fft_launch_n<512>(xd, frames, src, b, sms, st);
+    case 768: return fft_launch_n<768>(xd, frames, src, b, sms, st);
+    case 1024: return fft_launch_n<1024>(xd, frames, src, b, sms, st);
+    case 1152: return fft_launch_n<1152>(xd, frames, src, b, sms, st);
+    case 1280: return fft_launch_n<1280>(xd, frames, src, b, sms, st);
+    case 1536: return fft_launch_n<1536>(xd, frames, src, b, sms, st);
     default: return cudaErrorInvalidValue;
   }
 }

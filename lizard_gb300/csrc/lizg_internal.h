@@ -37,7 +37,7 @@ struct FftDev {
 // The transform's per-batch device buffers.
 struct FftBufs {
   double *hole;                      // frames x bands x 6: the shading fit's partial right-hand sides
-  double *colsum;                    // frames x n x 3: each column's z, z c(y), z q(y)
+  double *part;                      // frames x column tiles x 5: the detrend projections' raw sums a tile
   float2 *fac;                       // frames x (2 n + vrows): the surface spectrum's factors
   float2 *Y;                         // frames x vrows x n: the column transforms' kept rows
   float2 *T;                         // frames x vrows x n: the detrended spectrum
@@ -107,7 +107,7 @@ int device_ready(int *sms);
 int record_error(int code, const char *what);
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
-cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, cudaStream_t st);
+cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st);
 // The transform plan of picture size n (three passes' radices, lines a CTA): 0, or -1 for a size off the ladder.
 int fft_plan(int n, int radix[3], int *lines);
 // The shading fit's bands a frame.

@@ -28,7 +28,7 @@ struct lizg_rx {
   float *sub_rms = nullptr, *est = nullptr, *pilot = nullptr, *align = nullptr;
   uint8_t *decl = nullptr;
   int *counters = nullptr;
-  double *hole = nullptr, *colsum = nullptr;
+  double *hole = nullptr, *part = nullptr;
   float2 *fac = nullptr;
   float *grid = nullptr;              // sampled pictures (luma input)
   lizg::SampleDev sd{};
@@ -162,7 +162,7 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   ok(dev_alloc(r, &r->grid, F * n * n));
   ok(dev_alloc(r, &r->hole, F * lizg::fft_hole_bands(n) * 6));
   ok(dev_alloc(r, &r->fac, F * (2 * (size_t)n + r->xd.vrows)));
-  ok(dev_alloc(r, &r->colsum, F * n * 3));
+  ok(dev_alloc(r, &r->part, F * (size_t)(n / 2) * 5));   // column tiles (at most n / 2) x 5
   ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
   ok(dev_alloc(r, &r->T, F * (size_t)r->xd.vrows * n));
   ok(dev_alloc(r, &r->llrf, F * 2 * need));
@@ -307,8 +307,8 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
 static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const lizg_rx_out *out, float *d_coef, cudaStream_t st, int sms) {
   const int n = r->f.n;
   const int64_t tstride = (int64_t)r->xd.vrows * n;
-  const lizg::FftBufs b{r->hole, r->colsum, r->fac, r->Y, r->T};
-  cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, st);
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->T};
+  cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
   r->launches += 4;
   if (d_coef) {

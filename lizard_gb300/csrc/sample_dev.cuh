@@ -27,23 +27,41 @@ __device__ __forceinline__ float4 sample_row(const SampleDev &sd, int y) {
   return make_float4(my, __int_as_float(j), __fdiv_rn(__fsub_rn(my, sd.node_y[j]), __fsub_rn(sd.node_y[j + 1], sd.node_y[j])), 0.0f);
 }
 
-// Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh,
-// given the column's and the row's table entries. lut, when given, holds k / 255 for k < 256 made by the same
-// division, read in place of dividing.
-__device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
-                                           const float *nodes, float4 ct, float4 rt, const float *lut = nullptr) {
-  const float mx = ct.x, inv = ct.z, my = rt.x, v = rt.z, omv = __fsub_rn(1.0f, v);
-  const int i = __float_as_int(ct.y), j = __float_as_int(rt.y);
-  const float *n00 = nodes + 2 * (j * sd.nx + i), *n10 = n00 + 2, *n01 = n00 + 2 * sd.nx, *n11 = n01 + 2;
-  const float nxi = sd.node_x[i];
-  const float ex = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[0], n00[0]), omv), __fmul_rn(__fsub_rn(n11[0], n01[0]), v)), inv);
-  const float cx = __fsub_rn(__fadd_rn(__fmul_rn(n00[0], omv), __fmul_rn(n01[0], v)), __fmul_rn(ex, nxi));
-  const float ey = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[1], n00[1]), omv), __fmul_rn(__fsub_rn(n11[1], n01[1]), v)), inv);
-  const float cy = __fsub_rn(__fadd_rn(__fmul_rn(n00[1], omv), __fmul_rn(n01[1], v)), __fmul_rn(ey, nxi));
-  const float kw = __fadd_rn(__fmul_rn(H[7], my), 1.0f), ku = __fadd_rn(__fmul_rn(H[1], my), H[2]), kv = __fadd_rn(__fmul_rn(H[4], my), H[5]);
-  const float rw = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(H[6], mx), kw));
-  const float pu = __fmul_rn(__fadd_rn(__fmul_rn(H[0], mx), ku), rw), pv = __fmul_rn(__fadd_rn(__fmul_rn(H[3], mx), kv), rw);
-  const float dx = __fadd_rn(cx, __fmul_rn(ex, mx)), dy = __fadd_rn(cy, __fmul_rn(ey, mx));
+// The walk's quantities of one picture row: the row's place in its mesh cell and the homography's row terms.
+struct RowTerms {
+  float my, v, omv, kw, ku, kv;
+  int j;
+};
+__device__ __forceinline__ RowTerms row_terms(const float *H, float4 rt) {
+  RowTerms r;
+  r.my = rt.x; r.v = rt.z; r.omv = __fsub_rn(1.0f, r.v); r.j = __float_as_int(rt.y);
+  r.kw = __fadd_rn(__fmul_rn(H[7], r.my), 1.0f); r.ku = __fadd_rn(__fmul_rn(H[1], r.my), H[2]); r.kv = __fadd_rn(__fmul_rn(H[4], r.my), H[5]);
+  return r;
+}
+
+// The mesh displacement's line along a row within cell (i, j): d = c + e mx, each axis.
+struct CellTerms {
+  float ex, cx, ey, cy;
+};
+__device__ __forceinline__ CellTerms cell_terms(const SampleDev &sd, const float *nodes, int i, float inv, const RowTerms &r) {
+  const float *n00 = nodes + 2 * (r.j * sd.nx + i), *n10 = n00 + 2, *n01 = n00 + 2 * sd.nx, *n11 = n01 + 2;
+  const float nxi = sd.node_x[i], v = r.v, omv = r.omv;
+  CellTerms c;
+  c.ex = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[0], n00[0]), omv), __fmul_rn(__fsub_rn(n11[0], n01[0]), v)), inv);
+  c.cx = __fsub_rn(__fadd_rn(__fmul_rn(n00[0], omv), __fmul_rn(n01[0], v)), __fmul_rn(c.ex, nxi));
+  c.ey = __fmul_rn(__fadd_rn(__fmul_rn(__fsub_rn(n10[1], n00[1]), omv), __fmul_rn(__fsub_rn(n11[1], n01[1]), v)), inv);
+  c.cy = __fsub_rn(__fadd_rn(__fmul_rn(n00[1], omv), __fmul_rn(n01[1], v)), __fmul_rn(c.ey, nxi));
+  return c;
+}
+
+// The sample at module column mx of a row: h6 = H[6] mx, h0 = H[0] mx, h3 = H[3] mx (the column's products), then the
+// projection, the mesh's displacement, the frame-edge clamp and the bilinear grey read. lut, when given, holds
+// k / 255 for k < 256 made by the same division, read in place of dividing.
+__device__ __forceinline__ float sample_at(const uint8_t *px, int w, int h, int pitch, float mx, float h6, float h0, float h3,
+                                           const RowTerms &r, const CellTerms &c, const float *lut) {
+  const float rw = __fdiv_rn(1.0f, __fadd_rn(h6, r.kw));
+  const float pu = __fmul_rn(__fadd_rn(h0, r.ku), rw), pv = __fmul_rn(__fadd_rn(h3, r.kv), rw);
+  const float dx = __fadd_rn(c.cx, __fmul_rn(c.ex, mx)), dy = __fadd_rn(c.cy, __fmul_rn(c.ey, mx));
   float sx = __fsub_rn(__fadd_rn(pu, dx), 0.5f), sy = __fsub_rn(__fadd_rn(pv, dy), 0.5f);
   const float xm = __fsub_rn((float)w, 1.001f), ym = __fsub_rn((float)h, 1.001f);
   if (sx < 0) sx = 0; else if (sx > xm) sx = xm;
@@ -51,15 +69,25 @@ __device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *p
   const int xi = sx >= 0 ? (int)sx : 0, yi = sy >= 0 ? (int)sy : 0;   // a NaN coordinate reads pixel 0
   const float fx = __fsub_rn(sx, (float)xi), fy = __fsub_rn(sy, (float)yi);
   const uint8_t *p = px + (int64_t)yi * pitch + xi;
-  float a, b, c, d;
+  float a, b, cc, d;
   if (lut) {
-    a = lut[p[0]]; b = lut[p[1]]; c = lut[p[pitch]]; d = lut[p[pitch + 1]];
+    a = lut[p[0]]; b = lut[p[1]]; cc = lut[p[pitch]]; d = lut[p[pitch + 1]];
   } else {
     a = __fdiv_rn((float)p[0], 255.0f); b = __fdiv_rn((float)p[1], 255.0f);
-    c = __fdiv_rn((float)p[pitch], 255.0f); d = __fdiv_rn((float)p[pitch + 1], 255.0f);
+    cc = __fdiv_rn((float)p[pitch], 255.0f); d = __fdiv_rn((float)p[pitch + 1], 255.0f);
   }
   return __fadd_rn(__fmul_rn(__fadd_rn(a, __fmul_rn(__fsub_rn(b, a), fx)), __fsub_rn(1.0f, fy)),
-                   __fmul_rn(__fadd_rn(c, __fmul_rn(__fsub_rn(d, c), fx)), fy));
+                   __fmul_rn(__fadd_rn(cc, __fmul_rn(__fsub_rn(d, cc), fx)), fy));
+}
+
+// Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh,
+// given the column's and the row's table entries.
+__device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
+                                           const float *nodes, float4 ct, float4 rt, const float *lut = nullptr) {
+  const RowTerms r = row_terms(H, rt);
+  const CellTerms c = cell_terms(sd, nodes, __float_as_int(ct.y), ct.z, r);
+  const float mx = ct.x;
+  return sample_at(px, w, h, pitch, mx, __fmul_rn(H[6], mx), __fmul_rn(H[0], mx), __fmul_rn(H[3], mx), r, c, lut);
 }
 
 }  // namespace lizg
