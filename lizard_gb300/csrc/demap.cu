@@ -10,12 +10,10 @@
 
 namespace lizg {
 
-__device__ __forceinline__ float2 coef_at(const float2 *spec, const int32_t *idx, int i) { return spec[idx ? idx[i] : i]; }
-
-// Coefficient i turned back by the grid shift (dx, dy): the turn's index in float, nearest-even, mod 4096, and the
-// rotation by the table's cos / sin, as liblizard/src/lizard_phy.c:214-218 computes them.
-__device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, const int32_t *idx, int i, float dx, float dy) {
-  const float2 z = coef_at(spec, idx, i);
+// Coefficient i (spectra are in pos order) turned back by the grid shift (dx, dy): the turn's index in float,
+// nearest-even, mod 4096, and the rotation by the table's cos / sin, as liblizard/src/lizard_phy.c:214-218 computes them.
+__device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, int i, float dx, float dy) {
+  const float2 z = spec[i];
   const float uu = (float)fd.uv[2 * i], vv = (float)fd.uv[2 * i + 1];
   const float t = (uu * dx + vv * dy) * fd.turn_scale;
   const unsigned k = (unsigned)__float2int_rn(t) & (kTurnsDev - 1);
@@ -26,7 +24,7 @@ __device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, c
 // One CTA a frame. Its threads work out every pilot's six products in parallel into shared memory; six threads
 // then add one sum each in pilot order, so the double sums are the reference's (liblizard/src/lizard_phy.c:283-317).
 // Writes align[3 f ..] = dx, dy, and 1 where the shift is turned back.
-__global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align) {
+__global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, float *align) {
   extern __shared__ double tm[];              // npilot x 6
   __shared__ double sums[6], dxy[2];
   __shared__ int give_up;
@@ -39,7 +37,7 @@ __global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float
     const double dx = dxy[0], dy = dxy[1];
     for (int pi = threadIdx.x; pi < used; pi += blockDim.x) {
       const int i = fd.pilot_coef[pi], w = fd.pilot_white[pi];
-      const float2 y = turned(fd, sp, idx, i, (float)dx, (float)dy);
+      const float2 y = turned(fd, sp, i, (float)dx, (float)dy);
       const double xr = (w & 1) ? -1.0 : 1.0, xi = (w & 2) ? -1.0 : 1.0;
       const double zr = (double)y.x * xr + (double)y.y * xi, zi = (double)y.y * xr - (double)y.x * xi;
       const double cu = k * zr * fd.uv[2 * i], cv = k * zr * fd.uv[2 * i + 1];
@@ -48,8 +46,17 @@ __global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float
     }
     __syncthreads();
     if (threadIdx.x < 6) {
+      // in pilot order; the loads of eight terms issued ahead of their adds
       double acc = 0;
-      for (int pi = 0; pi < used; pi++) acc += tm[6 * pi + threadIdx.x];
+      int pi = 0;
+      for (; pi + 8 <= used; pi += 8) {
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) v[q] = tm[6 * (pi + q) + threadIdx.x];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc += v[q];
+      }
+      for (; pi < used; pi++) acc += tm[6 * pi + threadIdx.x];
       sums[threadIdx.x] = acc;
     }
     __syncthreads();
@@ -78,12 +85,14 @@ __global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float
 // ten Brink's J (liblizard/src/lizard_phy.c:73-75)
 __device__ __forceinline__ double axis_info(double g) { return g > 0 ? pow(1 - pow(2.0, -0.3073 * pow(2 * sqrt(g), 1.7870)), 1.1064) : 0; }
 
-// Four lanes a sub-channel, eight sub-channels a warp. Lane q of a group sums the moments of coefficients q, q + 4,
-// ... in order (the reference's four float chains), the chains are added (c0 + c1) + (c2 + c3), the scale is worked
-// out in double, and the soft values are each axis times 8 k, NaN to 0, clamped to +-80, rounded half to even.
-__global__ void demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, const float *align,
-                             int8_t *llrf, double *sub_est, float *sub_rms) {
-  const int gid = blockIdx.x * (blockDim.x >> 2) + (threadIdx.x >> 2), qd = threadIdx.x & 3;
+// Four lanes a sub-channel, 64 sub-channels a CTA. Lane q of a group sums the moments of coefficients q, q + 4, ...
+// in order (the reference's four float chains) and the chains are added (c0 + c1) + (c2 + c3); one thread a
+// sub-channel then works out the scale in double (so a warp's double work serves 32 sub-channels); the soft values
+// are each axis times 8 k, NaN to 0, clamped to +-80, rounded half to even.
+__global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
+                                                    int8_t *llrf, double *sub_est, float *sub_rms) {
+  __shared__ float s_m[64][2], s_k8[64];
+  const int grp = threadIdx.x >> 2, qd = threadIdx.x & 3, gid = blockIdx.x * 64 + grp;
   const int f = gid / fd.subch, j = gid - f * fd.subch;
   const bool live = f < fd.frames;
   const float2 *sp = spec + (live ? f : 0) * spec_stride;
@@ -93,7 +102,7 @@ __global__ void demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride,
   if (live) {
     for (int s = qd; s < kSubDev; s += 4) {
       const int i = j * kSubDev + s;
-      const float2 y = turn ? turned(fd, sp, idx, i, dx, dy) : coef_at(sp, idx, i);
+      const float2 y = turn ? turned(fd, sp, i, dx, dy) : sp[i];
       const float e = y.x * y.x + y.y * y.y;
       m2 = m2 + e; m4 = m4 + e * e;
     }
@@ -102,25 +111,31 @@ __global__ void demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride,
   const float o2 = __shfl_down_sync(0xffffffffu, m2, 1), o4 = __shfl_down_sync(0xffffffffu, m4, 1);
   const float p2 = m2 + o2, p4 = m4 + o4;
   const float r2 = __shfl_down_sync(0xffffffffu, p2, 2), r4 = __shfl_down_sync(0xffffffffu, p4, 2);
-  float k8 = 0;
-  if (qd == 0 && live) {
-    const float fm2 = p2 + r2, fm4 = p4 + r4;
-    const double M2 = (double)fm2 / kSubDev, M4 = (double)fm4 / kSubDev;
-    sub_rms[f * fd.subch + j] = M2 > 0 ? (float)sqrt(M2 / 2) : 0;
-    double a2 = 2 * M2 * M2 - M4;
-    a2 = a2 > 0 ? sqrt(a2) : 0;
-    double nv = M2 - a2;
-    if (nv < 0.02 * M2) nv = 0.02 * M2;
-    sub_est[f * fd.subch + j] = axis_info(a2 / nv);
-    const float kk = (float)(0.7 * 2 * sqrt(2 * a2) / nv);
-    k8 = 8 * kk;
+  if (qd == 0) { s_m[grp][0] = p2 + r2; s_m[grp][1] = p4 + r4; }
+  __syncthreads();
+  if (threadIdx.x < 64) {
+    const int g2 = blockIdx.x * 64 + threadIdx.x, f2 = g2 / fd.subch, j2 = g2 - f2 * fd.subch;
+    float k8 = 0;
+    if (f2 < fd.frames) {
+      const double M2 = (double)s_m[threadIdx.x][0] / kSubDev, M4 = (double)s_m[threadIdx.x][1] / kSubDev;
+      sub_rms[f2 * fd.subch + j2] = M2 > 0 ? (float)sqrt(M2 / 2) : 0;
+      double a2 = 2 * M2 * M2 - M4;
+      a2 = a2 > 0 ? sqrt(a2) : 0;
+      double nv = M2 - a2;
+      if (nv < 0.02 * M2) nv = 0.02 * M2;
+      sub_est[f2 * fd.subch + j2] = axis_info(a2 / nv);
+      const float kk = (float)(0.7 * 2 * sqrt(2 * a2) / nv);
+      k8 = 8 * kk;
+    }
+    s_k8[threadIdx.x] = k8;
   }
-  k8 = __shfl_sync(0xffffffffu, k8, threadIdx.x & ~3 & 31);
+  __syncthreads();
   if (!live) return;
+  const float k8 = s_k8[grp];
   int8_t *out = llrf + (int64_t)f * fd.subch * 2 * kSubDev + 2 * j * kSubDev;
   for (int s = qd; s < kSubDev; s += 4) {
     const int i = j * kSubDev + s;
-    const float2 y = turn ? turned(fd, sp, idx, i, dx, dy) : coef_at(sp, idx, i);
+    const float2 y = turn ? turned(fd, sp, i, dx, dy) : sp[i];
     float x = k8 * y.x, z = k8 * y.y;
     x = x != x ? 0.0f : fminf(fmaxf(x, -80.0f), 80.0f);
     z = z != z ? 0.0f : fminf(fmaxf(z, -80.0f), 80.0f);
@@ -134,7 +149,7 @@ __global__ void demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride,
 // One thread a block: its estimate (its sub-channels' information weighted by the slots it holds there, in double, in
 // order), its pilot reading (the tail's axis values against the whitening in units of their sub-channel's rms, in
 // double, in order; NaN where none was read) and the decline gate (est < 0.2 k / nt in float): decl[f blocks + b] = 1.
-__global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, const float *align,
+__global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
                               const double *sub_est, const float *sub_rms, float *est, float *pilot, uint8_t *decl) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= fd.frames * fd.blocks) return;
@@ -160,7 +175,7 @@ __global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride
       const int gs = s0 + i, ci = gs / 2;
       const float rms = sr[gs / (2 * kSubDev)];
       if (!(rms > 0)) continue;
-      const float2 y = turn ? turned(fd, sp, idx, ci, dx, dy) : coef_at(sp, idx, ci);
+      const float2 y = turn ? turned(fd, sp, ci, dx, dy) : sp[ci];
       const float yv = (i & 1) ? y.y : y.x;
       cs += (fd.white[gs] ? -1.0 : 1.0) * yv / rms;
       got++;
@@ -171,7 +186,7 @@ __global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride
   decl[g] = e < 0.2f * (float)fd.tier_k[t] / (float)nt;
 }
 
-cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
+cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st) {
   static bool attr = false;
   const int psm = 6 * (fd.npilot > 0 ? fd.npilot : 1) * (int)sizeof(double);
@@ -181,11 +196,11 @@ cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stri
     attr = true;
   }
   if (fd.npilot > 1024) return cudaErrorInvalidValue;
-  pilot_align_kernel<<<fd.frames, 256, psm, st>>>(fd, spec, spec_stride, idx, align);
+  pilot_align_kernel<<<fd.frames, 256, psm, st>>>(fd, spec, spec_stride, align);
   const int groups = fd.frames * fd.subch;
-  demap_kernel<<<(groups + 63) / 64, 256, 0, st>>>(fd, spec, spec_stride, idx, align, llrf, sub_est, sub_rms);
+  demap_kernel<<<(groups + 63) / 64, 256, 0, st>>>(fd, spec, spec_stride, align, llrf, sub_est, sub_rms);
   const int nbk = fd.frames * fd.blocks;
-  blocks_kernel<<<(nbk + 127) / 128, 128, 0, st>>>(fd, spec, spec_stride, idx, align, sub_est, sub_rms, est, pilot, decl);
+  blocks_kernel<<<(nbk + 127) / 128, 128, 0, st>>>(fd, spec, spec_stride, align, sub_est, sub_rms, est, pilot, decl);
   return cudaGetLastError();
 }
 

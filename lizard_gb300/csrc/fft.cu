@@ -11,7 +11,8 @@
 //   fac_kernel        one CTA a frame: the five projections from the columns' moments, then the surface spectrum's
 //                     per-column and per-row factors (the double products the reference rounds to float);
 //   fft_rows_kernel   a CTA takes L kept rows v of a frame, transforms along x and subtracts the surface's spectrum
-//                     (the xy term everywhere, the x terms on v = 0, the y terms on u = 0), writing T[v][u].
+//                     (the xy term everywhere, the x terms on v = 0, the y terms on u = 0), writing the used
+//                     coefficients in pos order.
 // L is the most lines of n points that fit 6144 complex points (so every CTA holds about the same 48 KB of samples).
 //
 // The transforms are Stockham autosort passes of radix 16, 9, 8, 6, 5, 4, 3 or 2 (every ladder size takes three),
@@ -225,27 +226,40 @@ __device__ __forceinline__ void hole_basis(const FftDev &xd, int x, int y, doubl
 }
 
 // The shading fit's right-hand side (liblizard/src/lizard_phy.c:1609-1623) over kHoleBand of the frame's
-// every-eighth rows: hole[f][band][0..5].
+// every-eighth rows: hole[f][band][0..5]. A warp takes a row: its samples outside the squares summed in float as
+// z, z c(x), z q(x) (the basis is separable: 1, c(x), q(x), c(y), q(y), c(x) c(y)), then the row's six terms added
+// in double; the warps' sums added in warp order.
 __global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, int bands, double *hole) {
   const int f = blockIdx.x / bands, band = blockIdx.x % bands, n = xd.n, c = n / 8;
-  const int ky0 = band * kHoleBand, ky1 = min(c, ky0 + kHoleBand);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, ky1 = min(c, (band + 1) * kHoleBand);
   double rhs[6] = {0, 0, 0, 0, 0, 0};
-  for (int k = threadIdx.x; k < (ky1 - ky0) * c; k += blockDim.x) {
-    const int x = 8 * (k % c), y = 8 * (ky0 + k / c);
-    if (in_square(xd, x) && in_square(xd, y)) continue;
-    const double v = src_at(src, f, x, y, nullptr);
-    double b[6];
-    hole_basis(xd, x, y, b);
-    for (int r = 0; r < 6; r++) rhs[r] += b[r] * v;
+  for (int ky = band * kHoleBand + warp; ky < ky1; ky += 8) {
+    const int y = 8 * ky;
+    const bool ysq = in_square(xd, y);
+    float s0 = 0, s1 = 0, s2 = 0;
+    for (int kx = lane; kx < c; kx += 32) {
+      const int x = 8 * kx;
+      if (ysq && in_square(xd, x)) continue;
+      const float v = src_at(src, f, x, y, nullptr);
+      s0 += v; s1 += __ldg(xd.cx + x) * v; s2 += __ldg(xd.qx + x) * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    const double cy = xd.cx[y], qy = xd.qx[y];
+    rhs[0] += s0; rhs[1] += s1; rhs[2] += s2; rhs[3] += cy * s0; rhs[4] += qy * s0; rhs[5] += cy * s1;
   }
-  __shared__ double red[6][256];
-  for (int r = 0; r < 6; r++) red[r][threadIdx.x] = rhs[r];
+  __shared__ double red[8][6];
+  if (lane == 0)
+    for (int r = 0; r < 6; r++) red[warp][r] = rhs[r];
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s) for (int r = 0; r < 6; r++) red[r][threadIdx.x] += red[r][threadIdx.x + s];
-    __syncthreads();
+  if (threadIdx.x < 6) {
+    double acc = 0;
+    for (int w = 0; w < 8; w++) acc += red[w][threadIdx.x];
+    hole[((int64_t)f * bands + band) * 6 + threadIdx.x] = acc;
   }
-  if (threadIdx.x < 6) hole[((int64_t)f * bands + band) * 6 + threadIdx.x] = red[threadIdx.x][0];
 }
 
 // The transform CTA's shared memory: the lines, the twiddles, the moments' reduction, the grey table.
@@ -412,45 +426,40 @@ __global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const do
 }
 
 // The row pass: a CTA takes (frame f, rows v0 .. v0 + L - 1), transforms them along x and takes the surface's
-// spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0.
+// spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0. The used
+// coefficients go straight to their place in pos order: C[f][tpos[v][u]] (tpos -1 where (u, v) is not used).
 template <int N>
-__global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, float2 *T) {
+__global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, const int32_t *tpos,
+                                                               int need, float2 *C) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N);
   const SmemMap sm = smem_map<N>(smraw);
   const int tid = threadIdx.x, tiles = (xd.vrows + L - 1) / L;
+  const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
   for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
-  {
-    const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
-    const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
-    for (int l = 0; l < Lr; l++)
-      for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
-    __syncthreads();
-    fft_lines<N>(sm.buf, sm.tw, Lr);
-    float2 *Tf = T + ((int64_t)f * xd.vrows + v0) * n;
-    const float2 *fx = fac + (int64_t)f * (2 * n + xd.vrows), *fx0 = fx + n, *fy0 = fx + 2 * n;
-    for (int u = tid; u < n; u += kThreads) {
-      const float2 a = fx[u];
-      for (int l = 0; l < Lr; l++) {
-        const int v = v0 + l;
-        float2 o = sm.buf[l * LSTR + pad(u)];
-        const float2 x1v = xd.x1[v];
-        o.x -= a.x * x1v.x - a.y * x1v.y;
-        o.y -= a.x * x1v.y + a.y * x1v.x;
-        if (v == 0) { const float2 c = fx0[u]; o.x -= c.x; o.y -= c.y; }
-        if (u == 0) { const float2 c = fy0[v]; o.x -= c.x; o.y -= c.y; }
-        Tf[(int64_t)l * n + u] = o;
-      }
+  const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
+  for (int l = 0; l < Lr; l++)
+    for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
+  __syncthreads();
+  fft_lines<N>(sm.buf, sm.tw, Lr);
+  float2 *Cf = C + (int64_t)f * need;
+  const int32_t *tp = tpos + (int64_t)v0 * n;
+  const float2 *fx = fac + (int64_t)f * (2 * n + xd.vrows), *fx0 = fx + n, *fy0 = fx + 2 * n;
+  for (int u = tid; u < n; u += kThreads) {
+    const float2 a = fx[u];
+    for (int l = 0; l < Lr; l++) {
+      const int i = tp[l * n + u];
+      if (i < 0) continue;
+      const int v = v0 + l;
+      float2 o = sm.buf[l * LSTR + pad(u)];
+      const float2 x1v = xd.x1[v];
+      o.x -= a.x * x1v.x - a.y * x1v.y;
+      o.y -= a.x * x1v.y + a.y * x1v.x;
+      if (v == 0) { const float2 c = fx0[u]; o.x -= c.x; o.y -= c.y; }
+      if (u == 0) { const float2 c = fy0[v]; o.x -= c.x; o.y -= c.y; }
+      Cf[i] = o;
     }
   }
-}
-
-// coef[f][i] = T[f][tix[i]]: the used coefficients in pos order (for a caller that wants the spectrum itself).
-__global__ void gather_coef_kernel(const float2 *T, int64_t tstride, const int32_t *tix, int need, int frames, float2 *coef) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= (int64_t)frames * need) return;
-  const int f = (int)(g / need), i = (int)(g % need);
-  coef[g] = T[f * tstride + tix[i]];
 }
 
 int fft_plan(int n, int radix[3], int *lines) {
@@ -480,7 +489,7 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
   hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
   fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, bands, b.hole, b.part, b.Y);
   fac_kernel<<<frames, 256, 0, st>>>(xd, tiles, b.part, b.fac);
-  fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, b.Y, b.T);
+  fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, b.Y, b.tpos, b.need, b.C);
   return cudaGetLastError();
 }
 
@@ -495,12 +504,6 @@ cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const Ff
     case 1536: return fft_launch_n<1536>(xd, frames, src, b, sms, st);
     default: return cudaErrorInvalidValue;
   }
-}
-
-cudaError_t gather_coef_launch(const float2 *T, int64_t tstride, const int32_t *tix, int need, int frames, float2 *coef, cudaStream_t st) {
-  const int64_t tot = (int64_t)frames * need;
-  gather_coef_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(T, tstride, tix, need, frames, coef);
-  return cudaGetLastError();
 }
 
 }  // namespace lizg

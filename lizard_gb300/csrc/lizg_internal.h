@@ -14,7 +14,6 @@ struct FmtDev {
   float turn_scale;                  // (float)4096 / (float)n
   int tier_first[4], tier_blocks[4], tier_slots[4], tier_nt[4], tier_k[4];
   const int16_t *uv;                 // (u, v) a coefficient, pos order
-  const int32_t *tix;                // its index in the spectrum array [v][u mod n]
   const uint8_t *white;              // whitening bit a frame slot
   const int16_t *perm[4];            // per tier: block slot -> codeword bit
   const int32_t *block_tier, *block_slot;
@@ -40,7 +39,9 @@ struct FftBufs {
   double *part;                      // frames x column tiles x 5: the detrend projections' raw sums a tile
   float2 *fac;                       // frames x (2 n + vrows): the surface spectrum's factors
   float2 *Y;                         // frames x vrows x n: the column transforms' kept rows
-  float2 *T;                         // frames x vrows x n: the detrended spectrum
+  const int32_t *tpos;               // vrows x n: the pos index of spectrum point (u mod n, v), -1 where unused
+  int need;                          // used coefficients a frame (subch x 320)
+  float2 *C;                         // frames x need: the detrended spectrum's used coefficients in pos order
 };
 
 // The transform CTA's dynamic shared memory bound and the complex points its lines hold at most.
@@ -105,7 +106,8 @@ cudaError_t ldpc_upload_tables();
 int device_ready(int *sms);
 // Records a failure message for lizg_last_error(); returns code.
 int record_error(int code, const char *what);
-cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const int32_t *idx, float *align, int8_t *llrf,
+// spec: frames x spec_stride complex coefficients in pos order.
+cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
 cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st);
 // The transform plan of picture size n (three passes' radices, lines a CTA): 0, or -1 for a size off the ladder.
@@ -117,7 +119,6 @@ cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, 
 cudaError_t sample_tables_launch(SampleDev sd, float4 *colt, float4 *rowt, cudaStream_t st);
 // The node lattice of a layout of side modules (liblizard/src/layout.c:110-117): returns nx (= ny).
 int layout_nodes(int side, float *pos);
-cudaError_t gather_coef_launch(const float2 *T, int64_t tstride, const int32_t *tix, int need, int frames, float2 *coef, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
 

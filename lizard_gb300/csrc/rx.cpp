@@ -15,7 +15,7 @@ struct lizg_rx {
   int max_frames = 0, device = -1;
   // device tables
   int16_t *uv = nullptr, *perm[4] = {nullptr, nullptr, nullptr, nullptr};
-  int32_t *tix = nullptr, *block_tier = nullptr, *block_slot = nullptr, *pilot_coef = nullptr;
+  int32_t *block_tier = nullptr, *block_slot = nullptr, *pilot_coef = nullptr;
   uint8_t *white = nullptr, *pilot_white = nullptr;
   float2 *rot = nullptr;
   // transform tables
@@ -34,7 +34,8 @@ struct lizg_rx {
   lizg::SampleDev sd{};
   float *node_xy = nullptr;
   float4 *sample_t = nullptr;
-  float2 *Y = nullptr, *T = nullptr;
+  float2 *Y = nullptr, *C = nullptr;   // column transforms' kept rows; the spectrum's used coefficients in pos order
+  int32_t *tpos = nullptr;             // vrows x n: the pos index of each kept spectrum point, -1 where unused
   // per-tier streams, forked from and joined to the caller's
   cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -75,7 +76,7 @@ lizg::FmtDev fmt_dev(const lizg_rx *r, int frames) {
     d.tier_first[t] = f.tier_first[t]; d.tier_blocks[t] = f.tier[t].blocks; d.tier_slots[t] = f.tier[t].slots;
     d.tier_nt[t] = f.tier[t].nt; d.tier_k[t] = f.tier[t].k; d.perm[t] = r->perm[t];
   }
-  d.uv = r->uv; d.tix = r->tix; d.white = r->white; d.block_tier = r->block_tier; d.block_slot = r->block_slot;
+  d.uv = r->uv; d.white = r->white; d.block_tier = r->block_tier; d.block_slot = r->block_slot;
   d.pilot_coef = r->pilot_coef; d.pilot_white = r->pilot_white; d.rot = r->rot;
   return d;
 }
@@ -107,7 +108,6 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   cudaError_t e = cudaSuccess;
   auto ok = [&](cudaError_t x) { if (e == cudaSuccess) e = x; return e == cudaSuccess; };
   ok(dev_copy(r, &r->uv, f.uv.data(), f.uv.size()));
-  ok(dev_copy(r, &r->tix, f.tix.data(), f.tix.size()));
   ok(dev_copy(r, &r->white, f.white.data(), f.white.size()));
   for (int t = 0; t < f.tiers; t++) ok(dev_copy(r, &r->perm[t], f.perm[t].data(), f.perm[t].size()));
   ok(dev_copy(r, &r->block_tier, f.block_tier.data(), f.block_tier.size()));
@@ -164,7 +164,12 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   ok(dev_alloc(r, &r->fac, F * (2 * (size_t)n + r->xd.vrows)));
   ok(dev_alloc(r, &r->part, F * (size_t)(n / 2) * 5));   // column tiles (at most n / 2) x 5
   ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
-  ok(dev_alloc(r, &r->T, F * (size_t)r->xd.vrows * n));
+  ok(dev_alloc(r, &r->C, F * need));
+  {
+    std::vector<int32_t> tp((size_t)r->xd.vrows * n, -1);
+    for (size_t i = 0; i < need; i++) tp[f.tix[i]] = (int32_t)i;
+    ok(dev_copy(r, &r->tpos, tp.data(), tp.size()));
+  }
   ok(dev_alloc(r, &r->llrf, F * 2 * need));
   ok(dev_alloc(r, &r->sub_est, F * f.subch));
   ok(dev_alloc(r, &r->sub_rms, F * f.subch));
@@ -256,10 +261,10 @@ int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm) {
 
 int lizg_rx_launches(const lizg_rx *r) { return r ? r->launches : LIZG_E_ARG; }
 
-// Rows (c), (d), (e) on a batch of spectra (spec: frame f's coefficient i at spec[f stride + (idx ? idx[i] : i)]):
+// Rows (c), (d), (e) on a batch of spectra (spec: frame f's coefficient i, pos order, at spec[f stride + i]):
 // the pilots' fit, the soft values, the block stage, then the LDPC and CRC of every block not declined, the four
 // codes on their own streams.
-static int finish_spec(lizg_rx *r, const float2 *spec, int64_t stride, const int32_t *idx, int frames, const lizg_rx_out *out, cudaStream_t st, int sms) {
+static int finish_spec(lizg_rx *r, const float2 *spec, int64_t stride, int frames, const lizg_rx_out *out, cudaStream_t st, int sms) {
   const lizg::Format &f = r->f;
   lizg::FmtDev fd = fmt_dev(r, frames);
   const int64_t need = (int64_t)f.subch * lizg::kSub;
@@ -269,7 +274,7 @@ static int finish_spec(lizg_rx *r, const float2 *spec, int64_t stride, const int
   float *est = out->est ? out->est : r->est;
   float *pilot = out->pilot ? out->pilot : r->pilot;
   float *align = out->align ? out->align : r->align;
-  cudaError_t e = lizg::demap_launch(fd, spec, stride, idx, align, llrf, sub_est, sub_rms, est, pilot, r->decl, st);
+  cudaError_t e = lizg::demap_launch(fd, spec, stride, align, llrf, sub_est, sub_rms, est, pilot, r->decl, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("demap: ") + cudaGetErrorString(e)).c_str());
   r->launches += 3;
   if ((e = cudaMemsetAsync(r->counters, 0, 4 * sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(r->fork, st)) != cudaSuccess)
@@ -300,23 +305,18 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
   int sms = 0;
   if (int rc = check_call(r, d_coef, frames, out, "lizg_rx_finish_coef_dev", &sms)) return rc;
   r->launches = 0;
-  return finish_spec(r, reinterpret_cast<const float2 *>(d_coef), (int64_t)r->f.subch * lizg::kSub, nullptr, frames, out, static_cast<cudaStream_t>(stream), sms);
+  return finish_spec(r, reinterpret_cast<const float2 *>(d_coef), (int64_t)r->f.subch * lizg::kSub, frames, out, static_cast<cudaStream_t>(stream), sms);
 }
 
 // Rows (b) to (e) from a picture source: the anchors' erase and the detrended 2D transform, then as above.
 static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const lizg_rx_out *out, float *d_coef, cudaStream_t st, int sms) {
-  const int n = r->f.n;
-  const int64_t tstride = (int64_t)r->xd.vrows * n;
-  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->T};
+  const int need = r->f.subch * lizg::kSub;
+  float2 *C = d_coef ? reinterpret_cast<float2 *>(d_coef) : r->C;   // the caller's spectrum buffer when given
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, C};
   cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
   r->launches += 4;
-  if (d_coef) {
-    if ((e = lizg::gather_coef_launch(r->T, tstride, r->tix, r->f.subch * lizg::kSub, frames, reinterpret_cast<float2 *>(d_coef), st)) != cudaSuccess)
-      return lizg::record_error(LIZG_E_CUDA, (std::string("gather: ") + cudaGetErrorString(e)).c_str());
-    r->launches++;
-  }
-  return finish_spec(r, r->T, tstride, r->tix, frames, out, st, sms);
+  return finish_spec(r, C, need, frames, out, st, sms);
 }
 
 int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const lizg_rx_out *out, float *d_coef, void *stream) {

@@ -60,9 +60,9 @@ def test_gpu_luma_path_matches_oracle(n, subch, W, H, warped):
     assert np.array_equal(out["llrf"][0], llrf)
     assert np.array_equal(out["ok"][0], res["ok"]) and out["ok"][0].all()
     assert np.array_equal(out["blocks"][0], blocks)
-    assert rx.launches == 1 + 4 + 1 + 3 + f.tiers
+    assert rx.launches == 1 + 4 + 3 + f.tiers
     # the sampler fused into the transform's passes (no grid asked for) gives the same spectrum, soft values, blocks
     fused = rx.finish_luma(np.stack([luma, luma]), np.stack([reg, reg]), grid=False)
     for k in ("coef", "llrf", "its", "ok", "blocks", "align"):
         assert np.array_equal(fused[k], out[k]), k
-    assert rx.launches == 4 + 1 + 3 + f.tiers
+    assert rx.launches == 4 + 3 + f.tiers
