@@ -6,7 +6,10 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <cooperative_groups.h>
 #include "lizg_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace lizg {
 
@@ -21,55 +24,75 @@ __device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, i
   return make_float2(z.x * cs.x + z.y * cs.y, z.y * cs.x - z.x * cs.y);
 }
 
-// One CTA a frame. Its threads work out every pilot's six products in parallel into shared memory; six threads
-// then add one sum each in pilot order, so the double sums are the reference's (liblizard/src/lizard_phy.c:283-317).
-// Writes align[3 f ..] = dx, dy, and 1 where the shift is turned back.
-__global__ void __launch_bounds__(256) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, float *align) {
-  extern __shared__ double tm[];              // npilot x 6
+// A cluster of kPilotCtas CTAs a frame: CTA r works out the six products of pilots [r chunk, (r + 1) chunk) into its
+// shared memory; then six threads of CTA 0 add one sum each in pilot order, reading the cluster's shared memory, so
+// the double sums are the reference's (liblizard/src/lizard_phy.c:283-317), and CTA 0's thread 0 solves for the
+// shift and hands it to every CTA for the second fit. Writes align[3 f ..] = dx, dy, and 1 where the shift is turned
+// back. (The products are spread over the cluster's SMs because double arithmetic is slow on one SM.)
+constexpr int kPilotCtas = 8;
+
+__global__ void __cluster_dims__(kPilotCtas, 1, 1) __launch_bounds__(128) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride,
+                                                                                           float *align) {
+  extern __shared__ double tm[];              // chunk x 6: this CTA's pilots' products
   __shared__ double sums[6], dxy[2];
   __shared__ int give_up;
-  const int f = blockIdx.x, used = fd.npilot;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank(), f = blockIdx.x / kPilotCtas, used = fd.npilot;
+  const int chunk = (used + kPilotCtas - 1) / kPilotCtas, p0 = rank * chunk, p1 = min(used, p0 + chunk);
   const float2 *sp = spec + f * spec_stride;
   const double k = 2.0 * 3.14159265358979323846 / fd.n;
   if (threadIdx.x == 0) { dxy[0] = dxy[1] = 0; give_up = 0; }
-  __syncthreads();
+  cl.sync();
   for (int it = 0; it < 2; it++) {
     const double dx = dxy[0], dy = dxy[1];
-    for (int pi = threadIdx.x; pi < used; pi += blockDim.x) {
+    for (int pi = p0 + (int)threadIdx.x; pi < p1; pi += blockDim.x) {
       const int i = fd.pilot_coef[pi], w = fd.pilot_white[pi];
       const float2 y = turned(fd, sp, i, (float)dx, (float)dy);
       const double xr = (w & 1) ? -1.0 : 1.0, xi = (w & 2) ? -1.0 : 1.0;
       const double zr = (double)y.x * xr + (double)y.y * xi, zi = (double)y.y * xr - (double)y.x * xi;
       const double cu = k * zr * fd.uv[2 * i], cv = k * zr * fd.uv[2 * i + 1];
-      double *t = tm + 6 * pi;
+      double *t = tm + 6 * (pi - p0);
       t[0] = cu * cu; t[1] = cu * cv; t[2] = cv * cv; t[3] = cu * zi; t[4] = cv * zi; t[5] = zi * zi;
     }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-      // in pilot order; the loads of eight terms issued ahead of their adds
-      double acc = 0;
-      int pi = 0;
-      for (; pi + 8 <= used; pi += 8) {
-        double v[8];
+    cl.sync();
+    if (rank == 0) {
+      if (threadIdx.x < 6) {
+        // in pilot order, CTA by CTA; the loads of eight terms issued ahead of their adds
+        double acc = 0;
+        for (int r = 0; r < kPilotCtas; r++) {
+          const double *rt = cl.map_shared_rank(tm, r) + threadIdx.x;
+          const int cnt = max(0, min(used, (r + 1) * chunk) - r * chunk);
+          int q = 0;
+          for (; q + 8 <= cnt; q += 8) {
+            double v[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) v[q] = tm[6 * (pi + q) + threadIdx.x];
+            for (int e = 0; e < 8; e++) v[e] = rt[6 * (q + e)];
 #pragma unroll
-        for (int q = 0; q < 8; q++) acc += v[q];
+            for (int e = 0; e < 8; e++) acc += v[e];
+          }
+          for (; q < cnt; q++) acc += rt[6 * q];
+        }
+        sums[threadIdx.x] = acc;
       }
-      for (; pi < used; pi++) acc += tm[6 * pi + threadIdx.x];
-      sums[threadIdx.x] = acc;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const double a = sums[0], b = sums[1], c = sums[2], p = sums[3], q = sums[4];
+        const double det = a * c - b * b;
+        int gu = 0;
+        double nx = dx, ny = dy;
+        if (used < 8 || !(det > 0)) gu = 1;
+        else { nx = dx + (p * c - q * b) / det; ny = dy + (a * q - b * p) / det; }
+        for (int r = 0; r < kPilotCtas; r++) {
+          double *rd = cl.map_shared_rank(dxy, r);
+          rd[0] = nx; rd[1] = ny;
+          *cl.map_shared_rank(&give_up, r) = gu;
+        }
+      }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const double a = sums[0], b = sums[1], c = sums[2], p = sums[3], q = sums[4];
-      const double det = a * c - b * b;
-      if (used < 8 || !(det > 0)) give_up = 1;
-      else { dxy[0] = dx + (p * c - q * b) / det; dxy[1] = dy + (a * q - b * p) / det; }
-    }
-    __syncthreads();
+    cl.sync();
     if (give_up) break;
   }
-  if (threadIdx.x != 0) return;
+  if (rank != 0 || threadIdx.x != 0) return;
   float d0 = 0, d1 = 0;
   if (!give_up) {
     const double a = sums[0], b = sums[1], c = sums[2], p = sums[3], q = sums[4], yy = sums[5], dx = dxy[0], dy = dxy[1];
@@ -188,15 +211,10 @@ __global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride
 
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st) {
-  static bool attr = false;
-  const int psm = 6 * (fd.npilot > 0 ? fd.npilot : 1) * (int)sizeof(double);
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(pilot_align_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * 1024 * (int)sizeof(double));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  if (fd.npilot > 1024) return cudaErrorInvalidValue;
-  pilot_align_kernel<<<fd.frames, 256, psm, st>>>(fd, spec, spec_stride, align);
+  const int chunk = (fd.npilot + kPilotCtas - 1) / kPilotCtas;
+  const int psm = 6 * (chunk > 0 ? chunk : 1) * (int)sizeof(double);
+  if (psm > 48 * 1024) return cudaErrorInvalidValue;
+  pilot_align_kernel<<<fd.frames * kPilotCtas, 128, psm, st>>>(fd, spec, spec_stride, align);
   const int groups = fd.frames * fd.subch;
   demap_kernel<<<(groups + 63) / 64, 256, 0, st>>>(fd, spec, spec_stride, align, llrf, sub_est, sub_rms);
   const int nbk = fd.frames * fd.blocks;
