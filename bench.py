@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-receiver", action="store_true", help="skip the frame receiver's workloads")
     ap.add_argument("--receiver-only", action="store_true", help="time only the frame receiver (profiling)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the decoder's default kernel variants")
     return ap.parse_args()
 
 
@@ -304,6 +305,14 @@ def main():
     assert torch.cuda.is_available(), "bench.py needs a CUDA device"
     dev = local
     torch.cuda.set_device(dev)
+    tune = None
+    if not args.no_autotune:
+        # the decoder's kernel variant per code chosen by timing on this device, before any timed work
+        t_tune = time.perf_counter()
+        chosen = lz.ldpc_autotune(8192, synth.EBN0_SWEEP_DB)
+        tune = {"variant": {name: {"index": v, "warps_a_codeword": lz.ldpc_variant(r)[1], "loop_form": lz.ldpc_variant(r)[2]}
+                            for name, r, v in zip(("7/8", "3/4", "2/3", "1/2"), (6, 4, 3, 2), chosen)},
+                "seconds": round(time.perf_counter() - t_tune, 2), "calibration": "8192 codewords a code, all-zero codeword, BPSK/AWGN over the workload's Eb/N0 sweep"}
     if args.receiver_only:
         print(json.dumps(bench_receiver(args, torch.cuda.current_stream())))
         return
@@ -383,7 +392,8 @@ def main():
         "codewords_per_s": round(ws * args.count / (ms / 1e3), 1),
         "ldpc": {"decoded": int((its > 0).sum()), "crc_ok": int(ok[its > 0].sum()), "stalled": int((its == -3).sum()),
                  "capped": int((its == -1).sum()), "mean_iterations": round(float(lz.iterations_run(its, batch["rates"], MAX_ITER, STALL_IT).mean()), 3),
-                 "edge_updates_per_step": edges, "edge_updates_per_s": round(edges / (launch_ms / 1e3), 1)},
+                 "edge_updates_per_step": edges, "edge_updates_per_s": round(edges / (launch_ms / 1e3), 1),
+                 "autotune": tune},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
                      "traffic": None if traffic is None else int(traffic), "peak_source": peak_src,
                      "kernel": "ldpc_decode_kernel<7/8,3/4,2/3,1/2> (the 4 launches of a step)",

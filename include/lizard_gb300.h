@@ -88,6 +88,21 @@ enum { LIZG_NOALLOC_MAX_CODEWORDS = 8192 };
 int lizg_ldpc_decode_noalloc(const int8_t *d_llr, const int32_t *d_rate, int count, int max_iter, int stall_it,
                              float stall_ratio, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream);
 
+// No counterpart in the reference (its decoder has one form a build): the decoder's kernel variants and their
+// choice. Each code has a few variants that decode bit for bit alike and differ in the warps a codeword takes (1, 2
+// or 4) and in the layer form (messages held in registers, or recomputed in a loop). Variant 0 is the default on
+// every device. lizg_ldpc_autotune times every variant of every code on the current device over a seeded batch of
+// `count` codewords, codeword c at ebn0_db[c mod n_ebn0] (BPSK/AWGN, the batch's LLR quantisation), and keeps the
+// fastest per code for that device; choice[4] (may be NULL) receives the indices in code order 7/8, 3/4, 2/3, 1/2.
+// Every later decode on the device (plans, the single-codeword call, the receiver, the allocation-free call) uses
+// the kept variant.
+// lizg_ldpc_set_variant fixes one by hand; lizg_ldpc_variant returns the current index and its warps a codeword and
+// form (1 = loop); lizg_ldpc_variants the number of variants of a rate.
+int lizg_ldpc_autotune(int count, const float *ebn0_db, int n_ebn0, int32_t *choice);
+int lizg_ldpc_variants(int rate);
+int lizg_ldpc_variant(int rate, int32_t *wpc, int32_t *loop_form);
+int lizg_ldpc_set_variant(int rate, int index);
+
 // ---------------------------------------------------------------- the receiver (rows a-e)
 //
 // A receiver handle for one format: the picture size n (384, 512, 768, 1024, 1152, 1280, 1536), the sub-channels

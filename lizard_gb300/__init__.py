@@ -55,6 +55,10 @@ def lib():
     L.lizg_ldpc_plan_run_dev.argtypes = [P, P, P, P, P, P]
     L.lizg_ldpc_plan_run.argtypes = [P, P, P, P, P, P]
     L.lizg_ldpc_plan_launches.argtypes = [P]
+    L.lizg_ldpc_autotune.argtypes = [I, P, I, P]
+    L.lizg_ldpc_variants.argtypes = [I]
+    L.lizg_ldpc_variant.argtypes = [I, P, P]
+    L.lizg_ldpc_set_variant.argtypes = [I, I]
     _lib = L
     return L
 
@@ -88,6 +92,32 @@ def ldpc_encode_many(rate, data):
     cw = np.zeros((data.shape[0], CODE_N[rate]), np.uint8)
     _check(lib().lizg_ldpc_encode_many(rate, _ptr(data), data.shape[0], _ptr(cw)), "lizg_ldpc_encode_many")
     return cw
+
+
+def ldpc_autotune(count=8192, ebn0_db=(1.0, 1.5, 2.0, 2.5, 3.0, 3.5, 4.0)):
+    """Times every decoder variant of every code on the current device over count codewords a code (codeword c at
+    ebn0_db[c % len]) and keeps the fastest per code; returns the chosen variant indices in code order 7/8, 3/4,
+    2/3, 1/2."""
+    e = np.ascontiguousarray(np.atleast_1d(ebn0_db), np.float32)
+    ch = np.zeros(4, np.int32)
+    _check(lib().lizg_ldpc_autotune(count, _ptr(e), e.size, _ptr(ch)), "lizg_ldpc_autotune")
+    return [int(x) for x in ch]
+
+
+def ldpc_variants(rate):
+    """How many decoder variants the code of this rate has."""
+    return _check(lib().lizg_ldpc_variants(rate), "lizg_ldpc_variants")
+
+
+def ldpc_variant(rate):
+    """The current device's variant of this rate's code: (index, warps a codeword, loop form)."""
+    w, lf = np.zeros(1, np.int32), np.zeros(1, np.int32)
+    v = _check(lib().lizg_ldpc_variant(rate, _ptr(w), _ptr(lf)), "lizg_ldpc_variant")
+    return v, int(w[0]), bool(lf[0])
+
+
+def ldpc_set_variant(rate, index):
+    _check(lib().lizg_ldpc_set_variant(rate, index), "lizg_ldpc_set_variant")
 
 
 def ldpc_decode_stall(rate, llr, max_iter, stall_it=0, stall_ratio=0.0):

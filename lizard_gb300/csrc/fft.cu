@@ -18,7 +18,7 @@
 // The transforms are Stockham autosort passes of radix 16, 9, 8, 6, 5, 4, 3 or 2 (every ladder size takes three),
 // each pass in place: every thread reads its butterflies' points into registers, the CTA waits, every thread writes
 // its outputs. Shared memory holds a line with one spare slot after every 16 points (so the passes' 16-point runs,
-// read or written, fall on distinct banks within a half-warp) and lines 4 (mod 16) slots apart; the passes'
+// read or written, fall on distinct banks within a half-warp) and lines 16 / L (mod 16) slots apart; the passes'
 // twiddles sit beside the lines, per pass [r - 1][k], so a warp reads consecutive entries. FP32 throughout, as the
 // reference's; the twiddles and the surface factors are worked out in double.
 #include <cuda_runtime.h>
@@ -143,8 +143,9 @@ __host__ __device__ constexpr Plan plan_of(int n) {
          : n == 1536 ? Plan{16, 16, 6, 4}
                      : Plan{0, 0, 0, 0};
 }
-// Slots from one line to the next: the padded line rounded up to 16 slots, plus 4.
-__host__ __device__ constexpr int lstride_of(int n) { return (n + n / 16 + 15) / 16 * 16 + 4; }
+// Slots from one line to the next: the padded line rounded up to 16 slots, plus 16 / L, so that the L lines x
+// 16 / L rows a half-warp stores while loading (and reads while separating) fall on 16 distinct slots.
+__host__ __device__ constexpr int lstride_of(int n) { return (n + n / 16 + 15) / 16 * 16 + 16 / plan_of(n).lines; }
 
 // One Stockham pass of radix R over the CTA's lines (Lr <= L of them) in place, n = N points a line. Butterfly j of
 // a line (j < NR = N / R, k = j mod NS) reads points j + r NR, turns point r by e^{-2 pi i r k / (NS R)}

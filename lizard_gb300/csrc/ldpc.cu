@@ -18,26 +18,31 @@
 #include "lizard_codes.h"
 #include "lizg_internal.h"
 #include "lizard_gb300.h"
+#include <cmath>
 #include <mutex>
+#include <random>
+#include <string>
+#include <vector>
 
 namespace lizg {
 
 // Per-code compile-time shape: block rows, codeword bits, data bits, data circulants, slots (data circulants plus
 // two staircase slots a row), and the warps a CTA runs (as many codeword states as fit in 227 KB of shared memory).
 template <int C> struct Code;
-// NDMAX: the most data circulants any block row has. WARPS: codewords a CTA holds; WPC: warps a codeword (lane l of
-// warp w of a codeword takes checks l + 32 t, t = w (4 / WPC) .. (w + 1) (4 / WPC) - 1, of every layer).
-template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, NDMAX = 21, WARPS = 9, WPC = 2; };
-template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, NDMAX = 14, WARPS = 7, WPC = 2; };
-template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, NDMAX = 10, WARPS = 6, WPC = 2; };
-template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5, WPC = 4; };
+// NDMAX: the most data circulants any block row has. WARPS: codewords a CTA holds. A kernel variant also fixes WPC,
+// the warps a codeword (lane l of warp w of a codeword takes checks l + 32 t, t = w (4 / WPC) .. (w + 1) (4 / WPC) - 1,
+// of every layer), and the layer form (registers, or the loop form that recomputes the extrinsics).
+template <> struct Code<0> { static constexpr int MB = 5, N = 4608, K = 3968, NDATA = 103, NDMAX = 21, WARPS = 9; };
+template <> struct Code<1> { static constexpr int MB = 10, N = 5120, K = 3840, NDATA = 132, NDMAX = 14, WARPS = 7; };
+template <> struct Code<2> { static constexpr int MB = 15, N = 5760, K = 3840, NDATA = 146, NDMAX = 10, WARPS = 6; };
+template <> struct Code<3> { static constexpr int MB = 30, N = 7680, K = 3840, NDATA = 150, NDMAX = 5, WARPS = 5; };
 
 template <int C> __host__ __device__ constexpr int slots() { return Code<C>::NDATA + 2 * Code<C>::MB; }
 // A warp's state: posteriors (N int16) then messages (slots x 128 int8), rounded to 16 bytes.
 template <int C> __host__ __device__ constexpr int warp_bytes() { return (Code<C>::N * 2 + slots<C>() * 128 + 15) & ~15; }
 constexpr int kCrcBytes = (256 + 32 + 1) * 4 + 12;   // table, per-lane shifts, init term; padded to 16
 template <int C> constexpr int cta_smem() { return kCrcBytes + Code<C>::WARPS * warp_bytes<C>(); }
-template <int C> constexpr int cta_threads() { return Code<C>::WARPS * Code<C>::WPC * 32; }
+template <int C, int WPC> __host__ __device__ constexpr int cta_threads() { return Code<C>::WARPS * WPC * 32; }
 
 static_assert(cta_smem<0>() <= 227 * 1024, "7/8 state does not fit");
 static_assert(cta_smem<1>() <= 227 * 1024, "3/4 state does not fit");
@@ -273,10 +278,11 @@ __device__ __forceinline__ void group_sync(int g) {
   else asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(WPC * 32) : "memory");
 }
 
-template <int C>
-__global__ void __launch_bounds__(cta_threads<C>(), 1) ldpc_decode_kernel(LdpcLaunch a) {
+template <int C, int WPC, bool LOOP>
+__global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(LdpcLaunch a) {
   using T = Code<C>;
-  constexpr int WPC = T::WPC, CPL = 4 / WPC, GT = WPC * 32;
+  constexpr int CPL = 4 / WPC, GT = WPC * 32;
+  static_assert(cta_threads<C, WPC>() <= 1024, "a CTA of at most 1024 threads");
   static_assert(T::WARPS <= 15, "one named barrier a codeword");
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int s_item[T::WARPS], s_red[T::WARPS][WPC];
@@ -351,8 +357,7 @@ __global__ void __launch_bounds__(cta_threads<C>(), 1) ldpc_decode_kernel(LdpcLa
     for (int it = 0; it < a.max_iter; it++) {
       for (int step = 0; step < T::MB; step++) {
         const int r = (it & 1) ? T::MB - 1 - step : step;
-        // the 7/8 code's 21-circulant rows run faster in the loop form
-        if (T::NDMAX > 16) layer_loop<C, CPL>(L, R, r, lane, t0);
+        if (LOOP) layer_loop<C, CPL>(L, R, r, lane, t0);
         else layer<C, CPL>(L, R, r, lane, t0);
         group_sync<WPC>(g);
       }
@@ -440,30 +445,202 @@ cudaError_t ldpc_upload_tables() {
   return cudaMemcpyToSymbol(c_crc_shift, k, sizeof k);
 }
 
-template <int C>
-static cudaError_t launch_one(const LdpcLaunch &a, int sms, cudaStream_t st) {
+// ---------------------------------------------------------------- kernel variants and their choice
+//
+// Every variant decodes bit for bit alike (the layers' arithmetic and order are the same); they differ in how a
+// codeword's checks are spread over warps and in register use, so which is fastest depends on the device, the code
+// and the channel. Variant 0 of each code is the default; lizg_ldpc_autotune times them all on the current device
+// and keeps the fastest per code.
+struct Variant {
+  int wpc;
+  bool loop;
+};
+constexpr int kMaxVariants = 4;
+static const Variant kVariants[4][kMaxVariants] = {
+    {{2, true}, {1, true}, {2, false}, {0, false}},   // 7/8: 21-circulant rows, the loop form first
+    {{2, false}, {1, true}, {4, false}, {2, true}},    // 3/4
+    {{2, false}, {1, true}, {4, false}, {0, false}},   // 2/3
+    {{4, false}, {2, false}, {1, false}, {0, false}},  // 1/2
+};
+static int variant_count(int code) {
+  int k = 0;
+  while (k < kMaxVariants && kVariants[code][k].wpc) k++;
+  return k;
+}
+
+constexpr int kMaxDevices = 64;
+static int g_choice[kMaxDevices][4];   // per device and code: the variant index (0 until tuned or set)
+static std::mutex g_choice_mu;
+
+static int choice_of(int code) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  return dev >= 0 && dev < kMaxDevices ? g_choice[dev][code] : 0;
+}
+
+template <int C, int WPC, bool LOOP>
+static cudaError_t launch_v(const LdpcLaunch &a, int sms, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(ldpc_decode_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, cta_smem<C>());
+    cudaError_t e = cudaFuncSetAttribute(ldpc_decode_kernel<C, WPC, LOOP>, cudaFuncAttributeMaxDynamicSharedMemorySize, cta_smem<C>());
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   const int need = (a.count + Code<C>::WARPS - 1) / Code<C>::WARPS;
   const int grid = need < sms ? need : sms;
-  ldpc_decode_kernel<C><<<grid, cta_threads<C>(), cta_smem<C>(), st>>>(a);
+  ldpc_decode_kernel<C, WPC, LOOP><<<grid, cta_threads<C, WPC>(), cta_smem<C>(), st>>>(a);
   return cudaGetLastError();
+}
+
+static cudaError_t launch_variant(int code, int v, const LdpcLaunch &a, int sms, cudaStream_t st) {
+  switch (code * kMaxVariants + v) {
+    case 0: return launch_v<0, 2, true>(a, sms, st);
+    case 1: return launch_v<0, 1, true>(a, sms, st);
+    case 2: return launch_v<0, 2, false>(a, sms, st);
+    case 4: return launch_v<1, 2, false>(a, sms, st);
+    case 5: return launch_v<1, 1, true>(a, sms, st);
+    case 6: return launch_v<1, 4, false>(a, sms, st);
+    case 7: return launch_v<1, 2, true>(a, sms, st);
+    case 8: return launch_v<2, 2, false>(a, sms, st);
+    case 9: return launch_v<2, 1, true>(a, sms, st);
+    case 10: return launch_v<2, 4, false>(a, sms, st);
+    case 12: return launch_v<3, 4, false>(a, sms, st);
+    case 13: return launch_v<3, 2, false>(a, sms, st);
+    case 14: return launch_v<3, 1, false>(a, sms, st);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st) {
   if (a.count <= 0) return cudaSuccess;
-  switch (code) {
-    case 0: return launch_one<0>(a, sms, st);
-    case 1: return launch_one<1>(a, sms, st);
-    case 2: return launch_one<2>(a, sms, st);
-    case 3: return launch_one<3>(a, sms, st);
-  }
-  return cudaErrorInvalidValue;
+  if (code < 0 || code > 3) return cudaErrorInvalidValue;
+  return launch_variant(code, choice_of(code), a, sms, st);
 }
+
+}  // namespace lizg
+
+extern "C" {
+
+int lizg_ldpc_variants(int rate) {
+  const int c = lizg_code_of_rate(rate);
+  if (c < 0) return lizg::record_error(LIZG_E_ARG, "lizg_ldpc_variants: rate must be 6, 4, 3 or 2");
+  return lizg::variant_count(c);
+}
+
+int lizg_ldpc_variant(int rate, int32_t *wpc, int32_t *loop_form) {
+  const int c = lizg_code_of_rate(rate);
+  if (c < 0) return lizg::record_error(LIZG_E_ARG, "lizg_ldpc_variant: rate must be 6, 4, 3 or 2");
+  int sms = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  const int v = lizg::choice_of(c);
+  if (wpc) *wpc = lizg::kVariants[c][v].wpc;
+  if (loop_form) *loop_form = lizg::kVariants[c][v].loop ? 1 : 0;
+  return v;
+}
+
+// The calibration batch of a code: count copies of the all-zero codeword (a min-sum decoder treats every codeword
+// alike, the channel being symmetric) sent as BPSK over AWGN, codeword c at ebn0_db[c mod n_ebn0], quantised as the
+// batch benchmark's LLRs (nearest of 8 clamp(2 y / sigma^2, +-10)), the 7/8 code's unsent known zeros at +127.
+static void calibration_llrs(int code, int count, const float *ebn0_db, int n_ebn0, std::vector<int8_t> &llr) {
+  const lizg_code_def_t &d = LIZG_CODES[code];
+  const int n = (d.mb + d.kb) * 128, k = d.kb * 128, sent = n - (k - LIZG_INFO_BITS);
+  const double rate = (double)LIZG_INFO_BITS / sent;
+  std::mt19937 gen(20240u + (unsigned)code);
+  std::normal_distribution<double> g(0.0, 1.0);
+  llr.resize((size_t)count * n);
+  for (int c = 0; c < count; c++) {
+    const double ebn0 = std::pow(10.0, ebn0_db[c % n_ebn0] / 10.0), sigma = std::sqrt(1.0 / (2.0 * rate * ebn0));
+    for (int i = 0; i < n; i++) {
+      int8_t q = 127;
+      if (i < LIZG_INFO_BITS || i >= k) {
+        double l = 2.0 * (1.0 + sigma * g(gen)) / (sigma * sigma);
+        l = l > 10 ? 10 : l < -10 ? -10 : l;
+        q = (int8_t)std::nearbyint(8 * l);
+      }
+      llr[(size_t)c * n + i] = q;
+    }
+  }
+}
+
+int lizg_ldpc_autotune(int count, const float *ebn0_db, int n_ebn0, int32_t *choice) {
+  if (count < 1 || count > (1 << 16)) return lizg::record_error(LIZG_E_ARG, "lizg_ldpc_autotune: count must be 1..65536");
+  if (!ebn0_db || n_ebn0 < 1) return lizg::record_error(LIZG_E_ARG, "lizg_ldpc_autotune: no Eb/N0 given");
+  int sms = 0, dev = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= lizg::kMaxDevices) return lizg::record_error(LIZG_E_STATE, "lizg_ldpc_autotune: device index out of range");
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::vector<void *> bufs;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int c = 0; c < 4 && e == cudaSuccess; c++) {
+    const lizg_code_def_t &d = LIZG_CODES[c];
+    const int n = (d.mb + d.kb) * 128;
+    std::vector<int8_t> llr;
+    calibration_llrs(c, count, ebn0_db, n_ebn0, llr);
+    std::vector<int32_t> list(count);
+    std::vector<int64_t> off(count);
+    for (int i = 0; i < count; i++) { list[i] = i; off[i] = (int64_t)i * n; }
+    void *d_llr = nullptr, *d_bits = nullptr, *d_its = nullptr, *d_ok = nullptr, *d_list = nullptr, *d_off = nullptr, *d_ctr = nullptr;
+    auto al = [&](void **p, size_t b) { if (e == cudaSuccess && (e = cudaMalloc(p, b)) == cudaSuccess) bufs.push_back(*p); };
+    al(&d_llr, llr.size()); al(&d_bits, (size_t)count * n / 8); al(&d_its, 4 * (size_t)count); al(&d_ok, (size_t)count);
+    al(&d_list, 4 * (size_t)count); al(&d_off, 8 * (size_t)count); al(&d_ctr, 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d_llr, llr.data(), llr.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_list, list.data(), 4 * (size_t)count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_off, off.data(), 8 * (size_t)count, cudaMemcpyHostToDevice);
+    lizg::LdpcLaunch a{};
+    a.llr = static_cast<const int8_t *>(d_llr); a.bits = static_cast<uint8_t *>(d_bits); a.its = static_cast<int32_t *>(d_its);
+    a.ok = static_cast<uint8_t *>(d_ok); a.list = static_cast<const int32_t *>(d_list); a.off = static_cast<const int64_t *>(d_off);
+    a.count = count; a.counter = static_cast<int *>(d_ctr); a.max_iter = 20; a.stall_it = 9; a.stall_ratio = 0.95f;
+    int best = 0;
+    float best_ms = 0;
+    for (int v = 0; v < lizg::variant_count(c) && e == cudaSuccess; v++) {
+      float ms_min = 0;
+      for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {   // the first run warms up
+        if ((e = cudaMemsetAsync(d_ctr, 0, 4, st)) != cudaSuccess || (e = cudaEventRecord(e0, st)) != cudaSuccess ||
+            (e = lizg::launch_variant(c, v, a, sms, st)) != cudaSuccess || (e = cudaEventRecord(e1, st)) != cudaSuccess ||
+            (e = cudaEventSynchronize(e1)) != cudaSuccess)
+          break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep == 1 || (rep > 1 && ms < ms_min)) ms_min = ms;
+      }
+      if (e == cudaSuccess && (v == 0 || ms_min < best_ms)) { best = v; best_ms = ms_min; }
+    }
+    if (e == cudaSuccess) {
+      std::lock_guard<std::mutex> lk(lizg::g_choice_mu);
+      lizg::g_choice[dev][c] = best;
+    }
+    if (choice) choice[c] = best;
+    for (void *p : bufs) cudaFree(p);
+    bufs.clear();
+  }
+  for (void *p : bufs) cudaFree(p);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("lizg_ldpc_autotune: ") + cudaGetErrorString(e)).c_str());
+  return 0;
+}
+
+int lizg_ldpc_set_variant(int rate, int index) {
+  const int c = lizg_code_of_rate(rate);
+  if (c < 0 || index < 0 || index >= lizg::variant_count(c)) return lizg::record_error(LIZG_E_ARG, "lizg_ldpc_set_variant: no such rate or variant");
+  int sms = 0, dev = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= lizg::kMaxDevices) return lizg::record_error(LIZG_E_STATE, "lizg_ldpc_set_variant: device index out of range");
+  std::lock_guard<std::mutex> lk(lizg::g_choice_mu);
+  lizg::g_choice[dev][c] = index;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace lizg {
 
 // ---------------------------------------------------------------- the decode without allocation
 //

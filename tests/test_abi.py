@@ -63,6 +63,16 @@ def test_bad_arguments_are_errors():
         lz.LdpcPlan(np.array([6, 7], np.int32))
     with pytest.raises(lz.LizgError):
         lz.LdpcPlan(np.array([6], np.int32), max_iter=0)
+    with pytest.raises(lz.LizgError):
+        lz.ldpc_variants(5)
+    with pytest.raises(lz.LizgError):
+        lz.ldpc_set_variant(6, 99)
+    with pytest.raises(lz.LizgError):
+        lz.ldpc_autotune(0)
+
+
+def test_decoder_variants_listed():
+    assert [lz.ldpc_variants(r) for r in (6, 4, 3, 2)] == [3, 4, 3, 3]
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU behaviour")

@@ -123,3 +123,31 @@ def test_full_size_batch_properties():
     assert (its[hi & (b["rates"] != 6)] > 0).mean() > 0.99
     sub = {k: v for k, v in synth.ldpc_batch(512, seed=0).items()}
     check_against_oracle(sub)
+
+
+@pytest.mark.parametrize("rate", [6, 4, 3, 2])
+def test_every_variant_decodes_alike(rate):
+    """Each kernel variant (warps a codeword, layer form) gives the oracle's decodes bit for bit."""
+    b = synth.ldpc_batch(600, seed=40 + rate, rates=np.full(600, rate, np.int32))
+    ob, oi, oo = oracle.ldpc_batch(oracle.port(), b["llr"], b["offsets"], b["rates"], 20, 9, 0.95, threads=os.cpu_count() or 4)
+    try:
+        for v in range(lz.ldpc_variants(rate)):
+            lz.ldpc_set_variant(rate, v)
+            assert lz.ldpc_variant(rate)[0] == v
+            bits, its, ok = lz.LdpcPlan(b["rates"], 20, 9, 0.95).run(b["llr"])
+            assert np.array_equal(its, oi), "variant %d" % v
+            assert np.array_equal(bits, ob) and np.array_equal(ok, oo), "variant %d" % v
+    finally:
+        lz.ldpc_set_variant(rate, 0)
+
+
+def test_autotune_keeps_a_variant_and_decodes_alike():
+    try:
+        ch = lz.ldpc_autotune(256, (1.5, 3.0))
+        assert [lz.ldpc_variant(r)[0] for r in (6, 4, 3, 2)] == ch
+        for c, r in zip(ch, (6, 4, 3, 2)):
+            assert 0 <= c < lz.ldpc_variants(r)
+        check_against_oracle(synth.ldpc_batch(1500, seed=77))
+    finally:
+        for r in (6, 4, 3, 2):
+            lz.ldpc_set_variant(r, 0)
