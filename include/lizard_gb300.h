@@ -177,6 +177,26 @@ int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int
 int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
                               int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
 
+// ---------------------------------------------------------------- registration assist: the anchor search
+//
+// Replaces anchor_find (liblizard/src/acquire.c:1876-2036), the registration's search for the picture's 7 x 7 anchors
+// about where H (and the lens model, when given) puts them, for a batch of frames on the GPU. The arithmetic is the
+// reference's portable build's (its scalar twins of the SIMD paths): a window of (16 + 2 r)^2 samples a / 16 modules
+// apart (a = span / 64 the anchor's side, r = ceil(3 / (a / 16)) steps of reach), the normalised correlation with
+// the anchor's two concentric squares at every offset, the first largest, a parabola each way. Anchor k of frame f
+// (k = j * 7 + i, row j, column i) is out[f * 49 + k]: ok (the peak reaches 0.6 off the window's edge), the peak,
+// dx, dy (its middle in the image less where H puts it, pixels) and u, v (its middle in the image).
+// Frame f: its w x h greys at d_luma + f * frame_stride (rows w apart, as the reference's image_t), its H (module ->
+// image, 9 floats) at d_H + f * h_stride (a receiver's registrations can be passed as they are: h_stride = 9 + 2 nx ny),
+// its lens model at d_lens + f * 15 (K, ax, ay, R, then 11 coefficients, the reference's lensm_t) or d_lens NULL for
+// none. d_skip (frames x 49, may be NULL) marks anchors found before: their outputs are left as they are.
+typedef struct {
+  uint8_t *ok;
+  float *peak, *dx, *dy, *u, *v;
+} lizg_anchor_out;
+int lizg_anchor_find_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
+                         const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -203,6 +203,7 @@ def _rx_sigs(L):
     L.lizg_rx_finish_grid_dev.argtypes = [P, P, I, P, P, P]
     L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
     L.lizg_rx_finish_luma_graph.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
+    L.lizg_anchor_find_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, P, P, I, P, P]
 
 
 class RxOut(ctypes.Structure):
@@ -334,3 +335,35 @@ class Receiver:
             out["grid"] = g.cpu().numpy()
         out["coef"] = c.cpu().numpy()
         return out
+
+
+class AnchorOut(ctypes.Structure):
+    _fields_ = [("ok", ctypes.c_void_p), ("peak", ctypes.c_void_p), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
+                ("u", ctypes.c_void_p), ("v", ctypes.c_void_p)]
+
+
+def anchor_find(span, luma, H, lens=None, skip=None, stream=None):
+    """The anchor search on the GPU for a batch of frames: luma frames x h x w uint8, H frames x 9 (or frames x
+    stride: a receiver's registrations), lens frames x 15 float64 or None, skip frames x 49 or None. Returns a dict of
+    frames x 49 arrays ok, peak, dx, dy, u, v."""
+    import torch
+    lib()
+    lu = np.ascontiguousarray(luma, np.uint8)
+    if lu.ndim == 2:
+        lu = lu[None]
+    frames, h, w = lu.shape
+    Hf = np.ascontiguousarray(np.asarray(H, np.float32).reshape(frames, -1))
+    d_l, d_h = torch.from_numpy(lu).cuda(), torch.from_numpy(Hf).cuda()
+    d_lens = None if lens is None else torch.from_numpy(np.ascontiguousarray(np.asarray(lens, np.float64).reshape(frames, 15))).cuda()
+    d_skip = None if skip is None else torch.from_numpy(np.ascontiguousarray(np.asarray(skip, np.uint8).reshape(frames, 49))).cuda()
+    o = {"ok": torch.zeros((frames, 49), dtype=torch.uint8, device="cuda")}
+    for k in ("peak", "dx", "dy", "u", "v"):
+        o[k] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
+    s = AnchorOut(*[o[k].data_ptr() for k in ("ok", "peak", "dx", "dy", "u", "v")])
+    st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+    _check(lib().lizg_anchor_find_dev(span, ctypes.c_void_p(d_l.data_ptr()), w, h, h * w, ctypes.c_void_p(d_h.data_ptr()), Hf.shape[1],
+                                      None if d_lens is None else ctypes.c_void_p(d_lens.data_ptr()),
+                                      None if d_skip is None else ctypes.c_void_p(d_skip.data_ptr()), frames, ctypes.byref(s), ctypes.c_void_p(st)),
+           "lizg_anchor_find_dev")
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in o.items()}

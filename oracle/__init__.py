@@ -13,10 +13,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+REF_SCALAR_PATH = os.path.join(HERE, "_ref", "libref_scalar.so")
 REF_SRC = "/root/reference/liblizard/src"
 
 _port = None
 _ref = None
+_ref_scalar = None
 
 
 class Code(ctypes.Structure):
@@ -46,6 +48,7 @@ def port():
         L.orc_crc32c.argtypes = [P, I]
         L.orc_crc32c.restype = ctypes.c_uint32
         L.orc_ldpc_batch.argtypes = [P, P, P, I, I, I, F, P, P, P, I]
+        L.orc_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
         _port = L
     return _port
 
@@ -70,8 +73,36 @@ def ref():
     return _ref
 
 
+def ref_scalar():
+    """The reference's portable build (-DOB_SCALAR) with the anchor search's harness, or None where it could not be
+    built here."""
+    global _ref_scalar
+    if _ref_scalar is None and os.path.exists(REF_SCALAR_PATH):
+        L = ctypes.CDLL(REF_SCALAR_PATH)
+        P, I = ctypes.c_void_p, ctypes.c_int
+        L.refs_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
+        _ref_scalar = L
+    return _ref_scalar
+
+
 def _p(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def anchor_find(lib, fn, span, luma, H, lens=None, ok_in=None):
+    """One frame's anchor search through lib.fn (the oracle's orc_anchor_find or the reference's refs_anchor_find):
+    a dict of 49-entry arrays ok, peak, dx, dy, u, v, and found."""
+    luma = np.ascontiguousarray(luma, np.uint8)
+    h, w = luma.shape
+    Hf = np.ascontiguousarray(H, np.float32).ravel()[:9]
+    ln = None if lens is None else np.ascontiguousarray(lens, np.float64)
+    oi = None if ok_in is None else np.ascontiguousarray(ok_in, np.uint8)
+    out = {"ok": np.zeros(49, np.uint8)}
+    for k in ("peak", "dx", "dy", "u", "v"):
+        out[k] = np.zeros(49, np.float32)
+    out["found"] = getattr(lib, fn)(span, _p(luma), w, h, _p(Hf), None if ln is None else _p(ln), None if oi is None else _p(oi),
+                                    _p(out["ok"]), _p(out["peak"]), _p(out["dx"]), _p(out["dy"]), _p(out["u"]), _p(out["v"]))
+    return out
 
 
 def code(rate):

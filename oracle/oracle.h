@@ -63,6 +63,12 @@ int orc_blocks(const orc_fmt_t *f, const int8_t *llrf, const double *sub_est, co
 int orc_layout_nodes(int side, float *pos);
 int orc_sample_grid(int n, int span, const uint8_t *luma, int w, int h, int pitch, const float *reg, float *grid);
 
+// The anchor search (liblizard/src/acquire.c:1876-2036, the portable build): one frame (w x h greys, rows w apart),
+// H (module -> image, 9 floats), the lens model (NULL, or K, ax, ay, R, then 11 coefficients), the anchors already
+// found (49 flags or NULL). Out per anchor (row-major j * 7 + i): ok, peak, dx, dy, u, v. Returns the anchors ok.
+int orc_anchor_find(int span, const uint8_t *px, int w, int h, const float *H, const double *lens, const uint8_t *ok_in,
+                    uint8_t *ok, float *peak, float *dx, float *dy, float *u, float *v);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,148 @@
+// Oracle (test infrastructure only): the anchor search of the registration's front half, restated in plain C from the
+// reference's portable build (liblizard/src/acquire.c:1876-2036 anchor_find, its #else branch: the scalar twin of the
+// SIMD paths), to hold the GPU's anchor search to. Compiled with -ffp-contract=off: every float and double operation
+// rounds once, in the reference's order. Pinned against the reference's own portable build (oracle/_ref/
+// libref_scalar.so) by the CPU tests and against fixtures it made (tests/golden/anchor_ref.npz).
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include "oracle.h"
+
+enum { ANK = 7, ANTS = 16, ANREACH = 3, LENSP = 11, MARGIN = 15 };
+static const float ANPEAK = 0.6f;
+
+// The layout's anchor lattice (liblizard/src/acquire.c:41-45): side a = span / 64 modules, anchor i's low edge m0.
+static int anchor_m0(int span, int i) {
+  const int a = span / 64;
+  return (int)floor(MARGIN + (double)span * (i + 0.5) / ANK - a / 2.0 + 0.5);
+}
+
+// H: module -> image (liblizard/src/internal.h:107-112).
+static void project(const float *h, float x, float y, float *u, float *v) {
+  const float w = h[6] * x + h[7] * y + 1;
+  *u = (h[0] * x + h[1] * y + h[2]) / w;
+  *v = (h[3] * x + h[4] * y + h[5]) / w;
+}
+
+// The lens model's displacement at image point (u, v) (liblizard/src/acquire.c:1506-1512 lens_rows, 1615-1620
+// lensm_at): lens = K, ax, ay, R, t[LENSP].
+static void lens_at(const double *lens, double u, double v, float *dx, float *dy) {
+  const int K = (int)lens[0];
+  const double x = (u - lens[1]) / lens[3], y = (v - lens[2]) / lens[3];
+  double rx[LENSP], ry[LENSP];
+  const double ex[8] = {x, y, 0, 0, 1, 0, -x * x, -x * y}, ey[8] = {0, 0, x, y, 0, 1, -x * y, -y * y};
+  for (int a = 0; a < 8; a++) { rx[a] = ex[a]; ry[a] = ey[a]; }
+  const double s = x * x + y * y;
+  double sk = s;
+  for (int k = 0; k < K; k++, sk *= s) { rx[8 + k] = sk * x; ry[8 + k] = sk * y; }
+  double fx = 0, fy = 0;
+  for (int a = 0; a < 8 + K; a++) { fx += lens[4 + a] * rx[a]; fy += lens[4 + a] * ry[a]; }
+  *dx = (float)fx; *dy = (float)fy;
+}
+
+// Module point -> image point through H and the lens model when given (liblizard/src/acquire.c:1699-1702).
+static void anchor_map(const float *h, const double *lens, float X, float Y, float *u, float *v) {
+  project(h, X, Y, u, v);
+  if (lens) { float dx, dy; lens_at(lens, *u, *v, &dx, &dy); *u += dx; *v += dy; }
+}
+
+// The bilinear grey read at gamma 1 (liblizard/src/internal.h:11-23), rows w apart.
+static float sample(const uint8_t *px, int w, int h, float x, float y) {
+  x -= 0.5f; y -= 0.5f;
+  if (x < 0) x = 0; else if (x > w - 1.001f) x = w - 1.001f;
+  if (y < 0) y = 0; else if (y > h - 1.001f) y = h - 1.001f;
+  const int xi = x >= 0 ? (int)x : 0, yi = y >= 0 ? (int)y : 0;
+  const float fx = x - xi, fy = y - yi;
+  const uint8_t *p = px + yi * w + xi;
+  const float a = p[0] / 255.0f, b = p[1] / 255.0f, c = p[w] / 255.0f, d = p[w + 1] / 255.0f;
+  return (a + (b - a) * fx) * (1 - fy) + (c + (d - c) * fx) * fy;
+}
+
+#define ABOX(I, x, y, s) ((I)[((y) + (s)) * W1 + (x) + (s)] - (I)[(y) * W1 + (x) + (s)] - (I)[((y) + (s)) * W1 + (x)] + (I)[(y) * W1 + (x)])
+
+int orc_anchor_find(int span, const uint8_t *px, int w, int h, const float *H, const double *lens, const uint8_t *ok_in,
+                    uint8_t *ok, float *peak, float *dxo, float *dyo, float *uo, float *vo) {
+  const int a = span / 64;
+  if (a < 1) return 0;
+  const float hs = (float)a / ANTS;
+  const int r = (int)ceilf((float)ANREACH / hs), W = ANTS + 2 * r, O = 2 * r + 1, W1 = W + 1;
+  // the template: concentric squares, +1 inside a quarter and outside six tenths of the half side, -1 between
+  float T[ANTS * ANTS], tm = 0, tn = 0;
+  for (int y = 0; y < ANTS; y++)
+    for (int x = 0; x < ANTS; x++) {
+      const float u = (x + 0.5f) * hs - a * 0.5f, v = (y + 0.5f) * hs - a * 0.5f, dc = fmaxf(fabsf(u), fabsf(v)) / (a * 0.5f);
+      T[y * ANTS + x] = dc < 0.25f || dc >= 0.6f ? 1.0f : -1.0f;
+      tm += T[y * ANTS + x];
+    }
+  tm /= (float)(ANTS * ANTS);
+  for (int k = 0; k < ANTS * ANTS; k++) { T[k] -= tm; tn += T[k] * T[k]; }
+  tn = sqrtf(tn);
+  int i25 = ANTS, j25 = -1, i6 = ANTS, j6 = -1;
+  for (int x = 0; x < ANTS; x++) {
+    const float d = fabsf((x + 0.5f) * hs - a * 0.5f) / (a * 0.5f);
+    if (d < 0.25f) { if (x < i25) i25 = x; j25 = x; }
+    if (d < 0.6f) { if (x < i6) i6 = x; j6 = x; }
+  }
+  float *win = malloc(sizeof(float) * W * W), *C = malloc(sizeof(float) * O * O);
+  double *I1 = malloc(sizeof(double) * W1 * W1), *I2 = malloc(sizeof(double) * W1 * W1);
+  int found = 0;
+  for (int j = 0; j < ANK; j++)
+    for (int i = 0; i < ANK; i++) {
+      const int k = j * ANK + i;
+      ok[k] = 0; peak[k] = 0; dxo[k] = dyo[k] = uo[k] = vo[k] = 0;
+      if (ok_in && ok_in[k]) { ok[k] = 1; found++; continue; }
+      const float x0 = (float)anchor_m0(span, i), y0 = (float)anchor_m0(span, j), X = x0 + a * 0.5f, Y = y0 + a * 0.5f;
+      // the window: W x W samples a template step apart about the anchor's place
+      for (int wy = 0; wy < W; wy++)
+        for (int wx = 0; wx < W; wx++) {
+          float u, v;
+          anchor_map(H, lens, x0 + (wx - r + 0.5f) * hs, y0 + (wy - r + 0.5f) * hs, &u, &v);
+          win[wy * W + wx] = sample(px, w, h, u, v);
+        }
+      // its integral images of the greys and their squares, in double, row by row
+      for (int x = 0; x < W1; x++) I1[x] = I2[x] = 0;
+      for (int wy = 0; wy < W; wy++) {
+        double s = 0, q = 0;
+        I1[(wy + 1) * W1] = I2[(wy + 1) * W1] = 0;
+        for (int wx = 0; wx < W; wx++) {
+          const double vv = win[wy * W + wx];
+          s += vv; q += vv * vv;
+          I1[(wy + 1) * W1 + wx + 1] = I1[wy * W1 + wx + 1] + s;
+          I2[(wy + 1) * W1 + wx + 1] = I2[wy * W1 + wx + 1] + q;
+        }
+      }
+      // the normalised correlation at every offset from box sums; the first largest in scan order
+      float best = -2;
+      int bx = 0, by = 0;
+      for (int oy = -r; oy <= r; oy++)
+        for (int ox = -r; ox <= r; ox++) {
+          const int qx = r + ox, qy = r + oy;
+          const double s1 = ABOX(I1, qx, qy, ANTS), s2 = ABOX(I2, qx, qy, ANTS), var = s2 - s1 * s1 / (ANTS * ANTS);
+          const double s25 = j25 >= i25 ? ABOX(I1, qx + i25, qy + i25, j25 - i25 + 1) : 0;
+          const double s6 = j6 >= i6 ? ABOX(I1, qx + i6, qy + i6, j6 - i6 + 1) : 0;
+          const double st = 2 * (s25 - s6) + s1 * (1 - (double)tm);
+          const float c = var > 1e-12 ? (float)(st / (sqrt(var) * tn)) : 0;
+          C[(oy + r) * O + ox + r] = c;
+          if (c > best) { best = c; bx = ox; by = oy; }
+        }
+      // a parabola through the peak and its neighbours, each way
+      float sx = 0, sy = 0;
+      if (bx > -r && bx < r) {
+        const float l = C[(by + r) * O + bx + r - 1], c = best, rr = C[(by + r) * O + bx + r + 1], d = l - 2 * c + rr;
+        if (d < 0) sx = 0.5f * (l - rr) / d;
+      }
+      if (by > -r && by < r) {
+        const float l = C[(by + r - 1) * O + bx + r], c = best, rr = C[(by + r + 1) * O + bx + r], d = l - 2 * c + rr;
+        if (d < 0) sy = 0.5f * (l - rr) / d;
+      }
+      float u, v, hu, hv;
+      anchor_map(H, lens, X + (bx + sx) * hs, Y + (by + sy) * hs, &u, &v);
+      project(H, X, Y, &hu, &hv);
+      peak[k] = best; dxo[k] = u - hu; dyo[k] = v - hv; uo[k] = u; vo[k] = v;
+      ok[k] = best >= ANPEAK && bx > -r && bx < r && by > -r && by < r;
+      found += ok[k];
+    }
+  free(win); free(C); free(I1); free(I2);
+  return found;
+}

@@ -1,0 +1,38 @@
+// Harness around the reference's anchor search (liblizard/src/acquire.c:1876-2036 anchor_find), compiled from the
+// reference's own sources where they lie. TEST INFRASTRUCTURE ONLY: oracle/Makefile builds it into the reference's
+// portable build (-DOB_SCALAR: the scalar twins of the SIMD paths), oracle/_ref/libref_scalar.so, where the
+// reference tree is present, so that the tests can hold the anchor search's restatement and the GPU kernel to the
+// reference's own outputs. anchor_find is private to acquire.c, so the harness compiles acquire.c in.
+#include "acquire.c"
+
+// One frame's search: the format's ring span (modules), the frame (w x h greys, rows w apart), H (module -> image,
+// 9 floats), the lens model (NULL for none: K, ax, ay, R, then the LENS_P coefficients) and the anchors already
+// found (ok_in, 49 flags or NULL, row-major j * 7 + i). Out per anchor: ok, peak, dx, dy, u, v (the fields
+// anchor_find leaves; an anchor found before keeps zeros here). Returns the anchors ok, or -1.
+int refs_anchor_find(int span, const uint8_t *px, int w, int h, const float *H9, const double *lens, const uint8_t *ok_in,
+                     uint8_t *ok, float *peak, float *dx, float *dy, float *u, float *v) {
+  ob_layout_t L;
+  if (ob_layout_init(&L, span + 2 * OB_MARGIN)) return -1;
+  image_t im;
+  ob_image_init(&im, px, w, h, 1.0f);
+  homo_t H;
+  memcpy(H.h, H9, sizeof H.h);
+  lensm_t lm;
+  memset(&lm, 0, sizeof lm);
+  if (lens) {
+    lm.K = (int)lens[0]; lm.ax = lens[1]; lm.ay = lens[2]; lm.R = lens[3];
+    for (int a = 0; a < LENS_P; a++) lm.t[a] = lens[4 + a];
+  }
+  anchor_t A[OB_ANCH_K * OB_ANCH_K];
+  memset(A, 0, sizeof A);
+  for (int k = 0; k < OB_ANCH_K * OB_ANCH_K; k++) A[k].ok = ok_in ? ok_in[k] : 0;
+  const int found = anchor_find(&L, &im, &H, lens ? &lm : NULL, A);
+  for (int k = 0; k < OB_ANCH_K * OB_ANCH_K; k++) {
+    ok[k] = (uint8_t)A[k].ok; peak[k] = A[k].peak; dx[k] = A[k].dx; dy[k] = A[k].dy; u[k] = A[k].u; v[k] = A[k].v;
+  }
+  ob_layout_free(&L);
+  return found;
+}
+
+// The lens model's coefficient count (LENS_P) and the anchors' grid (OB_ANCH_K), for the caller's buffers.
+int refs_lens_p(void) { return LENS_P; }

@@ -1,0 +1,67 @@
+"""The anchor search's oracle (oracle/oracle_anchor.c), held bit for bit to the reference's own portable build: its
+fixtures (tests/golden/anchor_ref.npz) and, where the reference tree is present, the reference compiled here on fresh
+seeded captures (three ring spans, with and without a lens model, anchors found before)."""
+import os
+
+import numpy as np
+import pytest
+
+import lizard_gb300 as lz
+import oracle
+from lizard_gb300 import synth
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+FIELDS = ("ok", "peak", "dx", "dy", "u", "v")
+
+
+def golden_cases():
+    g = np.load(os.path.join(GOLD, "anchor_ref.npz"))
+    for c in range(int(g["cases"])):
+        lens = g["c%d_lens" % c]
+        yield (int(g["c%d_span" % c]), g["c%d_luma" % c], g["c%d_H" % c], lens if lens.size else None, g["c%d_skip" % c],
+               {k: g["c%d_%s" % (c, k)] for k in FIELDS})
+
+
+def same(a, b):
+    return all(np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(b[k]).view(np.uint8)) for k in FIELDS)
+
+
+def test_oracle_matches_reference_golden():
+    n = 0
+    for span, luma, H, lens, skip, want in golden_cases():
+        got = oracle.anchor_find(oracle.port(), "orc_anchor_find", span, luma, H, lens, skip)
+        assert same(got, want), "span %d" % span
+        n += 1
+    assert n == 4
+
+
+def seeded_capture(span, n, subch, W, Hh, seed, with_lens):
+    fmt = lz.Format(n, subch, span)
+    rng = np.random.default_rng(seed)
+    grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, seed), parity=seed & 3)
+    Hw = synth.warp(fmt, W, Hh, rng, rot_deg=12)
+    luma, reg = synth.capture(fmt, grey, W, Hh, H=Hw, sigma=2.0, rng=rng)
+    H = reg[:9].astype(np.float32).copy()
+    pxm = n / span
+    H[2] += np.float32(rng.uniform(-1, 1) * pxm)
+    H[5] += np.float32(rng.uniform(-1, 1) * pxm)
+    lens = None
+    if with_lens:
+        lens = np.zeros(15)
+        lens[:4] = [1 + seed % 3, W / 2, Hh / 2, np.hypot(W, Hh) / 2]
+        lens[4:12] = rng.uniform(-0.5, 0.5, 8)
+        lens[12:12 + int(lens[0])] = rng.uniform(-0.05, 0.05, int(lens[0]))
+    return luma, H, lens
+
+
+@pytest.mark.skipif(oracle.ref_scalar() is None, reason="the reference's portable build is not here")
+@pytest.mark.parametrize("span,n,subch,W,Hh,seed,with_lens", [(128, 384, 64, 640, 600, 1, False), (128, 384, 80, 640, 600, 2, True),
+                                                               (256, 768, 320, 900, 880, 3, True), (512, 1536, 1024, 1700, 1700, 4, False)])
+def test_oracle_matches_reference_build(span, n, subch, W, Hh, seed, with_lens):
+    luma, H, lens = seeded_capture(span, n, subch, W, Hh, seed, with_lens)
+    skip = np.zeros(49, np.uint8)
+    skip[::5] = seed & 1
+    a = oracle.anchor_find(oracle.port(), "orc_anchor_find", span, luma, H, lens, skip)
+    b = oracle.anchor_find(oracle.ref_scalar(), "refs_anchor_find", span, luma, H, lens, skip)
+    assert same(a, b)
+    assert a["found"] == b["found"] and a["found"] >= 40
