@@ -265,6 +265,70 @@ def bench_receiver(args, stream):
     return res
 
 
+def bench_anchor(args, stream):
+    """The registration assist: the 7 x 7 anchor search (lizg_anchor_find_dev) on a batch of 64 captured 1920 x 1080
+    frames, each one LIZARD-1024 symbol (n = 1536) in the 128 ring at about 2.6 pixels a module, rotated up to 15
+    degrees, its map H put up to a module off. Device-timed with CUDA events; beside it the same search's arithmetic
+    on the host cores (the oracle's restatement of the reference's portable build, one frame a thread)."""
+    import concurrent.futures
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    import oracle
+    span, n, subch, W, Hh, frames, distinct = 256, 1536, 1024, 1920, 1080, 64, 8
+    fmt = lz.Format(n, subch, span)
+    lumas, Hs = [], []
+    for k in range(distinct):
+        rng = np.random.default_rng(500 + k)
+        grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 500 + k), parity=k & 3)
+        Hw = synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.42, 0.45))
+        luma, reg = synth.capture(fmt, grey, W, Hh, H=Hw, sigma=3.0, rng=rng)
+        H = reg[:9].copy()
+        H[2] += np.float32(rng.uniform(-1, 1) * 2.6)
+        H[5] += np.float32(rng.uniform(-1, 1) * 2.6)
+        lumas.append(luma)
+        Hs.append(H)
+    luma = np.stack([lumas[k % distinct] for k in range(frames)])
+    Hf = np.stack([Hs[k % distinct] for k in range(frames)]).astype(np.float32)
+    d_l, d_h = torch.from_numpy(luma).cuda(), torch.from_numpy(Hf).cuda()
+    o = {"ok": torch.zeros((frames, 49), dtype=torch.uint8, device="cuda")}
+    for key in ("peak", "dx", "dy", "u", "v"):
+        o[key] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
+    s = lz.AnchorOut(*[o[key].data_ptr() for key in ("ok", "peak", "dx", "dy", "u", "v")])
+    sp = stream.cuda_stream
+
+    def call():
+        lz._check(lz.lib().lizg_anchor_find_dev(span, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W * Hh, lz.ctypes.c_void_p(d_h.data_ptr()), 9,
+                                                None, None, frames, lz.ctypes.byref(s), lz.ctypes.c_void_p(sp)), "anchor_find")
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    reps = max(5, args.steps // 3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    found = int(o["ok"].sum().item())
+    # the host cores: the same search's arithmetic (the oracle's plain C), one frame a thread, every frame once
+    if not os.path.exists(oracle.PORT_PATH):
+        oracle.build(ref=False)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        cpu = list(ex.map(lambda k: oracle.anchor_find(oracle.port(), "orc_anchor_find", span, lumas[k % distinct], Hs[k % distinct]), range(frames)))
+    dt = time.perf_counter() - t0
+    same = all(np.array_equal(cpu[k]["ok"], o["ok"][k].cpu().numpy()) and np.array_equal(cpu[k]["dx"], o["dx"][k].cpu().numpy()) for k in range(distinct))
+    return {"workload": "anchor search, 64 frames of 1920x1080, LIZARD-1024 (n=1536) in the 128 ring at ~2.6 px a module, rotation up to 15 deg, H up to a module off, AWGN 3 DN",
+            "frames_per_s": round(frames / (ms / 1e3), 1), "anchors_per_s": round(49 * frames / (ms / 1e3), 1), "ms_per_call": round(ms, 4),
+            "anchors_found": found, "anchors": 49 * frames, "gpu_launches_per_call": 1, "identical_to_host": bool(same),
+            "cpu": {"frames_per_s": round(frames / dt, 1), "cores": threads, "kind": "port",
+                    "sample": "the 64 frames once, one frame a thread (%.2f s wall)" % dt}}
+
+
 def run_reference(args, rank, ws):
     """The reference arm: the reference's CPU decoder on the host cores, same metric and workload."""
     if rank != 0:
@@ -314,7 +378,8 @@ def main():
                             for name, r, v in zip(("7/8", "3/4", "2/3", "1/2"), (6, 4, 3, 2), chosen)},
                 "seconds": round(time.perf_counter() - t_tune, 2), "calibration": "8192 codewords a code, all-zero codeword, BPSK/AWGN over the workload's Eb/N0 sweep"}
     if args.receiver_only:
-        print(json.dumps(bench_receiver(args, torch.cuda.current_stream())))
+        st = torch.cuda.current_stream()
+        print(json.dumps({"receiver": bench_receiver(args, st), "registration": {"anchor_search": bench_anchor(args, st)}}))
         return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
     plan = lz.LdpcPlan(batch["rates"], MAX_ITER, STALL_IT, STALL_RATIO)
@@ -405,6 +470,7 @@ def main():
         out["e2e"] = e2e
     if not args.no_receiver:
         out["receiver"] = bench_receiver(args, stream)
+        out["registration"] = {"anchor_search": bench_anchor(args, stream)}
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt, kind = cpu_decode(batch, threads, args.count)
