@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--no-receiver", action="store_true", help="skip the frame receiver's workloads")
     ap.add_argument("--receiver-only", action="store_true", help="time only the frame receiver (profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the decoder's default kernel variants")
+    ap.add_argument("--batch-only", action="store_true", help="with --receiver-only: only the batched workloads (FFT demod batch, "
+                    "anchor search), for profiling")
     return ap.parse_args()
 
 
@@ -257,6 +259,8 @@ def bench_receiver(args, stream):
                 "payload_MBps": round(okb * 472 / (ms / 1e3) / 1e6, 3), "ms_per_call": round(ms, 4),
                 "blocks_verified": okb, "blocks": frames * rx.fmt.blocks, "gpu_launches_per_call": rx.launches}
 
+    if args.batch_only:
+        return res
     res["plain_one_frame"] = receiver_line(384, 64, 1280, 720, 1, False, 200, "LIZARD-64, n=384, 64 ring, 1280x720 luma, AWGN 2 DN, axis-aligned, one frame a call")
     res["plain_one_frame_graph"] = receiver_line(384, 64, 1280, 720, 1, True, 400, "the same, the call replayed from a CUDA graph")
     res["n1536_one_frame"] = receiver_line(1536, 1024, 3840, 2160, 1, False, 50, "LIZARD-1024, n=1536, 64 ring, 3840x2160 luma, AWGN 2 DN, one frame a call")

@@ -149,7 +149,7 @@ __host__ __device__ constexpr int lstride_of(int n) { return (n + n / 16 + 15) /
 
 // One Stockham pass of radix R over the CTA's lines (Lr <= L of them) in place, n = N points a line. Butterfly j of
 // a line (j < NR = N / R, k = j mod NS) reads points j + r NR, turns point r by e^{-2 pi i r k / (NS R)}
-// (tw[(r - 1) NS + k]) and writes its DFT's output r to (j / NS) NS R + k + r NS. A thread takes butterflies tid,
+// (tw[NS + (r - 1) NS + k]) and writes its DFT's output r to (j / NS) NS R + k + r NS. A thread takes butterflies tid,
 // tid + kThreads, ... (at most B = ceil(L NR / kThreads) of them).
 // The thread's index, read afresh: the passes' offsets hang on it, so a loop round the passes recomputes them pass by
 // pass instead of holding every pass's offsets live across the loop.
@@ -174,7 +174,7 @@ __device__ __forceinline__ void pass(float2 *buf, const float2 *tw, int Lr) {
       for (int r = 0; r < R; r++) v[b][r] = in[pad(j + r * NR)];
       if (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; r++) v[b][r] = cmul(v[b][r], tw[NS - 1 + (r - 1) * NS + k]);
+        for (int r = 1; r < R; r++) v[b][r] = cmul(v[b][r], tw[NS + (r - 1) * NS + k]);
       }
       dft<R>(v[b]);
     }
@@ -195,7 +195,8 @@ __device__ __forceinline__ void pass(float2 *buf, const float2 *tw, int Lr) {
 }
 
 // The Lr lines at buf (line l at buf + l lstride_of(N), point p at slot pad(p)) transformed along their N points in
-// place by the size's three passes. tw: the passes' twiddles, pass s's at NS - 1. Every thread of the CTA takes part.
+// place by the size's three passes. tw: the passes' twiddles, pass s's at NS (a multiple of 16 past the first pass,
+// so a half-warp's 16 twiddles are one aligned 128-byte row). Every thread of the CTA takes part.
 template <int N>
 __device__ __forceinline__ void fft_lines(float2 *buf, const float2 *tw, int Lr) {
   constexpr Plan P = plan_of(N);
@@ -318,7 +319,7 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, i
     h6a = __fmul_rn(Hr[6], mxa); h0a = __fmul_rn(Hr[0], mxa); h3a = __fmul_rn(Hr[3], mxa);
     h6b = __fmul_rn(Hr[6], mxb); h0b = __fmul_rn(Hr[0], mxb); h3b = __fmul_rn(Hr[3], mxb);
   }
-#pragma unroll 2
+#pragma unroll 4
   for (int y = threadIdx.x / L; y < N; y += ystep) {
     const bool ysq = (ina || inb) && in_square(xd, y);
     float va, vb;
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
   const SmemMap sm = smem_map<N>(smraw);
   const int tid = threadIdx.x, l = tid % L, warp = tid >> 5, lane = tid & 31;
-  for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
+  for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
   if (!src.grid) for (int i = tid; i < 256; i += kThreads) sm.lut[i] = __fdiv_rn((float)i, 255.0f);
   __shared__ double s_rhs[6], s_beta[6];
   __shared__ float s_part[kThreads / 32][5];
@@ -437,7 +438,7 @@ __global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const 
   const SmemMap sm = smem_map<N>(smraw);
   const int tid = threadIdx.x, tiles = (xd.vrows + L - 1) / L;
   const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
-  for (int i = tid; i < n - 1; i += kThreads) sm.tw[i] = xd.tws[i];
+  for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
   const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
   for (int l = 0; l < Lr; l++)
     for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
@@ -447,9 +448,13 @@ __global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const 
   const int32_t *tp = tpos + (int64_t)v0 * n;
   const float2 *fx = fac + (int64_t)f * (2 * n + xd.vrows), *fx0 = fx + n, *fy0 = fx + 2 * n;
   for (int u = tid; u < n; u += kThreads) {
+    int iv[L];   // the rows' pos indices at this u, loaded ahead of their use
+#pragma unroll
+    for (int l = 0; l < L; l++) iv[l] = l < Lr ? __ldg(tp + l * n + u) : -1;
     const float2 a = fx[u];
-    for (int l = 0; l < Lr; l++) {
-      const int i = tp[l * n + u];
+#pragma unroll
+    for (int l = 0; l < L; l++) {
+      const int i = iv[l];
       if (i < 0) continue;
       const int v = v0 + l;
       float2 o = sm.buf[l * LSTR + pad(u)];

@@ -25,7 +25,7 @@ struct FmtDev {
 // A format's transform tables (row b), passed by value to the transform kernels.
 struct FftDev {
   int n, vrows;                      // picture size; rows v kept (the used coefficients' v <= vrows - 1)
-  const float2 *tws;                 // the passes' twiddles: pass s at Ns - 1, [r - 1][k] = e^{-2 pi i r k / (Ns R)}
+  const float2 *tws;                 // the passes' twiddles: pass s at Ns, [r - 1][k] = e^{-2 pi i r k / (Ns R)}
   const float *cx, *qx;              // detrend basis
   const float2 *x1, *x2;             // their DFTs
   double sx2, sq2;

@@ -130,7 +130,7 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
       for (int q = 1; q < rad[st]; q++)
         for (int k = 0; k < ns; k++) {
           const double th = -2.0 * 3.14159265358979323846 * q * k / ((double)ns * rad[st]);
-          tws[ns - 1 + (q - 1) * ns + k] = make_float2((float)std::cos(th), (float)std::sin(th));
+          tws[ns + (q - 1) * ns + k] = make_float2((float)std::cos(th), (float)std::sin(th));
         }
     for (int t = 0; t < n; t++) { x1[t] = make_float2(f.x1r[t], f.x1i[t]); x2[t] = make_float2(f.x2r[t], f.x2i[t]); }
     ok(dev_copy(r, &r->tw, tws.data(), tws.size()));
