@@ -14,6 +14,7 @@
 #include <string>
 #include "lizard_gb300.h"
 #include "lizg_internal.h"
+#include "sample_dev.cuh"
 
 namespace lizg {
 
@@ -65,8 +66,8 @@ __device__ __forceinline__ void anchor_map(const float *h, const double *lens, f
   if (lens) { float dx, dy; lens_at(lens, *u, *v, &dx, &dy); *u += dx; *v += dy; }
 }
 
-// The bilinear grey read at gamma 1 (liblizard/src/internal.h:11-23), rows w apart; lut[k] = k / 255.
-__device__ __forceinline__ float sample(const uint8_t *px, int w, int h, const float *lut, float x, float y) {
+// The bilinear grey read at gamma 1 (liblizard/src/internal.h:11-23), rows w apart; a grey level k reads k / 255.
+__device__ __forceinline__ float sample(const uint8_t *px, int w, int h, float x, float y) {
   x -= 0.5f; y -= 0.5f;
   const float xm = (float)w - 1.001f, ym = (float)h - 1.001f;
   if (x < 0) x = 0; else if (x > xm) x = xm;
@@ -74,7 +75,7 @@ __device__ __forceinline__ float sample(const uint8_t *px, int w, int h, const f
   const int xi = x >= 0 ? (int)x : 0, yi = y >= 0 ? (int)y : 0;
   const float fx = x - (float)xi, fy = y - (float)yi;
   const uint8_t *p = px + (int64_t)yi * w + xi;
-  const float a = lut[p[0]], b = lut[p[1]], c = lut[p[w]], d = lut[p[w + 1]];
+  const float a = grey_of(p[0]), b = grey_of(p[1]), c = grey_of(p[w]), d = grey_of(p[w + 1]);
   return (a + (b - a) * fx) * (1 - fy) + (c + (d - c) * fx) * fy;
 }
 
@@ -102,11 +103,10 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
   const int r = g.r, W = g.W, O = g.O, W1 = W + 1, tid = threadIdx.x;
   const float hs = g.hs, ah = (float)g.a * 0.5f;
   double *I1 = reinterpret_cast<double *>(sm), *I2 = I1 + W1 * W1;
-  float *win = reinterpret_cast<float *>(I2 + W1 * W1), *C = win + W * W, *lut = C + O * O;
+  float *win = reinterpret_cast<float *>(I2 + W1 * W1), *C = win + W * W;
   __shared__ float s_h[9], s_tm, s_tn, s_bv[256];
   __shared__ double s_lens[kLensStride];
   __shared__ int s_r25[2], s_r6[2], s_bi[256];
-  for (int t = tid; t < 256; t += blockDim.x) lut[t] = (float)t / 255.0f;
   if (tid < 9) s_h[tid] = a.H[(int64_t)f * a.hstride + tid];
   if (a.lens && tid < kLensStride) s_lens[tid] = a.lens[(int64_t)f * kLensStride + tid];
   if (tid == 0) {
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
     const int wx = t % W, wy = t / W;
     float u, v;
     anchor_map(s_h, lens, x0 + ((float)(wx - r) + 0.5f) * hs, y0 + ((float)(wy - r) + 0.5f) * hs, &u, &v);
-    win[t] = sample(px, a.w, a.h, lut, u, v);
+    win[t] = sample(px, a.w, a.h, u, v);
   }
   for (int t = tid; t < W1; t += blockDim.x) { I1[t] = 0; I2[t] = 0; I1[t * W1] = 0; I2[t * W1] = 0; }
   __syncthreads();
@@ -226,7 +226,7 @@ extern "C" int lizg_anchor_find_dev(int span, const uint8_t *d_luma, int w, int 
   for (int i = 0; i < kAnchK; i++) a.m0[i] = (int)floor(kMarginM + (double)span * (i + 0.5) / kAnchK - a.g.a / 2.0 + 0.5);
   a.luma = d_luma; a.skip = d_skip; a.H = d_H; a.lens = d_lens; a.out = *out;
   const int W1 = a.g.W + 1;
-  const size_t smem = 2 * sizeof(double) * W1 * W1 + sizeof(float) * ((size_t)a.g.W * a.g.W + (size_t)a.g.O * a.g.O + 256);
+  const size_t smem = 2 * sizeof(double) * W1 * W1 + sizeof(float) * ((size_t)a.g.W * a.g.W + (size_t)a.g.O * a.g.O);
   static bool attr = false;
   cudaError_t e = cudaSuccess;
   if (!attr) {

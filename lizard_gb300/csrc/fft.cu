@@ -206,12 +206,11 @@ __device__ __forceinline__ void fft_lines(float2 *buf, const float2 *tw, int Lr)
 }
 
 // A frame's picture sample (x, y): read from a supplied grid, or sampled straight from the captured frame through
-// its registration (the sampler fused into the pass that reads it). lut, when given, holds k / 255 for the grey
-// levels (the sampler's own divisions, made once a CTA).
-__device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y, const float *lut) {
+// its registration (the sampler fused into the pass that reads it).
+__device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y) {
   if (s.grid) return s.grid[f * s.gstride + (int64_t)y * s.sd.n + x];
   const float *H = s.reg + (int64_t)f * s.regstride;
-  return sample_xy(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, s.sd.colt[x], s.sd.rowt[y], lut);
+  return sample_xy(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, s.sd.colt[x], s.sd.rowt[y]);
 }
 
 __device__ __forceinline__ bool in_square(const FftDev &xd, int t) {
@@ -242,7 +241,7 @@ __global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, in
     for (int kx = lane; kx < c; kx += 32) {
       const int x = 8 * kx;
       if (ysq && in_square(xd, x)) continue;
-      const float v = src_at(src, f, x, y, nullptr);
+      const float v = src_at(src, f, x, y);
       s0 += v; s1 += __ldg(xd.cx + x) * v; s2 += __ldg(xd.qx + x) * v;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -264,15 +263,13 @@ __global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, in
   }
 }
 
-// The transform CTA's shared memory: the lines, the twiddles, the moments' reduction, the grey table.
+// The transform CTA's shared memory: the lines, the twiddles, the moments' reduction.
 struct SmemMap {
   float2 *buf, *tw;
   double *red;
-  float *lut;
 };
 __host__ __device__ constexpr int smem_bytes_of(int n) {
-  return (plan_of(n).lines * lstride_of(n) + n) * (int)sizeof(float2) + (kThreads / 32) * 6 * plan_of(n).lines * (int)sizeof(double) +
-         256 * (int)sizeof(float);
+  return (plan_of(n).lines * lstride_of(n) + n) * (int)sizeof(float2) + (kThreads / 32) * 6 * plan_of(n).lines * (int)sizeof(double);
 }
 template <int N>
 __device__ __forceinline__ SmemMap smem_map(unsigned char *raw) {
@@ -280,7 +277,6 @@ __device__ __forceinline__ SmemMap smem_map(unsigned char *raw) {
   m.buf = reinterpret_cast<float2 *>(raw);
   m.tw = m.buf + plan_of(N).lines * lstride_of(N);
   m.red = reinterpret_cast<double *>(m.tw + N);
-  m.lut = reinterpret_cast<float *>(m.red + (kThreads / 32) * 6 * plan_of(N).lines);
   return m;
 }
 
@@ -297,8 +293,7 @@ __device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta
 // surface as they are read. Each row's two samples are summed into the five detrend projections' raw sums, z c(x),
 // z c(y), z c(x) c(y), z q(x), z q(y) (liblizard/src/lizard_phy.c:1584-1591, 1657-1667), in p.
 template <int N, bool GRID>
-__device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, int f, int x0, const double *beta, const float *lut,
-                                          float2 *line, float p[5]) {
+__device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, int f, int x0, const double *beta, float2 *line, float p[5]) {
   constexpr int L = plan_of(N).lines, ystep = kThreads / L;
   const int l = threadIdx.x % L, xa = x0 + l, xb = x0 + L + l;
   const bool ina = in_square(xd, xa), inb = in_square(xd, xb);
@@ -330,8 +325,8 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, i
       const RowTerms r = row_terms(Hr, src.sd.rowt[y]);
       const CellTerms ca = cell_terms(src.sd, nodes, ia, inva, r);
       const CellTerms cb = ib == ia ? ca : cell_terms(src.sd, nodes, ib, invb, r);
-      va = sample_at(px, src.w, src.h, src.pitch, mxa, h6a, h0a, h3a, r, ca, lut);
-      vb = sample_at(px, src.w, src.h, src.pitch, mxb, h6b, h0b, h3b, r, cb, lut);
+      va = sample_at(px, src.w, src.h, src.pitch, mxa, h6a, h0a, h3a, r, ca);
+      vb = sample_at(px, src.w, src.h, src.pitch, mxb, h6b, h0b, h3b, r, cb);
     }
     if (ina && ysq) va = hole_value(xd, beta, xa, y);
     if (inb && ysq) vb = hole_value(xd, beta, xb, y);
@@ -353,7 +348,6 @@ __global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev
   const SmemMap sm = smem_map<N>(smraw);
   const int tid = threadIdx.x, l = tid % L, warp = tid >> 5, lane = tid & 31;
   for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
-  if (!src.grid) for (int i = tid; i < 256; i += kThreads) sm.lut[i] = __fdiv_rn((float)i, 255.0f);
   __shared__ double s_rhs[6], s_beta[6];
   __shared__ float s_part[kThreads / 32][5];
   float2 *line = sm.buf + l * LSTR;
@@ -376,8 +370,8 @@ __global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev
     }
     __syncthreads();
     float p[5] = {0, 0, 0, 0, 0};
-    if (src.grid) load_tile<N, true>(xd, src, f, x0, s_beta, nullptr, line, p);
-    else load_tile<N, false>(xd, src, f, x0, s_beta, sm.lut, line, p);
+    if (src.grid) load_tile<N, true>(xd, src, f, x0, s_beta, line, p);
+    else load_tile<N, false>(xd, src, f, x0, s_beta, line, p);
 #pragma unroll
     for (int q = 0; q < 5; q++)
       for (int o = 16; o > 0; o >>= 1) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);

@@ -27,6 +27,14 @@ __device__ __forceinline__ float4 sample_row(const SampleDev &sd, int y) {
   return make_float4(my, __int_as_float(j), __fdiv_rn(__fsub_rn(my, sd.node_y[j]), __fsub_rn(sd.node_y[j + 1], sd.node_y[j])), 0.0f);
 }
 
+// k / 255 rounded to nearest for a grey level k (0..255), with no division and no table: q = k r, r the float
+// nearest 1 / 255, then one correction from the exact remainder k - 255 q (Markstein's method). It equals the
+// correctly rounded quotient, the reference's i / 255.0f, for every k (checked exhaustively in exact arithmetic).
+__device__ __forceinline__ float grey_of(unsigned k) {
+  const float r = 0.003921568859368563f, kf = (float)k, q = __fmul_rn(kf, r);
+  return __fmaf_rn(__fmaf_rn(-q, 255.0f, kf), r, q);
+}
+
 // The walk's quantities of one picture row: the row's place in its mesh cell and the homography's row terms.
 struct RowTerms {
   float my, v, omv, kw, ku, kv;
@@ -55,10 +63,9 @@ __device__ __forceinline__ CellTerms cell_terms(const SampleDev &sd, const float
 }
 
 // The sample at module column mx of a row: h6 = H[6] mx, h0 = H[0] mx, h3 = H[3] mx (the column's products), then the
-// projection, the mesh's displacement, the frame-edge clamp and the bilinear grey read. lut, when given, holds
-// k / 255 for k < 256 made by the same division, read in place of dividing.
+// projection, the mesh's displacement, the frame-edge clamp and the bilinear grey read.
 __device__ __forceinline__ float sample_at(const uint8_t *px, int w, int h, int pitch, float mx, float h6, float h0, float h3,
-                                           const RowTerms &r, const CellTerms &c, const float *lut) {
+                                           const RowTerms &r, const CellTerms &c) {
   const float rw = __fdiv_rn(1.0f, __fadd_rn(h6, r.kw));
   const float pu = __fmul_rn(__fadd_rn(h0, r.ku), rw), pv = __fmul_rn(__fadd_rn(h3, r.kv), rw);
   const float dx = __fadd_rn(c.cx, __fmul_rn(c.ex, mx)), dy = __fadd_rn(c.cy, __fmul_rn(c.ey, mx));
@@ -69,13 +76,7 @@ __device__ __forceinline__ float sample_at(const uint8_t *px, int w, int h, int 
   const int xi = sx >= 0 ? (int)sx : 0, yi = sy >= 0 ? (int)sy : 0;   // a NaN coordinate reads pixel 0
   const float fx = __fsub_rn(sx, (float)xi), fy = __fsub_rn(sy, (float)yi);
   const uint8_t *p = px + (int64_t)yi * pitch + xi;
-  float a, b, cc, d;
-  if (lut) {
-    a = lut[p[0]]; b = lut[p[1]]; cc = lut[p[pitch]]; d = lut[p[pitch + 1]];
-  } else {
-    a = __fdiv_rn((float)p[0], 255.0f); b = __fdiv_rn((float)p[1], 255.0f);
-    cc = __fdiv_rn((float)p[pitch], 255.0f); d = __fdiv_rn((float)p[pitch + 1], 255.0f);
-  }
+  const float a = grey_of(p[0]), b = grey_of(p[1]), cc = grey_of(p[pitch]), d = grey_of(p[pitch + 1]);
   return __fadd_rn(__fmul_rn(__fadd_rn(a, __fmul_rn(__fsub_rn(b, a), fx)), __fsub_rn(1.0f, fy)),
                    __fmul_rn(__fadd_rn(cc, __fmul_rn(__fsub_rn(d, cc), fx)), fy));
 }
@@ -83,11 +84,11 @@ __device__ __forceinline__ float sample_at(const uint8_t *px, int w, int h, int 
 // Sample (x, y) of the picture grid from frame px (w x h, rows pitch apart) through H (9 floats) and the node mesh,
 // given the column's and the row's table entries.
 __device__ __forceinline__ float sample_xy(const SampleDev &sd, const uint8_t *px, int w, int h, int pitch, const float *H,
-                                           const float *nodes, float4 ct, float4 rt, const float *lut = nullptr) {
+                                           const float *nodes, float4 ct, float4 rt) {
   const RowTerms r = row_terms(H, rt);
   const CellTerms c = cell_terms(sd, nodes, __float_as_int(ct.y), ct.z, r);
   const float mx = ct.x;
-  return sample_at(px, w, h, pitch, mx, __fmul_rn(H[6], mx), __fmul_rn(H[0], mx), __fmul_rn(H[3], mx), r, c, lut);
+  return sample_at(px, w, h, pitch, mx, __fmul_rn(H[6], mx), __fmul_rn(H[0], mx), __fmul_rn(H[3], mx), r, c);
 }
 
 }  // namespace lizg
