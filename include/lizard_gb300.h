@@ -177,6 +177,33 @@ int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int
 int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
                               int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
 
+// ---------------------------------------------------------------- the multi-stream engine
+//
+// The device side of the reference's batched receiver engine (liz_receiver_new / _push / _batch_cap,
+// liblizard/include/lizard.h:252-294) for frames already registered: many camera streams of different formats
+// decoded together. An engine holds one receiver handle per picture format (lizg_engine_add_format returns its
+// index; lizg_engine_rx the handle, for lizg_rx_info and the like). lizg_engine_run_dev takes one batch per format
+// (each format at most once a run): the format's frames, registrations and outputs as lizg_rx_finish_luma_dev
+// takes them; every batch runs on its format's own stream, replayed from that format's CUDA graph (captured on the
+// first run with those buffers), forked from `stream` and joined back to it, so the formats' work overlaps on the
+// GPU. Queued; returns once launched. lizg_engine_launches: the kernels the last run launched.
+typedef struct lizg_engine lizg_engine;
+typedef struct {
+  int format;
+  const uint8_t *d_luma;
+  int w, h, pitch;
+  int64_t frame_stride;
+  const float *d_reg;
+  int frames;
+  lizg_rx_out out;
+} lizg_engine_batch;
+lizg_engine *lizg_engine_new(void);
+void lizg_engine_free(lizg_engine *e);
+int lizg_engine_add_format(lizg_engine *e, int n, int subch, int span, int max_frames);
+lizg_rx *lizg_engine_rx(lizg_engine *e, int format);
+int lizg_engine_run_dev(lizg_engine *e, const lizg_engine_batch *b, int nb, void *stream);
+int lizg_engine_launches(const lizg_engine *e);
+
 // ---------------------------------------------------------------- registration assist: the anchor search
 //
 // Replaces anchor_find (liblizard/src/acquire.c:1876-2036), the registration's search for the picture's 7 x 7 anchors

@@ -204,6 +204,14 @@ def _rx_sigs(L):
     L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
     L.lizg_rx_finish_luma_graph.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
     L.lizg_anchor_find_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, P, P, I, P, P]
+    L.lizg_engine_new.argtypes = []
+    L.lizg_engine_new.restype = P
+    L.lizg_engine_free.argtypes = [P]
+    L.lizg_engine_add_format.argtypes = [P, I, I, I, I]
+    L.lizg_engine_rx.argtypes = [P, I]
+    L.lizg_engine_rx.restype = P
+    L.lizg_engine_run_dev.argtypes = [P, P, I, P]
+    L.lizg_engine_launches.argtypes = [P]
 
 
 class RxOut(ctypes.Structure):
@@ -245,6 +253,25 @@ class Format:
         return v * self.n + (u + self.n) % self.n
 
 
+def rx_outputs(fmt, frames, keep=False):
+    """Device output buffers of a receive call for frames frames of a format (torch tensors) and the lizg_rx_out
+    naming them."""
+    import torch
+    f = fmt
+    o = {"blocks": torch.zeros((frames, f.blocks, BLOCK_BYTES), dtype=torch.uint8, device="cuda"),
+         "ok": torch.zeros((frames, f.blocks), dtype=torch.uint8, device="cuda"),
+         "its": torch.zeros((frames, f.blocks), dtype=torch.int32, device="cuda"),
+         "est": torch.zeros((frames, f.blocks), dtype=torch.float32, device="cuda"),
+         "pilot": torch.zeros((frames, f.blocks), dtype=torch.float32, device="cuda"),
+         "align": torch.zeros((frames, 3), dtype=torch.float32, device="cuda")}
+    if keep:
+        o["llrf"] = torch.zeros((frames, 2 * f.subch * SUB), dtype=torch.int8, device="cuda")
+        o["sub_est"] = torch.zeros((frames, f.subch), dtype=torch.float64, device="cuda")
+        o["sub_rms"] = torch.zeros((frames, f.subch), dtype=torch.float32, device="cuda")
+    s = RxOut(*[o[k].data_ptr() if k in o else None for k in ("blocks", "ok", "its", "est", "pilot", "align", "llrf", "sub_est", "sub_rms")])
+    return o, s
+
+
 class Receiver:
     """A receiver handle (lizg_rx_*) for one format and up to max_frames frames a call."""
 
@@ -270,19 +297,7 @@ class Receiver:
         return int(lib().lizg_rx_launches(self._h))
 
     def _outputs(self, frames, torch, keep):
-        f = self.fmt
-        o = {"blocks": torch.zeros((frames, f.blocks, BLOCK_BYTES), dtype=torch.uint8, device="cuda"),
-             "ok": torch.zeros((frames, f.blocks), dtype=torch.uint8, device="cuda"),
-             "its": torch.zeros((frames, f.blocks), dtype=torch.int32, device="cuda"),
-             "est": torch.zeros((frames, f.blocks), dtype=torch.float32, device="cuda"),
-             "pilot": torch.zeros((frames, f.blocks), dtype=torch.float32, device="cuda"),
-             "align": torch.zeros((frames, 3), dtype=torch.float32, device="cuda")}
-        if keep:
-            o["llrf"] = torch.zeros((frames, 2 * f.subch * SUB), dtype=torch.int8, device="cuda")
-            o["sub_est"] = torch.zeros((frames, f.subch), dtype=torch.float64, device="cuda")
-            o["sub_rms"] = torch.zeros((frames, f.subch), dtype=torch.float32, device="cuda")
-        s = RxOut(*[o[k].data_ptr() if k in o else None for k in ("blocks", "ok", "its", "est", "pilot", "align", "llrf", "sub_est", "sub_rms")])
-        return o, s
+        return rx_outputs(self.fmt, frames, keep)
 
     def finish_coef(self, coef, keep=True, stream=None):
         """coef: frames x subch x 320 complex64 (or float32 pairs). Returns a dict of numpy arrays."""
@@ -367,3 +382,44 @@ def anchor_find(span, luma, H, lens=None, skip=None, stream=None):
            "lizg_anchor_find_dev")
     torch.cuda.synchronize()
     return {k: v.cpu().numpy() for k, v in o.items()}
+
+
+class EngineBatch(ctypes.Structure):
+    _fields_ = [("format", ctypes.c_int), ("d_luma", ctypes.c_void_p), ("w", ctypes.c_int), ("h", ctypes.c_int), ("pitch", ctypes.c_int),
+                ("frame_stride", ctypes.c_int64), ("d_reg", ctypes.c_void_p), ("frames", ctypes.c_int), ("out", RxOut)]
+
+
+class Engine:
+    """The multi-stream engine: one receiver handle per picture format; run() decodes one batch per format, each on
+    its format's own stream from its own CUDA graph, together."""
+
+    def __init__(self):
+        self._h = lib().lizg_engine_new()
+        if not self._h:
+            raise LizgError("lizg_engine_new failed: %s" % lib().lizg_last_error().decode())
+        self.formats = []
+
+    def add_format(self, n, subch, span, max_frames):
+        i = _check(lib().lizg_engine_add_format(self._h, n, subch, span, max_frames), "lizg_engine_add_format")
+        self.formats.append(Format(n, subch, span))
+        return i
+
+    def run_dev(self, batches, stream):
+        """batches: list of (format, d_luma ptr, w, h, pitch, frame_stride, d_reg ptr, frames, RxOut)."""
+        arr = (EngineBatch * len(batches))(*[EngineBatch(*b) for b in batches])
+        _check(lib().lizg_engine_run_dev(self._h, ctypes.cast(arr, ctypes.c_void_p), len(batches), ctypes.c_void_p(stream)), "lizg_engine_run_dev")
+
+    @property
+    def launches(self):
+        return lib().lizg_engine_launches(self._h)
+
+    def close(self):
+        if self._h:
+            lib().lizg_engine_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -80,6 +80,8 @@ def test_no_gpu_fails_loudly():
     with pytest.raises(lz.LizgError) as e:
         lz.LdpcPlan(np.array([6, 4], np.int32))
     assert "cuda" in str(e.value).lower() or "device" in str(e.value).lower()
+    with pytest.raises(lz.LizgError):
+        lz.Engine()
 
 
 def test_synth_batch_shapes():

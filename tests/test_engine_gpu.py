@@ -1,0 +1,69 @@
+"""The multi-stream engine (lizg_engine_*): batches of three formats decoded together, each on its own stream from
+its own CUDA graph, give exactly what each format's receiver gives alone (blocks, CRC flags, iterations); replays of
+the captured graphs give it again; bad runs are refused."""
+import numpy as np
+import pytest
+import torch
+
+import lizard_gb300 as lz
+from lizard_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+FORMATS = [(384, 64, 128, 1280, 720), (768, 320, 128, 1100, 1000), (1152, 720, 256, 1400, 1400)]
+
+
+def captures(n, subch, span, W, H, frames, seed):
+    fmt = lz.Format(n, subch, span)
+    rng = np.random.default_rng(seed)
+    lumas, regs = [], []
+    for k in range(frames):
+        grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, seed + k), parity=k & 3)
+        Hw = synth.warp(fmt, W, H, rng, rot_deg=10, scale=(0.95, 1.0))
+        luma, reg = synth.capture(fmt, grey, W, H, H=Hw, sigma=2.0, rng=rng)
+        lumas.append(luma)
+        regs.append(reg)
+    return np.stack(lumas), np.stack(regs)
+
+
+def test_engine_matches_each_receiver():
+    eng = lz.Engine()
+    st = torch.cuda.current_stream().cuda_stream
+    batches, keep, want = [], [], []
+    for i, (n, subch, span, W, H) in enumerate(FORMATS):
+        frames = 3 - (i % 2)
+        assert eng.add_format(n, subch, span, frames) == i
+        luma, reg = captures(n, subch, span, W, H, frames, 100 * i)
+        want.append(lz.Receiver(n, subch, span, max_frames=frames).finish_luma(luma, reg, keep=False, grid=False))
+        d_l, d_r = torch.from_numpy(luma).cuda(), torch.from_numpy(reg).cuda()
+        o, s = lz.rx_outputs(eng.formats[i], frames)
+        keep.append((d_l, d_r, o))
+        batches.append((i, d_l.data_ptr(), W, H, W, W * H, d_r.data_ptr(), frames, s))
+    for rep in range(3):   # the first run captures the graphs, the others replay them
+        for _, _, o in keep:
+            for t in o.values():
+                t.zero_()
+        eng.run_dev(batches, st)
+        torch.cuda.synchronize()
+        for i, (_, _, o) in enumerate(keep):
+            for k in ("blocks", "ok", "its"):
+                assert np.array_equal(o[k].cpu().numpy(), want[i][k]), (rep, i, k)
+            assert want[i]["ok"].all()
+    assert eng.launches == sum(4 + 3 + f.tiers for f in eng.formats)
+    eng.close()
+
+
+def test_engine_refuses_bad_runs():
+    eng = lz.Engine()
+    eng.add_format(384, 64, 128, 1)
+    o, s = lz.rx_outputs(eng.formats[0], 1)
+    d = torch.zeros((720, 1280), dtype=torch.uint8, device="cuda")
+    r = torch.zeros(9 + 2 * 40 * 40, dtype=torch.float32, device="cuda")
+    b = (0, d.data_ptr(), 1280, 720, 1280, 1280 * 720, r.data_ptr(), 1, s)
+    with pytest.raises(lz.LizgError):
+        eng.run_dev([b, b], 0)          # a format twice
+    with pytest.raises(lz.LizgError):
+        eng.run_dev([(3,) + b[1:]], 0)  # no such format
+    with pytest.raises(lz.LizgError):
+        eng.add_format(500, 64, 128, 1)  # no such picture size
+    eng.close()
