@@ -405,6 +405,93 @@ def bench_multistream(args, stream):
     return res
 
 
+def _render_distorted(job):
+    """One distorted capture (a worker of bench_refinement's process pool): job = (index, k1, blur)."""
+    import numpy as np
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    k, k1, blur = job
+    fmt = lz.Format(1536, 1024, 256)
+    rng = np.random.default_rng(9000 + k)
+    grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 9000 + k), parity=k & 3)
+    view = synth.distorted_view(fmt, 1920, 1080, rng, base_side=1000.0)
+    return synth.distorted_capture(fmt, grey, 1920, 1080, view, k1=k1, blur=blur, sigma=3.0, rng=rng)
+
+
+def bench_refinement(args, stream):
+    """The full receiver on distorted captures, plain against refined registration: 1920 x 1080 frames, one
+    LIZARD-1024 (n = 1536) symbol in the 128 ring, rotation U(+-15 deg), tilt U(+-20 deg) about a random in-plane axis,
+    scale U(0.8, 1.1) x a 1000-pixel layout side, radial k1 about the frame centre, Gaussian blur in linear light
+    (gamma 2.2), AWGN 3 DN, seed = frame index. Plain: the homography through the layout's four corners as the camera
+    sees them (a finder's corners), no lens. Refined: plus three rounds of the anchor search and the lens model the
+    anchors give, written into the node mesh (lizg_refine_dev). Three sets: the configuration's spread (k1 U(+-0.05),
+    blur U(0.5, 2.0)), the point blur 1.5 / k1 0.03, and mild blur (k1 U(+-0.05), blur 0.5). Device-timed."""
+    import concurrent.futures
+    import multiprocessing
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    sets = []
+    rng = np.random.default_rng(123)
+    sets.append(("spread", [(k, float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for k in range(48)]))
+    sets.append(("blur1.5_k1_0.03", [(100 + k, 0.03, 1.5) for k in range(16)]))
+    sets.append(("mild_blur0.5", [(200 + k, float(rng.uniform(-0.05, 0.05)), 0.5) for k in range(32)]))
+    jobs = [j for _, js in sets for j in js]
+    with concurrent.futures.ProcessPoolExecutor(max_workers=os.cpu_count() or 4, mp_context=multiprocessing.get_context("spawn")) as ex:
+        caps = list(ex.map(_render_distorted, jobs, chunksize=2))
+    sp = stream.cuda_stream
+    res = {"workload": "1920x1080, LIZARD-1024 (n=1536) in the 128 ring, rotation 15 deg, tilt 20 deg, scale 0.8-1.1 x 1000 px, "
+                       "radial k1, blur in linear light, AWGN 3 DN; plain = corners' homography, refined = + 3 rounds of anchors and lens model"}
+    at = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, js in sets:
+        frames = len(js)
+        luma = np.stack([caps[at + i][0] for i in range(frames)])
+        reg = np.stack([caps[at + i][1] for i in range(frames)])
+        at += frames
+        rx = lz.Receiver(1536, 1024, 256, max_frames=frames)
+        ref = lz.Refiner(256, frames)
+        d_l = torch.from_numpy(luma).cuda()
+        d_plain = torch.from_numpy(reg).cuda()
+        d_ref = torch.empty_like(d_plain)
+        d_found = torch.zeros(frames, dtype=torch.int32, device="cuda")
+        o_p, s_p = rx._outputs(frames, torch, keep=False)
+        o_r, s_r = rx._outputs(frames, torch, keep=False)
+
+        def plain():
+            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
+                                                       lz.ctypes.c_void_p(d_plain.data_ptr()), frames, lz.ctypes.byref(s_p), None, None,
+                                                       lz.ctypes.c_void_p(sp)), "finish_luma")
+
+        def refined():
+            d_ref.copy_(d_plain)
+            ref.refine_dev(d_l.data_ptr(), 1920, 1080, 1920 * 1080, d_ref.data_ptr(), frames, 3, d_found.data_ptr(), None, sp)
+            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
+                                                       lz.ctypes.c_void_p(d_ref.data_ptr()), frames, lz.ctypes.byref(s_r), None, None,
+                                                       lz.ctypes.c_void_p(sp)), "finish_luma")
+        out = {"frames": frames}
+        for tag, fn, o in (("plain", plain, o_p), ("refined", refined, o_r)):
+            for _ in range(2):
+                fn()
+            torch.cuda.synchronize()
+            reps = 3
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            ok = o["ok"].cpu().numpy()
+            out[tag] = {"blocks_verified": int(ok.sum()), "blocks": int(ok.size), "block_pass_rate": round(float(ok.mean()), 4),
+                        "frames_with_a_block": int((ok.sum(axis=1) > 0).sum()), "frames_all_blocks": int(ok.all(axis=1).sum()),
+                        "frames_per_s": round(frames / (ms / 1e3), 1)}
+        out["anchors_found_mean"] = round(float(d_found.float().mean().item()), 1)
+        out["block_pass_points_gained"] = round(100 * (out["refined"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
+        res[name] = out
+        ref.close()
+    return res
+
+
 def run_reference(args, rank, ws):
     """The reference arm: the reference's CPU decoder on the host cores, same metric and workload."""
     if rank != 0:
@@ -457,7 +544,7 @@ def main():
         st = torch.cuda.current_stream()
         rec = bench_receiver(args, st)
         rec["multistream"] = bench_multistream(args, st)
-        print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st)}}))
+        print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st)}}))
         return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
     plan = lz.LdpcPlan(batch["rates"], MAX_ITER, STALL_IT, STALL_RATIO)
@@ -548,7 +635,7 @@ def main():
         out["e2e"] = e2e
     if not args.no_receiver:
         out["receiver"] = bench_receiver(args, stream)
-        out["registration"] = {"anchor_search": bench_anchor(args, stream)}
+        out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream)}
         out["receiver"]["multistream"] = bench_multistream(args, stream)
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

@@ -224,6 +224,25 @@ typedef struct {
 int lizg_anchor_find_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
                          const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out *out, void *stream);
 
+// ---------------------------------------------------------------- registration assist: refinement from the anchors
+//
+// For frames registered by a homography alone (a finder's four corners), the lens the camera adds, found from the
+// anchors and written into the registration's node mesh, on the GPU. Each of `rounds` rounds (1..8) searches the
+// anchors not yet found (lizg_anchor_find_dev's search, through H and, after the first round, the lens model so
+// far) and fits the lens model the found anchors give about H: the reference's anchor_model
+// (liblizard/src/acquire.c:2038-2055: the four corner nodes with no displacement and the anchors found, the model of
+// 8 + K terms, K = 0..3 chosen by AICc, lensm_fit's first round 1630-1669), in double. The reference's registration
+// goes on from there (anchor_homo's homography re-fit, the corners' outliers, node refinement: 2128-2200); this
+// refinement keeps H and writes the model's displacement at every node into the mesh (zeros where no model fits).
+// d_reg: frames x (9 + 2 nx ny) floats, H kept, the mesh overwritten. d_found (frames, may be NULL): anchors found;
+// d_lens (frames x 15, may be NULL): the model (K, ax, ay, R, 11 coefficients). The handle keeps the anchors'
+// device buffers for up to max_frames frames of one ring span (128, 256 or 512).
+typedef struct lizg_refiner lizg_refiner;
+lizg_refiner *lizg_refiner_new(int span, int max_frames);
+void lizg_refiner_free(lizg_refiner *r);
+int lizg_refine_dev(lizg_refiner *r, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int rounds,
+                    int32_t *d_found, double *d_lens, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -212,6 +212,10 @@ def _rx_sigs(L):
     L.lizg_engine_rx.restype = P
     L.lizg_engine_run_dev.argtypes = [P, P, I, P]
     L.lizg_engine_launches.argtypes = [P]
+    L.lizg_refiner_new.argtypes = [I, I]
+    L.lizg_refiner_new.restype = P
+    L.lizg_refiner_free.argtypes = [P]
+    L.lizg_refine_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
 
 
 class RxOut(ctypes.Structure):
@@ -416,6 +420,47 @@ class Engine:
     def close(self):
         if self._h:
             lib().lizg_engine_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Refiner:
+    """The registration's refinement from the anchors (lizg_refine_*) for frames of one ring span."""
+
+    def __init__(self, span, max_frames):
+        self._h = lib().lizg_refiner_new(span, max_frames)
+        if not self._h:
+            raise LizgError("lizg_refiner_new failed: %s" % lib().lizg_last_error().decode())
+
+    def refine_dev(self, d_luma, w, h, frame_stride, d_reg, frames, rounds, d_found=None, d_lens=None, stream=0):
+        _check(lib().lizg_refine_dev(self._h, ctypes.c_void_p(d_luma), w, h, frame_stride, ctypes.c_void_p(d_reg), frames, rounds,
+                                     None if d_found is None else ctypes.c_void_p(d_found), None if d_lens is None else ctypes.c_void_p(d_lens),
+                                     ctypes.c_void_p(stream)), "lizg_refine_dev")
+
+    def refine(self, luma, reg, rounds=3):
+        """luma frames x h x w uint8, reg frames x (9 + 2 nx ny): returns (refined reg, anchors found, lens frames x 15)."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        if lu.ndim == 2:
+            lu = lu[None]
+        frames, h, w = lu.shape
+        d_l = torch.from_numpy(lu).cuda()
+        d_r = torch.from_numpy(np.ascontiguousarray(np.asarray(reg, np.float32).reshape(frames, -1))).cuda()
+        d_f = torch.zeros(frames, dtype=torch.int32, device="cuda")
+        d_lens = torch.zeros((frames, 15), dtype=torch.float64, device="cuda")
+        self.refine_dev(d_l.data_ptr(), w, h, w * h, d_r.data_ptr(), frames, rounds, d_f.data_ptr(), d_lens.data_ptr(),
+                        torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return d_r.cpu().numpy(), d_f.cpu().numpy(), d_lens.cpu().numpy()
+
+    def close(self):
+        if self._h:
+            lib().lizg_refiner_free(self._h)
             self._h = None
 
     def __del__(self):

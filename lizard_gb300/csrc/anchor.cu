@@ -208,6 +208,26 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
   a.out.ok[o] = best >= kAnchPeak && bx > -r && bx < r && by > -r && by < r;
 }
 
+// Queues the search for a batch of frames (arguments as lizg_anchor_find_dev's, already checked).
+cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
+                               const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st) {
+  AnchArgs a{};
+  a.span = span; a.w = w; a.h = h; a.frames = frames; a.hstride = h_stride; a.fstride = frame_stride;
+  a.g = anch_geom(span);
+  for (int i = 0; i < kAnchK; i++) a.m0[i] = (int)floor(kMarginM + (double)span * (i + 0.5) / kAnchK - a.g.a / 2.0 + 0.5);
+  a.luma = d_luma; a.skip = d_skip; a.H = d_H; a.lens = d_lens; a.out = out;
+  const int W1 = a.g.W + 1;
+  const size_t smem = 2 * sizeof(double) * W1 * W1 + sizeof(float) * ((size_t)a.g.W * a.g.W + (size_t)a.g.O * a.g.O);
+  static bool attr = false;
+  cudaError_t e;
+  if (!attr) {
+    if ((e = cudaFuncSetAttribute(anchor_find_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024)) != cudaSuccess) return e;
+    attr = true;
+  }
+  anchor_find_kernel<<<frames * kAnchK * kAnchK, 256, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace lizg
 
 extern "C" int lizg_anchor_find_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
@@ -220,21 +240,7 @@ extern "C" int lizg_anchor_find_dev(int span, const uint8_t *d_luma, int w, int 
     return record_error(LIZG_E_ARG, "lizg_anchor_find_dev: bad frame geometry, H stride or frame count");
   int sms = 0;
   if (int rc = device_ready(&sms)) return rc;
-  AnchArgs a{};
-  a.span = span; a.w = w; a.h = h; a.frames = frames; a.hstride = h_stride; a.fstride = frame_stride;
-  a.g = anch_geom(span);
-  for (int i = 0; i < kAnchK; i++) a.m0[i] = (int)floor(kMarginM + (double)span * (i + 0.5) / kAnchK - a.g.a / 2.0 + 0.5);
-  a.luma = d_luma; a.skip = d_skip; a.H = d_H; a.lens = d_lens; a.out = *out;
-  const int W1 = a.g.W + 1;
-  const size_t smem = 2 * sizeof(double) * W1 * W1 + sizeof(float) * ((size_t)a.g.W * a.g.W + (size_t)a.g.O * a.g.O);
-  static bool attr = false;
-  cudaError_t e = cudaSuccess;
-  if (!attr) {
-    e = cudaFuncSetAttribute(anchor_find_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    if (e != cudaSuccess) return record_error(LIZG_E_CUDA, (std::string("lizg_anchor_find_dev: ") + cudaGetErrorString(e)).c_str());
-    attr = true;
-  }
-  anchor_find_kernel<<<frames * kAnchK * kAnchK, 256, smem, static_cast<cudaStream_t>(stream)>>>(a);
-  if ((e = cudaGetLastError()) != cudaSuccess) return record_error(LIZG_E_CUDA, (std::string("lizg_anchor_find_dev: ") + cudaGetErrorString(e)).c_str());
+  const cudaError_t e = anchor_find_launch(span, d_luma, w, h, frame_stride, d_H, h_stride, d_lens, d_skip, frames, *out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return record_error(LIZG_E_CUDA, (std::string("lizg_anchor_find_dev: ") + cudaGetErrorString(e)).c_str());
   return 0;
 }

@@ -3,6 +3,7 @@
 #define LIZG_INTERNAL_H
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include "lizard_gb300.h"
 
 namespace lizg {
 
@@ -119,6 +120,9 @@ cudaError_t sample_launch(const SampleDev &sd, int frames, const uint8_t *luma, 
 cudaError_t sample_tables_launch(SampleDev sd, float4 *colt, float4 *rowt, cudaStream_t st);
 // The node lattice of a layout of side modules (liblizard/src/layout.c:110-117): returns nx (= ny).
 int layout_nodes(int side, float *pos);
+// The anchor search for a batch of frames (arguments as lizg_anchor_find_dev's, already checked).
+cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
+                               const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
 

@@ -229,3 +229,102 @@ def warp(fmt, width, height, rng, rot_deg=15.0, tilt=0.0002, scale=(0.9, 1.05)):
     T1 = np.array([[1, 0, width / 2], [0, 1, height / 2], [0, 0, 1]])
     H = T1 @ P @ A @ T0
     return (H / H[2, 2]).ravel()
+
+
+def distorted_view(fmt, width, height, rng, base_side=700.0, rot_deg=15.0, tilt_deg=20.0, scale=(0.8, 1.1), focal=None, tries=50):
+    """A camera's view of the layout: rotation U(+-rot_deg) in the image plane, a tilt U(+-tilt_deg) of the symbol's
+    plane about a random in-plane axis (a pinhole camera of focal length `focal` pixels, default the frame's width),
+    the layout's side base_side x U(scale) pixels at the frame centre. Redrawn until the layout's four corners stay
+    inside the frame. Returns H (module -> ideal image pixels, 3 x 3)."""
+    side = fmt.span + 30
+    f = float(width) if focal is None else focal
+    for _ in range(tries):
+        rot = np.deg2rad(rng.uniform(-rot_deg, rot_deg))
+        tilt = np.deg2rad(rng.uniform(-tilt_deg, tilt_deg))
+        phi = rng.uniform(0, np.pi)
+        s = base_side * rng.uniform(*scale) / side
+        ax = np.array([np.cos(phi), np.sin(phi), 0.0])
+        Kx = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+        Rt = np.eye(3) + np.sin(tilt) * Kx + (1 - np.cos(tilt)) * (Kx @ Kx)   # Rodrigues: the tilt about ax
+        Rz = np.array([[np.cos(rot), -np.sin(rot), 0], [np.sin(rot), np.cos(rot), 0], [0, 0, 1]])
+        R = Rz @ Rt
+        Kc = np.array([[f, 0, width / 2.0], [0, f, height / 2.0], [0, 0, 1]])
+        M = Kc @ np.column_stack([R[:, 0], R[:, 1], np.array([0, 0, f])])
+        A = np.array([[s, 0, -s * side / 2.0], [0, s, -s * side / 2.0], [0, 0, 1]])
+        H = M @ A
+        H = H / H[2, 2]
+        corners = np.array([[0, 0, 1], [side, 0, 1], [side, side, 1], [0, side, 1]], np.float64).T
+        q = H @ corners
+        u, v = q[0] / q[2], q[1] / q[2]
+        if (u > 2).all() and (u < width - 3).all() and (v > 2).all() and (v < height - 3).all():
+            return H
+    raise RuntimeError("no view keeps the layout inside the frame")
+
+
+def radial(u, v, width, height, k1):
+    """Radial distortion about the frame centre: p -> c + (p - c)(1 + k1 r^2), r = |p - c| / the half-diagonal."""
+    cx, cy, R = width / 2.0, height / 2.0, np.hypot(width, height) / 2.0
+    dx, dy = u - cx, v - cy
+    g = 1 + k1 * (dx * dx + dy * dy) / (R * R)
+    return cx + dx * g, cy + dy * g
+
+
+def _unradial(ud, vd, width, height, k1, rounds=8):
+    """The inverse of radial() by fixed-point rounds (|k1| small)."""
+    cx, cy, R = width / 2.0, height / 2.0, np.hypot(width, height) / 2.0
+    u, v = ud.copy(), vd.copy()
+    for _ in range(rounds):
+        dx, dy = u - cx, v - cy
+        g = 1 + k1 * (dx * dx + dy * dy) / (R * R)
+        u, v = cx + (ud - cx) / g, cy + (vd - cy) / g
+    return u, v
+
+
+def homography_4(src, dst):
+    """The homography (h33 = 1) taking four points src to dst (each 4 x 2), by the 8 x 8 linear system."""
+    A, b = [], []
+    for (x, y), (u, v) in zip(src, dst):
+        A.append([x, y, 1, 0, 0, 0, -u * x, -u * y]); b.append(u)
+        A.append([0, 0, 0, x, y, 1, -v * x, -v * y]); b.append(v)
+    h = np.linalg.solve(np.array(A, np.float64), np.array(b, np.float64))
+    return np.append(h, 1.0)
+
+
+def distorted_capture(fmt, grey, width, height, H, k1=0.0, blur=0.0, sigma=3.0, rng=None, mid=128, gamma=2.2):
+    """A capture through a real lens: the n x n grey picture inside its light layout, seen through the view H (module
+    -> ideal image), radial distortion k1 about the frame centre, a Gaussian blur of `blur` pixels in linear light
+    (grey -> (g / 255)^gamma -> blur -> ^(1 / gamma)), AWGN of sigma grey levels, 8 bits. Returns (luma, the plain
+    registration: the homography through the layout's four corners as the camera sees them, then a zero node mesh)."""
+    from scipy.ndimage import gaussian_filter
+    n, span = fmt.n, fmt.span
+    pxm = n / span
+    side = span + 30
+    px = int(round(side * pxm))
+    drive = np.full((px, px), 255.0)
+    o = int(round(15 * pxm))
+    drive[o:o + n, o:o + n] = grey
+    Hm = np.asarray(H, np.float64).reshape(3, 3)
+    Hi = np.linalg.inv(Hm)
+    V, U = np.mgrid[0:height, 0:width].astype(np.float64)
+    ui, vi = _unradial(U.ravel() + 0.5, V.ravel() + 0.5, width, height, k1)
+    q = Hi @ np.stack([ui, vi, np.ones(ui.size)])
+    mx, my = q[0] / q[2], q[1] / q[2]
+    sx, sy = mx * pxm - 0.5, my * pxm - 0.5
+    inside = (sx >= 0) & (sy >= 0) & (sx <= px - 1.001) & (sy <= px - 1.001)
+    x0 = np.clip(np.floor(sx).astype(np.int64), 0, px - 2)
+    y0 = np.clip(np.floor(sy).astype(np.int64), 0, px - 2)
+    fx, fy = np.clip(sx - x0, 0, 1), np.clip(sy - y0, 0, 1)
+    val = (drive[y0, x0] * (1 - fx) + drive[y0, x0 + 1] * fx) * (1 - fy) + (drive[y0 + 1, x0] * (1 - fx) + drive[y0 + 1, x0 + 1] * fx) * fy
+    img = np.where(inside, val, float(mid)).reshape(height, width)
+    if blur > 0:
+        lin = (img / 255.0) ** gamma
+        img = 255.0 * np.clip(gaussian_filter(lin, blur, mode="nearest"), 0, 1) ** (1.0 / gamma)
+    rng = np.random.default_rng(0) if rng is None else rng
+    luma = np.clip(np.rint(img + sigma * rng.standard_normal(img.shape)), 0, 255).astype(np.uint8)
+    corners = np.array([[0, 0], [side, 0], [side, side], [0, side]], np.float64)
+    qc = Hm @ np.column_stack([corners, np.ones(4)]).T
+    cu, cv = radial(qc[0] / qc[2], qc[1] / qc[2], width, height, k1)
+    Hp = homography_4(corners, np.column_stack([cu, cv]))
+    nn = layout_nodes(span).size
+    reg = np.concatenate([Hp.astype(np.float32), np.zeros(2 * nn * nn, np.float32)])
+    return luma, reg

@@ -49,6 +49,7 @@ def port():
         L.orc_crc32c.restype = ctypes.c_uint32
         L.orc_ldpc_batch.argtypes = [P, P, P, I, I, I, F, P, P, P, I]
         L.orc_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
+        L.orc_lens_fit.argtypes = [I, I, I, P, P, P, P, P]
         _port = L
     return _port
 
@@ -81,12 +82,22 @@ def ref_scalar():
         L = ctypes.CDLL(REF_SCALAR_PATH)
         P, I = ctypes.c_void_p, ctypes.c_int
         L.refs_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
+        L.refs_anchor_model.argtypes = [I, I, I, P, P, P, P, P]
         _ref_scalar = L
     return _ref_scalar
 
 
 def _p(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def lens_fit(lib, fn, span, iw, ih, H, ok, dx, dy):
+    """The lens model from one frame's anchors through lib.fn (orc_lens_fit or refs_anchor_model): (fit, lens[15])."""
+    Hf = np.ascontiguousarray(H, np.float32).ravel()[:9]
+    ok, dx, dy = (np.ascontiguousarray(a, t) for a, t in ((ok, np.uint8), (dx, np.float32), (dy, np.float32)))
+    lens = np.zeros(15, np.float64)
+    fit = getattr(lib, fn)(span, iw, ih, _p(Hf), _p(ok), _p(dx), _p(dy), _p(lens))
+    return fit, lens
 
 
 def anchor_find(lib, fn, span, luma, H, lens=None, ok_in=None):

@@ -68,6 +68,9 @@ int orc_sample_grid(int n, int span, const uint8_t *luma, int w, int h, int pitc
 // found (49 flags or NULL). Out per anchor (row-major j * 7 + i): ok, peak, dx, dy, u, v. Returns the anchors ok.
 int orc_anchor_find(int span, const uint8_t *px, int w, int h, const float *H, const double *lens, const uint8_t *ok_in,
                     uint8_t *ok, float *peak, float *dx, float *dy, float *u, float *v);
+// The lens model from the anchors about H (liblizard/src/acquire.c:2038-2055 anchor_model, lensm_fit's first round):
+// lens out K, ax, ay, R, then 11 coefficients; 1 where a model fits.
+int orc_lens_fit(int span, int iw, int ih, const float *H, const uint8_t *ok, const float *dx, const float *dy, double *lens);
 
 #ifdef __cplusplus
 }

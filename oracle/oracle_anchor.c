@@ -146,3 +146,92 @@ int orc_anchor_find(int span, const uint8_t *px, int w, int h, const float *H, c
   free(win); free(C); free(I1); free(I2);
   return found;
 }
+
+// ---------------------------------------------------------------- the lens model from the anchors
+
+// Gauss-Jordan with partial pivoting on the first n rows of the normal equations, right-hand side in column LENSP
+// (liblizard/src/acquire.c:1491-1504 solve_lens).
+static int solve_lens(double A[LENSP][LENSP + 1], int n) {
+  for (int c = 0; c < n; c++) {
+    int p = c;
+    for (int r = c + 1; r < n; r++) if (fabs(A[r][c]) > fabs(A[p][c])) p = r;
+    if (fabs(A[p][c]) < 1e-14) return 0;
+    for (int k = 0; k <= LENSP; k++) { const double t = A[c][k]; A[c][k] = A[p][k]; A[p][k] = t; }
+    for (int r = 0; r < n; r++) {
+      if (r == c) continue;
+      const double f = A[r][c] / A[c][c];
+      for (int k = c; k <= LENSP; k++) A[r][k] -= f * A[c][k];
+    }
+  }
+  return 1;
+}
+
+static void lens_rows(double x, double y, int K, double *rx, double *ry) {
+  const double ex[8] = {x, y, 0, 0, 1, 0, -x * x, -x * y}, ey[8] = {0, 0, x, y, 0, 1, -x * y, -y * y};
+  for (int a = 0; a < 8; a++) { rx[a] = ex[a]; ry[a] = ey[a]; }
+  const double s = x * x + y * y;
+  double sk = s;
+  for (int k = 0; k < K; k++, sk *= s) { rx[8 + k] = sk * x; ry[8 + k] = sk * y; }
+}
+
+// The lens model the anchors and the four corner nodes give about H (liblizard/src/acquire.c:2043-2061 anchor_model,
+// with lensm_fit's first round, 1630-1669: the normal equations summed once in the points' order, every model of
+// 0..3 radial terms solved, the one of least AICc kept). The axis is the frame's centre and R its half-diagonal
+// (lensm_axis, 1622-1628, with no axis set). nodes: the layout's node lattice (nn a side). lens out: K, ax, ay, R,
+// then the 11 coefficients. Returns 1 where a model fits, else 0.
+int orc_lens_fit(int span, int iw, int ih, const float *H, const uint8_t *ok, const float *adx, const float *ady, double *lens) {
+  const int a = span / 64;
+  float nodes[40];
+  const int nn = orc_layout_nodes(span + 2 * MARGIN, nodes);
+  const double ax = iw * 0.5f, ay = ih * 0.5f;
+  double R = 0;
+  for (int c = 0; c < 4; c++) { const double d = hypot((c & 1 ? iw : 0) - ax, (c & 2 ? ih : 0) - ay); if (d > R) R = d; }
+  if (!(R > 0)) R = 1;
+  double qx[ANK * ANK + 4], qy[ANK * ANK + 4], dx[ANK * ANK + 4], dy[ANK * ANK + 4];
+  int np = 0;
+  for (int c = 0; c < 4; c++) {
+    float u, v;
+    project(H, nodes[(c == 1 || c == 2) ? nn - 1 : 0], nodes[c >= 2 ? nn - 1 : 0], &u, &v);
+    qx[np] = (u - ax) / R; qy[np] = (v - ay) / R; dx[np] = 0; dy[np] = 0; np++;
+  }
+  for (int k = 0; k < ANK * ANK; k++) {
+    if (!ok[k]) continue;
+    const float X = (float)anchor_m0(span, k % ANK) + a * 0.5f, Y = (float)anchor_m0(span, k / ANK) + a * 0.5f;
+    float u, v;
+    project(H, X, Y, &u, &v);
+    qx[np] = (u - ax) / R; qy[np] = (v - ay) / R; dx[np] = adx[k]; dy[np] = ady[k]; np++;
+  }
+  double A3[LENSP][LENSP + 1], rx[LENSP], ry[LENSP];
+  memset(A3, 0, sizeof A3);
+  for (int i = 0; i < np; i++) {
+    lens_rows(qx[i], qy[i], 3, rx, ry);
+    for (int p = 0; p < LENSP; p++) {
+      for (int q = p; q < LENSP; q++) A3[p][q] += rx[p] * rx[q] + ry[p] * ry[q];
+      A3[p][LENSP] += rx[p] * dx[i] + ry[p] * dy[i];
+    }
+  }
+  for (int p = 1; p < LENSP; p++) for (int q = 0; q < p; q++) A3[p][q] = A3[q][p];
+  double best = INFINITY, tb[LENSP] = {0};
+  int K = -1;
+  for (int k = 0; k <= 3; k++) {
+    const int p = 8 + k;
+    double A[LENSP][LENSP + 1];
+    memcpy(A, A3, sizeof A);
+    for (int c = 0; c < p; c++) A[c][c] += 1e-12;
+    if (2 * np - p - 1 <= 0 || !solve_lens(A, p)) continue;
+    double t[LENSP] = {0}, rss = 0;
+    for (int c = 0; c < p; c++) t[c] = A[c][LENSP] / A[c][c];
+    for (int i = 0; i < np; i++) {
+      lens_rows(qx[i], qy[i], k, rx, ry);
+      double fx = 0, fy = 0;
+      for (int c = 0; c < p; c++) { fx += t[c] * rx[c]; fy += t[c] * ry[c]; }
+      rss += (dx[i] - fx) * (dx[i] - fx) + (dy[i] - fy) * (dy[i] - fy);
+    }
+    const double n2 = 2.0 * np, aicc = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
+    if (aicc < best) { best = aicc; K = k; memcpy(tb, t, sizeof tb); }
+  }
+  if (K < 0) return 0;
+  lens[0] = K; lens[1] = ax; lens[2] = ay; lens[3] = R;
+  for (int c = 0; c < LENSP; c++) lens[4 + c] = tb[c];
+  return 1;
+}

@@ -36,3 +36,29 @@ int refs_anchor_find(int span, const uint8_t *px, int w, int h, const float *H9,
 
 // The lens model's coefficient count (LENS_P) and the anchors' grid (OB_ANCH_K), for the caller's buffers.
 int refs_lens_p(void) { return LENS_P; }
+
+// The lens model the reference fits from the anchors about H (liblizard/src/acquire.c:2038-2055 anchor_model), for a
+// frame of iw x ih pixels: ok, dx, dy per anchor (row-major j * 7 + i). lens out: K, ax, ay, R, then the LENS_P
+// coefficients. Returns 1 where a model fits, else 0.
+int refs_anchor_model(int span, int iw, int ih, const float *H9, const uint8_t *ok, const float *dx, const float *dy, double *lens) {
+  ob_layout_t L;
+  if (ob_layout_init(&L, span + 2 * OB_MARGIN)) return -1;
+  homo_t H;
+  memcpy(H.h, H9, sizeof H.h);
+  const int a = ob_anchor_side(&L);
+  anchor_t A[OB_ANCH_K * OB_ANCH_K];
+  memset(A, 0, sizeof A);
+  for (int j = 0; j < OB_ANCH_K; j++)
+    for (int i = 0; i < OB_ANCH_K; i++) {
+      anchor_t *an = &A[j * OB_ANCH_K + i];
+      an->X = (float)ob_anchor_m0(&L, i) + a * 0.5f; an->Y = (float)ob_anchor_m0(&L, j) + a * 0.5f;
+      an->ok = ok[j * OB_ANCH_K + i]; an->dx = dx[j * OB_ANCH_K + i]; an->dy = dy[j * OB_ANCH_K + i];
+    }
+  lensm_t m;
+  memset(&m, 0, sizeof m);
+  const int fit = anchor_model(&L, &H, iw, ih, A, &m);
+  lens[0] = m.K; lens[1] = m.ax; lens[2] = m.ay; lens[3] = m.R;
+  for (int k = 0; k < LENS_P; k++) lens[4 + k] = m.t[k];
+  ob_layout_free(&L);
+  return fit;
+}

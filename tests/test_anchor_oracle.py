@@ -65,3 +65,20 @@ def test_oracle_matches_reference_build(span, n, subch, W, Hh, seed, with_lens):
     b = oracle.anchor_find(oracle.ref_scalar(), "refs_anchor_find", span, luma, H, lens, skip)
     assert same(a, b)
     assert a["found"] == b["found"] and a["found"] >= 40
+
+
+@pytest.mark.skipif(oracle.ref_scalar() is None, reason="the reference's portable build is not here")
+@pytest.mark.parametrize("seed,k1", [(1, 0.0), (2, 0.03), (3, -0.04), (4, 0.05)])
+def test_lens_fit_matches_reference(seed, k1):
+    """The lens model from the anchors (anchor_model) on distorted captures, bit for bit."""
+    fmt = lz.Format(1536, 1024, 256)
+    rng = np.random.default_rng(seed)
+    grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, seed), parity=seed & 3)
+    H = synth.distorted_view(fmt, 1920, 1080, rng, base_side=1000)
+    luma, reg = synth.distorted_capture(fmt, grey, 1920, 1080, H, k1=k1, blur=1.0, sigma=3.0, rng=rng)
+    a = oracle.anchor_find(oracle.port(), "orc_anchor_find", 256, luma, reg[:9])
+    assert a["found"] >= 30
+    f1, l1 = oracle.lens_fit(oracle.port(), "orc_lens_fit", 256, 1920, 1080, reg[:9], a["ok"], a["dx"], a["dy"])
+    f2, l2 = oracle.lens_fit(oracle.ref_scalar(), "refs_anchor_model", 256, 1920, 1080, reg[:9], a["ok"], a["dx"], a["dy"])
+    assert f1 == f2 == 1
+    assert np.array_equal(l1.view(np.uint64), l2.view(np.uint64)), (l1, l2)
