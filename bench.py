@@ -405,6 +405,76 @@ def bench_multistream(args, stream):
     return res
 
 
+def bench_ingest(args, stream):
+    """Camera-format ingest to luma on the GPU, 16 frames a call: 3840 x 2160 RGBA8 (liz_decode's conversion), and a
+    3840 x 2160 sensor's RAW10 developed at bin 1 (3840 x 2160 out) and bin 2 (1920 x 1080 out), and P010. Device-timed;
+    GB/s = the frames' bytes read (the whole plane a format's samples occupy) and written over the time; the fraction is
+    of the measured HBM copy peak. Beside it the same conversions on the host cores (the oracle's C, a frame a thread)."""
+    import concurrent.futures
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    import oracle
+    frames, W, H = 16, 3840, 2160
+    peak, peak_src = peaks()
+    rng = np.random.default_rng(77)
+    sp = stream.cuda_stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lv = (lz.ctypes.c_float * 9)(64.0, 66.0, 63.0, 65.0, 1023.0, 1.9, 1.0, 1.0, 1.6)
+    res = {}
+    cases = [("rgba8_3840x2160", 4 * W, H, W, H, None), ("raw10_bin1_3840x2160", (W + 3) // 4 * 5, H, W, H, 1),
+             ("raw10_bin2_to_1920x1080", (W + 3) // 4 * 5, H, W // 2, H // 2, 2), ("p010_3840x2160", 2 * W, H, W, H, 0)]
+    if not os.path.exists(oracle.PORT_PATH):
+        oracle.build(ref=False)
+    for name, rowb, rows, w, h, kind in cases:
+        host = rng.integers(0, 256, (frames, rows * rowb), dtype=np.uint8)
+        d_in = torch.from_numpy(host).cuda()
+        d_out = torch.zeros((frames, h, w), dtype=torch.uint8, device="cuda")
+        if kind is None:
+            def call():
+                lz._check(lz.lib().lizg_ingest_pixels_dev(lz.ctypes.c_void_p(d_in.data_ptr()), W, H, rowb, rows * rowb, 3, frames,
+                                                          lz.ctypes.c_void_p(d_out.data_ptr()), lz.ctypes.c_void_p(sp)), "ingest")
+        else:
+            fmt = 0x36 if kind == 0 else 0x25
+            r = lz.RawFrame(fmt, rowb, 2, 0, 0, max(kind, 1), lv)
+
+            def call():
+                lz._check(lz.lib().lizg_develop_dev(lz.ctypes.byref(r), lz.ctypes.c_void_p(d_in.data_ptr()), rows * rowb, rows * rowb, frames,
+                                                    0, 0, w, h, lz.ctypes.c_void_p(d_out.data_ptr()), lz.ctypes.c_void_p(sp)), "develop")
+        for _ in range(3):
+            call()
+        torch.cuda.synchronize()
+        reps = 20
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        moved = frames * (rows * rowb + w * h)
+        gbs = moved / (ms / 1e3) / 1e9
+        # the host cores: the same conversion of every frame once
+
+        def cpu(f):
+            o = np.zeros((h, w), np.uint8)
+            if kind is None:
+                oracle.port().orc_ingest_pixels(oracle._p(host[f]), W, H, rowb, 3, oracle._p(o))
+            else:
+                oracle.port().orc_develop(0x36 if kind == 0 else 0x25, oracle._p(host[f]), rowb, 2, 0, 0, max(kind, 1),
+                                          oracle._p(np.array(list(lv), np.float32)), 0, 0, w, h, oracle._p(o), w)
+            return o
+        t0 = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+            outs = list(ex.map(cpu, range(frames)))
+        dt = time.perf_counter() - t0
+        same = all(np.array_equal(outs[f], d_out[f].cpu().numpy()) for f in (0, frames - 1))
+        res[name] = {"frames_per_s": round(frames / (ms / 1e3), 1), "GBps": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
+                     "ms_per_call": round(ms, 4), "identical_to_host": bool(same),
+                     "cpu": {"frames_per_s": round(frames / dt, 1), "cores": os.cpu_count() or 1, "kind": "port"}}
+    res["peak"] = {"GBps": peak, "source": peak_src}
+    return res
+
+
 def _render_distorted(job):
     """One distorted capture (a worker of bench_refinement's process pool): job = (index, k1, blur)."""
     import numpy as np
@@ -544,7 +614,8 @@ def main():
         st = torch.cuda.current_stream()
         rec = bench_receiver(args, st)
         rec["multistream"] = bench_multistream(args, st)
-        print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st)}}))
+        print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st)},
+                          "ingest": bench_ingest(args, st)}))
         return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
     plan = lz.LdpcPlan(batch["rates"], MAX_ITER, STALL_IT, STALL_RATIO)
@@ -636,6 +707,7 @@ def main():
     if not args.no_receiver:
         out["receiver"] = bench_receiver(args, stream)
         out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream)}
+        out["ingest"] = bench_ingest(args, stream)
         out["receiver"]["multistream"] = bench_multistream(args, stream)
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

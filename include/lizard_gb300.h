@@ -224,6 +224,29 @@ typedef struct {
 int lizg_anchor_find_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
                          const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out *out, void *stream);
 
+// ---------------------------------------------------------------- camera-format ingest
+//
+// Replaces the host's conversion of a captured image to the decoder's luma: liz_decode's pixel formats
+// (liblizard/api/codec.cpp:128-140; ob_luma, liblizard/src/acquire.c:67-83) and the camera develop of P010, RAW16,
+// RAW10 and RAW12 (liblizard/core/ingest/develop.cpp:9-102, developLuma), on the GPU for a batch of frames, byte for
+// byte the reference's. Outputs are tight luma rows: frame f's w x h bytes at d_luma + f w h.
+enum { LIZG_PIX_GREY8 = 1, LIZG_PIX_RGBX8 = 2, LIZG_PIX_RGBA8 = 3, LIZG_PIX_BGRA8 = 4 };               // liz_pixfmt's values
+enum { LIZG_RAW_RAW16 = 0x20, LIZG_RAW_RAW10 = 0x25, LIZG_RAW_RAW12 = 0x26, LIZG_RAW_P010 = 0x36 };   // ImageFormat's values
+// frames x (w x h pixels of fmt, rows stride bytes apart) at d_px + f frame_stride.
+int lizg_ingest_pixels_dev(const uint8_t *d_px, int w, int h, int stride, int64_t frame_stride, int fmt, int frames, uint8_t *d_luma, void *stream);
+// A camera frame's plane 0 as the reference's RawFrame (develop.h): its format, rowStride bytes a row, pixelStride
+// bytes a sample (RAW16, P010), the developed frame's (0, 0) at sample (x0, y0), bin 1 or 2 (P010: 1), levels: the
+// black level per 2 x 2 position, the white level, the gain per position.
+typedef struct {
+  int format;
+  uint32_t row_stride, pixel_stride, x0, y0, bin;
+  float levels[9];
+} lizg_raw_frame;
+// The developed crop of w x h pixels at (ox, oy) of frames planes (frame f at d_plane + f plane_stride, each
+// plane_bytes long; a crop that would read past a row or the plane is refused with LIZG_E_ARG).
+int lizg_develop_dev(const lizg_raw_frame *r, const uint8_t *d_plane, int64_t plane_bytes, int64_t plane_stride, int frames, uint32_t ox,
+                     uint32_t oy, uint32_t w, uint32_t h, uint8_t *d_out, void *stream);
+
 // ---------------------------------------------------------------- registration assist: refinement from the anchors
 //
 // For frames registered by a homography alone (a finder's four corners), the lens the camera adds, found from the

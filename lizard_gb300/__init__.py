@@ -212,6 +212,8 @@ def _rx_sigs(L):
     L.lizg_engine_rx.restype = P
     L.lizg_engine_run_dev.argtypes = [P, P, I, P]
     L.lizg_engine_launches.argtypes = [P]
+    L.lizg_ingest_pixels_dev.argtypes = [P, I, I, I, ctypes.c_int64, I, I, P, P]
+    L.lizg_develop_dev.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, I, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, P, P]
     L.lizg_refiner_new.argtypes = [I, I]
     L.lizg_refiner_new.restype = P
     L.lizg_refiner_free.argtypes = [P]
@@ -468,3 +470,45 @@ class Refiner:
             self.close()
         except Exception:
             pass
+
+
+class RawFrame(ctypes.Structure):
+    _fields_ = [("format", ctypes.c_int), ("row_stride", ctypes.c_uint32), ("pixel_stride", ctypes.c_uint32), ("x0", ctypes.c_uint32),
+                ("y0", ctypes.c_uint32), ("bin", ctypes.c_uint32), ("levels", ctypes.c_float * 9)]
+
+
+def ingest_pixels(px, fmt, w=None):
+    """frames x h x stride bytes of liz_pixfmt fmt (or one frame, 2-D), w pixels a row (default the stride's worth), to
+    luma on the GPU: frames x h x w."""
+    import torch
+    a = np.ascontiguousarray(px, np.uint8)
+    if a.ndim == 2:
+        a = a[None]
+    frames, h, stride = a.shape
+    bpp = 1 if fmt == LIZG_PIX_GREY8 else 4
+    w = stride // bpp if w is None else w
+    d = torch.from_numpy(a).cuda()
+    o = torch.zeros((frames, h, w), dtype=torch.uint8, device="cuda")
+    _check(lib().lizg_ingest_pixels_dev(ctypes.c_void_p(d.data_ptr()), w, h, stride, h * stride, fmt, frames, ctypes.c_void_p(o.data_ptr()),
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "lizg_ingest_pixels_dev")
+    torch.cuda.synchronize()
+    return o.cpu().numpy()
+
+
+LIZG_PIX_GREY8, LIZG_PIX_RGBX8, LIZG_PIX_RGBA8, LIZG_PIX_BGRA8 = 1, 2, 3, 4
+
+
+def develop(fmt, planes, row_stride, pixel_stride, x0, y0, bin_, levels, ox, oy, w, h):
+    """frames x plane bytes (or one plane, 1-D) developed on the GPU: frames x h x w luma."""
+    import torch
+    a = np.ascontiguousarray(planes, np.uint8)
+    if a.ndim == 1:
+        a = a[None]
+    frames, nbytes = a.shape
+    r = RawFrame(fmt, row_stride, pixel_stride, x0, y0, bin_, (ctypes.c_float * 9)(*[float(v) for v in levels]))
+    d = torch.from_numpy(a).cuda()
+    o = torch.zeros((frames, h, w), dtype=torch.uint8, device="cuda")
+    _check(lib().lizg_develop_dev(ctypes.byref(r), ctypes.c_void_p(d.data_ptr()), nbytes, nbytes, frames, ox, oy, w, h,
+                                  ctypes.c_void_p(o.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "lizg_develop_dev")
+    torch.cuda.synchronize()
+    return o.cpu().numpy()

@@ -14,11 +14,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
 REF_SCALAR_PATH = os.path.join(HERE, "_ref", "libref_scalar.so")
+REF_DEVELOP_PATH = os.path.join(HERE, "_ref", "libref_develop.so")
 REF_SRC = "/root/reference/liblizard/src"
 
 _port = None
 _ref = None
 _ref_scalar = None
+_ref_develop = None
 
 
 class Code(ctypes.Structure):
@@ -50,6 +52,10 @@ def port():
         L.orc_ldpc_batch.argtypes = [P, P, P, I, I, I, F, P, P, P, I]
         L.orc_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
         L.orc_lens_fit.argtypes = [I, I, I, P, P, P, P, P]
+        U = ctypes.c_uint32
+        L.orc_ingest_pixels.argtypes = [P, I, I, I, I, P]
+        L.orc_gamma_lut.argtypes = [P]
+        L.orc_develop.argtypes = [I, P, U, U, U, U, U, P, U, U, U, U, P, ctypes.c_size_t]
         _port = L
     return _port
 
@@ -87,8 +93,30 @@ def ref_scalar():
     return _ref_scalar
 
 
+def ref_develop():
+    """The reference's own camera develop (develop.cpp) compiled here, or None where it could not be built."""
+    global _ref_develop
+    if _ref_develop is None and os.path.exists(REF_DEVELOP_PATH):
+        L = ctypes.CDLL(REF_DEVELOP_PATH)
+        P, I, U = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32
+        L.refd_develop.argtypes = [I, P, U, U, U, U, U, P, U, U, U, U, P, ctypes.c_size_t]
+        L.refd_gamma_lut.argtypes = [P]
+        _ref_develop = L
+    return _ref_develop
+
+
 def _p(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def develop(lib, fn, fmt, plane, row_stride, pixel_stride, x0, y0, bin_, levels, ox, oy, w, h):
+    """One develop through lib.fn (orc_develop or refd_develop): w x h luma bytes."""
+    plane = np.ascontiguousarray(plane, np.uint8)
+    lv = np.ascontiguousarray(levels, np.float32)
+    out = np.zeros((h, w), np.uint8)
+    rc = getattr(lib, fn)(fmt, _p(plane), row_stride, pixel_stride, x0, y0, bin_, _p(lv), ox, oy, w, h, _p(out), w)
+    assert rc == 0
+    return out
 
 
 def lens_fit(lib, fn, span, iw, ih, H, ok, dx, dy):

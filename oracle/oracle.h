@@ -9,6 +9,7 @@
 // itself, compiled from its sources here (oracle/Makefile -> oracle/_ref/), on seeded random channels.
 #ifndef LIZARD_ORACLE_H
 #define LIZARD_ORACLE_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -71,6 +72,13 @@ int orc_anchor_find(int span, const uint8_t *px, int w, int h, const float *H, c
 // The lens model from the anchors about H (liblizard/src/acquire.c:2038-2055 anchor_model, lensm_fit's first round):
 // lens out K, ax, ay, R, then 11 coefficients; 1 where a model fits.
 int orc_lens_fit(int span, int iw, int ih, const float *H, const uint8_t *ok, const float *dx, const float *dy, double *lens);
+
+// Camera-format ingest (liblizard/api/codec.cpp:128-140; liblizard/core/ingest/develop.cpp): a frame's pixels in one of
+// liz_pixfmt's formats to tight luma rows, and the develop of P010 / RAW16 / RAW10 / RAW12 (ImageFormat values).
+int orc_ingest_pixels(const uint8_t *px, int w, int h, int stride, int fmt, uint8_t *out);
+void orc_gamma_lut(uint8_t *t);
+int orc_develop(int fmt, const uint8_t *plane, uint32_t row_stride, uint32_t pixel_stride, uint32_t x0, uint32_t y0, uint32_t bin,
+                const float *levels, uint32_t ox, uint32_t oy, uint32_t w, uint32_t h, uint8_t *out, size_t out_stride);
 
 #ifdef __cplusplus
 }
