@@ -406,8 +406,9 @@ def bench_multistream(args, stream):
 
 
 def bench_ingest(args, stream):
-    """Camera-format ingest to luma on the GPU, 16 frames a call: 3840 x 2160 RGBA8 (liz_decode's conversion), and a
-    3840 x 2160 sensor's RAW10 developed at bin 1 (3840 x 2160 out) and bin 2 (1920 x 1080 out), and P010. Device-timed;
+    """Camera-format ingest to luma on the GPU, 16 frames a call of smooth synthetic scenes with sensor noise: 3840 x 2160
+    RGBA8 (liz_decode's conversion), and a 3840 x 2160 sensor's RAW10 developed at bin 1 (3840 x 2160 out) and bin 2
+    (1920 x 1080 out), and P010. Device-timed;
     GB/s = the frames' bytes read (the whole plane a format's samples occupy) and written over the time; the fraction is
     of the measured HBM copy peak. Beside it the same conversions on the host cores (the oracle's C, a frame a thread)."""
     import concurrent.futures
@@ -418,6 +419,24 @@ def bench_ingest(args, stream):
     frames, W, H = 16, 3840, 2160
     peak, peak_src = peaks()
     rng = np.random.default_rng(77)
+    # smooth scenes, as a camera sees them: gradients and a ripple, sensor noise, 10 bits
+    yy, xx = np.mgrid[0:H, 0:W].astype(np.float32)
+
+    def scene(k):
+        v = 120 + 700 * xx / W + 90 * np.sin(yy / (40.0 + k) + k) + rng.normal(0, 6, (H, W)).astype(np.float32)
+        return np.clip(np.rint(v), 0, 1023).astype(np.uint16)
+
+    def pack(kind, v):
+        if kind is None:   # RGBA8: the scene in three tinted channels
+            g = (v >> 2).astype(np.uint8)
+            return np.stack([g, (g * 0.9).astype(np.uint8), (g * 0.8).astype(np.uint8), np.full_like(g, 255)], -1).reshape(H, -1)
+        if kind == 0:      # P010: ten bits at the top of little-endian 16-bit samples
+            w16 = (v.astype(np.uint16) << 6)
+            return np.stack([(w16 & 255).astype(np.uint8), (w16 >> 8).astype(np.uint8)], -1).reshape(H, -1)
+        g4 = v.reshape(H, W // 4, 4)   # RAW10: four samples' top bytes, then their low bits
+        low = (g4[..., 0] & 3) | ((g4[..., 1] & 3) << 2) | ((g4[..., 2] & 3) << 4) | ((g4[..., 3] & 3) << 6)
+        return np.concatenate([(g4 >> 2).astype(np.uint8), low[..., None].astype(np.uint8)], -1).reshape(H, -1)
+    scenes = [scene(k) for k in range(4)]
     sp = stream.cuda_stream
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     lv = (lz.ctypes.c_float * 9)(64.0, 66.0, 63.0, 65.0, 1023.0, 1.9, 1.0, 1.0, 1.6)
@@ -427,7 +446,8 @@ def bench_ingest(args, stream):
     if not os.path.exists(oracle.PORT_PATH):
         oracle.build(ref=False)
     for name, rowb, rows, w, h, kind in cases:
-        host = rng.integers(0, 256, (frames, rows * rowb), dtype=np.uint8)
+        host = np.stack([pack(kind, scenes[f % 4]).reshape(-1) for f in range(frames)])
+        assert host.shape[1] == rows * rowb
         d_in = torch.from_numpy(host).cuda()
         d_out = torch.zeros((frames, h, w), dtype=torch.uint8, device="cuda")
         if kind is None:
