@@ -26,37 +26,44 @@ constexpr int kRaw16 = 0x20, kRaw10 = 0x25, kRaw12 = 0x26, kP010 = 0x36;
 
 static __device__ __align__(16) uint8_t g_gamma[4112];   // the 4097 steps of gamma 1 / 2.2 (develop.cpp:17-22), made on the host
 
+// ob_luma of one RGBA / RGBX / BGRA pixel word (liblizard/src/acquire.c:67-83).
+template <int FMT>
+__device__ __forceinline__ uint32_t luma_of(uint32_t p) {
+  const uint32_t c0 = p & 255, c1 = (p >> 8) & 255, c2 = (p >> 16) & 255;
+  return FMT == LIZG_PIX_BGRA8 ? (77 * c2 + 150 * c1 + 29 * c0 + 128) >> 8 : (77 * c0 + 150 * c1 + 29 * c2 + 128) >> 8;
+}
+
+// A CTA takes a band of kBand rows, a warp a row, a lane 16 pixels at a time: four 16-byte loads in and one 16-byte
+// store out where both ends are aligned, pixel by pixel elsewhere.
 template <int FMT>
 __global__ void __launch_bounds__(kIngThreads) pixels_kernel(const uint8_t *px, int w, int h, int stride, int64_t fstride, uint8_t *out) {
   const int bands = (h + kBand - 1) / kBand, f = blockIdx.x / bands, y0 = (blockIdx.x % bands) * kBand, y1 = min(h, y0 + kBand);
-  const uint8_t *src = px + f * fstride;
-  uint8_t *dst = out + (int64_t)f * w * h;
-  const int quads = (w + 3) / 4;
-  for (int t = threadIdx.x; t < (y1 - y0) * quads; t += blockDim.x) {
-    const int y = y0 + t / quads, x = 4 * (t % quads);
-    const uint8_t *row = src + (int64_t)y * stride;
-    uint8_t o[4];
-    if (FMT != LIZG_PIX_GREY8 && x + 4 <= w && ((reinterpret_cast<uintptr_t>(row + 4 * x) & 15) == 0)) {
-      // four pixels in one 16-byte load
-      const uint4 q = *reinterpret_cast<const uint4 *>(row + 4 * x);
-      const uint32_t wd[4] = {q.x, q.y, q.z, q.w};
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int bpp = FMT == LIZG_PIX_GREY8 ? 1 : 4;
+  for (int y = y0 + warp; y < y1; y += kIngThreads / 32) {
+    const uint8_t *row = px + f * fstride + (int64_t)y * stride;
+    uint8_t *d = out + ((int64_t)f * h + y) * w;
+    for (int x = 16 * lane; x < w; x += 512) {
+      const uint8_t *src = row + bpp * x;
+      if (x + 16 <= w && ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(d + x)) & 15) == 0) {
+        if (FMT == LIZG_PIX_GREY8) {
+          *reinterpret_cast<uint4 *>(d + x) = *reinterpret_cast<const uint4 *>(src);
+        } else {
+          uint32_t o[4];
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int c0 = wd[k] & 255, c1 = (wd[k] >> 8) & 255, c2 = (wd[k] >> 16) & 255;
-        o[k] = FMT == LIZG_PIX_BGRA8 ? (uint8_t)((77 * c2 + 150 * c1 + 29 * c0 + 128) >> 8) : (uint8_t)((77 * c0 + 150 * c1 + 29 * c2 + 128) >> 8);
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int xx = min(x + k, w - 1);
-        if (FMT == LIZG_PIX_GREY8) o[k] = row[xx];
-        else if (FMT == LIZG_PIX_BGRA8) o[k] = (uint8_t)((77 * row[4 * xx + 2] + 150 * row[4 * xx + 1] + 29 * row[4 * xx] + 128) >> 8);
-        else o[k] = (uint8_t)((77 * row[4 * xx] + 150 * row[4 * xx + 1] + 29 * row[4 * xx + 2] + 128) >> 8);
+          for (int j = 0; j < 4; j++) {
+            const uint4 q = *reinterpret_cast<const uint4 *>(src + 16 * j);
+            o[j] = luma_of<FMT>(q.x) | luma_of<FMT>(q.y) << 8 | luma_of<FMT>(q.z) << 16 | luma_of<FMT>(q.w) << 24;
+          }
+          *reinterpret_cast<uint4 *>(d + x) = make_uint4(o[0], o[1], o[2], o[3]);
+        }
+      } else {
+        for (int k = x; k < min(w, x + 16); k++) {
+          if (FMT == LIZG_PIX_GREY8) d[k] = row[k];
+          else d[k] = (uint8_t)luma_of<FMT>(row[4 * k] | row[4 * k + 1] << 8 | row[4 * k + 2] << 16);
+        }
       }
     }
-    uint8_t *d = dst + (int64_t)y * w + x;
-    if (x + 4 <= w && ((reinterpret_cast<uintptr_t>(d) & 3) == 0)) *reinterpret_cast<uchar4 *>(d) = make_uchar4(o[0], o[1], o[2], o[3]);
-    else for (int k = 0; k < 4 && x + k < w; k++) d[k] = o[k];
   }
 }
 
@@ -153,27 +160,24 @@ __device__ __forceinline__ void put(uint8_t *q, const uint32_t (&o)[NB / 4]) {
   }
 }
 
-// P010: each sample's top byte, straight from the plane (four samples a thread, one 8-byte load where the pixel stride
-// is 2 and the address aligned).
+// P010: each sample's top byte, straight from the plane. A CTA takes a band of kBand rows, a warp a row, a lane 16
+// samples at a time (two 16-byte loads, one 16-byte store where the pixel stride is 2 and both ends aligned).
 __global__ void __launch_bounds__(kIngThreads) p010_kernel(const uint8_t *plane, Develop d, uint8_t *out) {
   const int bands = ((int)d.h + kBand - 1) / kBand, f = blockIdx.x / bands, ya = (blockIdx.x % bands) * kBand, yb = min((int)d.h, ya + kBand);
-  const uint8_t *pl = plane + f * d.pstride;
-  uint8_t *dst = out + (int64_t)f * d.w * d.h;
-  const int quads = ((int)d.w + 3) / 4;
-  for (int t = threadIdx.x; t < (yb - ya) * quads; t += blockDim.x) {
-    const int y = ya + t / quads, x = 4 * (t % quads);
-    const uint8_t *row = pl + (size_t)(d.y0 + d.oy + y) * d.row_stride + (size_t)(d.x0 + d.ox) * d.pixel_stride;
-    uint8_t o[4];
-    if (d.pixel_stride == 2 && x + 4 <= (int)d.w && ((reinterpret_cast<uintptr_t>(row + 2 * x) & 7) == 0)) {
-      const uint2 q = *reinterpret_cast<const uint2 *>(row + 2 * x);
-      o[0] = (q.x >> 8) & 255; o[1] = q.x >> 24; o[2] = (q.y >> 8) & 255; o[3] = q.y >> 24;
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; k++) o[k] = row[(size_t)min(x + k, (int)d.w - 1) * d.pixel_stride + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, w = (int)d.w;
+  for (int y = ya + warp; y < yb; y += kIngThreads / 32) {
+    const uint8_t *row = plane + f * d.pstride + (size_t)(d.y0 + d.oy + y) * d.row_stride + (size_t)(d.x0 + d.ox) * d.pixel_stride;
+    uint8_t *q = out + ((int64_t)f * d.h + y) * w;
+    for (int x = 16 * lane; x < w; x += 512) {
+      const uint8_t *src = row + 2 * x;
+      if (d.pixel_stride == 2 && x + 16 <= w && ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(q + x)) & 15) == 0) {
+        const uint4 a = *reinterpret_cast<const uint4 *>(src), b = *reinterpret_cast<const uint4 *>(src + 16);
+        *reinterpret_cast<uint4 *>(q + x) = make_uint4(__byte_perm(a.x, a.y, 0x7531u), __byte_perm(a.z, a.w, 0x7531u),
+                                                        __byte_perm(b.x, b.y, 0x7531u), __byte_perm(b.z, b.w, 0x7531u));
+      } else {
+        for (int k = x; k < min(w, x + 16); k++) q[k] = row[(size_t)k * d.pixel_stride + 1];
+      }
     }
-    uint8_t *q = dst + (int64_t)y * d.w + x;
-    if (x + 4 <= (int)d.w && ((reinterpret_cast<uintptr_t>(q) & 3) == 0)) *reinterpret_cast<uchar4 *>(q) = make_uchar4(o[0], o[1], o[2], o[3]);
-    else for (int k = 0; k < 4 && x + k < (int)d.w; k++) q[k] = o[k];
   }
 }
 
