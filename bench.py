@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the decoder's default kernel variants")
     ap.add_argument("--batch-only", action="store_true", help="with --receiver-only: only the batched workloads (FFT demod batch, "
                     "anchor search), for profiling")
+    ap.add_argument("--ingest-only", action="store_true", help="time only the camera-format ingest (profiling)")
     return ap.parse_args()
 
 
@@ -622,6 +623,9 @@ def main():
     assert torch.cuda.is_available(), "bench.py needs a CUDA device"
     dev = local
     torch.cuda.set_device(dev)
+    if args.ingest_only:
+        print(json.dumps({"ingest": bench_ingest(args, torch.cuda.current_stream())}))
+        return
     tune = None
     if not args.no_autotune:
         # the decoder's kernel variant per code chosen by timing on this device, before any timed work
