@@ -328,3 +328,174 @@ def distorted_capture(fmt, grey, width, height, H, k1=0.0, blur=0.0, sigma=3.0, 
     nn = layout_nodes(span).size
     reg = np.concatenate([Hp.astype(np.float32), np.zeros(2 * nn * nn, np.float32)])
     return luma, reg
+
+
+# ---------------------------------------------------------------- the border and its format word
+
+CELL_DATA, CELL_LIGHT, CELL_DARK, CELL_WORD = 0, 1, 2, 8
+
+
+def _gf():
+    exp, log = np.zeros(512, np.int64), np.zeros(256, np.int64)
+    x = 1
+    for i in range(255):
+        exp[i], log[x] = x, i
+        x <<= 1
+        if x & 256:
+            x ^= 0x11D
+    exp[255:] = exp[:257]
+    return exp, log
+
+
+_EXP, _LOG = _gf()
+
+
+def _gmul(a, b):
+    return int(_EXP[_LOG[a] + _LOG[b]]) if a and b else 0
+
+
+def rs_encode(data, nroots):
+    """Reed-Solomon parity over GF(256) (polynomial 0x11d, roots alpha^0 .. alpha^(nroots - 1)), systematic, as
+    liblizard/src/rs.c:19-35 computes it: the data bytes then nroots parity bytes."""
+    g = [1] + [0] * nroots
+    for i in range(nroots):
+        for j in range(i + 1, 0, -1):
+            g[j] ^= _gmul(g[j - 1], int(_EXP[i]))
+    par = [0] * nroots
+    for d in data:
+        fb = d ^ par[0]
+        par = par[1:] + [0]
+        if fb:
+            par = [p ^ _gmul(fb, g[j + 1]) for j, p in enumerate(par)]
+    return bytes(list(data) + par)
+
+
+def fmt_geometry(span):
+    """Word cells a side and the codeword's bytes for a ring of span modules (border side span + 30;
+    liblizard/src/fmt.c:6-20, layout.c:66)."""
+    side = span + 30
+    thin = (side - 30) // 2 if side > 30 else 0
+    cells = thin // 8 * 4
+    cells = cells if cells >= 32 else 0
+    return cells, min(64, 4 * (cells // 8))
+
+
+def fmt_word(version, fps, span):
+    """The format word a sender paints (liblizard/src/fmt.c:32-41): magic 0x4c, version, fps, RS parity."""
+    _, nbytes = fmt_geometry(span)
+    return rs_encode([0x4C, version, fps], nbytes - 3)
+
+
+def track_bit(side, j):
+    """Whether track cell j of a side is dark (liblizard/src/layout.c:57-61)."""
+    v = ((side * 4099 + (j >> 1)) * 2654435761 + 40503) & 0xFFFFFFFF
+    v ^= v >> 15
+    v = (v * 2246822519) & 0xFFFFFFFF
+    v ^= v >> 13
+    return (v ^ j) & 1
+
+
+def border_kind(span, cw=None):
+    """The layout's cell kinds, side x side modules (CELL_DATA / LIGHT / DARK, | CELL_WORD on word cells): the corner
+    marks, the line, the timing track and the word's cells (liblizard/src/layout.c:69-141, thin_init, thin_corner,
+    ob_layout_set_fmt). cw: the word's codeword (None: the word cells light)."""
+    side = span + 30
+    S, reserve, margin = 12, 15, 15
+    y, x = np.mgrid[0:side, 0:side]
+    dx, dy = np.minimum(x, side - 1 - x), np.minimum(y, side - 1 - y)
+    d = np.minimum(dx, dy)
+    kind = np.where(d >= margin - 3, CELL_DATA, CELL_LIGHT).astype(np.uint8)
+    kind[(d >= 1) & (d <= 2) & (d < margin - 3)] = CELL_DARK
+    horiz = dy <= dx
+    along = np.where(horiz, x, y)
+    sidev = np.where(horiz, np.where(y < side // 2, 0, 2), np.where(x < side // 2, 3, 1))
+    band = (d >= 5) & (d < 7) & (along >= reserve) & (along < side - reserve)
+    cell = (along - reserve) // 2
+    run = cell // 4
+    for yy, xx in zip(*np.nonzero(band & (run % 2 == 0))):
+        if track_bit(int(sidev[yy, xx]), int(run[yy, xx] // 2 * 4 + cell[yy, xx] % 4)):
+            kind[yy, xx] = CELL_DARK
+    # the corner marks: a solid square, its outer and inner rings light, the gap band light
+    cx, cy = dx, dy
+    corner = (cx < S) & (cy < S)
+    inner = (cx >= 1) & (cx <= S - 2) & (cy >= 1) & (cy <= S - 2)
+    cd = np.minimum(cx, cy)
+    kind[corner] = np.where(inner & ~((cd >= 3) & (cd < 5)), CELL_DARK, CELL_LIGHT)[corner]
+    cells, nbytes = fmt_geometry(span)
+    for s in range(4):
+        for i in range(cells):
+            k = 4 * (i >> 3) + s
+            bit = (cw[k] >> (7 - (i & 7))) & 1 if cw is not None and k < nbytes else 0
+            v = (CELL_DARK if bit else CELL_LIGHT) | CELL_WORD
+            off = ((i // 4) * 8 + i % 4 + 4) * 2
+            for j in range(2):
+                for e in range(2):
+                    t, dd = reserve + off + j, 5 + e
+                    xx = t if s in (0, 2) else (dd if s == 3 else side - 1 - dd)
+                    yy = dd if s == 0 else (side - 1 - dd if s == 2 else t)
+                    kind[yy, xx] = v
+    return kind
+
+
+def border_drive(span, pxm, cw, picture=None):
+    """The symbol's drive in grey levels at pxm pixels a module: the border's dark cells 0, its light cells 255
+    (liblizard/src/lizard_phy.c:1155-1163), the picture (n x n at exact-copy scale) inside when given, else white."""
+    kind = border_kind(span, cw)
+    side = span + 30
+    drive = np.where((kind & 3) == CELL_DARK, 0.0, 255.0).repeat(pxm, 0).repeat(pxm, 1)
+    if picture is not None:
+        n = picture.shape[0]
+        o = 15 * pxm
+        drive[o:o + n, o:o + n] = picture
+    return drive
+
+
+def render_drive(drive, pxm, width, height, H, k1=0.0, blur=0.0, sigma=3.0, rng=None, mid=128, gamma=2.2, glare=None):
+    """A capture of a drive (pxm pixels a module) through the view H (module -> ideal image), radial k1 about the frame
+    centre, blur in linear light, AWGN; glare: (u0, v0, radius, strength) a bright disc added in linear light over
+    part of the frame. Returns luma."""
+    from scipy.ndimage import gaussian_filter
+    px = drive.shape[0]
+    Hi = np.linalg.inv(np.asarray(H, np.float64).reshape(3, 3))
+    V, U = np.mgrid[0:height, 0:width].astype(np.float64)
+    ui, vi = _unradial(U.ravel() + 0.5, V.ravel() + 0.5, width, height, k1)
+    q = Hi @ np.stack([ui, vi, np.ones(ui.size)])
+    sx, sy = q[0] / q[2] * pxm - 0.5, q[1] / q[2] * pxm - 0.5
+    inside = (sx >= 0) & (sy >= 0) & (sx <= px - 1.001) & (sy <= px - 1.001)
+    x0 = np.clip(np.floor(sx).astype(np.int64), 0, px - 2)
+    y0 = np.clip(np.floor(sy).astype(np.int64), 0, px - 2)
+    fx, fy = np.clip(sx - x0, 0, 1), np.clip(sy - y0, 0, 1)
+    val = (drive[y0, x0] * (1 - fx) + drive[y0, x0 + 1] * fx) * (1 - fy) + (drive[y0 + 1, x0] * (1 - fx) + drive[y0 + 1, x0 + 1] * fx) * fy
+    img = np.where(inside, val, float(mid)).reshape(height, width)
+    lin = (img / 255.0) ** gamma
+    if blur > 0:
+        lin = gaussian_filter(lin, blur, mode="nearest")
+    if glare is not None:
+        gu, gv, gr, gs = glare
+        lin = lin + gs * np.exp(-((U - gu) ** 2 + (V - gv) ** 2) / (2.0 * gr * gr))
+    img = 255.0 * np.clip(lin, 0, 1) ** (1.0 / gamma)
+    rng = np.random.default_rng(0) if rng is None else rng
+    return np.clip(np.rint(img + sigma * rng.standard_normal(img.shape)), 0, 255).astype(np.uint8)
+
+
+def word_capture(span, pxm, version, fps, width, height, rng, rot_deg=12.0, tilt=0.0003, scale=(0.85, 1.05), blur=0.0,
+                 sigma=3.0, glare=None, mesh=0.0):
+    """A capture of a symbol's border carrying the format word (version, fps) of a ring of span modules, at pxm pixels
+    a module, under a random view; returns (luma, registration: H then the node mesh's (dx, dy), each node displaced
+    by up to `mesh` pixels, a registration that far off; the codeword)."""
+    side = span + 30
+    cw = fmt_word(version, fps, span)
+    drive = border_drive(span, pxm, cw)
+    th = np.deg2rad(rng.uniform(-rot_deg, rot_deg))
+    s = rng.uniform(*scale) * min(width, height) * 0.9 / side
+    c, sn = np.cos(th) * s, np.sin(th) * s
+    A = np.array([[c, -sn], [sn, c]])
+    ctr = A @ np.array([side / 2.0, side / 2.0])
+    H = np.array([[c, -sn, width / 2.0 - ctr[0]], [sn, c, height / 2.0 - ctr[1]],
+                  [rng.uniform(-tilt, tilt), rng.uniform(-tilt, tilt), 1.0]])
+    luma = render_drive(drive, pxm, width, height, H, blur=blur, sigma=sigma, rng=rng, glare=glare)
+    nn = layout_nodes(span).size
+    reg = np.concatenate([(H / H[2, 2]).astype(np.float32).ravel(), np.zeros(2 * nn * nn, np.float32)])
+    if mesh > 0:
+        reg[9:] = rng.uniform(-mesh, mesh, 2 * nn * nn).astype(np.float32)
+    return luma, reg, cw

@@ -80,6 +80,21 @@ void orc_gamma_lut(uint8_t *t);
 int orc_develop(int fmt, const uint8_t *plane, uint32_t row_stride, uint32_t pixel_stride, uint32_t x0, uint32_t y0, uint32_t bin,
                 const float *levels, uint32_t ox, uint32_t oy, uint32_t w, uint32_t h, uint8_t *out, size_t out_stride);
 
+// ---------------------------------------------------------------- the format word (oracle_fmt.c)
+// Reed-Solomon over GF(256), polynomial 0x11d, roots alpha^0 .. alpha^(nroots - 1) (liblizard/src/rs.c).
+void orc_rs_encode(uint8_t *cw, int k, int nroots);
+int orc_rs_decode(uint8_t *cw, int n, int nroots);
+int orc_rs_decode_er(uint8_t *cw, int n, int nroots, const int *eras, int neras);
+// The word's geometry, encode, cell bits, the track's bits and the soft decode (liblizard/src/fmt.c, layout.c:57-87).
+int orc_fmt_side_cells(int side, int reserve);
+int orc_fmt_bytes(int side, int reserve);
+int orc_fmt_bit(const uint8_t *cw, int bytes, int edge, int cell);
+int orc_fmt_encode(int version, int fps, uint8_t *cw, int bytes);
+int orc_thin_track(int side, int j);
+int orc_fmt_decode(const float *q, int cells, int bytes, int32_t *vf);
+// The word's soft values off a frame through a registration (liblizard/src/acquire.c:4503-4559).
+int orc_fmt_read(int span, const uint8_t *px, int iw, int ih, const float *reg, const float *nodes, int nn, float *q);
+
 #ifdef __cplusplus
 }
 #endif

@@ -204,3 +204,56 @@ int ref_sample_grid(lizard_t *f, const uint8_t *luma, int iw, int ih, const floa
   free(r.nodes);
   return 0;
 }
+
+// ------------------------------------------------------------------ the format word
+
+// The format word's read and decode as acquire_hold runs them (lizard_phy.c:1553-1556), on a frame of a ring of
+// `span` modules through the registration reg (H, then (dx, dy) of the layout's nodes): q (4 x cells soft values),
+// word: read, ok, version, fps. Returns the cells a side (0: the band holds no word).
+int refh_fmt_read(int span, const uint8_t *luma, int iw, int ih, const float *reg, float *q, int32_t *word) {
+  ob_layout_t L;
+  if (ob_layout_init(&L, span + 2 * OB_MARGIN)) return -1;
+  image_t im;
+  ob_image_init(&im, luma, iw, ih, 1.0f);
+  ob_reg_t r;
+  memcpy(r.H.h, reg, 9 * sizeof(float));
+  r.nodes = calloc((size_t)L.nx * L.ny, sizeof(node_t));
+  for (int k = 0; k < L.nx * L.ny; k++) { r.nodes[k].dx = reg[9 + 2 * k]; r.nodes[k].dy = reg[10 + 2 * k]; }
+  const int cells = ob_fmt_side_cells(L.w, L.reserve), bytes = ob_fmt_bytes(L.w, L.reserve);
+  ob_fmt_t ft = {0, 0};
+  word[0] = cells && ob_thin_read_fmt(&L, &im, &r, q, cells);
+  word[1] = word[0] && ob_fmt_decode(q, cells, bytes, &ft) == 0;
+  word[2] = word[1] ? ft.version : 0;
+  word[3] = word[1] ? ft.fps : 0;
+  free(r.nodes);
+  ob_layout_free(&L);
+  return cells;
+}
+
+// ob_fmt_decode on given soft values (fmt.c:54-86), the word's version and fps into vf.
+int refh_fmt_decode(const float *q, int cells, int bytes, int32_t *vf) {
+  ob_fmt_t ft = {0, 0};
+  const int rc = ob_fmt_decode(q, cells, bytes, &ft);
+  vf[0] = ft.version;
+  vf[1] = ft.fps;
+  return rc;
+}
+
+// The layout's word geometry for a ring of `span` modules: cells a side, bytes; and the painted word of a format
+// with sub-channels subch and display rate fps (fmt.c:32-41 through lizard_phy.c fmt_paint).
+int refh_fmt_geometry(int span, int32_t *cells_bytes) {
+  const int side = span + 2 * OB_MARGIN;
+  cells_bytes[0] = ob_fmt_side_cells(side, OB_THIN_RESERVE);
+  cells_bytes[1] = ob_fmt_bytes(side, OB_THIN_RESERVE);
+  return 0;
+}
+int refh_fmt_encode(int version, int fps, uint8_t *cw, int bytes) {
+  const ob_fmt_t ft = {version, fps};
+  return ob_fmt_encode(&ft, cw, bytes);
+}
+// The layout's cell kinds (side x side modules, CELL_* values) of a format with the word for fps painted.
+int refh_layout_kind(lizard_t *f, int fps, uint8_t *kind) {
+  lizard_fmt_fps(f, fps);
+  memcpy(kind, f->frame.kind, (size_t)f->frame.w * f->frame.h);
+  return f->frame.w;
+}
