@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--batch-only", action="store_true", help="with --receiver-only: only the batched workloads (FFT demod batch, "
                     "anchor search), for profiling")
     ap.add_argument("--ingest-only", action="store_true", help="time only the camera-format ingest (profiling)")
+    ap.add_argument("--fmt-only", action="store_true", help="time only the format word's read and decode (profiling)")
     return ap.parse_args()
 
 
@@ -496,6 +497,83 @@ def bench_ingest(args, stream):
     return res
 
 
+def bench_fmt_word(args, stream):
+    """The format word (lizg_fmt_read_dev): its read off the border of a batch of 2048 registered 1280 x 720 frames
+    (the 128 ring's word, RS(32, 3); 32 distinct captures at about 2 pixels a module, rotation up to 12 degrees, blur
+    0.5-1.5 pixels, AWGN, a quarter with glare over a side so that the decode needs erasures) and its decode, one
+    launch. Device-timed with CUDA events; the soft values and words checked identical to the oracle's on every
+    distinct capture; beside it the oracle's read and decode on the host cores, a frame a thread."""
+    import concurrent.futures
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    import oracle
+    span, W, Hh, frames, distinct = 256, 1280, 720, 2048, 32
+    lumas, regs, words = [], [], []
+    for k in range(distinct):
+        rng = np.random.default_rng(900 + k)
+        version, fps = int(rng.integers(4, 65)), int(rng.integers(0, 256))
+        glare = None
+        if k % 4 == 3:
+            glare = (float(rng.choice([W / 2, W - 200, 200])), float(rng.choice([60, Hh - 60, Hh / 2])), 150.0, 3.0)
+        luma, reg, _ = synth.word_capture(span, 2, version, fps, W, Hh, rng, blur=float(rng.uniform(0.5, 1.5)), sigma=3.0, glare=glare)
+        lumas.append(luma)
+        regs.append(reg)
+        words.append((version, fps))
+    cells, _ = synth.fmt_geometry(span)
+    d_l = torch.from_numpy(np.stack([lumas[k % distinct] for k in range(frames)])).cuda()
+    d_r = torch.from_numpy(np.stack([regs[k % distinct] for k in range(frames)])).cuda()
+    d_q = torch.zeros((frames, 4 * cells), dtype=torch.float32, device="cuda")
+    d_w = torch.zeros((frames, 4), dtype=torch.int32, device="cuda")
+    sp = stream.cuda_stream
+
+    def call():
+        lz._check(lz.lib().lizg_fmt_read_dev(span, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W * Hh, lz.ctypes.c_void_p(d_r.data_ptr()), d_r.shape[1],
+                                             frames, lz.ctypes.c_void_p(d_q.data_ptr()), lz.ctypes.c_void_p(d_w.data_ptr()), lz.ctypes.c_void_p(sp)), "fmt_read")
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    reps = max(5, args.steps // 3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    word, q = d_w.cpu().numpy(), d_q.cpu().numpy()
+    if not os.path.exists(oracle.PORT_PATH):
+        oracle.build(ref=False)
+    nodes = synth.layout_nodes(span).astype(np.float32)
+    P = oracle.port()
+    _, nbytes = synth.fmt_geometry(span)
+
+    def host(k):
+        qo = np.zeros(4 * cells, np.float32)
+        got = P.orc_fmt_read(span, oracle._p(lumas[k]), W, Hh, oracle._p(regs[k]), oracle._p(nodes), nodes.size, oracle._p(qo))
+        vf = np.zeros(2, np.int32)
+        ok = bool(got) and P.orc_fmt_decode(oracle._p(qo), cells, nbytes, oracle._p(vf)) == 0
+        return qo, [int(got > 0), int(ok), int(vf[0]) if ok else 0, int(vf[1]) if ok else 0]
+    same = True
+    for k in range(distinct):
+        qo, wo = host(k)
+        same &= list(word[k]) == wo and (not wo[0] or np.array_equal(q[k].view(np.uint32), qo.view(np.uint32)))
+    threads = os.cpu_count() or 1
+    done, t0 = 0, time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        while time.perf_counter() - t0 < 2.0:
+            list(ex.map(host, range(distinct)))
+            done += distinct
+    dt = time.perf_counter() - t0
+    right = sum(int(word[k][1] == 1 and (word[k][2], word[k][3]) == words[k % distinct]) for k in range(frames))
+    return {"workload": "format word read + RS(32,3) soft decode, 2048 registered 1280x720 frames, 128 ring at ~2 px a module, blur 0.5-1.5 px, AWGN 3 DN, a quarter with glare over a side",
+            "frames_per_s": round(frames / (ms / 1e3), 1), "ms_per_call": round(ms, 4), "words_right": right, "frames": frames,
+            "gpu_launches_per_call": 1, "identical_to_oracle": bool(same),
+            "cpu": {"frames_per_s": round(done / dt, 1), "cores": threads, "kind": "port",
+                    "sample": "the 32 distinct frames read and decoded repeatedly for %.1f s, a frame a thread" % dt}}
+
+
 def _render_distorted(job):
     """One distorted capture (a worker of bench_refinement's process pool): job = (index, k1, blur)."""
     import numpy as np
@@ -626,6 +704,9 @@ def main():
     if args.ingest_only:
         print(json.dumps({"ingest": bench_ingest(args, torch.cuda.current_stream())}))
         return
+    if args.fmt_only:
+        print(json.dumps({"format_word": bench_fmt_word(args, torch.cuda.current_stream())}))
+        return
     tune = None
     if not args.no_autotune:
         # the decoder's kernel variant per code chosen by timing on this device, before any timed work
@@ -638,7 +719,8 @@ def main():
         st = torch.cuda.current_stream()
         rec = bench_receiver(args, st)
         rec["multistream"] = bench_multistream(args, st)
-        print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st)},
+        print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st),
+                                                            "format_word": bench_fmt_word(args, st)},
                           "ingest": bench_ingest(args, st)}))
         return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
@@ -730,7 +812,8 @@ def main():
         out["e2e"] = e2e
     if not args.no_receiver:
         out["receiver"] = bench_receiver(args, stream)
-        out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream)}
+        out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream),
+                               "format_word": bench_fmt_word(args, stream)}
         out["ingest"] = bench_ingest(args, stream)
         out["receiver"]["multistream"] = bench_multistream(args, stream)
     if ws == 1 and not args.no_cpu_baseline:

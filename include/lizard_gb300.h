@@ -247,6 +247,23 @@ typedef struct {
 int lizg_develop_dev(const lizg_raw_frame *r, const uint8_t *d_plane, int64_t plane_bytes, int64_t plane_stride, int frames, uint32_t ox,
                      uint32_t oy, uint32_t w, uint32_t h, uint8_t *d_out, void *stream);
 
+// ---------------------------------------------------------------- format word
+//
+// Replaces the read of the format word when a registration is held (liblizard/src/lizard_phy.c:1553-1556:
+// ob_thin_read_fmt, liblizard/src/acquire.c:4503-4559, then ob_fmt_decode, liblizard/src/fmt.c:54-86) for a batch of
+// registered frames, so that a batch can learn each frame's version on the device. Soft values and words are the
+// reference's bit for bit.
+// The word's cells a side and codeword bytes in a ring of span modules (128, 256, 512: 32 / 16, 64 / 32, 128 / 64).
+int lizg_fmt_geometry(int span, int32_t *cells, int32_t *bytes);
+// frames x (w x h luma, rows w apart) at d_luma + f frame_stride; d_reg: frames x reg_stride floats, H (9) then
+// (dx, dy) of the layout's nodes, as the receiver takes it. Out: d_q (NULL, or frames x 4 cells soft values,
+// side * cells + cell, > 0 dark; 0 where the band was not read) and d_word (frames x 4: read, ok, version, fps).
+int lizg_fmt_read_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_reg, int reg_stride, int frames,
+                      float *d_q, int32_t *d_word, void *stream);
+// ob_fmt_decode alone on soft values read elsewhere (lizard_fmt_check, lizard_phy.c:1881-1889): frames x 4 cells in,
+// frames x 4 (1, ok, version, fps) out.
+int lizg_fmt_decode_dev(int span, const float *d_q, int frames, int32_t *d_word, void *stream);
+
 // ---------------------------------------------------------------- registration assist: refinement from the anchors
 //
 // For frames registered by a homography alone (a finder's four corners), the lens the camera adds, found from the

@@ -218,6 +218,9 @@ def _rx_sigs(L):
     L.lizg_refiner_new.restype = P
     L.lizg_refiner_free.argtypes = [P]
     L.lizg_refine_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
+    L.lizg_fmt_geometry.argtypes = [I, P, P]
+    L.lizg_fmt_read_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
+    L.lizg_fmt_decode_dev.argtypes = [I, P, I, P, P]
 
 
 class RxOut(ctypes.Structure):
@@ -388,6 +391,49 @@ def anchor_find(span, luma, H, lens=None, skip=None, stream=None):
            "lizg_anchor_find_dev")
     torch.cuda.synchronize()
     return {k: v.cpu().numpy() for k, v in o.items()}
+
+
+def fmt_geometry(span):
+    """(cells a side, codeword bytes) of the format word in a ring of span modules."""
+    c, b = ctypes.c_int32(), ctypes.c_int32()
+    _check(lib().lizg_fmt_geometry(span, ctypes.byref(c), ctypes.byref(b)), "lizg_fmt_geometry")
+    return c.value, b.value
+
+
+def fmt_read(span, luma, regs, stream=None):
+    """The format word read and decoded on the GPU for a batch of registered frames: luma frames x h x w uint8, regs
+    frames x (9 + 2 nodes) float32 (H then the mesh). Returns (q frames x 4 cells soft values, word frames x 4:
+    read, ok, version, fps)."""
+    import torch
+    lu = np.ascontiguousarray(luma, np.uint8)
+    if lu.ndim == 2:
+        lu = lu[None]
+    frames, h, w = lu.shape
+    rg = np.ascontiguousarray(np.asarray(regs, np.float32).reshape(frames, -1))
+    cells, _ = fmt_geometry(span)
+    d_l, d_r = torch.from_numpy(lu).cuda(), torch.from_numpy(rg).cuda()
+    d_q = torch.zeros((frames, 4 * cells), dtype=torch.float32, device="cuda")
+    d_w = torch.zeros((frames, 4), dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+    _check(lib().lizg_fmt_read_dev(span, ctypes.c_void_p(d_l.data_ptr()), w, h, h * w, ctypes.c_void_p(d_r.data_ptr()), rg.shape[1], frames,
+                                   ctypes.c_void_p(d_q.data_ptr()), ctypes.c_void_p(d_w.data_ptr()), ctypes.c_void_p(st)), "lizg_fmt_read_dev")
+    torch.cuda.synchronize()
+    return d_q.cpu().numpy(), d_w.cpu().numpy()
+
+
+def fmt_decode(span, q, stream=None):
+    """The format word's soft decode alone on the GPU: q frames x 4 cells. Returns frames x 4 (1, ok, version, fps)."""
+    import torch
+    qq = np.ascontiguousarray(np.asarray(q, np.float32))
+    if qq.ndim == 1:
+        qq = qq[None]
+    d_q = torch.from_numpy(qq).cuda()
+    d_w = torch.zeros((qq.shape[0], 4), dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+    _check(lib().lizg_fmt_decode_dev(span, ctypes.c_void_p(d_q.data_ptr()), qq.shape[0], ctypes.c_void_p(d_w.data_ptr()), ctypes.c_void_p(st)),
+           "lizg_fmt_decode_dev")
+    torch.cuda.synchronize()
+    return d_w.cpu().numpy()
 
 
 class EngineBatch(ctypes.Structure):

@@ -69,6 +69,21 @@ def test_bad_arguments_are_errors():
         lz.ldpc_set_variant(6, 99)
     with pytest.raises(lz.LizgError):
         lz.ldpc_autotune(0)
+    with pytest.raises(lz.LizgError):
+        lz.fmt_geometry(200)
+    P = ctypes.c_void_p(8)
+    assert lz.lib().lizg_fmt_read_dev(300, P, 64, 64, 4096, P, 4000, 1, None, P, None) == -1
+    assert lz.lib().lizg_fmt_read_dev(256, P, 64, 64, 4096, P, 20, 1, None, P, None) == -1   # reg_stride short
+    assert lz.lib().lizg_fmt_read_dev(256, P, 1, 64, 4096, P, 4000, 1, None, P, None) == -1    # frame under 2 x 2
+    assert lz.lib().lizg_fmt_decode_dev(128, None, 1, P, None) == -1
+
+
+def test_fmt_geometry_matches_oracle():
+    """The format word's cells and bytes a ring, as the reference's fmt.c computes them (through the oracle)."""
+    import oracle
+    for span in (128, 256, 512):
+        side = span + 30
+        assert lz.fmt_geometry(span) == (oracle.port().orc_fmt_side_cells(side, 15), oracle.port().orc_fmt_bytes(side, 15))
 
 
 def test_decoder_variants_listed():
