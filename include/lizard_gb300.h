@@ -247,6 +247,27 @@ typedef struct {
 int lizg_develop_dev(const lizg_raw_frame *r, const uint8_t *d_plane, int64_t plane_bytes, int64_t plane_stride, int frames, uint32_t ox,
                      uint32_t oy, uint32_t w, uint32_t h, uint8_t *d_out, void *stream);
 
+// ---------------------------------------------------------------- the sender (GPU encoder)
+//
+// Replaces the sender's lizard_encode + lizard_paint_grey (liblizard/src/lizard_phy.c:1087-1236, 700-716; with
+// lizard_parity and lizard_fmt_fps, :446-450, 478-481) for a batch of frames: blocks to the ring's drive and its grey
+// page. The transform's floats are this library's, so a drive value may differ from the reference's in its last
+// bits and a grey level by one at a rounding tie; every block reads back the same.
+typedef struct lizg_encoder lizg_encoder;
+// The format (n, subch, span as lizg_rx_new takes them) and the most frames a call.
+lizg_encoder *lizg_encoder_new(int n, int subch, int span, int max_frames);
+void lizg_encoder_free(lizg_encoder *e);
+// The display rate the format word states (lizard_fmt_fps): 0..255, 0 none (the default).
+int lizg_encoder_fps(lizg_encoder *e, int fps);
+// blocks, pxm (pixels a module), px (the drive's side), W (the page's side, px + 4 pxm), max_frames.
+int lizg_encoder_info(const lizg_encoder *e, int32_t *out);
+// d_blocks: frames x blocks x 476 bytes. pilots: the painted count's two bits (lizard_parity, 0..3). Out (either may be
+// NULL, not both): d_drive frames x px x px floats in 0..1, d_grey frames x W x W bytes.
+int lizg_encode_dev(lizg_encoder *e, const uint8_t *d_blocks, int frames, int pilots, float *d_drive, uint8_t *d_grey, void *stream);
+// The border's cell kinds of a ring of span modules with the format word (version, fps) painted: (span + 30)^2 bytes,
+// 2 dark, 1 light, 0 the picture's (liblizard/src/layout.c:69-141). Host only. Returns the side.
+int lizg_layout_kind(int span, int version, int fps, uint8_t *kind);
+
 // ---------------------------------------------------------------- format word
 //
 // Replaces the read of the format word when a registration is held (liblizard/src/lizard_phy.c:1553-1556:

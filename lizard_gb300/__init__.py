@@ -218,6 +218,13 @@ def _rx_sigs(L):
     L.lizg_refiner_new.restype = P
     L.lizg_refiner_free.argtypes = [P]
     L.lizg_refine_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
+    L.lizg_encoder_new.argtypes = [I, I, I, I]
+    L.lizg_encoder_new.restype = P
+    L.lizg_encoder_free.argtypes = [P]
+    L.lizg_encoder_fps.argtypes = [P, I]
+    L.lizg_encoder_info.argtypes = [P, P]
+    L.lizg_encode_dev.argtypes = [P, P, I, I, P, P, P]
+    L.lizg_layout_kind.argtypes = [I, I, I, P]
     L.lizg_fmt_geometry.argtypes = [I, P, P]
     L.lizg_fmt_read_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
     L.lizg_fmt_decode_dev.argtypes = [I, P, I, P, P]
@@ -391,6 +398,51 @@ def anchor_find(span, luma, H, lens=None, skip=None, stream=None):
            "lizg_anchor_find_dev")
     torch.cuda.synchronize()
     return {k: v.cpu().numpy() for k, v in o.items()}
+
+
+class Encoder:
+    """The sender on the GPU (lizg_encoder_*): blocks (frames x blocks x 476 bytes) to the drive (frames x px x px
+    floats) and the grey page (frames x W x W)."""
+
+    def __init__(self, n, subch, span, max_frames=8):
+        self._h = lib().lizg_encoder_new(n, subch, span, max_frames)
+        if not self._h:
+            raise LizgError("lizg_encoder_new: " + lib().lizg_last_error().decode())
+        info = np.zeros(5, np.int32)
+        _check(lib().lizg_encoder_info(self._h, _ptr(info)), "lizg_encoder_info")
+        self.blocks, self.pxm, self.px, self.W, self.max_frames = (int(v) for v in info)
+
+    def set_fps(self, fps):
+        _check(lib().lizg_encoder_fps(self._h, fps), "lizg_encoder_fps")
+
+    def encode(self, blocks, pilots=0, drive=True, stream=None):
+        """blocks: frames x blocks x 476 uint8. Returns (drive or None, grey)."""
+        import torch
+        b = np.ascontiguousarray(blocks, np.uint8).reshape(-1, self.blocks, BLOCK_BYTES)
+        frames = b.shape[0]
+        d_b = torch.from_numpy(b).cuda()
+        d_g = torch.zeros((frames, self.W, self.W), dtype=torch.uint8, device="cuda")
+        d_d = torch.zeros((frames, self.px, self.px), dtype=torch.float32, device="cuda") if drive else None
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_encode_dev(self._h, ctypes.c_void_p(d_b.data_ptr()), frames, pilots,
+                                     None if d_d is None else ctypes.c_void_p(d_d.data_ptr()), ctypes.c_void_p(d_g.data_ptr()), ctypes.c_void_p(st)),
+               "lizg_encode_dev")
+        torch.cuda.synchronize()
+        return (None if d_d is None else d_d.cpu().numpy()), d_g.cpu().numpy()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().lizg_encoder_free(self._h)
+            self._h = None
+
+
+def layout_kind(span, version, fps):
+    """The border's cell kinds, (span + 30)^2 (2 dark, 1 light, 0 the picture's), with the word (version, fps)."""
+    side = span + 30
+    k = np.zeros(side * side, np.uint8)
+    rc = lib().lizg_layout_kind(span, version, fps, _ptr(k))
+    _check(rc if rc < 0 else 0, "lizg_layout_kind")
+    return k.reshape(side, side)
 
 
 def fmt_geometry(span):

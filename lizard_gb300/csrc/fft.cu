@@ -493,6 +493,105 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- the sender's inverse (liblizard/src/lizard_phy.c:1134-1199)
+
+// The half-plane spectrum's rows (v < vrows, each along u) inverse-transformed in place: S[v][x] = sum_u S[v][u]
+// e^{+2 pi i u x / n}, as the conjugate of the forward transform of the conjugate. L rows a CTA.
+template <int N>
+__global__ void __launch_bounds__(kThreads, 2) enc_cols_kernel(EncFft e, float2 *S) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int L = plan_of(N).lines, LSTR = lstride_of(N);
+  float2 *buf = reinterpret_cast<float2 *>(smraw), *tw = buf + L * LSTR;
+  const int tiles = (e.vrows + L - 1) / L, f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, e.vrows - v0);
+  for (int i = threadIdx.x; i < N; i += kThreads) tw[i] = e.tws[i];
+  float2 *rows = S + ((int64_t)f * e.vrows + v0) * N;
+  for (int t = threadIdx.x; t < Lr * N; t += kThreads) {
+    const int l = t / N, p = t - l * N;
+    const float2 z = rows[(int64_t)l * N + p];
+    buf[l * LSTR + pad(p)] = make_float2(z.x, -z.y);
+  }
+  __syncthreads();
+  fft_lines<N>(buf, tw, Lr);
+  for (int t = threadIdx.x; t < Lr * N; t += kThreads) {
+    const int l = t / N, p = t - l * N;
+    const float2 z = buf[l * LSTR + pad(p)];
+    rows[(int64_t)l * N + p] = make_float2(z.x, -z.y);
+  }
+}
+
+// The picture's columns: 2L of them a CTA, columns xa = x0 + l and xb = x0 + L + l sharing line l as H_a + i H_b, each
+// H the column's Hermitian completion over v (H(0) = 2 Re T(0), H(v) = T(v), H(n - v) = conj T(v) for 0 < v < vrows,
+// zero between), inverse-transformed along v: the real part column xa, the imaginary part column xb
+// (liblizard/src/lizard_phy.c:733-773 turn_pack). Then clipped at +-lim and mapped to 0.5 + v sc (clip_row, :775-782),
+// into pic[y][x].
+template <int N>
+__global__ void __launch_bounds__(kThreads, 2) enc_rows_kernel(EncFft e, const float2 *T, float *pic) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int L = plan_of(N).lines, LSTR = lstride_of(N), tiles = N / (2 * L);
+  float2 *buf = reinterpret_cast<float2 *>(smraw), *tw = buf + L * LSTR;
+  const int f = blockIdx.x / tiles, x0 = (blockIdx.x % tiles) * 2 * L;
+  for (int i = threadIdx.x; i < N; i += kThreads) tw[i] = e.tws[i];
+  const float2 *Tf = T + (int64_t)f * e.vrows * N;
+  for (int t = threadIdx.x; t < L * N; t += kThreads) {   // l fastest: a row's 2L columns read together
+    const int v = t / L, l = t - v * L;
+    float2 z = make_float2(0.0f, 0.0f);
+    if (v == 0) {
+      const float2 a = Tf[x0 + l], b = Tf[x0 + L + l];
+      z = make_float2(2.0f * a.x, 2.0f * b.x);
+    } else if (v < e.vrows) {
+      const float2 a = Tf[(int64_t)v * N + x0 + l], b = Tf[(int64_t)v * N + x0 + L + l];
+      z = make_float2(a.x - b.y, a.y + b.x);
+    } else if (v > N - e.vrows) {
+      const int m = N - v;
+      const float2 a = Tf[(int64_t)m * N + x0 + l], b = Tf[(int64_t)m * N + x0 + L + l];
+      z = make_float2(a.x + b.y, b.x - a.y);
+    }
+    buf[l * LSTR + pad(v)] = make_float2(z.x, -z.y);
+  }
+  __syncthreads();
+  fft_lines<N>(buf, tw, L);
+  float *pf = pic + (int64_t)f * N * N;
+  for (int t = threadIdx.x; t < L * N; t += kThreads) {
+    const int y = t / L, l = t - y * L;
+    const float2 z = buf[l * LSTR + pad(y)];
+    float a = z.x, b = -z.y;
+    a = a > e.lim ? e.lim : a;
+    a = a < -e.lim ? -e.lim : a;
+    b = b > e.lim ? e.lim : b;
+    b = b < -e.lim ? -e.lim : b;
+    pf[(int64_t)y * N + x0 + l] = __fadd_rn(0.5f, __fmul_rn(a, e.sc));   // rounded as clip_row rounds, unfused
+    pf[(int64_t)y * N + x0 + L + l] = __fadd_rn(0.5f, __fmul_rn(b, e.sc));
+  }
+}
+
+template <int N>
+static cudaError_t enc_fft_launch_n(const EncFft &e, int frames, float2 *S, float *pic, cudaStream_t st) {
+  constexpr int L = plan_of(N).lines, smem = (L * lstride_of(N) + N) * (int)sizeof(float2);
+  static bool attr = false;
+  cudaError_t err;
+  if (!attr) {
+    if ((err = cudaFuncSetAttribute(enc_cols_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return err;
+    if ((err = cudaFuncSetAttribute(enc_rows_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return err;
+    attr = true;
+  }
+  enc_cols_kernel<N><<<frames * ((e.vrows + L - 1) / L), kThreads, smem, st>>>(e, S);
+  enc_rows_kernel<N><<<frames * (N / (2 * L)), kThreads, smem, st>>>(e, S, pic);
+  return cudaGetLastError();
+}
+
+cudaError_t enc_fft_launch(const EncFft &e, int frames, float2 *S, float *pic, cudaStream_t st) {
+  switch (e.n) {
+    case 384: return enc_fft_launch_n<384>(e, frames, S, pic, st);
+    case 512: return enc_fft_launch_n<512>(e, frames, S, pic, st);
+    case 768: return enc_fft_launch_n<768>(e, frames, S, pic, st);
+    case 1024: return enc_fft_launch_n<1024>(e, frames, S, pic, st);
+    case 1152: return enc_fft_launch_n<1152>(e, frames, S, pic, st);
+    case 1280: return enc_fft_launch_n<1280>(e, frames, S, pic, st);
+    case 1536: return enc_fft_launch_n<1536>(e, frames, S, pic, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st) {
   switch (xd.n) {
     case 384: return fft_launch_n<384>(xd, frames, src, b, sms, st);

@@ -112,6 +112,14 @@ cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stri
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
 cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st);
 // The transform plan of picture size n (three passes' radices, lines a CTA): 0, or -1 for a size off the ladder.
+// The sender's inverse transform: the half-plane spectrum S (frames x vrows x n, rows along u, overwritten) to the
+// clipped picture pic (frames x n x n, 0.5 + clamp(P, +-lim) sc). tws: the transform's twiddles.
+struct EncFft {
+  int n, vrows;
+  const float2 *tws;
+  float lim, sc;
+};
+cudaError_t enc_fft_launch(const EncFft &e, int frames, float2 *S, float *pic, cudaStream_t st);
 int fft_plan(int n, int radix[3], int *lines);
 // The shading fit's bands a frame.
 int fft_hole_bands(int n);

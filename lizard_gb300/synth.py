@@ -499,3 +499,100 @@ def word_capture(span, pxm, version, fps, width, height, rng, rot_deg=12.0, tilt
     if mesh > 0:
         reg[9:] = rng.uniform(-mesh, mesh, 2 * nn * nn).astype(np.float32)
     return luma, reg, cw
+
+
+# ---------------------------------------------------------------- the sender's drive
+
+def pxm_for(n, span):
+    """Whole pixels a module the ring is painted at (liblizard/src/lizard_phy.c:1497-1501)."""
+    return int(np.ceil(np.float32(n) / np.float32(span) - np.float32(1e-4)))
+
+
+def _lanczos3(x):
+    x = abs(x)
+    if x >= 3:
+        return 0.0
+    px = np.pi * x
+    return 3 * np.sin(px) * np.sin(px / 3) / (px * px)
+
+
+def resample_taps(n, span, pxm, cp=3):
+    """The Lanczos-3 resampler's taps from the picture's n samples to the ring's pixels (liblizard/src/lizard_phy.c:
+    962-1025 resample_init): for each of q = (span + 2 cp) pxm pixels its first tap i0 and six float weights."""
+    q = (span + 2 * cp) * pxm
+    sc = n / span
+    i0 = np.zeros(q, np.int64)
+    w = np.zeros((q, 6), np.float32)
+    for x in range(q):
+        u = (x + 0.5) * sc / pxm - cp * sc - 0.5
+        r = np.floor(u + 0.5)
+        if abs(u - r) < 1e-6:
+            i0[x] = int(r) - 2
+            w[x, 2] = 1.0
+            continue
+        a = int(np.floor(u)) - 2
+        tw = np.array([_lanczos3(u - (a + t)) for t in range(6)])
+        i0[x] = a
+        w[x] = (tw / tw.sum()).astype(np.float32)
+    return i0, w
+
+
+def picture_float(fmt, block_rows, parity=0):
+    """The picture before painting, n x n floats in 0..1 (liblizard/src/lizard_phy.c:1134-1199): the QPSK spectrum's
+    Hermitian inverse in double, clipped and mapped as the sender does in float."""
+    n = fmt.n
+    sb = slots(fmt, block_rows, parity)
+    a = np.float32(0.70710678)
+    sym = np.where(sb[0::2], -a, a).astype(np.float64) + 1j * np.where(sb[1::2], -a, a).astype(np.float64)
+    S = np.zeros((n, n), np.complex128)
+    u, v = fmt.uv[0::2].astype(np.int64), fmt.uv[1::2].astype(np.int64)
+    S[v, (u + n) % n] = sym
+    z = 2.0 * np.real(np.fft.ifft2(S)) * (n * n)
+    lim = np.float32(2.0 * 2.0 * np.sqrt(np.float32(0.5 * fmt.subch * SUB)))
+    sc = np.float32(0.5) / lim
+    return (np.float32(0.5) + np.clip(z.astype(np.float32), -lim, lim) * sc).astype(np.float32)
+
+
+def encode_drive(fmt, block_rows, parity=0, fps=0):
+    """The sender's drive and its grey page (liblizard/src/lizard_phy.c:1087-1236 lizard_encode, :700-716
+    lizard_paint_grey): the border's cells 0 or 1 at pxm pixels a module (its format word for version subch / 16 at
+    fps), the picture resampled onto the ring's pixels over the picture and its 3-module guard (the picture periodic),
+    each pass six weights in order, clamped to 0..1; the anchors' squares over it; then round(drive 255) inside a
+    2-module white margin. Returns (drive px x px float32, grey W x W uint8)."""
+    n, span = fmt.n, fmt.span
+    pxm = pxm_for(n, span)
+    side = span + 30
+    px = side * pxm
+    cp = 3
+    pic = picture_float(fmt, block_rows, parity)
+    kind = border_kind(span, fmt_word(fmt.subch // 16, fps, span) if fmt.subch % 16 == 0 else None)
+    drive = np.where((kind & 3) == CELL_DARK, 0.0, 1.0).astype(np.float32).repeat(pxm, 0).repeat(pxm, 1)
+    i0, w = resample_taps(n, span, pxm, cp)
+    q, o = i0.size, (15 - cp) * pxm
+    rows = (i0[:, None] + np.arange(6)[None, :]) % n            # q x 6 picture rows
+    tmp = np.zeros((q, n), np.float32)
+    for t in range(6):
+        tmp = (tmp + w[:, t:t + 1] * pic[rows[:, t]]).astype(np.float32) if t else (w[:, 0:1] * pic[rows[:, 0]]).astype(np.float32)
+    cols = (i0[:, None] + np.arange(6)[None, :]) % n            # q x 6 picture columns
+    out = np.zeros((q, q), np.float32)
+    for t in range(6):
+        term = (tmp[:, cols[:, t]] * w[None, :, t]).astype(np.float32)
+        out = (out + term).astype(np.float32) if t else term
+    drive[o:o + q, o:o + q] = np.clip(out, 0, 1)
+    a = span // 64
+    sidep = a * pxm
+    half = np.float32(0.5 * sidep)
+    ii = np.arange(sidep, dtype=np.float32) + np.float32(0.5) - half
+    dd = np.maximum(np.abs(ii)[None, :], np.abs(ii)[:, None]) / half
+    pat = np.where((dd < 0.25) | (dd >= 0.6), 1.0, 0.0).astype(np.float32)
+    for j in range(7):
+        for i in range(7):
+            x0 = int(np.floor(15 + span * (i + 0.5) / 7 - a / 2.0 + 0.5)) * pxm
+            y0 = int(np.floor(15 + span * (j + 0.5) / 7 - a / 2.0 + 0.5)) * pxm
+            drive[y0:y0 + sidep, x0:x0 + sidep] = pat
+    m = 2 * pxm
+    W = px + 2 * m
+    grey = np.full((W, W), 255, np.uint8)
+    t = drive.astype(np.float32) * np.float32(255.0) + np.float32(0.5)
+    grey[m:m + px, m:m + px] = np.clip(np.floor(t), 0, 255).astype(np.uint8)
+    return drive, grey
