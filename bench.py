@@ -46,6 +46,7 @@ def parse():
                     "anchor search), for profiling")
     ap.add_argument("--ingest-only", action="store_true", help="time only the camera-format ingest (profiling)")
     ap.add_argument("--fmt-only", action="store_true", help="time only the format word's read and decode (profiling)")
+    ap.add_argument("--encode-only", action="store_true", help="time only the sender on the GPU (profiling)")
     return ap.parse_args()
 
 
@@ -574,6 +575,50 @@ def bench_fmt_word(args, stream):
                     "sample": "the 32 distinct frames read and decoded repeatedly for %.1f s, a frame a thread" % dt}}
 
 
+def bench_encoder(args, stream):
+    """The sender on the GPU (lizg_encode_dev): seeded blocks to the ring's grey page, a batch a call: LIZARD-1024
+    (n = 1536) in the 128 ring (1740 x 1740 pages, 6 pixels a module) and LIZARD-64 (n = 384) in the 64 ring (486 x 486).
+    Device-timed with CUDA events; the first page of each checked against the oracle (the numpy restatement of the
+    reference's lizard_encode, grey levels within one at rounding ties); beside it the oracle on one host core."""
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    res = {}
+    for name, (n, subch, span, frames) in (("lizard1024_128ring", (1536, 1024, 256, 32)), ("lizard64_64ring", (384, 64, 128, 256))):
+        fmt = lz.Format(n, subch, span)
+        enc = lz.Encoder(n, subch, span, max_frames=frames)
+        blocks = np.stack([synth.random_blocks(fmt.blocks, 700 + k) for k in range(frames)])
+        d_b = torch.from_numpy(blocks).cuda()
+        d_g = torch.zeros((frames, enc.W, enc.W), dtype=torch.uint8, device="cuda")
+        sp = stream.cuda_stream
+
+        def call():
+            lz._check(lz.lib().lizg_encode_dev(enc._h, lz.ctypes.c_void_p(d_b.data_ptr()), frames, 1, None, lz.ctypes.c_void_p(d_g.data_ptr()),
+                                               lz.ctypes.c_void_p(sp)), "encode")
+        for _ in range(3):
+            call()
+        torch.cuda.synchronize()
+        reps = max(5, args.steps // 3)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        t0 = time.perf_counter()
+        _, g = synth.encode_drive(fmt, blocks[0], parity=1)
+        dt = time.perf_counter() - t0
+        diff = d_g[0].cpu().numpy().astype(int) - g.astype(int)
+        res[name] = {"frames_per_s": round(frames / (ms / 1e3), 1), "ms_per_call": round(ms, 4), "frames": frames, "page": [enc.W, enc.W],
+                     "page_GBps": round(frames * enc.W * enc.W / (ms / 1e3) / 1e9, 2), "blocks_per_frame": fmt.blocks,
+                     "within_one_of_oracle": bool(np.abs(diff).max() <= 1), "grey_off_by_one": int(np.count_nonzero(diff)),
+                     "gpu_launches_per_call": 6, "cpu": {"frames_per_s": round(1 / dt, 2), "cores": 1, "kind": "port",
+                                                          "sample": "one page by the numpy oracle (FP64 transform), one core"}}
+    return res
+
+
 def _render_distorted(job):
     """One distorted capture (a worker of bench_refinement's process pool): job = (index, k1, blur)."""
     import numpy as np
@@ -707,6 +752,9 @@ def main():
     if args.fmt_only:
         print(json.dumps({"format_word": bench_fmt_word(args, torch.cuda.current_stream())}))
         return
+    if args.encode_only:
+        print(json.dumps({"sender": bench_encoder(args, torch.cuda.current_stream())}))
+        return
     tune = None
     if not args.no_autotune:
         # the decoder's kernel variant per code chosen by timing on this device, before any timed work
@@ -720,7 +768,7 @@ def main():
         rec = bench_receiver(args, st)
         rec["multistream"] = bench_multistream(args, st)
         print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st),
-                                                            "format_word": bench_fmt_word(args, st)},
+                                                            "format_word": bench_fmt_word(args, st)}, "sender": bench_encoder(args, st),
                           "ingest": bench_ingest(args, st)}))
         return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
@@ -814,6 +862,7 @@ def main():
         out["receiver"] = bench_receiver(args, stream)
         out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream),
                                "format_word": bench_fmt_word(args, stream)}
+        out["sender"] = bench_encoder(args, stream)
         out["ingest"] = bench_ingest(args, stream)
         out["receiver"]["multistream"] = bench_multistream(args, stream)
     if ws == 1 and not args.no_cpu_baseline:
