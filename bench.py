@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--batch-only", action="store_true", help="with --receiver-only: only the batched workloads (FFT demod batch, "
                     "anchor search), for profiling")
     ap.add_argument("--ingest-only", action="store_true", help="time only the camera-format ingest (profiling)")
-    ap.add_argument("--fmt-only", action="store_true", help="time only the format word's read and decode (profiling)")
+    ap.add_argument("--fmt-only", action="store_true", help="time only the format word and the border nodes (profiling)")
     ap.add_argument("--encode-only", action="store_true", help="time only the sender on the GPU (profiling)")
     return ap.parse_args()
 
@@ -498,6 +498,77 @@ def bench_ingest(args, stream):
     return res
 
 
+def bench_border_nodes(args, stream):
+    """The registration's border nodes (lizg_border_nodes_dev): refine_node over the border lattice of 64 captured
+    1920 x 1080 frames (8 distinct), each LIZARD-1024 (n = 1536) in the 128 ring at about 2.6 pixels a module, rotated
+    up to 15 degrees, H put up to a pixel off. Device-timed with CUDA events; every distinct frame's nodes checked
+    identical to the oracle's (the reference's portable build, restated); beside it the oracle on the host cores, a
+    frame a thread."""
+    import concurrent.futures
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    import oracle
+    span, n, subch, W, Hh, frames, distinct = 256, 1536, 1024, 1920, 1080, 64, 8
+    fmt = lz.Format(n, subch, span)
+    nn = synth.layout_nodes(span).size
+    lumas, Hs = [], []
+    for k in range(distinct):
+        rng = np.random.default_rng(800 + k)
+        grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 800 + k), parity=k & 3)
+        pxm = synth.pxm_for(n, span)
+        drive = synth.border_drive(span, pxm, synth.fmt_word(subch // 16, 0, span), picture=grey)
+        Hw = np.asarray(synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.42, 0.45)), np.float64).reshape(3, 3)
+        luma = synth.render_drive(drive, pxm, W, Hh, Hw, sigma=3.0, rng=rng)
+        H = (Hw / Hw[2, 2]).astype(np.float32).ravel()
+        H[2] += np.float32(rng.uniform(-1, 1))
+        H[5] += np.float32(rng.uniform(-1, 1))
+        lumas.append(luma)
+        Hs.append(H)
+    d_l = torch.from_numpy(np.stack([lumas[k % distinct] for k in range(frames)])).cuda()
+    d_h = torch.from_numpy(np.stack([Hs[k % distinct] for k in range(frames)])).cuda()
+    d_n = torch.zeros((frames, nn, nn, 4), dtype=torch.float32, device="cuda")
+    sp = stream.cuda_stream
+
+    def call():
+        lz._check(lz.lib().lizg_border_nodes_dev(span, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W * Hh, lz.ctypes.c_void_p(d_h.data_ptr()), 9,
+                                                 None, frames, lz.ctypes.c_void_p(d_n.data_ptr()), lz.ctypes.c_void_p(sp)), "border_nodes")
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    reps = max(5, args.steps // 3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    got = d_n.cpu().numpy()
+    P = oracle.port()
+
+    def host(k):
+        out = np.zeros(4 * nn * nn, np.float32)
+        P.orc_border_nodes(span, oracle._p(lumas[k]), W, Hh, oracle._p(Hs[k]), None, oracle._p(out))
+        return out.reshape(nn, nn, 4)
+    same = all(np.array_equal(got[k].view(np.uint32), host(k).view(np.uint32)) for k in range(distinct))
+    marked = 4 * (nn - 2)
+    held = int((got[..., 2] >= 0.35).sum())
+    threads = os.cpu_count() or 1
+    done, t0 = 0, time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        while time.perf_counter() - t0 < 2.0:
+            list(ex.map(host, range(distinct)))
+            done += distinct
+    dt = time.perf_counter() - t0
+    return {"workload": "border nodes (refine_node over the 128 ring's border lattice, %d nodes a frame), 64 frames of 1920x1080, LIZARD-1024 at ~2.6 px a module, rotation up to 15 deg, H up to a pixel off, AWGN 3 DN" % marked,
+            "frames_per_s": round(frames / (ms / 1e3), 1), "nodes_per_s": round(frames * marked / (ms / 1e3), 1), "ms_per_call": round(ms, 4),
+            "nodes_held": held, "nodes": frames * marked, "gpu_launches_per_call": 1, "identical_to_oracle": bool(same),
+            "cpu": {"frames_per_s": round(done / dt, 1), "cores": threads, "kind": "port",
+                    "sample": "the 8 distinct frames repeatedly for %.1f s, a frame a thread" % dt}}
+
+
 def bench_fmt_word(args, stream):
     """The format word (lizg_fmt_read_dev): its read off the border of a batch of 2048 registered 1280 x 720 frames
     (the 128 ring's word, RS(32, 3); 32 distinct captures at about 2 pixels a module, rotation up to 12 degrees, blur
@@ -750,7 +821,8 @@ def main():
         print(json.dumps({"ingest": bench_ingest(args, torch.cuda.current_stream())}))
         return
     if args.fmt_only:
-        print(json.dumps({"format_word": bench_fmt_word(args, torch.cuda.current_stream())}))
+        print(json.dumps({"format_word": bench_fmt_word(args, torch.cuda.current_stream()),
+                          "border_nodes": bench_border_nodes(args, torch.cuda.current_stream())}))
         return
     if args.encode_only:
         print(json.dumps({"sender": bench_encoder(args, torch.cuda.current_stream())}))
@@ -768,7 +840,8 @@ def main():
         rec = bench_receiver(args, st)
         rec["multistream"] = bench_multistream(args, st)
         print(json.dumps({"receiver": rec, "registration": {"anchor_search": bench_anchor(args, st), "refinement": bench_refinement(args, st),
-                                                            "format_word": bench_fmt_word(args, st)}, "sender": bench_encoder(args, st),
+                                                            "format_word": bench_fmt_word(args, st), "border_nodes": bench_border_nodes(args, st)},
+                          "sender": bench_encoder(args, st),
                           "ingest": bench_ingest(args, st)}))
         return
     batch = synth.ldpc_batch(args.count, seed=1000 + rank)
@@ -861,7 +934,7 @@ def main():
     if not args.no_receiver:
         out["receiver"] = bench_receiver(args, stream)
         out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream),
-                               "format_word": bench_fmt_word(args, stream)}
+                               "format_word": bench_fmt_word(args, stream), "border_nodes": bench_border_nodes(args, stream)}
         out["sender"] = bench_encoder(args, stream)
         out["ingest"] = bench_ingest(args, stream)
         out["receiver"]["multistream"] = bench_multistream(args, stream)

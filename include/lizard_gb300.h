@@ -265,7 +265,8 @@ int lizg_encoder_info(const lizg_encoder *e, int32_t *out);
 // NULL, not both): d_drive frames x px x px floats in 0..1, d_grey frames x W x W bytes.
 int lizg_encode_dev(lizg_encoder *e, const uint8_t *d_blocks, int frames, int pilots, float *d_drive, uint8_t *d_grey, void *stream);
 // The border's cell kinds of a ring of span modules with the format word (version, fps) painted: (span + 30)^2 bytes,
-// 2 dark, 1 light, 0 the picture's (liblizard/src/layout.c:69-141). Host only. Returns the side.
+// 2 dark, 1 light, 0 the picture's, | 8 on the word's cells (liblizard/src/layout.c:69-141, CELL_*). Host only.
+// Returns the side.
 int lizg_layout_kind(int span, int version, int fps, uint8_t *kind);
 
 // ---------------------------------------------------------------- format word
@@ -284,6 +285,17 @@ int lizg_fmt_read_dev(int span, const uint8_t *d_luma, int w, int h, int64_t fra
 // ob_fmt_decode alone on soft values read elsewhere (lizard_fmt_check, lizard_phy.c:1881-1889): frames x 4 cells in,
 // frames x 4 (1, ok, version, fps) out.
 int lizg_fmt_decode_dev(int span, const float *d_q, int frames, int32_t *d_word, void *stream);
+
+// ---------------------------------------------------------------- registration assist: the border nodes
+//
+// Replaces the registration's border pass (liblizard/src/acquire.c:5044-5058: refine_node, acquire.c:1242-1374, over
+// the border lattice's marked nodes in rings outward from the corners) for a batch of frames: the corners taken as
+// measured, each other node's displacement from its measured neighbours and the border pattern's correlation,
+// bit for bit the reference's portable build. d_H: frames x h_stride floats (H first); d_lens: frames x 15 doubles
+// (K, ax, ay, R, 11 coefficients, as lizg_refine_dev fits them) or NULL. Out: d_nodes, frames x nn x nn x (dx, dy,
+// score, done), nn the layout's nodes an axis (lizg_layout_nodes).
+int lizg_border_nodes_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
+                          const double *d_lens, int frames, float *d_nodes, void *stream);
 
 // ---------------------------------------------------------------- registration assist: refinement from the anchors
 //

@@ -225,6 +225,7 @@ def _rx_sigs(L):
     L.lizg_encoder_info.argtypes = [P, P]
     L.lizg_encode_dev.argtypes = [P, P, I, I, P, P, P]
     L.lizg_layout_kind.argtypes = [I, I, I, P]
+    L.lizg_border_nodes_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, P, I, P, P]
     L.lizg_fmt_geometry.argtypes = [I, P, P]
     L.lizg_fmt_read_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
     L.lizg_fmt_decode_dev.argtypes = [I, P, I, P, P]
@@ -486,6 +487,28 @@ def fmt_decode(span, q, stream=None):
            "lizg_fmt_decode_dev")
     torch.cuda.synchronize()
     return d_w.cpu().numpy()
+
+
+def border_nodes(span, luma, H, lens=None, stream=None):
+    """The registration's border nodes on the GPU for a batch of frames: luma frames x h x w uint8, H frames x 9 (or
+    frames x stride, H first), lens frames x 15 float64 or None. Returns frames x nn x nn x 4 (dx, dy, score, done)."""
+    import torch
+    lu = np.ascontiguousarray(luma, np.uint8)
+    if lu.ndim == 2:
+        lu = lu[None]
+    frames, h, w = lu.shape
+    Hf = np.ascontiguousarray(np.asarray(H, np.float32).reshape(frames, -1))
+    from . import synth
+    nn = synth.layout_nodes(span).size
+    d_l, d_h = torch.from_numpy(lu).cuda(), torch.from_numpy(Hf).cuda()
+    d_lens = None if lens is None else torch.from_numpy(np.ascontiguousarray(np.asarray(lens, np.float64).reshape(frames, 15))).cuda()
+    d_n = torch.zeros((frames, nn, nn, 4), dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+    _check(lib().lizg_border_nodes_dev(span, ctypes.c_void_p(d_l.data_ptr()), w, h, h * w, ctypes.c_void_p(d_h.data_ptr()), Hf.shape[1],
+                                       None if d_lens is None else ctypes.c_void_p(d_lens.data_ptr()), frames, ctypes.c_void_p(d_n.data_ptr()),
+                                       ctypes.c_void_p(st)), "lizg_border_nodes_dev")
+    torch.cuda.synchronize()
+    return d_n.cpu().numpy()
 
 
 class EngineBatch(ctypes.Structure):

@@ -19,7 +19,8 @@ COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + CSRC, "-I" + os.pat
 # multiply-add): they reproduce the reference's soft values bit for bit.
 EXACT = {"demap.cu": ["-fmad=false"], "sample.cu": ["-fmad=false"], "anchor.cu": ["-fmad=false"], "refine.cu": ["-fmad=false"], "ingest.cu": ["-fmad=false"],
          "fmtword.cu": ["-fmad=false"],
-         "encode.cu": ["-fmad=false"]}
+         "encode.cu": ["-fmad=false"],
+         "mesh.cu": ["-fmad=false"]}
 
 
 def sources():

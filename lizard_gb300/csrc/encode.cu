@@ -231,8 +231,9 @@ static int track_bit(int side, int j) {   // liblizard/src/layout.c:57-61
 }
 
 // The border's cell kinds, side x side modules: the corner marks, the line, the timing track, the format word's
-// cells (liblizard/src/layout.c:69-141 thin_init, thin_corner, ob_layout_set_fmt). 2 dark, 1 light, 0 the picture's.
-static void layout_kind(int span, int version, int fps, std::vector<uint8_t> &kind) {
+// cells (liblizard/src/layout.c:69-141 thin_init, thin_corner, ob_layout_set_fmt). 2 dark, 1 light, 0 the picture's;
+// | 8 on the word's cells (CELL_WORD: the registration's templates skip them).
+void layout_kind(int span, int version, int fps, std::vector<uint8_t> &kind) {
   const int side = span + 2 * kMargin, S = 12, reserve = 15, margin = kMargin;
   kind.assign((size_t)side * side, 1);
   for (int y = 0; y < side; y++)
@@ -272,7 +273,7 @@ static void layout_kind(int span, int version, int fps, std::vector<uint8_t> &ki
           const int t = reserve + off + j, dd = 5 + ee;
           const int x = sd == 0 || sd == 2 ? t : sd == 3 ? dd : side - 1 - dd;
           const int y = sd == 0 ? dd : sd == 2 ? side - 1 - dd : t;
-          kind[(size_t)y * side + x] = bit ? 2 : 1;
+          kind[(size_t)y * side + x] = (bit ? 2 : 1) | 8;
         }
     }
 }

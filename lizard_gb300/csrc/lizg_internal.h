@@ -3,6 +3,7 @@
 #define LIZG_INTERNAL_H
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <vector>
 #include "lizard_gb300.h"
 
 namespace lizg {
@@ -120,6 +121,9 @@ struct EncFft {
   float lim, sc;
 };
 cudaError_t enc_fft_launch(const EncFft &e, int frames, float2 *S, float *pic, cudaStream_t st);
+// The border's cell kinds of a ring of span modules, (span + 30)^2: 2 dark, 1 light, 0 the picture's, | 8 on the format
+// word's cells (encode.cu).
+void layout_kind(int span, int version, int fps, std::vector<uint8_t> &kind);
 int fft_plan(int n, int radix[3], int *lines);
 // The shading fit's bands a frame.
 int fft_hole_bands(int n);

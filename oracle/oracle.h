@@ -72,6 +72,9 @@ int orc_anchor_find(int span, const uint8_t *px, int w, int h, const float *H, c
 // The lens model from the anchors about H (liblizard/src/acquire.c:2038-2055 anchor_model, lensm_fit's first round):
 // lens out K, ax, ay, R, then 11 coefficients; 1 where a model fits.
 int orc_lens_fit(int span, int iw, int ih, const float *H, const uint8_t *ok, const float *dx, const float *dy, double *lens);
+// The registration's border nodes (acquire.c:1242-1374 refine_node, 5044-5058 the pass): nn * nn x (dx, dy, score,
+// done) out. Returns nn.
+int orc_border_nodes(int span, const uint8_t *px, int w, int h, const float *H, const double *lens, float *nodes_out);
 
 // Camera-format ingest (liblizard/api/codec.cpp:128-140; liblizard/core/ingest/develop.cpp): a frame's pixels in one of
 // liz_pixfmt's formats to tight luma rows, and the develop of P010 / RAW16 / RAW10 / RAW12 (ImageFormat values).

@@ -235,3 +235,236 @@ int orc_lens_fit(int span, int iw, int ih, const float *H, const uint8_t *ok, co
   for (int c = 0; c < LENSP; c++) lens[4 + c] = tb[c];
   return 1;
 }
+
+// ---------------------------------------------------------------- the border nodes (acquire.c:839-859, 1205-1374)
+
+enum { NCORNER = 12, NRESERVE = 15, FB = 18, NMAXN = 40 };
+static const float NODE_NONE = -2.0f;
+
+// The layout's cell kinds with the format word's cells flagged (liblizard/src/layout.c:69-141): 2 dark, 1 light, 0
+// the picture's, | 8 on a word cell.
+static void mesh_kind(int span, unsigned char *kind) {
+  const int side = span + 2 * MARGIN;
+  for (int y = 0; y < side; y++)
+    for (int x = 0; x < side; x++) {
+      const int dx = x < side - 1 - x ? x : side - 1 - x, dy = y < side - 1 - y ? y : side - 1 - y, d = dx < dy ? dx : dy;
+      unsigned char k;
+      if (dx < NCORNER && dy < NCORNER) {
+        const int in = dx >= 1 && dx <= NCORNER - 2 && dy >= 1 && dy <= NCORNER - 2, cd = dx < dy ? dx : dy;
+        k = in && !(cd >= 3 && cd < 5) ? 2 : 1;
+      } else {
+        int dark = d >= 1 && d <= 2;
+        if (d >= 5 && d < 7) {
+          const int along = dy <= dx ? x : y, sd = dy <= dx ? (y < side / 2 ? 0 : 2) : (x < side / 2 ? 3 : 1);
+          const int cell = (along - NRESERVE) / 2, run = cell / 4;
+          if (along >= NRESERVE && along < side - NRESERVE && !(run & 1)) dark = orc_thin_track(sd, run / 2 * 4 + cell % 4);
+        }
+        k = d >= MARGIN - 3 ? 0 : dark ? 2 : 1;
+      }
+      kind[y * side + x] = k;
+    }
+  const int cells = orc_fmt_side_cells(side, NRESERVE);
+  for (int sd = 0; sd < 4; sd++)
+    for (int i = 0; i < cells; i++) {
+      const int off = ((i / 4) * 8 + i % 4 + 4) * 2;
+      for (int j = 0; j < 2; j++)
+        for (int e = 0; e < 2; e++) {
+          const int t = NRESERVE + off + j, dd = 5 + e;
+          const int x = sd == 0 || sd == 2 ? t : sd == 3 ? dd : side - 1 - dd, y = sd == 0 ? dd : sd == 2 ? side - 1 - dd : t;
+          kind[y * side + x] = 1 | 8;   // the word painted blank: only the flag matters to the templates
+        }
+    }
+}
+
+static int in_capture(int w, int h, float u, float v) { return u >= 0.5f && u <= w - 0.5f && v >= 0.5f && v <= h - 0.5f; }
+
+static int node_inside(int w, int h, const float *H, int cx0, int cy0, const int *r, float pdx, float pdy, float ax, float bx, float ay, float by) {
+  const float x0 = cx0 + r[0] + 0.5f + ax, x1 = cx0 + r[1] - 0.5f + bx, y0 = cy0 + r[2] + 0.5f + ay, y1 = cy0 + r[3] - 0.5f + by;
+  for (int c = 0; c < 4; c++) {
+    const float x = c & 1 ? x1 : x0, y = c & 2 ? y1 : y0;
+    float u, v;
+    if (!(H[6] * x + H[7] * y + 1 > 0)) return 0;
+    project(H, x, y, &u, &v);
+    if (!(u + pdx >= 1.5f && u + pdx <= w - 1.5f && v + pdy >= 1.5f && v + pdy <= h - 1.5f)) return 0;
+  }
+  return 1;
+}
+
+typedef struct { float dx, dy, score; int done; } onode_t;
+typedef struct { const unsigned char *kind; int side, nn; const float *pos; } omesh_t;
+
+// The template's correlation with the node shifted (ox, oy) modules (acquire.c:1205-1238, the scalar build).
+static float node_ncc(const omesh_t *M, const uint8_t *px, int w, int h, int cx0, int cy0, const int *r, const float *H, float pdx, float pdy,
+                      float ox, float oy, int edge, int nmin) {
+  float st = 0, ss = 0, stt = 0, sss = 0, sts = 0;
+  int n = 0, nin = 0;
+  const int lo = r[0], hi = r[1], ylo = r[2], yhi = r[3], side = hi - lo;
+  float S[FB * FB];
+  for (int dy = ylo; dy < yhi; dy++) {
+    const float my = cy0 + dy + 0.5f + oy;
+    for (int dx = lo; dx < hi; dx++) {
+      const float mx = cx0 + dx + 0.5f + ox;
+      float u, v;
+      project(H, mx, my, &u, &v);
+      S[(dy - ylo) * side + dx - lo] = sample(px, w, h, u + pdx, v + pdy);
+    }
+  }
+  for (int dy = ylo; dy < yhi; dy++)
+    for (int dx = lo; dx < hi; dx++) {
+      const int kind = M->kind[(cy0 + dy) * M->side + cx0 + dx];
+      if (kind == 0 || (kind & 8)) continue;
+      if (edge) {
+        float u, v;
+        project(H, cx0 + dx + 0.5f + ox, cy0 + dy + 0.5f + oy, &u, &v);
+        nin += in_capture(w, h, u + pdx, v + pdy);
+      }
+      const float t = (kind & 3) == 2 ? -1.0f : 1.0f, s = S[(dy - ylo) * side + dx - lo];
+      st += t; ss += s; stt += t * t; sss += s * s; sts += t * s; n++;
+    }
+  if (edge && nin < nmin) return NODE_NONE;
+  const float vt = stt - st * st / n, vs = sss - ss * ss / n;
+  if (vt <= 0 || vs <= 1e-9f) return 0;
+  return (sts - st * ss / n) / sqrtf(vt * vs);
+}
+
+// One node's refinement (acquire.c:1242-1374 refine_node, the scalar build): the prior from the measured neighbours
+// (less the lens model's part, then the model's at the node), a coarse search over 7 x 7 half-module offsets read off
+// one grid of samples, then two passes of 3 x 3 searches at a quarter and an eighth of a module, a parabola each way.
+static void refine_node(const omesh_t *M, const uint8_t *px, int w, int h, const float *H, int i, int j, onode_t *nodes, const double *lens) {
+  const int nn = M->nn, cx0 = (int)M->pos[i], cy0 = (int)M->pos[j];
+  const float mcx = cx0 + 0.5f, mcy = cy0 + 0.5f;
+  int rect[4];
+  {
+    int ex = (j == 0 || j == nn - 1) ? 6 : 2, ey = (i == 0 || i == nn - 1) ? 6 : 2;
+    if (ex == 6 && ey == 6) { ex = NCORNER - 1 < FB - 3 ? NCORNER - 1 : FB - 3; ey = ex; }
+    rect[0] = -ex < -cx0 ? -cx0 : -ex; rect[1] = ex + 1 > M->side - cx0 ? M->side - cx0 : ex + 1;
+    rect[2] = -ey < -cy0 ? -cy0 : -ey; rect[3] = ey + 1 > M->side - cy0 ? M->side - cy0 : ey + 1;
+  }
+  float pdx = 0, pdy = 0;
+  int pn = 0;
+  for (int dj = -1; dj <= 1; dj++)
+    for (int di = -1; di <= 1; di++) {
+      const int ii = i + di, jj = j + dj;
+      if (ii < 0 || jj < 0 || ii >= nn || jj >= nn || !nodes[jj * nn + ii].done) continue;
+      float rx = nodes[jj * nn + ii].dx, ry = nodes[jj * nn + ii].dy;
+      if (lens) { float u, v, mx, my; project(H, M->pos[ii], M->pos[jj], &u, &v); lens_at(lens, u, v, &mx, &my); rx -= mx; ry -= my; }
+      pdx += rx; pdy += ry; pn++;
+    }
+  if (pn) { pdx /= pn; pdy /= pn; }
+  if (lens) { float u, v, mx, my; project(H, M->pos[i], M->pos[j], &u, &v); lens_at(lens, u, v, &mx, &my); pdx += mx; pdy += my; }
+  const int edge = !node_inside(w, h, H, cx0, cy0, rect, pdx, pdy, -1.5f, 1.5f, -1.5f, 1.5f);
+  float ppx, ppy, ax, ay, bx, by;
+  project(H, mcx, mcy, &ppx, &ppy); project(H, mcx + 1, mcy, &ax, &ay); project(H, mcx, mcy + 1, &bx, &by);
+  const float jxx = ax - ppx, jxy = ay - ppy, jyx = bx - ppx, jyy = by - ppy;
+  enum { GMAX = 2 * FB + 5 };
+  float G[GMAX * GMAX + 8], GM[GMAX * GMAX + 8], tv[FB * FB];
+  int at[FB * FB], cells = 0;
+  const int lo = rect[0], ylo = rect[2], side = rect[1] - rect[0], tall = rect[3] - rect[2], GW = 2 * side + 5, GH = 2 * tall + 5;
+  for (int gy = 0; gy < GH; gy++) {
+    const float my = (float)(2 * (cy0 + ylo) + gy - 2) * 0.5f;
+    for (int gx = 0; gx < GW; gx++) {
+      const float mx = (float)(2 * (cx0 + lo) + gx - 2) * 0.5f;
+      float u, v;
+      project(H, mx, my, &u, &v);
+      G[gy * GW + gx] = sample(px, w, h, u + pdx, v + pdy);
+      GM[gy * GW + gx] = !edge || in_capture(w, h, u + pdx, v + pdy) ? 1.0f : 0;
+    }
+  }
+  float st = 0, stt = 0;
+  for (int dy = 0; dy < tall; dy++)
+    for (int dx = 0; dx < side; dx++) {
+      const int kind = M->kind[(cy0 + ylo + dy) * M->side + cx0 + lo + dx];
+      if (kind == 0 || (kind & 8)) continue;
+      tv[cells] = (kind & 3) == 2 ? -1.0f : 1.0f;
+      at[cells] = (2 * dy + 3) * GW + 2 * dx + 3;
+      st += tv[cells]; stt += tv[cells] * tv[cells]; cells++;
+    }
+  const float vt = stt - st * st / cells;
+  const int nmin = (cells + 1) / 2;
+  float best = NODE_NONE, box = 0, boy = 0;
+  for (int k = 0; k < 4; k++) G[GW * GH + k] = GM[GW * GH + k] = 0;
+  for (int b = -3; b <= 3; b++)
+    for (int a = -3; a <= 3; a++) {
+      const float *g0 = G + b * GW + a, *m0 = GM + b * GW + a;
+      float ss = 0, sss = 0, sts = 0, sn = 0;
+      for (int k = 0; k < cells; k++) { const float v = g0[at[k]]; ss += v; sss += v * v; sts += tv[k] * v; }
+      if (edge) for (int k = 0; k < cells; k++) sn += m0[at[k]];
+      const float vs = sss - ss * ss / cells;
+      const float sc = edge && sn < nmin ? NODE_NONE : vt <= 0 || vs <= 1e-9f ? 0 : (sts - st * ss / cells) / sqrtf(vt * vs);
+      if (sc > best) { best = sc; box = a * 0.5f; boy = b * 0.5f; }
+    }
+  float g[3][3], step = 0.25f;
+  int have[3][3] = {{0}}, ma = 1, mb = 1;
+  g[1][1] = best; have[1][1] = 1;
+  for (int pass = 0; pass < 2; pass++, step *= 0.5f) {
+    for (int move = 0; move < 8; move++) {
+      if (ma != 1 || mb != 1) {
+        float ng[3][3];
+        int nh[3][3];
+        for (int b2 = 0; b2 < 3; b2++)
+          for (int a2 = 0; a2 < 3; a2++) {
+            const int sb = b2 + mb - 1, sa = a2 + ma - 1, in = sb >= 0 && sb < 3 && sa >= 0 && sa < 3;
+            nh[b2][a2] = in && have[sb][sa];
+            ng[b2][a2] = in ? g[sb][sa] : 0;
+          }
+        memcpy(g, ng, sizeof g); memcpy(have, nh, sizeof have); ma = mb = 1;
+      }
+      const int ce = !node_inside(w, h, H, cx0, cy0, rect, pdx, pdy, box - step, box + step, boy - step, boy + step);
+      for (int b2 = -1; b2 <= 1; b2++)
+        for (int a2 = -1; a2 <= 1; a2++)
+          if (!have[b2 + 1][a2 + 1]) {
+            g[b2 + 1][a2 + 1] = node_ncc(M, px, w, h, cx0, cy0, rect, H, pdx, pdy, box + a2 * step, boy + b2 * step, ce, nmin);
+            have[b2 + 1][a2 + 1] = 1;
+          }
+      int ba = 1, bb = 1;
+      for (int b2 = 0; b2 < 3; b2++) for (int a2 = 0; a2 < 3; a2++) if (g[b2][a2] > g[bb][ba]) { ba = a2; bb = b2; }
+      if (ba == 1 && bb == 1) break;
+      box += (ba - 1) * step; boy += (bb - 1) * step; ma = ba; mb = bb;
+    }
+    if (pass == 0) {
+      const float c = g[mb][ma];
+      memset(have, 0, sizeof have); g[1][1] = c; have[1][1] = 1; ma = mb = 1;
+    }
+  }
+  best = g[1][1];
+  const float dxx = g[1][0] - 2 * g[1][1] + g[1][2], dyy = g[0][1] - 2 * g[1][1] + g[2][1];
+  if (dxx < -1e-6f && g[1][0] > NODE_NONE && g[1][2] > NODE_NONE) box += 0.125f * 0.5f * (g[1][0] - g[1][2]) / dxx;
+  if (dyy < -1e-6f && g[0][1] > NODE_NONE && g[2][1] > NODE_NONE) boy += 0.125f * 0.5f * (g[0][1] - g[2][1]) / dyy;
+  onode_t *nd = &nodes[j * nn + i];
+  nd->done = 1; nd->score = best;
+  if (best < 0.35f) { nd->dx = pdx; nd->dy = pdy; return; }
+  nd->dx = pdx + box * jxx + boy * jyx;
+  nd->dy = pdy + box * jxy + boy * jyy;
+}
+
+// The border nodes of a frame through H (and the lens model, or NULL): corners as measured, the marked nodes in rings
+// outward from the corners (acquire.c:5044-5058). nodes_out: nn * nn x (dx, dy, score, done). Returns nn.
+int orc_border_nodes(int span, const uint8_t *px, int w, int h, const float *H, const double *lens, float *nodes_out) {
+  const int side = span + 2 * MARGIN;
+  unsigned char *kind = malloc((size_t)side * side);
+  float pos[NMAXN];
+  const int nn = orc_layout_nodes(side, pos);
+  onode_t *nodes = calloc((size_t)nn * nn, sizeof(onode_t));
+  if (!kind || !nodes) { free(kind); free(nodes); return -1; }
+  mesh_kind(span, kind);
+  const omesh_t M = {kind, side, nn, pos};
+  for (int c = 0; c < 4; c++) nodes[((c >= 2) ? nn - 1 : 0) * nn + ((c == 1 || c == 2) ? nn - 1 : 0)].done = 1;
+  int order[4 * NMAXN], no = 0;
+  for (int ring = 0; ring <= nn; ring++)   // ring by ring, rows within a ring
+    for (int j = 0; j < nn; j++)
+      for (int i = 0; i < nn; i++) {
+        const int ex = i == 0 || i == nn - 1, ey = j == 0 || j == nn - 1;
+        if (!((ex || ey) && !(ex && ey))) continue;
+        const int r = (i < nn - 1 - i ? i : nn - 1 - i) + (j < nn - 1 - j ? j : nn - 1 - j);
+        if (r == ring) order[no++] = j * nn + i;
+      }
+  for (int k = 0; k < no; k++) {
+    if (nodes[order[k]].done) continue;
+    refine_node(&M, px, w, h, H, order[k] % nn, order[k] / nn, nodes, lens);
+  }
+  for (int k = 0; k < nn * nn; k++) {
+    nodes_out[4 * k] = nodes[k].dx; nodes_out[4 * k + 1] = nodes[k].dy; nodes_out[4 * k + 2] = nodes[k].score; nodes_out[4 * k + 3] = (float)nodes[k].done;
+  }
+  free(kind); free(nodes);
+  return nn;
+}

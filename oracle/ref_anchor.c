@@ -62,3 +62,46 @@ int refs_anchor_model(int span, int iw, int ih, const float *H9, const uint8_t *
   ob_layout_free(&L);
   return fit;
 }
+
+// The border nodes' refinement as the registration's mesh step runs it (liblizard/src/acquire.c:5044-5058): the four
+// corners taken as measured (done, no displacement), then every marked node in rings outward from the corners, each
+// refine_node'd from its measured neighbours, with the lens model when given (NULL: none). The layout's format word
+// cells are flagged as the format's frame flags them (lizard_phy.c fmt_paint). nodes_out: nx * ny x (dx, dy, score,
+// done). Returns nx (= ny), or -1.
+int refs_border_nodes(int span, const uint8_t *px, int w, int h, const float *H9, const double *lens, float *nodes_out) {
+  ob_layout_t L;
+  if (ob_layout_init(&L, span + 2 * OB_MARGIN)) return -1;
+  uint8_t cw[OB_FMT_BYTES_MAX];
+  memset(cw, 0, sizeof cw);
+  ob_layout_set_fmt(&L, cw);
+  image_t im;
+  ob_image_init(&im, px, w, h, 1.0f);
+  homo_t H;
+  memcpy(H.h, H9, sizeof H.h);
+  lensm_t lm;
+  memset(&lm, 0, sizeof lm);
+  if (lens) {
+    lm.K = (int)lens[0]; lm.ax = lens[1]; lm.ay = lens[2]; lm.R = lens[3];
+    for (int a = 0; a < LENS_P; a++) lm.t[a] = lens[4 + a];
+  }
+  const int nx = L.nx, ny = L.ny, nn = nx * ny;
+  node_t *nodes = calloc((size_t)nn, sizeof(node_t));
+  for (int c = 0; c < 4; c++) nodes[((c >= 2) ? ny - 1 : 0) * nx + ((c == 1 || c == 2) ? nx - 1 : 0)].done = 1;
+  // the marked nodes ring by ring, rows within a ring (the counting sort of acquire.c:5046-5052)
+  int start[OB_MAX_NODES + 2] = {0}, order[4 * OB_MAX_NODES], no = 0;
+#define RING(i, j) (((i) < nx - 1 - (i) ? (i) : nx - 1 - (i)) + ((j) < ny - 1 - (j) ? (j) : ny - 1 - (j)))
+  for (int j = 0; j < ny; j++) for (int i = 0; i < nx; i++) if (L.node_mark[j * nx + i]) start[RING(i, j) + 1]++;
+  for (int k = 1; k < OB_MAX_NODES + 2; k++) start[k] += start[k - 1];
+  for (int j = 0; j < ny; j++) for (int i = 0; i < nx; i++) if (L.node_mark[j * nx + i]) { order[start[RING(i, j)]++] = j * nx + i; no++; }
+#undef RING
+  for (int k = 0; k < no; k++) {
+    if (nodes[order[k]].done) continue;
+    refine_node(&L, &im, &H, order[k] % nx, order[k] / nx, nodes, lens ? &lm : 0);
+  }
+  for (int k = 0; k < nn; k++) {
+    nodes_out[4 * k] = nodes[k].dx; nodes_out[4 * k + 1] = nodes[k].dy; nodes_out[4 * k + 2] = nodes[k].score; nodes_out[4 * k + 3] = (float)nodes[k].done;
+  }
+  free(nodes);
+  ob_layout_free(&L);
+  return nx;
+}
