@@ -43,6 +43,7 @@ struct EncDev {
   const uint8_t *white;
   EncTier tier[kMaxTiers];
   int pxm, px, W, q, o, side, aside, a0[kAnchK];   // drive geometry (pixels), the anchors' first pixels
+  int copy;   // every tap is the one sample's (the ring's pixels an exact copy of the picture's samples)
   const int32_t *rs_i0;
   const float *rs_w;
   const uint8_t *kind;
@@ -174,6 +175,13 @@ __global__ void __launch_bounds__(kEncThreads) enc_paint_kernel(EncDev e, const 
       const float ddx = fabsf((float)(dx - e.a0[ai]) + 0.5f - half), ddy = fabsf((float)(dy - e.a0[aj]) + 0.5f - half);
       const float r = fmaxf(ddx, ddy) / half;
       d = r < 0.25f || r >= 0.6f ? 1.0f : 0.0f;
+    } else if (e.copy && dx >= e.o && dx < e.o + e.q && dy >= e.o && dy < e.o + e.q) {
+      // an exact copy: both passes' six terms are 0 x, 1 x the sample, 0 x ..., whose sums are the sample itself
+      int ry = (e.rs_i0[dy - e.o] + 2) % e.n, cx = (e.rs_i0[dx - e.o] + 2) % e.n;
+      if (ry < 0) ry += e.n;
+      if (cx < 0) cx += e.n;
+      const float v = tmp[((int64_t)f * e.n + ry) * e.n + cx];
+      d = v < 0 ? 0.0f : v > 1 ? 1.0f : v;
     } else if (dx >= e.o && dx < e.o + e.q && dy >= e.o && dy < e.o + e.q) {   // the picture and its guard interval
       const int x = dx - e.o;
       const float *wt = e.rs_w + 6 * x, *row = tmp + ((int64_t)f * e.q + (dy - e.o)) * e.n;
@@ -375,6 +383,9 @@ lizg_encoder *lizg_encoder_new(int n, int subch, int span, int max_frames) {
     for (int t = 0; t < 6; t++) w[6 * p + t] = (float)(tw[t] / sum);
   }
   ok = ok && upload(x, &e.rs_i0, i0.data(), i0.size()) && upload(x, &e.rs_w, w.data(), w.size());
+  e.copy = 1;
+  for (int p = 0; p < e.q && e.copy; p++)
+    for (int t = 0; t < 6; t++) e.copy &= w[6 * p + t] == (t == 2 ? 1.0f : 0.0f);
   // the transform's twiddles
   std::vector<float2> tws(n);
   for (int st = 0, ns = 1; st < 3; ns *= rad[st], st++)
@@ -443,8 +454,8 @@ int lizg_encode_dev(lizg_encoder *x, const uint8_t *d_blocks, int frames, int pi
   }
   if (err == cudaSuccess) err = enc_fft_launch(x->xf, frames, x->S, x->pic, st);
   if (err == cudaSuccess) {
-    enc_vert_kernel<<<frames * e.q, kEncThreads, 0, st>>>(e, x->pic, x->tmp);
-    enc_paint_kernel<<<frames * e.W, kEncThreads, 0, st>>>(e, x->tmp, d_drive, d_grey);
+    if (!e.copy) enc_vert_kernel<<<frames * e.q, kEncThreads, 0, st>>>(e, x->pic, x->tmp);
+    enc_paint_kernel<<<frames * e.W, kEncThreads, 0, st>>>(e, e.copy ? x->pic : x->tmp, d_drive, d_grey);   // a copy reads the picture
     err = cudaGetLastError();
   }
   return err == cudaSuccess ? 0 : record_error(LIZG_E_CUDA, (std::string("lizg_encode_dev: ") + cudaGetErrorString(err)).c_str());
