@@ -718,7 +718,7 @@ def bench_refinement(args, stream):
     import lizard_gb300 as lz
     sets = []
     rng = np.random.default_rng(123)
-    sets.append(("spread", [(k, float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for k in range(48)]))
+    sets.append(("spread", [(k, float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for k in range(256)]))   # 256 of the 1024
     sets.append(("blur1.5_k1_0.03", [(100 + k, 0.03, 1.5) for k in range(16)]))
     sets.append(("mild_blur0.5", [(200 + k, float(rng.uniform(-0.05, 0.05)), 0.5) for k in range(32)]))
     jobs = [j for _, js in sets for j in js]
@@ -726,7 +726,8 @@ def bench_refinement(args, stream):
         caps = list(ex.map(_render_distorted, jobs, chunksize=2))
     sp = stream.cuda_stream
     res = {"workload": "1920x1080, LIZARD-1024 (n=1536) in the 128 ring, rotation 15 deg, tilt 20 deg, scale 0.8-1.1 x 1000 px, "
-                       "radial k1, blur in linear light, AWGN 3 DN; plain = corners' homography, refined = + 3 rounds of anchors and lens model"}
+                       "radial k1, blur in linear light, AWGN 3 DN, a seed a frame (the spread: 256 frames of the configuration's 1024); "
+                       "plain = corners' homography, refined = + 3 rounds of anchors and lens model"}
     at = 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for name, js in sets:
