@@ -161,6 +161,10 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
 // (frames x subch x 320 complex floats, pos order). The replacement for lizard_finish(f, grid, ...)
 // (liblizard/src/lizard_phy.h:236). d_grid is not modified.
 int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const lizg_rx_out *out, float *d_coef, void *stream);
+// The transform alone (row b: the anchors' erase, the detrend, the 2D transform) on picture grids, the used
+// coefficients into d_coef (frames x subch x 320 complex, pos order), as lizard_finish computes them before the soft
+// stage (liblizard/src/lizard_phy.c:1566-1716). For callers that read spectra (the refinement's tangent pictures).
+int lizg_rx_spectrum_grid_dev(lizg_rx *r, const float *d_grid, int frames, float *d_coef, void *stream);
 // Rows a-e from captured frames: d_luma holds frames 8-bit luma images (w x h, rows pitch bytes apart, frames
 // frame_stride bytes apart); d_reg holds each frame's registration, 9 + 2 nx ny floats: the homography H (module
 // coordinates to image pixels, h[8] = 1, liblizard/src/internal.h:105-112) then the node mesh's (dx, dy) pixel
@@ -296,6 +300,24 @@ int lizg_fmt_decode_dev(int span, const float *d_q, int frames, int32_t *d_word,
 // score, done), nn the layout's nodes an axis (lizg_layout_nodes).
 int lizg_border_nodes_dev(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
                           const double *d_lens, int frames, float *d_nodes, void *stream);
+
+// ---------------------------------------------------------------- registration refined from the pilots
+//
+// Gauss-Newton on the 8 homography parameters against the known pilots, measured through the receiver's own front
+// (lizg_rx_spectrum_grid_dev), the Jacobian from eight tangent pictures (forward mode); the plain registration kept
+// where the pilots' mismatch does not fall. Not in the reference: the benchmark spec's refinement step, ahead of the
+// soft stage.
+typedef struct lizg_gn lizg_gn;
+// The format, and the frames refined at once (chunk, 1..64: each holds 9 pictures and their spectra).
+lizg_gn *lizg_gn_new(int n, int subch, int span, int chunk);
+void lizg_gn_free(lizg_gn *g);
+// d_reg: frames x (9 + 2 nodes) registrations, H refined in place (the mesh kept). steps: Gauss-Newton steps (3 is
+// the benchmark spec's). Out (either NULL): d_loss, each frame's final mismatch; d_improved, 1 where a step was kept.
+int lizg_gn_refine_dev(lizg_gn *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int steps, float *d_loss,
+                       int32_t *d_improved, void *stream);
+// The 9 pictures a step reads (the sampled picture, then its tangents in h0..h7), frames x 9 x n x n, frames <= chunk.
+int lizg_gn_pictures_dev(lizg_gn *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_reg, int frames, float *d_pics,
+                         void *stream);
 
 // ---------------------------------------------------------------- registration assist: refinement from the anchors
 //

@@ -226,6 +226,12 @@ def _rx_sigs(L):
     L.lizg_encode_dev.argtypes = [P, P, I, I, P, P, P]
     L.lizg_layout_kind.argtypes = [I, I, I, P]
     L.lizg_border_nodes_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, P, I, P, P]
+    L.lizg_rx_spectrum_grid_dev.argtypes = [P, P, I, P, P]
+    L.lizg_gn_new.argtypes = [I, I, I, I]
+    L.lizg_gn_new.restype = P
+    L.lizg_gn_free.argtypes = [P]
+    L.lizg_gn_refine_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
+    L.lizg_gn_pictures_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, P, P]
     L.lizg_fmt_geometry.argtypes = [I, P, P]
     L.lizg_fmt_read_dev.argtypes = [I, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
     L.lizg_fmt_decode_dev.argtypes = [I, P, I, P, P]
@@ -327,6 +333,20 @@ class Receiver:
         _check(lib().lizg_rx_finish_coef_dev(self._h, ctypes.c_void_p(d.data_ptr()), frames, ctypes.byref(s), ctypes.c_void_p(st)), "lizg_rx_finish_coef_dev")
         torch.cuda.synchronize()
         return {k: v.cpu().numpy() for k, v in o.items()}
+
+    def spectrum_grid(self, grids, stream=None):
+        """The transform alone on grids (frames x n x n float32): frames x subch*320 complex64 (pos order)."""
+        import torch
+        g = np.ascontiguousarray(grids, np.float32)
+        frames = g.shape[0]
+        d = torch.from_numpy(g).cuda()
+        c = torch.zeros((frames, 2 * self.fmt.subch * SUB), dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_rx_spectrum_grid_dev(self._h, ctypes.c_void_p(d.data_ptr()), frames, ctypes.c_void_p(c.data_ptr()), ctypes.c_void_p(st)),
+               "lizg_rx_spectrum_grid_dev")
+        torch.cuda.synchronize()
+        out = c.cpu().numpy()
+        return out[:, 0::2] + 1j * out[:, 1::2]
 
     def finish_grid(self, grids, keep=True, coef=True, stream=None):
         """grids: frames x n x n float32 (grey / 255). Returns a dict of numpy arrays (coef: frames x subch*320 complex64)."""
@@ -509,6 +529,50 @@ def border_nodes(span, luma, H, lens=None, stream=None):
                                        ctypes.c_void_p(st)), "lizg_border_nodes_dev")
     torch.cuda.synchronize()
     return d_n.cpu().numpy()
+
+
+class PilotRefiner:
+    """Gauss-Newton on H against the known pilots (lizg_gn_*), chunk frames at once."""
+
+    def __init__(self, n, subch, span, chunk=8):
+        self._h = lib().lizg_gn_new(n, subch, span, chunk)
+        if not self._h:
+            raise LizgError("lizg_gn_new: " + lib().lizg_last_error().decode())
+        self.n, self.chunk = n, chunk
+
+    def refine(self, luma, reg, steps=3, stream=None):
+        """luma frames x h x w uint8, reg frames x (9 + 2 nodes) float32. Returns (reg refined, loss, improved)."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        frames, h, w = lu.shape
+        d_l = torch.from_numpy(lu).cuda()
+        d_r = torch.from_numpy(np.ascontiguousarray(reg, np.float32).copy()).cuda()
+        d_loss = torch.zeros(frames, dtype=torch.float32, device="cuda")
+        d_imp = torch.zeros(frames, dtype=torch.int32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_gn_refine_dev(self._h, ctypes.c_void_p(d_l.data_ptr()), w, h, h * w, ctypes.c_void_p(d_r.data_ptr()), frames, steps,
+                                        ctypes.c_void_p(d_loss.data_ptr()), ctypes.c_void_p(d_imp.data_ptr()), ctypes.c_void_p(st)), "lizg_gn_refine_dev")
+        torch.cuda.synchronize()
+        return d_r.cpu().numpy(), d_loss.cpu().numpy(), d_imp.cpu().numpy()
+
+    def pictures(self, luma, reg, stream=None):
+        """The sampled picture and its 8 tangents: frames x 9 x n x n float32."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        frames, h, w = lu.shape
+        d_l = torch.from_numpy(lu).cuda()
+        d_r = torch.from_numpy(np.ascontiguousarray(reg, np.float32)).cuda()
+        d_p = torch.zeros((frames, 9, self.n, self.n), dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_gn_pictures_dev(self._h, ctypes.c_void_p(d_l.data_ptr()), w, h, h * w, ctypes.c_void_p(d_r.data_ptr()), frames,
+                                          ctypes.c_void_p(d_p.data_ptr()), ctypes.c_void_p(st)), "lizg_gn_pictures_dev")
+        torch.cuda.synchronize()
+        return d_p.cpu().numpy()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().lizg_gn_free(self._h)
+            self._h = None
 
 
 class EngineBatch(ctypes.Structure):

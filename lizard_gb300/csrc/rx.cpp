@@ -328,6 +328,22 @@ int lizg_rx_finish_grid_dev(lizg_rx *r, const float *d_grid, int frames, const l
   return finish_src(r, src, frames, out, d_coef, static_cast<cudaStream_t>(stream), sms);
 }
 
+// Row (b) alone on picture grids: the anchors' erase, the detrend and the 2D transform, the used coefficients into
+// d_coef (frames x subch x 320 complex, pos order). No soft values, no decode.
+int lizg_rx_spectrum_grid_dev(lizg_rx *r, const float *d_grid, int frames, float *d_coef, void *stream) {
+  if (!r || !d_grid || !d_coef) return lizg::record_error(LIZG_E_ARG, "lizg_rx_spectrum_grid_dev: NULL argument");
+  if (frames < 1 || frames > r->max_frames) return lizg::record_error(LIZG_E_ARG, "lizg_rx_spectrum_grid_dev: frames out of 1..max_frames");
+  int sms = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  lizg::SrcDev src{};
+  src.grid = d_grid; src.gstride = (int64_t)r->f.n * r->f.n; src.sd = r->sd;
+  const int need = r->f.subch * lizg::kSub;
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, reinterpret_cast<float2 *>(d_coef)};
+  cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, static_cast<cudaStream_t>(stream));
+  r->launches = 4;
+  return e == cudaSuccess ? 0 : lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_spectrum_grid_dev: ") + cudaGetErrorString(e)).c_str());
+}
+
 // Rows (a) to (e) on a batch of captured luma frames, each with its registration (H, then the node mesh). The
 // sampler runs inside the transform's passes (no grid in HBM) unless the caller asks for the grid.
 int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
