@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--ingest-only", action="store_true", help="time only the camera-format ingest (profiling)")
     ap.add_argument("--fmt-only", action="store_true", help="time only the format word and the border nodes (profiling)")
     ap.add_argument("--encode-only", action="store_true", help="time only the sender on the GPU (profiling)")
+    ap.add_argument("--refine-only", action="store_true", help="time only the distorted captures' registration comparison")
     return ap.parse_args()
 
 
@@ -709,7 +710,8 @@ def bench_refinement(args, stream):
     scale U(0.8, 1.1) x a 1000-pixel layout side, radial k1 about the frame centre, Gaussian blur in linear light
     (gamma 2.2), AWGN 3 DN, seed = frame index. Plain: the homography through the layout's four corners as the camera
     sees them (a finder's corners), no lens. Refined: plus three rounds of the anchor search and the lens model the
-    anchors give, written into the node mesh (lizg_refine_dev). Three sets: the configuration's spread (k1 U(+-0.05),
+    anchors give, written into the node mesh (lizg_refine_dev). Refined with pilots: plus three Gauss-Newton steps on H
+    against the known pilots (lizg_gn_refine_dev). Three sets: the configuration's spread (k1 U(+-0.05),
     blur U(0.5, 2.0)), the point blur 1.5 / k1 0.03, and mild blur (k1 U(+-0.05), blur 0.5). Device-timed."""
     import concurrent.futures
     import multiprocessing
@@ -743,6 +745,10 @@ def bench_refinement(args, stream):
         d_found = torch.zeros(frames, dtype=torch.int32, device="cuda")
         o_p, s_p = rx._outputs(frames, torch, keep=False)
         o_r, s_r = rx._outputs(frames, torch, keep=False)
+        o_g, s_g = rx._outputs(frames, torch, keep=False)
+        gn = lz.PilotRefiner(1536, 1024, 256, chunk=16)
+        d_gn = torch.empty_like(d_plain)
+        d_imp = torch.zeros(frames, dtype=torch.int32, device="cuda")
 
         def plain():
             lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
@@ -755,8 +761,16 @@ def bench_refinement(args, stream):
             lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
                                                        lz.ctypes.c_void_p(d_ref.data_ptr()), frames, lz.ctypes.byref(s_r), None, None,
                                                        lz.ctypes.c_void_p(sp)), "finish_luma")
+        def refined_pilots():   # the anchors' refinement, then 3 Gauss-Newton steps on H against the pilots
+            d_gn.copy_(d_plain)
+            ref.refine_dev(d_l.data_ptr(), 1920, 1080, 1920 * 1080, d_gn.data_ptr(), frames, 3, d_found.data_ptr(), None, sp)
+            lz._check(lz.lib().lizg_gn_refine_dev(gn._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920 * 1080, lz.ctypes.c_void_p(d_gn.data_ptr()),
+                                                  frames, 3, None, lz.ctypes.c_void_p(d_imp.data_ptr()), lz.ctypes.c_void_p(sp)), "gn_refine")
+            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
+                                                       lz.ctypes.c_void_p(d_gn.data_ptr()), frames, lz.ctypes.byref(s_g), None, None,
+                                                       lz.ctypes.c_void_p(sp)), "finish_luma")
         out = {"frames": frames}
-        for tag, fn, o in (("plain", plain, o_p), ("refined", refined, o_r)):
+        for tag, fn, o in (("plain", plain, o_p), ("refined", refined, o_r), ("refined_pilots", refined_pilots, o_g)):
             for _ in range(2):
                 fn()
             torch.cuda.synchronize()
@@ -773,6 +787,9 @@ def bench_refinement(args, stream):
                         "frames_per_s": round(frames / (ms / 1e3), 1)}
         out["anchors_found_mean"] = round(float(d_found.float().mean().item()), 1)
         out["block_pass_points_gained"] = round(100 * (out["refined"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
+        out["pilot_steps_kept_frames"] = int(d_imp.sum().item())
+        out["pilot_points_gained_over_plain"] = round(100 * (out["refined_pilots"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
+        del gn
         res[name] = out
         ref.close()
     return res
@@ -824,6 +841,9 @@ def main():
     if args.fmt_only:
         print(json.dumps({"format_word": bench_fmt_word(args, torch.cuda.current_stream()),
                           "border_nodes": bench_border_nodes(args, torch.cuda.current_stream())}))
+        return
+    if args.refine_only:
+        print(json.dumps({"refinement": bench_refinement(args, torch.cuda.current_stream())}))
         return
     if args.encode_only:
         print(json.dumps({"sender": bench_encoder(args, torch.cuda.current_stream())}))
