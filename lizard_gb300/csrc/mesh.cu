@@ -54,6 +54,7 @@ __device__ bool node_inside(int w, int h, const float *H, int cx0, int cy0, cons
 struct MeshShared {
   float G[kGMax * kGMax + 8], GM[kGMax * kGMax + 8];
   float tv[kFB * kFB];
+  uint8_t kind[kFB * kFB];                 // the rect's cell kinds, staged for the template
   int at[kFB * kFB], pk[kFB * kFB];        // a template cell's place in the coarse grid, and in the rect (dy side + dx)
   float S[8][kFB * kFB];                   // the search step's candidates' samples at the template's cells
   uint8_t SI[8][kFB * kFB];                // and whether each is inside the capture
@@ -110,12 +111,18 @@ __global__ void __launch_bounds__(kMeshThreads) border_nodes_kernel(MeshArgs a) 
       m.jxx = ax - ppx; m.jxy = ay - ppy; m.jyx = bx - ppx; m.jyy = by - ppy;
       m.side = m.rect[1] - m.rect[0]; m.tall = m.rect[3] - m.rect[2];
       m.GW = 2 * m.side + 5; m.GH = 2 * m.tall + 5;
+    }
+    __syncthreads();
+    for (int t = tid; t < m.side * m.tall; t += blockDim.x)   // the rect's kinds, read once across the CTA
+      m.kind[t] = a.kind[(cy0 + m.rect[2] + t / m.side) * a.side + cx0 + m.rect[0] + t % m.side];
+    __syncthreads();
+    if (tid == 0) {
       // the template: the border's own cells about the node (not the picture's, not the word's), in row order
       float st = 0, stt = 0;
       int cells = 0;
       for (int dy = 0; dy < m.tall; dy++)
         for (int dx = 0; dx < m.side; dx++) {
-          const int kind = a.kind[(cy0 + m.rect[2] + dy) * a.side + cx0 + m.rect[0] + dx];
+          const int kind = m.kind[dy * m.side + dx];
           if (kind == 0 || (kind & 8)) continue;
           m.tv[cells] = (kind & 3) == 2 ? -1.0f : 1.0f;
           m.at[cells] = (2 * dy + 3) * m.GW + 2 * dx + 3;
