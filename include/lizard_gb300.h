@@ -70,8 +70,18 @@ void lizg_ldpc_plan_free(lizg_ldpc_plan *p);
 int64_t lizg_ldpc_plan_llr_bytes(const lizg_ldpc_plan *p);
 // Decodes the planned batch from device memory into device memory, queued on `stream`.
 int lizg_ldpc_plan_run_dev(lizg_ldpc_plan *p, const int8_t *d_llr, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream);
-// The same from host memory to host memory (pinned or not): copies in, decodes, copies out, waits.
+// The same from host memory to host memory (pinned or not), waiting for the result. When all four buffers are
+// page-locked (cudaHostAlloc, cudaHostRegister) and llr and bits 16-byte aligned, the decoder reads the LLRs and
+// writes the results in place in host memory; otherwise the batch is staged through device memory in chunks of
+// consecutive codewords (two from 64 MB of LLRs up), each chunk's copy in and out overlapping the other's decode.
+// The outputs do not depend on the route or the chunking.
 int lizg_ldpc_plan_run(lizg_ldpc_plan *p, const int8_t *llr, uint8_t *bits, int32_t *its, uint8_t *ok, void *stream);
+// Sets the chunk count of the staged route (1..16, clamped to the codeword count); returns the count set.
+int lizg_ldpc_plan_set_chunks(lizg_ldpc_plan *p, int chunks);
+// in_place 1 (the default) allows the in-place route for page-locked buffers, 0 always stages.
+int lizg_ldpc_plan_set_transfer(lizg_ldpc_plan *p, int in_place);
+// The route the last lizg_ldpc_plan_run took: 1 in place, 0 staged.
+int lizg_ldpc_plan_transfer(const lizg_ldpc_plan *p);
 // Kernel launches the last run made (for the benchmark's launch count).
 int lizg_ldpc_plan_launches(const lizg_ldpc_plan *p);
 

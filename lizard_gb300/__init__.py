@@ -54,6 +54,9 @@ def lib():
     L.lizg_ldpc_plan_llr_bytes.restype = ctypes.c_int64
     L.lizg_ldpc_plan_run_dev.argtypes = [P, P, P, P, P, P]
     L.lizg_ldpc_plan_run.argtypes = [P, P, P, P, P, P]
+    L.lizg_ldpc_plan_set_chunks.argtypes = [P, ctypes.c_int]
+    L.lizg_ldpc_plan_set_transfer.argtypes = [P, ctypes.c_int]
+    L.lizg_ldpc_plan_transfer.argtypes = [P]
     L.lizg_ldpc_plan_launches.argtypes = [P]
     L.lizg_ldpc_autotune.argtypes = [I, P, I, P]
     L.lizg_ldpc_variants.argtypes = [I]
@@ -155,6 +158,19 @@ class LdpcPlan:
     @property
     def launches(self):
         return int(lib().lizg_ldpc_plan_launches(self._h))
+
+    def set_transfer(self, in_place):
+        """1: page-locked host buffers are read and written in place by the decoder; 0: always staged."""
+        _check(lib().lizg_ldpc_plan_set_transfer(self._h, int(in_place)), "lizg_ldpc_plan_set_transfer")
+
+    @property
+    def transfer(self):
+        """The route the last run took: 1 in place, 0 staged."""
+        return int(lib().lizg_ldpc_plan_transfer(self._h))
+
+    def set_chunks(self, chunks):
+        """Chunk count of the pipelined host-memory run (1..16); returns the count set."""
+        return _check(lib().lizg_ldpc_plan_set_chunks(self._h, int(chunks)), "lizg_ldpc_plan_set_chunks")
 
     def run(self, llr, bits=None, its=None, ok=None, stream=0):
         """Host memory in and out: returns (packed bits, its, ok)."""

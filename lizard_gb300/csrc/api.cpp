@@ -5,6 +5,7 @@
 #include "lizard_codes.h"
 #include "lizg_internal.h"
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -53,23 +54,81 @@ int device_ready(int *sms) { return device_setup(sms); }
 int record_error(int code, const char *what) { return fail(code, what); }
 }  // namespace lizg
 
+// The host-memory entry point splits the batch into up to kLdpcChunks runs of consecutive codewords, so chunk j + 1
+// copies in while chunk j decodes and chunk j's results copy out while chunk j + 1 decodes.
+constexpr int kLdpcChunks = 16;
+
 struct lizg_ldpc_plan {
   int count = 0, max_iter = 0, stall_it = 0, launches = 0;
   float ratio = 0;
   int64_t llr_bytes = 0;
   int counts[4] = {0, 0, 0, 0};
-  int32_t *d_list = nullptr;       // codeword indices grouped by code
+  int32_t *d_list = nullptr;       // codeword indices grouped by code, each code's in ascending order
   int64_t *d_off = nullptr;        // per codeword LLR offset
-  int *d_counter = nullptr;        // four work counters
+  int *d_counter = nullptr;        // four work counters a chunk
   int list_at[4] = {0, 0, 0, 0};   // each code's first entry in d_list
+  std::vector<int> list;           // host copy of d_list
+  std::vector<int64_t> off;        // host copy of d_off
+  // the host-memory entry: 1 lets the decoder read and write pinned host buffers in place, 0 always stages; the
+  // last run's route (1 in place, 0 staged)
+  int in_place = 1, last_in_place = 0;
+  // the pipelined chunks: chunk j is codewords first[j] .. first[j + 1] - 1, its code c entries d_list[at[j][c]] on
+  int chunks = 1;
+  int first[kLdpcChunks + 1] = {};
+  int at[kLdpcChunks][4] = {}, cnt[kLdpcChunks][4] = {};
   // staging for the host-memory entry point, made on its first use
   int8_t *s_llr = nullptr; uint8_t *s_bits = nullptr; int32_t *s_its = nullptr; uint8_t *s_ok = nullptr;
   int device = -1;
   // The four codes' launches run on their own streams, forked from and joined back to the caller's stream, so one
-  // code's persistent CTAs take over the SMs another code's tail frees.
-  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
+  // code's persistent CTAs take over the SMs another code's tail frees. The chunks' copies out run on `out`.
+  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr}, out = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr, in[kLdpcChunks] = {}, join[kLdpcChunks][4] = {};
 };
+
+namespace {
+
+// Splits the batch into `k` chunks of about equal LLR bytes at codeword boundaries, and finds each chunk's entries in
+// each code's ascending list.
+void plan_chunks(lizg_ldpc_plan *p, int k) {
+  k = std::max(1, std::min({k, kLdpcChunks, p->count}));
+  p->chunks = k;
+  p->first[0] = 0;
+  int i = 0;
+  for (int j = 1; j < k; j++) {
+    const int64_t target = p->llr_bytes * j / k;
+    while (i < p->count && p->off[(size_t)i] < target) i++;
+    p->first[j] = std::max(i, p->first[j - 1] + 1);
+  }
+  p->first[k] = p->count;
+  for (int c = 0; c < 4; c++) {
+    const int *b = p->list.data() + p->list_at[c], *e = b + p->counts[c];
+    for (int j = 0; j < k; j++) {
+      const int *lo = std::lower_bound(b, e, p->first[j]), *hi = std::lower_bound(b, e, p->first[j + 1]);
+      p->at[j][c] = (int)(lo - p->list.data());
+      p->cnt[j][c] = (int)(hi - lo);
+    }
+  }
+}
+
+// Queues the code launches of one chunk (or of the whole batch): each code's side stream waits for `after`, runs its
+// entries, and records its join event.
+int launch_codes(lizg_ldpc_plan *p, const int8_t *d_llr, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, const int *at,
+                 const int *cnt, int *counter, cudaEvent_t after, cudaEvent_t *join, int sms) {
+  cudaError_t e;
+  for (int c = 0; c < 4; c++) {   // longest code first: 7/8 has the most codewords
+    if (!cnt[c]) continue;
+    if ((e = cudaStreamWaitEvent(p->side[c], after, 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
+    lizg::LdpcLaunch a{};
+    a.llr = d_llr; a.bits = d_bits; a.its = d_its; a.ok = d_ok; a.list = p->d_list + at[c]; a.off = p->d_off;
+    a.count = cnt[c]; a.counter = counter + c; a.max_iter = p->max_iter; a.stall_it = p->stall_it; a.stall_ratio = p->ratio;
+    if ((e = lizg::ldpc_launch(c, a, sms, p->side[c])) != cudaSuccess) return fail_cuda(e, "LDPC kernel launch");
+    if ((e = cudaEventRecord(join[c], p->side[c])) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
+    p->launches++;
+  }
+  return 0;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -134,33 +193,46 @@ lizg_ldpc_plan *lizg_ldpc_plan_new(const int32_t *rate, int count, int max_iter,
   if (!p) { fail(LIZG_E_NOMEM, "lizg_ldpc_plan_new: out of host memory"); return nullptr; }
   p->count = count; p->max_iter = max_iter; p->stall_it = stall_it; p->ratio = stall_ratio;
   cudaGetDevice(&p->device);
-  std::vector<int64_t> off((size_t)count);
-  std::vector<int32_t> list((size_t)count);
+  p->off.assign((size_t)count, 0);
+  p->list.assign((size_t)count, 0);
   int64_t at = 0;
   for (int i = 0; i < count; i++) {
     const int c = lizg_code_of_rate(rate[i]);
     if (c < 0) { fail(LIZG_E_ARG, "lizg_ldpc_plan_new: a rate with no code"); delete p; return nullptr; }
-    off[(size_t)i] = at; at += code_n(c); p->counts[c]++;
+    p->off[(size_t)i] = at; at += code_n(c); p->counts[c]++;
   }
   p->llr_bytes = at;
   int fill[4];
   for (int c = 0, s = 0; c < 4; s += p->counts[c], c++) { p->list_at[c] = s; fill[c] = s; }
-  for (int i = 0; i < count; i++) list[(size_t)fill[lizg_code_of_rate(rate[i])]++] = i;
+  for (int i = 0; i < count; i++) p->list[(size_t)fill[lizg_code_of_rate(rate[i])]++] = i;
+  // two chunks from 64 MB of LLRs up: half the copy in overlaps decode; more chunks add more launch tails than the
+  // overlap saves (65,536 codewords on a GB300: 19.6 ms at 1 chunk, 19.2 at 2, 20.6 at 8, 22.1 at 16)
+  plan_chunks(p, p->llr_bytes >= (64 << 20) ? 2 : 1);
   cudaError_t e;
   if ((e = cudaMalloc(&p->d_list, sizeof(int32_t) * (size_t)count)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_off, sizeof(int64_t) * (size_t)count)) != cudaSuccess ||
-      (e = cudaMalloc(&p->d_counter, sizeof(int) * 4)) != cudaSuccess ||
-      (e = cudaMemcpy(p->d_list, list.data(), sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = cudaMemcpy(p->d_off, off.data(), sizeof(int64_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming)) != cudaSuccess) {
+      (e = cudaMalloc(&p->d_counter, sizeof(int) * 4 * kLdpcChunks)) != cudaSuccess ||
+      (e = cudaMemcpy(p->d_list, p->list.data(), sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(p->d_off, p->off.data(), sizeof(int64_t) * (size_t)count, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking)) != cudaSuccess) {
     fail_cuda(e, "lizg_ldpc_plan_new");
     lizg_ldpc_plan_free(p);
     return nullptr;
   }
   for (int c = 0; c < 4; c++) {
-    if ((e = cudaStreamCreateWithFlags(&p->side[c], cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&p->join[c], cudaEventDisableTiming)) != cudaSuccess) {
+    if ((e = cudaStreamCreateWithFlags(&p->side[c], cudaStreamNonBlocking)) != cudaSuccess) {
       fail_cuda(e, "lizg_ldpc_plan_new: streams");
+      lizg_ldpc_plan_free(p);
+      return nullptr;
+    }
+  }
+  for (int j = 0; j < kLdpcChunks; j++) {
+    bool bad = (e = cudaEventCreateWithFlags(&p->in[j], cudaEventDisableTiming)) != cudaSuccess;
+    for (int c = 0; c < 4 && !bad; c++) bad = (e = cudaEventCreateWithFlags(&p->join[j][c], cudaEventDisableTiming)) != cudaSuccess;
+    if (bad) {
+      fail_cuda(e, "lizg_ldpc_plan_new: events");
       lizg_ldpc_plan_free(p);
       return nullptr;
     }
@@ -172,9 +244,29 @@ void lizg_ldpc_plan_free(lizg_ldpc_plan *p) {
   if (!p) return;
   cudaFree(p->d_list); cudaFree(p->d_off); cudaFree(p->d_counter);
   cudaFree(p->s_llr); cudaFree(p->s_bits); cudaFree(p->s_its); cudaFree(p->s_ok);
-  for (int c = 0; c < 4; c++) { if (p->side[c]) cudaStreamDestroy(p->side[c]); if (p->join[c]) cudaEventDestroy(p->join[c]); }
+  for (int c = 0; c < 4; c++) if (p->side[c]) cudaStreamDestroy(p->side[c]);
+  if (p->out) cudaStreamDestroy(p->out);
+  for (int j = 0; j < kLdpcChunks; j++) {
+    if (p->in[j]) cudaEventDestroy(p->in[j]);
+    for (int c = 0; c < 4; c++) if (p->join[j][c]) cudaEventDestroy(p->join[j][c]);
+  }
   if (p->fork) cudaEventDestroy(p->fork);
+  if (p->done) cudaEventDestroy(p->done);
   delete p;
+}
+
+int lizg_ldpc_plan_set_transfer(lizg_ldpc_plan *p, int in_place) {
+  if (!p || (in_place != 0 && in_place != 1)) return fail(LIZG_E_ARG, "lizg_ldpc_plan_set_transfer: in_place must be 0 or 1");
+  p->in_place = in_place;
+  return 0;
+}
+
+int lizg_ldpc_plan_transfer(const lizg_ldpc_plan *p) { return p ? p->last_in_place : LIZG_E_ARG; }
+
+int lizg_ldpc_plan_set_chunks(lizg_ldpc_plan *p, int chunks) {
+  if (!p || chunks < 1 || chunks > kLdpcChunks) return fail(LIZG_E_ARG, "lizg_ldpc_plan_set_chunks: chunks must be 1..16");
+  plan_chunks(p, chunks);
+  return p->chunks;
 }
 
 int64_t lizg_ldpc_plan_llr_bytes(const lizg_ldpc_plan *p) { return p ? p->llr_bytes : LIZG_E_ARG; }
@@ -192,39 +284,92 @@ int lizg_ldpc_plan_run_dev(lizg_ldpc_plan *p, const int8_t *d_llr, uint8_t *d_bi
     if (e != cudaSuccess) return fail_cuda(e, "cudaMemsetAsync");
     if ((e = cudaEventRecord(p->fork, st)) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
     p->launches = 0;
-    for (int c = 0; c < 4; c++) {   // longest code first: 7/8 has the most codewords
-      if (!p->counts[c]) continue;
-      if ((e = cudaStreamWaitEvent(p->side[c], p->fork, 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
-      lizg::LdpcLaunch a{};
-      a.llr = d_llr; a.bits = d_bits; a.its = d_its; a.ok = d_ok; a.list = p->d_list + p->list_at[c]; a.off = p->d_off;
-      a.count = p->counts[c]; a.counter = p->d_counter + c; a.max_iter = p->max_iter; a.stall_it = p->stall_it; a.stall_ratio = p->ratio;
-      if ((e = lizg::ldpc_launch(c, a, sms, p->side[c])) != cudaSuccess) return fail_cuda(e, "LDPC kernel launch");
-      if ((e = cudaEventRecord(p->join[c], p->side[c])) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
-      if ((e = cudaStreamWaitEvent(st, p->join[c], 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
-      p->launches++;
-    }
+    if (int rc = launch_codes(p, d_llr, d_bits, d_its, d_ok, p->list_at, p->counts, p->d_counter, p->fork, p->join[0], sms)) return rc;
+    for (int c = 0; c < 4; c++)
+      if (p->counts[c] && (e = cudaStreamWaitEvent(st, p->join[0][c], 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
     return 0;
   } catch (...) {
     return fail(LIZG_E_STATE, "lizg_ldpc_plan_run_dev: unexpected exception");
   }
 }
 
+namespace {
+
+// The device address of `bytes` bytes of page-locked host memory at h, or null: both ends must lie in memory the
+// runtime reports as host memory mapped for this device, at one device offset apart.
+void *mapped_host(const void *h, int64_t bytes) {
+  cudaPointerAttributes a0{}, a1{};
+  const char *c = static_cast<const char *>(h);
+  if (cudaPointerGetAttributes(&a0, c) != cudaSuccess || cudaPointerGetAttributes(&a1, c + bytes - 1) != cudaSuccess) {
+    cudaGetLastError();   // a pointer the runtime does not know is not an error here
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer) return nullptr;
+  if (static_cast<char *>(a1.devicePointer) - static_cast<char *>(a0.devicePointer) != bytes - 1) return nullptr;
+  return a0.devicePointer;
+}
+
+}  // namespace
+
+// Host memory in and out. When all four buffers are page-locked (cudaHostAlloc, cudaHostRegister) and llr and bits
+// are 16-byte aligned, the decoder reads each codeword's LLRs once from host memory and writes its bits, its and ok
+// there (NVLink-C2C on a Grace host): the transfer overlaps the decode with no staging copy. Otherwise the batch is
+// staged through device memory, pipelined over the plan's chunks: the caller's stream copies chunk j in and forks chunk j's
+// code launches; the copy-out stream waits for them and copies chunk j's bits, its and ok back. Chunk j's copy out
+// is queued after chunk j + 1's launches, so a copy to pageable memory (which returns only when done) still lets
+// the next chunk's copy in and decode run meanwhile.
 int lizg_ldpc_plan_run(lizg_ldpc_plan *p, const int8_t *llr, uint8_t *bits, int32_t *its, uint8_t *ok, void *stream) {
   try {
     if (!p || !llr || !bits || !its || !ok) return fail(LIZG_E_ARG, "lizg_ldpc_plan_run: NULL argument");
+    int sms = 0;
+    if (int rc = device_setup(&sms)) return rc;
     cudaError_t e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    p->last_in_place = 0;
+    if (p->in_place) {
+      void *dl = mapped_host(llr, p->llr_bytes), *db = mapped_host(bits, p->llr_bytes / 8);
+      void *di = mapped_host(its, sizeof(int32_t) * (int64_t)p->count), *dk = mapped_host(ok, p->count);
+      if (dl && db && di && dk && !((reinterpret_cast<uintptr_t>(dl) | reinterpret_cast<uintptr_t>(db)) & 15)) {
+        if (int rc = lizg_ldpc_plan_run_dev(p, static_cast<const int8_t *>(dl), static_cast<uint8_t *>(db), static_cast<int32_t *>(di),
+                                            static_cast<uint8_t *>(dk), stream)) return rc;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "lizg_ldpc_plan_run: decode");
+        p->last_in_place = 1;
+        return 0;
+      }
+    }
     if (!p->s_llr) {
       if ((e = cudaMalloc(&p->s_llr, (size_t)p->llr_bytes)) != cudaSuccess || (e = cudaMalloc(&p->s_bits, (size_t)p->llr_bytes / 8)) != cudaSuccess ||
           (e = cudaMalloc(&p->s_its, sizeof(int32_t) * (size_t)p->count)) != cudaSuccess || (e = cudaMalloc(&p->s_ok, (size_t)p->count)) != cudaSuccess)
         return fail_cuda(e, "lizg_ldpc_plan_run: staging buffers");
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if ((e = cudaMemcpyAsync(p->s_llr, llr, (size_t)p->llr_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail_cuda(e, "copy in");
-    if (int rc = lizg_ldpc_plan_run_dev(p, p->s_llr, p->s_bits, p->s_its, p->s_ok, stream)) return rc;
-    if ((e = cudaMemcpyAsync(bits, p->s_bits, (size_t)p->llr_bytes / 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(its, p->s_its, sizeof(int32_t) * (size_t)p->count, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(ok, p->s_ok, (size_t)p->count, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-      return fail_cuda(e, "copy out");
+    if ((e = cudaMemsetAsync(p->d_counter, 0, sizeof(int) * 4 * (size_t)p->chunks, st)) != cudaSuccess) return fail_cuda(e, "cudaMemsetAsync");
+    // the copy-out stream starts after whatever the caller queued before this call
+    if ((e = cudaEventRecord(p->fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(p->out, p->fork, 0)) != cudaSuccess)
+      return fail_cuda(e, "lizg_ldpc_plan_run: fork");
+    p->launches = 0;
+    auto copy_out = [&](int j) -> int {
+      for (int c = 0; c < 4; c++)
+        if (p->cnt[j][c] && (e = cudaStreamWaitEvent(p->out, p->join[j][c], 0)) != cudaSuccess) return fail_cuda(e, "cudaStreamWaitEvent");
+      const int i0 = p->first[j], i1 = p->first[j + 1];
+      const int64_t b0 = p->off[(size_t)i0] / 8, b1 = (i1 < p->count ? p->off[(size_t)i1] : p->llr_bytes) / 8;
+      if ((e = cudaMemcpyAsync(bits + b0, p->s_bits + b0, (size_t)(b1 - b0), cudaMemcpyDeviceToHost, p->out)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(its + i0, p->s_its + i0, sizeof(int32_t) * (size_t)(i1 - i0), cudaMemcpyDeviceToHost, p->out)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(ok + i0, p->s_ok + i0, (size_t)(i1 - i0), cudaMemcpyDeviceToHost, p->out)) != cudaSuccess)
+        return fail_cuda(e, "copy out");
+      return 0;
+    };
+    for (int j = 0; j < p->chunks; j++) {
+      const int i0 = p->first[j], i1 = p->first[j + 1];
+      const int64_t b0 = p->off[(size_t)i0], b1 = i1 < p->count ? p->off[(size_t)i1] : p->llr_bytes;
+      if ((e = cudaMemcpyAsync(p->s_llr + b0, llr + b0, (size_t)(b1 - b0), cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail_cuda(e, "copy in");
+      if ((e = cudaEventRecord(p->in[j], st)) != cudaSuccess) return fail_cuda(e, "cudaEventRecord");
+      if (int rc = launch_codes(p, p->s_llr, p->s_bits, p->s_its, p->s_ok, p->at[j], p->cnt[j], p->d_counter + 4 * j, p->in[j], p->join[j], sms)) return rc;
+      if (j)
+        if (int rc = copy_out(j - 1)) return rc;
+    }
+    if (int rc = copy_out(p->chunks - 1)) return rc;
+    if ((e = cudaEventRecord(p->done, p->out)) != cudaSuccess || (e = cudaStreamWaitEvent(st, p->done, 0)) != cudaSuccess)
+      return fail_cuda(e, "lizg_ldpc_plan_run: join");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "lizg_ldpc_plan_run: decode");
     return 0;
   } catch (...) {

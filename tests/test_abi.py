@@ -57,6 +57,8 @@ def test_host_crc_matches_oracle():
 
 def test_bad_arguments_are_errors():
     assert lz.lib().lizg_ldpc_n(5) == 0
+    assert lz.lib().lizg_ldpc_plan_set_chunks(None, 2) == -1
+    assert lz.lib().lizg_ldpc_plan_set_transfer(None, 1) == -1 and lz.lib().lizg_ldpc_plan_transfer(None) == -1
     with pytest.raises(lz.LizgError):
         lz.ldpc_encode(5, np.zeros(3840, np.uint8))
     with pytest.raises(lz.LizgError):

@@ -105,6 +105,38 @@ def test_device_entry_on_a_side_stream_matches_host_entry():
     assert plan.launches == 4
 
 
+@pytest.mark.parametrize("chunks", [1, 2, 7, 16])
+def test_chunked_host_entry_matches_device_entry(chunks):
+    """The host-memory entry pipelines the batch over chunks of consecutive codewords: the outputs are those of the
+    one-pass device entry, from pageable and from pinned host memory."""
+    torch = pytest.importorskip("torch")
+    b = synth.ldpc_batch(1000, seed=4)
+    plan = lz.LdpcPlan(b["rates"], 20, 9, 0.95)
+    d_llr = torch.from_numpy(b["llr"]).cuda()
+    d_bits = torch.empty(plan.llr_bytes // 8, dtype=torch.uint8, device="cuda")
+    d_its = torch.empty(plan.count, dtype=torch.int32, device="cuda")
+    d_ok = torch.empty(plan.count, dtype=torch.uint8, device="cuda")
+    plan.run_dev(d_llr.data_ptr(), d_bits.data_ptr(), d_its.data_ptr(), d_ok.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    want = d_bits.cpu().numpy(), d_its.cpu().numpy(), d_ok.cpu().numpy()
+    assert plan.set_chunks(chunks) == chunks
+    got = plan.run(b["llr"])
+    assert plan.launches >= chunks and plan.transfer == 0
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+    pinned = [torch.empty(n, dtype=t).pin_memory() for n, t in
+              ((plan.llr_bytes, torch.int8), (plan.llr_bytes // 8, torch.uint8), (plan.count, torch.int32), (plan.count, torch.uint8))]
+    pinned[0].copy_(torch.from_numpy(b["llr"]))
+    for in_place in (0, 1):
+        for t in pinned[1:]:
+            t.fill_(0x5A)
+        plan.set_transfer(in_place)
+        got = plan.run(*(t.numpy() for t in pinned))
+        assert plan.transfer == in_place
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+
+
 def test_full_size_batch_properties():
     """The benchmark's batch (65,536 codewords): every decoded block is its sent codeword and passes its CRC, the
     CRC flags agree with a host CRC of the output, clean-channel codewords all decode, and a sample matches the oracle."""
