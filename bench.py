@@ -853,7 +853,7 @@ def main():
         # the decoder's kernel variant per code chosen by timing on this device, before any timed work
         t_tune = time.perf_counter()
         chosen = lz.ldpc_autotune(8192, synth.EBN0_SWEEP_DB)
-        tune = {"variant": {name: {"index": v, "warps_a_codeword": lz.ldpc_variant(r)[1], "loop_form": lz.ldpc_variant(r)[2]}
+        tune = {"variant": {name: {"index": v, "warps_a_codeword": lz.ldpc_variant(r)[1], "loop_form": lz.ldpc_variant(r)[2], "pair_form": lz.ldpc_variant(r)[3]}
                             for name, r, v in zip(("7/8", "3/4", "2/3", "1/2"), (6, 4, 3, 2), chosen)},
                 "seconds": round(time.perf_counter() - t_tune, 2), "calibration": "8192 codewords a code, all-zero codeword, BPSK/AWGN over the workload's Eb/N0 sweep"}
     if args.receiver_only:

@@ -107,7 +107,8 @@ int lizg_ldpc_decode_noalloc(const int8_t *d_llr, const int32_t *d_rate, int cou
 // Every later decode on the device (plans, the single-codeword call, the receiver, the allocation-free call) uses
 // the kept variant.
 // lizg_ldpc_set_variant fixes one by hand; lizg_ldpc_variant returns the current index and its warps a codeword and
-// form (1 = loop); lizg_ldpc_variants the number of variants of a rate.
+// form (bit 0: the loop form; bit 1: the pair form, two checks a thread in 16-bit halves); lizg_ldpc_variants the
+// number of variants of a rate.
 int lizg_ldpc_autotune(int count, const float *ebn0_db, int n_ebn0, int32_t *choice);
 int lizg_ldpc_variants(int rate);
 int lizg_ldpc_variant(int rate, int32_t *wpc, int32_t *loop_form);

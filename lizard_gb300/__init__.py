@@ -113,10 +113,10 @@ def ldpc_variants(rate):
 
 
 def ldpc_variant(rate):
-    """The current device's variant of this rate's code: (index, warps a codeword, loop form)."""
+    """The current device's variant of this rate's code: (index, warps a codeword, loop form, pair form)."""
     w, lf = np.zeros(1, np.int32), np.zeros(1, np.int32)
     v = _check(lib().lizg_ldpc_variant(rate, _ptr(w), _ptr(lf)), "lizg_ldpc_variant")
-    return v, int(w[0]), bool(lf[0])
+    return v, int(w[0]), bool(lf[0] & 1), bool(lf[0] & 2)
 
 
 def ldpc_set_variant(rate, index):

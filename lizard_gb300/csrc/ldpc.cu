@@ -271,6 +271,251 @@ __device__ __forceinline__ int unsat(const int16_t *L, int lane, int T0, int cou
   return count ? __reduce_add_sync(0xffffffffu, bad) : 0;
 }
 
+// ---------------------------------------------------------------- the 16-bit pair form
+//
+// Checks i and i + 64 of a layer (i < 64) share a thread, their extrinsics, minima, signs and messages riding in the
+// two 16-bit halves of one 32-bit register (low half check i), so one 16x2 instruction serves two checks. Every
+// 128-column block of posteriors is stored as 64 words, word w = (column w, column w + 64): the columns a circulant
+// of shift sh gives checks i and i + 64, (i - sh) mod 128 and that plus 64, always share a word, in check order when
+// (i - sh) mod 128 < 64 and swapped otherwise; one byte permute puts them in check order and the same one puts them
+// back. A slot's messages are 64 byte pairs (low byte check i). 16x2 add/subtract and min/max are native on sm_103a;
+// the absolute value and equality tests are built from them (the 16x2 abs and compare forms are slow sequences).
+// The arithmetic per check is that of layer_part, half for half.
+
+__device__ __forceinline__ uint32_t add2(uint32_t a, uint32_t b) { uint32_t d; asm("add.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b)); return d; }
+__device__ __forceinline__ uint32_t sub2(uint32_t a, uint32_t b) { return __vsub2(a, b); }
+__device__ __forceinline__ uint32_t minu2(uint32_t a, uint32_t b) { uint32_t d; asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b)); return d; }
+__device__ __forceinline__ uint32_t maxu2(uint32_t a, uint32_t b) { uint32_t d; asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b)); return d; }
+__device__ __forceinline__ uint32_t maxs2(uint32_t a, uint32_t b) { uint32_t d; asm("max.s16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b)); return d; }
+// byte permute; a selector nibble with bit 3 set replicates the sign of the byte its low bits name
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t s) { uint32_t d; asm("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(a), "r"(s)); return d; }
+
+constexpr uint32_t kKeep = 0x3210u, kSwap = 0x1032u;   // halves as they are; halves exchanged
+constexpr uint32_t kSext = 0x9180u;                    // two int8 (bytes 0, 1) -> two int16
+constexpr uint32_t kSign = 0xBB99u;                    // each half's sign spread over the half
+constexpr uint32_t kPack = 0x0020u;                    // each half's low byte -> bytes 0, 1
+constexpr uint32_t k127 = 0x007F007Fu, k255 = 0x00FF00FFu;
+
+// Index of code-order bit v (data bits, then parity bit k + c, c = i mb + r) in the pair layout of the posteriors.
+template <int C>
+__device__ __forceinline__ int lpos_pair(int v) {
+  using T = Code<C>;
+  if (v < T::K) return (v & ~127) + ((v & 63) << 1) + ((v >> 6) & 1);
+  const int c = v - T::K, r = c % T::MB, i = c / T::MB;
+  return T::K + r * 128 + ((i & 63) << 1) + (i >> 6);
+}
+
+// min(|q|, 127) of both halves (q's halves within +-32767)
+__device__ __forceinline__ uint32_t mag127(uint32_t q) { return minu2(maxs2(q, sub2(0u, q)), k127); }
+
+// The check pair's state after pass 1: least and second magnitudes, their scaled messages, the sign parity.
+struct PairCheck {
+  uint32_t s2, dl, nm1_7, sg;
+  __device__ __forceinline__ void finish(uint32_t a1, uint32_t a2, uint32_t b1, uint32_t b2, uint32_t s) {
+    const uint32_t m1 = minu2(a1, b1), m2 = minu2(maxu2(a1, b1), minu2(a2, b2));
+    // (m * 13) >> 4 a half: m <= 127, so m * 13 stays inside its half and the result under 104 (the cap at 127
+    // never binds); the shift's spill from the high half into the low half's top bits is masked off
+    const uint32_t s1 = ((m1 * 13u) >> 4) & 0x0FFF0FFFu;
+    s2 = ((m2 * 13u) >> 4) & 0x0FFF0FFFu;
+    dl = s2 - s1;             // both halves >= 0: no borrow between them
+    nm1_7 = 0u - (m1 << 7);
+    sg = s;
+  }
+  // The message to an edge of extrinsic q (halves): s2 where min(|q|, 127) is the least magnitude, else s1
+  // ((a - m1) << 7 is 0 there and at least 128 > dl elsewhere), negated where the other edges' signs multiply to -1.
+  __device__ __forceinline__ uint32_t msg(uint32_t q) const {
+    const uint32_t t = minu2(dl, (mag127(q) << 7) + nm1_7);
+    const uint32_t mag = s2 - t;
+    const uint32_t neg = prmt(q ^ sg, kSign);
+    return sub2(mag ^ neg, neg);
+  }
+};
+
+__device__ __forceinline__ void fold(uint32_t &m1, uint32_t &m2, uint32_t a) {
+  m2 = minu2(m2, maxu2(m1, a));
+  m1 = minu2(m1, a);
+}
+
+// One layer in the pair form, the row's slots unrolled to the code's widest row (registers hold each edge's
+// extrinsics, word index and permute; the magnitudes are recomputed in pass 2). Pair ip = lane + 32 (P0 + p).
+template <int C, int NP>
+__device__ __forceinline__ void layer_pair(int16_t *L, int8_t *R, int r, int lane, int P0) {
+  using T = Code<C>;
+  constexpr int NDM = T::NDMAX;
+  const DevCode &cd = c_codes[C];
+  const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+  uint32_t *Lw = reinterpret_cast<uint32_t *>(L);
+  uint32_t *Pw = Lw + T::K / 2;   // parity words: row r's pair i at r * 64 + i
+  uint16_t *Rh = reinterpret_cast<uint16_t *>(R) + (p0 + 2 * r) * 64;
+  uint32_t q[NDM][NP], sel[NDM][NP];
+  int w[NDM][NP];
+  uint32_t a1[NP], a2[NP], b1[NP], b2[NP], sg[NP], qp[NP], qo[NP], lp[NP];
+  int wp[NP];
+  uint32_t sp[NP];
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    const int ip = lane + 32 * (P0 + p);
+    // the staircase: previous row's parity (row 0: the last row's, one check back; check 0 has none and takes a
+    // certain zero of 8191), then this row's
+    wp[p] = r > 0 ? (r - 1) * 64 + ip : (T::MB - 1) * 64 + ((ip - 1) & 63);
+    sp[p] = (r == 0 && ip == 0) ? kSwap : kKeep;
+    lp[p] = prmt(Pw[wp[p]], sp[p]);
+    qp[p] = sub2(lp[p], prmt(Rh[nd * 64 + ip], kSext));
+    if (r == 0 && ip == 0) qp[p] = (qp[p] & 0xFFFF0000u) | 8191u;
+    qo[p] = sub2(Pw[r * 64 + ip], prmt(Rh[(nd + 1) * 64 + ip], kSext));
+    a1[p] = mag127(qp[p]); a2[p] = k255;
+    b1[p] = mag127(qo[p]); b2[p] = k255;
+    sg[p] = qp[p] ^ qo[p];
+  }
+#pragma unroll
+  for (int e = 0; e < NDM; e++) {
+    if (e < nd) {
+      const int cs = cd.circ[p0 + e], colw = (cs >> 8) * 64, sh = cs & 255;
+#pragma unroll
+      for (int p = 0; p < NP; p++) {
+        const int d = (lane + 32 * (P0 + p) - sh) & 127;
+        w[e][p] = colw | (d & 63);
+        sel[e][p] = (d & 64) ? kSwap : kKeep;
+        q[e][p] = sub2(prmt(Lw[w[e][p]], sel[e][p]), prmt(Rh[e * 64 + lane + 32 * (P0 + p)], kSext));
+        sg[p] ^= q[e][p];
+        if (e & 1) fold(b1[p], b2[p], mag127(q[e][p]));
+        else fold(a1[p], a2[p], mag127(q[e][p]));
+      }
+    }
+  }
+  PairCheck ck[NP];
+#pragma unroll
+  for (int p = 0; p < NP; p++) ck[p].finish(a1[p], a2[p], b1[p], b2[p], sg[p]);
+#pragma unroll
+  for (int e = 0; e < NDM; e++) {
+    if (e < nd) {
+#pragma unroll
+      for (int p = 0; p < NP; p++) {
+        const uint32_t m = ck[p].msg(q[e][p]);
+        Rh[e * 64 + lane + 32 * (P0 + p)] = (uint16_t)prmt(m, kPack);
+        Lw[w[e][p]] = prmt(add2(q[e][p], m), sel[e][p]);
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    const int ip = lane + 32 * (P0 + p);
+    uint32_t m = ck[p].msg(qp[p]);
+    Rh[nd * 64 + ip] = (uint16_t)prmt(m, kPack);   // check 0's half of row 0 is never read back
+    uint32_t v = add2(qp[p], m);
+    if (r == 0 && ip == 0) v = (v & 0xFFFF0000u) | (lp[p] & 0xFFFFu);   // that column belongs to no check here
+    Pw[wp[p]] = prmt(v, sp[p]);
+    m = ck[p].msg(qo[p]);
+    Rh[(nd + 1) * 64 + ip] = (uint16_t)prmt(m, kPack);
+    Pw[r * 64 + ip] = add2(qo[p], m);
+  }
+}
+
+// The same with the row's data slots in a loop, the extrinsics reloaded and recomputed in pass 2 (the 7/8 code's
+// 21-circulant rows).
+template <int C, int NP>
+__device__ __forceinline__ void layer_pair_loop(int16_t *L, int8_t *R, int r, int lane, int P0) {
+  using T = Code<C>;
+  const DevCode &cd = c_codes[C];
+  const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+  uint32_t *Lw = reinterpret_cast<uint32_t *>(L);
+  uint32_t *Pw = Lw + T::K / 2;
+  uint16_t *Rh = reinterpret_cast<uint16_t *>(R) + (p0 + 2 * r) * 64;
+  uint32_t a1[NP], a2[NP], b1[NP], b2[NP], sg[NP], qp[NP], qo[NP], lp[NP];
+  int wp[NP];
+  uint32_t sp[NP];
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    const int ip = lane + 32 * (P0 + p);
+    wp[p] = r > 0 ? (r - 1) * 64 + ip : (T::MB - 1) * 64 + ((ip - 1) & 63);
+    sp[p] = (r == 0 && ip == 0) ? kSwap : kKeep;
+    lp[p] = prmt(Pw[wp[p]], sp[p]);
+    qp[p] = sub2(lp[p], prmt(Rh[nd * 64 + ip], kSext));
+    if (r == 0 && ip == 0) qp[p] = (qp[p] & 0xFFFF0000u) | 8191u;
+    qo[p] = sub2(Pw[r * 64 + ip], prmt(Rh[(nd + 1) * 64 + ip], kSext));
+    a1[p] = mag127(qp[p]); a2[p] = k255;
+    b1[p] = mag127(qo[p]); b2[p] = k255;
+    sg[p] = qp[p] ^ qo[p];
+  }
+  for (int e = 0; e < nd; e++) {
+    const int cs = cd.circ[p0 + e], colw = (cs >> 8) * 64, sh = cs & 255;
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+      const int d = (lane + 32 * (P0 + p) - sh) & 127;
+      const uint32_t q = sub2(prmt(Lw[colw | (d & 63)], (d & 64) ? kSwap : kKeep), prmt(Rh[e * 64 + lane + 32 * (P0 + p)], kSext));
+      sg[p] ^= q;
+      fold(a1[p], a2[p], mag127(q));
+    }
+  }
+  PairCheck ck[NP];
+#pragma unroll
+  for (int p = 0; p < NP; p++) ck[p].finish(a1[p], a2[p], b1[p], b2[p], sg[p]);
+  for (int e = 0; e < nd; e++) {
+    const int cs = cd.circ[p0 + e], colw = (cs >> 8) * 64, sh = cs & 255;
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+      const int d = (lane + 32 * (P0 + p) - sh) & 127, wi = colw | (d & 63);
+      const uint32_t sl = (d & 64) ? kSwap : kKeep;
+      uint16_t *rp = Rh + e * 64 + lane + 32 * (P0 + p);
+      const uint32_t q = sub2(prmt(Lw[wi], sl), prmt(*rp, kSext));
+      const uint32_t m = ck[p].msg(q);
+      *rp = (uint16_t)prmt(m, kPack);
+      Lw[wi] = prmt(add2(q, m), sl);
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    const int ip = lane + 32 * (P0 + p);
+    uint32_t m = ck[p].msg(qp[p]);
+    Rh[nd * 64 + ip] = (uint16_t)prmt(m, kPack);
+    uint32_t v = add2(qp[p], m);
+    if (r == 0 && ip == 0) v = (v & 0xFFFF0000u) | (lp[p] & 0xFFFFu);
+    Pw[wp[p]] = prmt(v, sp[p]);
+    m = ck[p].msg(qo[p]);
+    Rh[(nd + 1) * 64 + ip] = (uint16_t)prmt(m, kPack);
+    Pw[r * 64 + ip] = add2(qo[p], m);
+  }
+}
+
+// unsat in the pair form: the sign bits (15 and 31) of the XOR of a check pair's posteriors.
+template <int C, int NP>
+__device__ __forceinline__ int unsat_pair(const int16_t *L, int lane, int P0, int count, int rev) {
+  using T = Code<C>;
+  constexpr int NDM = T::NDMAX;
+  const DevCode &cd = c_codes[C];
+  const uint32_t *Lw = reinterpret_cast<const uint32_t *>(L);
+  const uint32_t *Pw = Lw + T::K / 2;
+  int bad = 0;
+  for (int k = 0; k < T::MB; k++) {
+    const int r = rev ? T::MB - 1 - k : k;
+    const int p0 = cd.rowptr[r], nd = cd.rowptr[r + 1] - p0;
+    uint32_t x[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+      const int ip = lane + 32 * (P0 + p);
+      uint32_t prev;
+      if (r > 0) prev = Pw[(r - 1) * 64 + ip];
+      else prev = ip == 0 ? prmt(Pw[(T::MB - 1) * 64 + 63], kSwap) & 0xFFFF0000u : Pw[(T::MB - 1) * 64 + ip - 1];
+      x[p] = Pw[r * 64 + ip] ^ prev;
+    }
+#pragma unroll
+    for (int e = 0; e < NDM; e++) {
+      if (e < nd) {
+        const int cs = cd.circ[p0 + e], colw = (cs >> 8) * 64, sh = cs & 255;
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+          const int d = (lane + 32 * (P0 + p) - sh) & 127;
+          x[p] ^= prmt(Lw[colw | (d & 63)], (d & 64) ? kSwap : kKeep);
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; p++) bad += __popc(x[p] & 0x80008000u);
+    if (!count && __any_sync(0xffffffffu, bad)) return 1;
+  }
+  return count ? __reduce_add_sync(0xffffffffu, bad) : 0;
+}
+
 // The WPC warps of one codeword meet here between layers (a named barrier a codeword; 0 is __syncthreads').
 template <int WPC>
 __device__ __forceinline__ void group_sync(int g) {
@@ -278,10 +523,22 @@ __device__ __forceinline__ void group_sync(int g) {
   else asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(WPC * 32) : "memory");
 }
 
-template <int C, int WPC, bool LOOP>
+// Index of code-order bit v in the posteriors: the pair layout, or data bits in order then parity bit k + c
+// (c = i mb + r) at [r][i].
+template <int C, bool PAIR>
+__device__ __forceinline__ int lpos(int v) {
+  using T = Code<C>;
+  if (PAIR) return lpos_pair<C>(v);
+  if (v < T::K) return v;
+  const int c = v - T::K;
+  return T::K + (c % T::MB) * 128 + c / T::MB;
+}
+
+template <int C, int WPC, bool LOOP, bool PAIR>
 __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(LdpcLaunch a) {
   using T = Code<C>;
-  constexpr int CPL = 4 / WPC, GT = WPC * 32;
+  constexpr int CPL = 4 / WPC, GT = WPC * 32, NP = PAIR ? 2 / WPC : 1;
+  static_assert(!PAIR || WPC <= 2, "the pair form runs 64 check pairs a layer on one or two warps");
   static_assert(cta_threads<C, WPC>() <= 1024, "a CTA of at most 1024 threads");
   static_assert(T::WARPS <= 15, "one named barrier a codeword");
   extern __shared__ __align__(16) uint8_t smem[];
@@ -328,10 +585,9 @@ __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(L
         const int v = perm[i];
         const int8_t x = sl[i];
         const int8_t y = wh[i] ? (int8_t)(-x) : x;
-        if (v < T::K) L[v] = y;
-        else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = y; }
+        L[lpos<C, PAIR>(v)] = y;
       }
-      for (int v = LIZG_INFO_BITS + tg; v < T::K; v += GT) L[v] = 127;
+      for (int v = LIZG_INFO_BITS + tg; v < T::K; v += GT) L[lpos<C, PAIR>(v)] = 127;
     } else {
       cw = a.list[item];
       off = a.off[cw];
@@ -342,9 +598,7 @@ __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(L
         const int8_t *bb = reinterpret_cast<const int8_t *>(&w);
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-          const int v = t * 16 + j;
-          if (v < T::K) L[v] = bb[j];
-          else { const int c = v - T::K; L[T::K + (c % T::MB) * 128 + c / T::MB] = bb[j]; }
+          L[lpos<C, PAIR>(t * 16 + j)] = bb[j];
         }
       }
     }
@@ -357,13 +611,15 @@ __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(L
     for (int it = 0; it < a.max_iter; it++) {
       for (int step = 0; step < T::MB; step++) {
         const int r = (it & 1) ? T::MB - 1 - step : step;
-        if (LOOP) layer_loop<C, CPL>(L, R, r, lane, t0);
+        if (PAIR && LOOP) layer_pair_loop<C, NP>(L, R, r, lane, sub * NP);
+        else if (PAIR) layer_pair<C, NP>(L, R, r, lane, sub * NP);
+        else if (LOOP) layer_loop<C, CPL>(L, R, r, lane, t0);
         else layer<C, CPL>(L, R, r, lane, t0);
         group_sync<WPC>(g);
       }
       // the count only where the stall rule reads it (after the first iteration and at stall_it), else a clear test
       const bool counted = a.stall_it > 1 && (it == 0 || it == a.stall_it - 1);
-      int bad = unsat<C, CPL>(L, lane, t0, counted, it & 1);
+      int bad = PAIR ? unsat_pair<C, NP>(L, lane, sub * NP, counted, it & 1) : unsat<C, CPL>(L, lane, t0, counted, it & 1);
       if (WPC > 1) {
         if (lane == 0) s_red[g][sub] = bad;
         group_sync<WPC>(g);
@@ -385,9 +641,7 @@ __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(L
 #pragma unroll
       for (int t = 0; t < 8; t++) {
         const int v = 8 * j + t;
-        int16_t x;
-        if (v < T::K) x = L[v];
-        else { const int c = v - T::K; x = L[T::K + (c % T::MB) * 128 + c / T::MB]; }
+        const int16_t x = L[lpos<C, PAIR>(v)];
         byte = (byte << 1) | (x < 0);
       }
       pk[j] = (uint8_t)byte;
@@ -453,14 +707,15 @@ cudaError_t ldpc_upload_tables() {
 // and keeps the fastest per code.
 struct Variant {
   int wpc;
-  bool loop;
+  bool loop, pair;
 };
-constexpr int kMaxVariants = 4;
+constexpr int kMaxVariants = 8;
 static const Variant kVariants[4][kMaxVariants] = {
-    {{2, true}, {1, true}, {2, false}, {0, false}},   // 7/8: 21-circulant rows, the loop form first
-    {{2, false}, {1, true}, {4, false}, {2, true}},    // 3/4
-    {{2, false}, {1, true}, {4, false}, {0, false}},   // 2/3
-    {{4, false}, {2, false}, {1, false}, {0, false}},  // 1/2
+    // 7/8: 21-circulant rows, the loop form first
+    {{2, true, false}, {1, true, false}, {2, false, false}, {2, true, true}, {2, false, true}, {1, true, true}},
+    {{2, false, false}, {1, true, false}, {4, false, false}, {2, true, false}, {2, false, true}, {1, false, true}},   // 3/4
+    {{2, false, false}, {1, true, false}, {4, false, false}, {2, false, true}, {1, false, true}},                     // 2/3
+    {{4, false, false}, {2, false, false}, {1, false, false}, {2, false, true}, {1, false, true}},                    // 1/2
 };
 static int variant_count(int code) {
   int k = 0;
@@ -479,35 +734,44 @@ static int choice_of(int code) {
   return dev >= 0 && dev < kMaxDevices ? g_choice[dev][code] : 0;
 }
 
-template <int C, int WPC, bool LOOP>
+template <int C, int WPC, bool LOOP, bool PAIR>
 static cudaError_t launch_v(const LdpcLaunch &a, int sms, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(ldpc_decode_kernel<C, WPC, LOOP>, cudaFuncAttributeMaxDynamicSharedMemorySize, cta_smem<C>());
+    cudaError_t e = cudaFuncSetAttribute(ldpc_decode_kernel<C, WPC, LOOP, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, cta_smem<C>());
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   const int need = (a.count + Code<C>::WARPS - 1) / Code<C>::WARPS;
   const int grid = need < sms ? need : sms;
-  ldpc_decode_kernel<C, WPC, LOOP><<<grid, cta_threads<C, WPC>(), cta_smem<C>(), st>>>(a);
+  ldpc_decode_kernel<C, WPC, LOOP, PAIR><<<grid, cta_threads<C, WPC>(), cta_smem<C>(), st>>>(a);
   return cudaGetLastError();
 }
 
 static cudaError_t launch_variant(int code, int v, const LdpcLaunch &a, int sms, cudaStream_t st) {
   switch (code * kMaxVariants + v) {
-    case 0: return launch_v<0, 2, true>(a, sms, st);
-    case 1: return launch_v<0, 1, true>(a, sms, st);
-    case 2: return launch_v<0, 2, false>(a, sms, st);
-    case 4: return launch_v<1, 2, false>(a, sms, st);
-    case 5: return launch_v<1, 1, true>(a, sms, st);
-    case 6: return launch_v<1, 4, false>(a, sms, st);
-    case 7: return launch_v<1, 2, true>(a, sms, st);
-    case 8: return launch_v<2, 2, false>(a, sms, st);
-    case 9: return launch_v<2, 1, true>(a, sms, st);
-    case 10: return launch_v<2, 4, false>(a, sms, st);
-    case 12: return launch_v<3, 4, false>(a, sms, st);
-    case 13: return launch_v<3, 2, false>(a, sms, st);
-    case 14: return launch_v<3, 1, false>(a, sms, st);
+    case 0: return launch_v<0, 2, true, false>(a, sms, st);
+    case 1: return launch_v<0, 1, true, false>(a, sms, st);
+    case 2: return launch_v<0, 2, false, false>(a, sms, st);
+    case 3: return launch_v<0, 2, true, true>(a, sms, st);
+    case 4: return launch_v<0, 2, false, true>(a, sms, st);
+    case 5: return launch_v<0, 1, true, true>(a, sms, st);
+    case 8: return launch_v<1, 2, false, false>(a, sms, st);
+    case 9: return launch_v<1, 1, true, false>(a, sms, st);
+    case 10: return launch_v<1, 4, false, false>(a, sms, st);
+    case 11: return launch_v<1, 2, true, false>(a, sms, st);
+    case 12: return launch_v<1, 2, false, true>(a, sms, st);
+    case 13: return launch_v<1, 1, false, true>(a, sms, st);
+    case 16: return launch_v<2, 2, false, false>(a, sms, st);
+    case 17: return launch_v<2, 1, true, false>(a, sms, st);
+    case 18: return launch_v<2, 4, false, false>(a, sms, st);
+    case 19: return launch_v<2, 2, false, true>(a, sms, st);
+    case 20: return launch_v<2, 1, false, true>(a, sms, st);
+    case 24: return launch_v<3, 4, false, false>(a, sms, st);
+    case 25: return launch_v<3, 2, false, false>(a, sms, st);
+    case 26: return launch_v<3, 1, false, false>(a, sms, st);
+    case 27: return launch_v<3, 2, false, true>(a, sms, st);
+    case 28: return launch_v<3, 1, false, true>(a, sms, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -535,7 +799,7 @@ int lizg_ldpc_variant(int rate, int32_t *wpc, int32_t *loop_form) {
   if (int rc = lizg::device_ready(&sms)) return rc;
   const int v = lizg::choice_of(c);
   if (wpc) *wpc = lizg::kVariants[c][v].wpc;
-  if (loop_form) *loop_form = lizg::kVariants[c][v].loop ? 1 : 0;
+  if (loop_form) *loop_form = (lizg::kVariants[c][v].loop ? 1 : 0) | (lizg::kVariants[c][v].pair ? 2 : 0);
   return v;
 }
 

@@ -89,7 +89,7 @@ def test_fmt_geometry_matches_oracle():
 
 
 def test_decoder_variants_listed():
-    assert [lz.ldpc_variants(r) for r in (6, 4, 3, 2)] == [3, 4, 3, 3]
+    assert [lz.ldpc_variants(r) for r in (6, 4, 3, 2)] == [6, 6, 5, 5]
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU behaviour")
