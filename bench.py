@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--fmt-only", action="store_true", help="time only the format word and the border nodes (profiling)")
     ap.add_argument("--encode-only", action="store_true", help="time only the sender on the GPU (profiling)")
     ap.add_argument("--refine-only", action="store_true", help="time only the distorted captures' registration comparison")
+    ap.add_argument("--ldpc-variants", action="store_true", help="time every decoder kernel variant of every code on the "
+                    "workload's codewords of that code (device-resident), outputs checked identical across variants")
     return ap.parse_args()
 
 
@@ -822,6 +824,49 @@ def run_reference(args, rank, ws):
                       "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def bench_ldpc_variants(args, stream):
+    """Each code's codewords of the workload batch decoded by every kernel variant of that code: ms a decode of them,
+    and whether bits and iteration counts equal variant 0's. Launch order: code by code (7/8, 3/4, 2/3, 1/2), variant
+    by variant, 2 untimed then 5 timed launches each."""
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300 import synth
+    b = synth.ldpc_batch(args.count, seed=1000)
+    out = {}
+    for name, r in zip(("7/8", "3/4", "2/3", "1/2"), (6, 4, 3, 2)):
+        sel = np.nonzero(b["rates"] == r)[0]
+        n = lz.CODE_N[r]
+        llr = np.concatenate([b["llr"][b["offsets"][i]:b["offsets"][i] + n] for i in sel])
+        plan = lz.LdpcPlan(np.full(sel.size, r, np.int32), MAX_ITER, STALL_IT, STALL_RATIO)
+        d_llr = torch.from_numpy(llr).cuda()
+        d_bits = torch.empty(plan.llr_bytes // 8, dtype=torch.uint8, device="cuda")
+        d_its = torch.empty(plan.count, dtype=torch.int32, device="cuda")
+        d_ok = torch.empty(plan.count, dtype=torch.uint8, device="cuda")
+        run = lambda: plan.run_dev(d_llr.data_ptr(), d_bits.data_ptr(), d_its.data_ptr(), d_ok.data_ptr(), stream.cuda_stream)
+        first, rows = None, []
+        for v in range(lz.ldpc_variants(r)):
+            lz.ldpc_set_variant(r, v)
+            for _ in range(2):
+                run()
+            torch.cuda.synchronize()
+            got = (d_bits.cpu().numpy(), d_its.cpu().numpy())
+            first = first or got
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(5):
+                run()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            _, wpc, loop, pair = lz.ldpc_variant(r)
+            rows.append({"index": v, "warps_a_codeword": wpc, "loop_form": loop, "pair_form": pair,
+                         "ms": round(e0.elapsed_time(e1) / 5, 3),
+                         "identical": bool(np.array_equal(got[0], first[0]) and np.array_equal(got[1], first[1]))})
+        lz.ldpc_set_variant(r, 0)
+        out[name] = {"codewords": int(sel.size), "variants": rows}
+    return out
+
+
 def main():
     args = parse()
     rank, ws, local = dist_init()
@@ -847,6 +892,9 @@ def main():
         return
     if args.encode_only:
         print(json.dumps({"sender": bench_encoder(args, torch.cuda.current_stream())}))
+        return
+    if args.ldpc_variants:
+        print(json.dumps({"ldpc_variants": bench_ldpc_variants(args, torch.cuda.current_stream())}))
         return
     tune = None
     if not args.no_autotune:
