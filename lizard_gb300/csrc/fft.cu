@@ -342,7 +342,7 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, i
 // y, and the two real columns of each line separated: A(v) = (Z(v) + conj Z(n - v)) / 2, B(v) = -i (Z(v) - conj
 // Z(n - v)) / 2, written to Y[f][v][x] for the kept rows v.
 template <int N>
-__global__ void __launch_bounds__(kThreads, 2) fft_cols_kernel(FftDev xd, SrcDev src, int bands, const double *hole, double *part, float2 *Y) {
+__global__ void __launch_bounds__(kThreads, 3) fft_cols_kernel(FftDev xd, SrcDev src, int bands, const double *hole, double *part, float2 *Y) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
   const SmemMap sm = smem_map<N>(smraw);
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const do
 // spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0. The used
 // coefficients go straight to their place in pos order: C[f][tpos[v][u]] (tpos -1 where (u, v) is not used).
 template <int N>
-__global__ void __launch_bounds__(kThreads, 2) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, const int32_t *tpos,
+__global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, const int32_t *tpos,
                                                                int need, float2 *C) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N);
