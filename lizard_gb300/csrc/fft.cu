@@ -1,9 +1,11 @@
 // Row (b) of the hot path on sm_103a: the anchors' erase, the detrend projections and the 2D mixed-radix FFT of the
 // n x n picture grid, restated from the reference's decode (liblizard/src/lizard_phy.c:1596-1716) for the GPU.
 //
-// Four kernels a batch:
+// Four kernels a batch (five when the samples come straight from captured frames):
 //   hole_rhs_kernel   a CTA takes a band of the frame's every-eighth-sample rows: the shading fit's right-hand side
 //                     over the samples outside the anchors' squares, one partial sum a band (6 doubles);
+//   cell_table_kernel (captured frames only) each picture row's homography terms and the mesh displacement line of
+//                     each mesh cell along it, so the column pass reads them instead of walking the mesh per sample;
 //   fft_cols_kernel   a CTA takes 2L picture columns of a frame (L complex lines: column x0 + l real, x0 + L + l
 //                     imaginary), forms the shading surface beta from the bands' partials, erases the anchors' squares
 //                     as it loads them, sums each column's detrend moments, transforms the L lines along y in shared
@@ -288,31 +290,53 @@ __device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta
   return (float)h;
 }
 
+// The sampler's per-row quantities of a batch, worked out once a frame before the column pass reads them: for
+// picture row y and mesh cell i < nx - 1 the displacement line cell_terms gives, and at i = nx - 1 the homography's
+// row terms (kw, ku, kv). The same functions and inputs as the per-sample walk (the cell's 1 / width as the column
+// table computes it), so the column pass reads the walk's own values. A thread an entry, entries in table order.
+__global__ void __launch_bounds__(256) cell_table_kernel(SrcDev src, int per_frame, float4 *ctab) {
+  const int f = blockIdx.y, t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= per_frame) return;
+  const SampleDev &sd = src.sd;
+  const int nn = sd.nx, y = t / nn, i = t - y * nn;
+  const float *H = src.reg + (int64_t)f * src.regstride;
+  const RowTerms r = row_terms(H, sd.rowt[y]);
+  float4 o;
+  if (i == nn - 1) {
+    o = make_float4(r.kw, r.ku, r.kv, 0.0f);
+  } else {
+    const float inv = __fdiv_rn(1.0f, __fsub_rn(sd.node_x[i + 1], sd.node_x[i]));
+    const CellTerms c = cell_terms(sd, H + 9, i, inv, r);
+    o = make_float4(c.ex, c.cx, c.ey, c.cy);
+  }
+  ctab[(int64_t)f * per_frame + t] = o;
+}
+
 // One column tile's samples: thread t takes line l = t mod L (columns xa = x0 + l as the real part, xb = x0 + L + l as
 // the imaginary part) at rows y = t / L, t / L + kThreads / L, ...; the anchors' squares erased to the shading
 // surface as they are read. Each row's two samples are summed into the five detrend projections' raw sums, z c(x),
 // z c(y), z c(x) c(y), z q(x), z q(y) (liblizard/src/lizard_phy.c:1584-1591, 1657-1667), in p.
 template <int N, bool GRID>
-__device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, int f, int x0, const double *beta, float2 *line, float p[5]) {
+__device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, const float4 *ctab, int f, int x0, const double *beta,
+                                          float2 *line, float p[5]) {
   constexpr int L = plan_of(N).lines, ystep = kThreads / L;
   const int l = threadIdx.x % L, xa = x0 + l, xb = x0 + L + l;
   const bool ina = in_square(xd, xa), inb = in_square(xd, xb);
   const float cxa = __ldg(xd.cx + xa), qxa = __ldg(xd.qx + xa), cxb = __ldg(xd.cx + xb), qxb = __ldg(xd.qx + xb);
-  float Hr[9], mxa = 0, mxb = 0, h6a = 0, h0a = 0, h3a = 0, h6b = 0, h0b = 0, h3b = 0, inva = 0, invb = 0;
-  int ia = 0, ib = 0;
-  const float *nodes = nullptr;
+  float mxa = 0, mxb = 0, h6a = 0, h0a = 0, h3a = 0, h6b = 0, h0b = 0, h3b = 0;
+  int ia = 0, ib = 0, nn = 1;
   const uint8_t *px = nullptr;
+  const float4 *T = nullptr;   // the frame's row and cell table, row y at T + y nn
   if (!GRID) {
     const float *H = src.reg + (int64_t)f * src.regstride;
-#pragma unroll
-    for (int k = 0; k < 9; k++) Hr[k] = H[k];
-    nodes = H + 9;
+    nn = src.sd.nx;
+    T = ctab + (int64_t)f * N * nn;
     px = src.luma + f * src.fstride;
     const float4 ca = src.sd.colt[xa], cb = src.sd.colt[xb];
-    mxa = ca.x; ia = __float_as_int(ca.y); inva = ca.z;
-    mxb = cb.x; ib = __float_as_int(cb.y); invb = cb.z;
-    h6a = __fmul_rn(Hr[6], mxa); h0a = __fmul_rn(Hr[0], mxa); h3a = __fmul_rn(Hr[3], mxa);
-    h6b = __fmul_rn(Hr[6], mxb); h0b = __fmul_rn(Hr[0], mxb); h3b = __fmul_rn(Hr[3], mxb);
+    mxa = ca.x; ia = __float_as_int(ca.y);
+    mxb = cb.x; ib = __float_as_int(cb.y);
+    h6a = __fmul_rn(H[6], mxa); h0a = __fmul_rn(H[0], mxa); h3a = __fmul_rn(H[3], mxa);
+    h6b = __fmul_rn(H[6], mxb); h0b = __fmul_rn(H[0], mxb); h3b = __fmul_rn(H[3], mxb);
   }
 #pragma unroll 4
   for (int y = threadIdx.x / L; y < N; y += ystep) {
@@ -322,9 +346,11 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, i
       const float *g = src.grid + f * src.gstride + (int64_t)y * N;
       va = g[xa]; vb = g[xb];
     } else {
-      const RowTerms r = row_terms(Hr, src.sd.rowt[y]);
-      const CellTerms ca = cell_terms(src.sd, nodes, ia, inva, r);
-      const CellTerms cb = ib == ia ? ca : cell_terms(src.sd, nodes, ib, invb, r);
+      const float4 *Ty = T + y * nn;
+      const float4 rt = Ty[nn - 1], ta = Ty[ia], tb = ib == ia ? ta : Ty[ib];
+      RowTerms r;
+      r.kw = rt.x; r.ku = rt.y; r.kv = rt.z;
+      const CellTerms ca{ta.x, ta.y, ta.z, ta.w}, cb{tb.x, tb.y, tb.z, tb.w};
       va = sample_at(px, src.w, src.h, src.pitch, mxa, h6a, h0a, h3a, r, ca);
       vb = sample_at(px, src.w, src.h, src.pitch, mxb, h6b, h0b, h3b, r, cb);
     }
@@ -342,7 +368,8 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, i
 // y, and the two real columns of each line separated: A(v) = (Z(v) + conj Z(n - v)) / 2, B(v) = -i (Z(v) - conj
 // Z(n - v)) / 2, written to Y[f][v][x] for the kept rows v.
 template <int N>
-__global__ void __launch_bounds__(kThreads, 3) fft_cols_kernel(FftDev xd, SrcDev src, int bands, const double *hole, double *part, float2 *Y) {
+__global__ void __launch_bounds__(kThreads, 3) fft_cols_kernel(FftDev xd, SrcDev src, const float4 *ctab, int bands, const double *hole, double *part,
+                                                                float2 *Y) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
   const SmemMap sm = smem_map<N>(smraw);
@@ -370,8 +397,8 @@ __global__ void __launch_bounds__(kThreads, 3) fft_cols_kernel(FftDev xd, SrcDev
     }
     __syncthreads();
     float p[5] = {0, 0, 0, 0, 0};
-    if (src.grid) load_tile<N, true>(xd, src, f, x0, s_beta, line, p);
-    else load_tile<N, false>(xd, src, f, x0, s_beta, line, p);
+    if (src.grid) load_tile<N, true>(xd, src, ctab, f, x0, s_beta, line, p);
+    else load_tile<N, false>(xd, src, ctab, f, x0, s_beta, line, p);
 #pragma unroll
     for (int q = 0; q < 5; q++)
       for (int o = 16; o > 0; o >>= 1) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
@@ -487,7 +514,12 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
   (void)sms;
   const int bands = fft_hole_bands(N), rtiles = (xd.vrows + L - 1) / L;
   hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
-  fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, bands, b.hole, b.part, b.Y);
+  if (!src.grid) {
+    if (!b.ctab) return cudaErrorInvalidValue;
+    const int per_frame = N * src.sd.nx;
+    cell_table_kernel<<<dim3((per_frame + 255) / 256, frames), 256, 0, st>>>(src, per_frame, b.ctab);
+  }
+  fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, b.ctab, bands, b.hole, b.part, b.Y);
   fac_kernel<<<frames, 256, 0, st>>>(xd, tiles, b.part, b.fac);
   fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, b.Y, b.tpos, b.need, b.C);
   return cudaGetLastError();

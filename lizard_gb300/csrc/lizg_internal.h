@@ -44,6 +44,10 @@ struct FftBufs {
   const int32_t *tpos;               // vrows x n: the pos index of spectrum point (u mod n, v), -1 where unused
   int need;                          // used coefficients a frame (subch x 320)
   float2 *C;                         // frames x need: the detrended spectrum's used coefficients in pos order
+  // frames x n x nx: for each picture row y of a frame, the mesh displacement line of each cell i < nx - 1 (ex, cx,
+  // ey, cy, as cell_terms gives them) and at i = nx - 1 the homography's row terms (kw, ku, kv, 0); filled before
+  // the column pass when the samples come straight from captured frames
+  float4 *ctab;
 };
 
 // The transform CTA's dynamic shared memory bound and the complex points its lines hold at most.

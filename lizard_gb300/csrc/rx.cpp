@@ -35,6 +35,7 @@ struct lizg_rx {
   float *node_xy = nullptr;
   float4 *sample_t = nullptr;
   float2 *Y = nullptr, *C = nullptr;   // column transforms' kept rows; the spectrum's used coefficients in pos order
+  float4 *ctab = nullptr;              // the sampler's row and mesh-cell terms, frames x n x nx
   int32_t *tpos = nullptr;             // vrows x n: the pos index of each kept spectrum point, -1 where unused
   // per-tier streams, forked from and joined to the caller's
   cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -164,6 +165,7 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   ok(dev_alloc(r, &r->fac, F * (2 * (size_t)n + r->xd.vrows)));
   ok(dev_alloc(r, &r->part, F * (size_t)(n / 2) * 5));   // column tiles (at most n / 2) x 5
   ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
+  ok(dev_alloc(r, &r->ctab, F * n * (size_t)r->sd.nx));
   ok(dev_alloc(r, &r->C, F * need));
   {
     std::vector<int32_t> tp((size_t)r->xd.vrows * n, -1);
@@ -312,10 +314,10 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
 static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const lizg_rx_out *out, float *d_coef, cudaStream_t st, int sms) {
   const int need = r->f.subch * lizg::kSub;
   float2 *C = d_coef ? reinterpret_cast<float2 *>(d_coef) : r->C;   // the caller's spectrum buffer when given
-  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, C};
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, C, r->ctab};
   cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
-  r->launches += 4;
+  r->launches += src.grid ? 4 : 5;   // the luma source adds the sampler's row and cell table
   return finish_spec(r, C, need, frames, out, st, sms);
 }
 
@@ -338,7 +340,7 @@ int lizg_rx_spectrum_grid_dev(lizg_rx *r, const float *d_grid, int frames, float
   lizg::SrcDev src{};
   src.grid = d_grid; src.gstride = (int64_t)r->f.n * r->f.n; src.sd = r->sd;
   const int need = r->f.subch * lizg::kSub;
-  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, reinterpret_cast<float2 *>(d_coef)};
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, reinterpret_cast<float2 *>(d_coef), r->ctab};
   cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, static_cast<cudaStream_t>(stream));
   r->launches = 4;
   return e == cudaSuccess ? 0 : lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_spectrum_grid_dev: ") + cudaGetErrorString(e)).c_str());

@@ -49,7 +49,7 @@ def test_engine_matches_each_receiver():
             for k in ("blocks", "ok", "its"):
                 assert np.array_equal(o[k].cpu().numpy(), want[i][k]), (rep, i, k)
             assert want[i]["ok"].all()
-    assert eng.launches == sum(4 + 3 + f.tiers for f in eng.formats)
+    assert eng.launches == sum(5 + 3 + f.tiers for f in eng.formats)
     eng.close()
 
 

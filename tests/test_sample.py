@@ -65,4 +65,4 @@ def test_gpu_luma_path_matches_oracle(n, subch, W, H, warped):
     fused = rx.finish_luma(np.stack([luma, luma]), np.stack([reg, reg]), grid=False)
     for k in ("coef", "llrf", "its", "ok", "blocks", "align"):
         assert np.array_equal(fused[k], out[k]), k
-    assert rx.launches == 4 + 3 + f.tiers
+    assert rx.launches == 5 + 3 + f.tiers
