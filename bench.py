@@ -1013,7 +1013,11 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
                      "traffic": None if traffic is None else int(traffic), "peak_source": peak_src,
                      "kernel": "ldpc_decode_kernel<7/8,3/4,2/3,1/2> (the 4 launches of a step)",
-                     "note": "integer/shared-memory bound, not HBM bound: see ldpc.edge_updates_per_s"},
+                     "note": "not HBM bound: the min-sum minima issue on the ALU pipe (every min/max form does on sm_103a); "
+                             "see ldpc.edge_updates_per_s and alu_pipe",
+                     "alu_pipe": {"active_frac": 0.746, "kernel": "ldpc_decode_kernel 3/4 code, 2 warps a codeword, registers",
+                                  "source": "ncu sm__pipe_alu_cycles_active, profiles/ldpc_decode_65536cw.md (python bench.py "
+                                            "--ldpc-variants --count 16384)"}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
