@@ -14,7 +14,9 @@ OUT = os.path.join(HERE, "liblizard_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
+# Host code rounds once an operation on every host (gcc contracts a * b + c into one fused operation by default on
+# aarch64, not on x86-64), so the library's host-side tables are the same numbers wherever it is built.
+COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 # Translation units whose float and double arithmetic must round once an operation, in source order (no fused
 # multiply-add): they reproduce the reference's soft values bit for bit.
 EXACT = {"demap.cu": ["-fmad=false"], "sample.cu": ["-fmad=false"], "anchor.cu": ["-fmad=false"], "refine.cu": ["-fmad=false"], "ingest.cu": ["-fmad=false"],

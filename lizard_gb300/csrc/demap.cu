@@ -112,6 +112,9 @@ __device__ __forceinline__ double axis_info(double g) { return g > 0 ? pow(1 - p
 // in order (the reference's four float chains) and the chains are added (c0 + c1) + (c2 + c3); one thread a
 // sub-channel then works out the scale in double (so a warp's double work serves 32 sub-channels); the soft values
 // are each axis times 8 k, NaN to 0, clamped to +-80, rounded half to even.
+constexpr int kDemapBatch = 8;   // 320 / 4 = 80 coefficients a lane, 10 batches
+static_assert(kSubDev % (4 * kDemapBatch) == 0, "whole batches");
+
 __global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
                                                     int8_t *llrf, double *sub_est, float *sub_rms) {
   __shared__ float s_m[64][2], s_k8[64];
@@ -123,11 +126,19 @@ __global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spe
   const float dx = live ? align[3 * f] : 0, dy = live ? align[3 * f + 1] : 0;
   float m2 = 0, m4 = 0;
   if (live) {
-    for (int s = qd; s < kSubDev; s += 4) {
-      const int i = j * kSubDev + s;
-      const float2 y = turn ? turned(fd, sp, i, dx, dy) : sp[i];
-      const float e = y.x * y.x + y.y * y.y;
-      m2 = m2 + e; m4 = m4 + e * e;
+    // eight of the lane's coefficients loaded at a time (independent loads in flight), then summed in order
+    for (int s0 = qd; s0 < kSubDev; s0 += 4 * kDemapBatch) {
+      float2 y[kDemapBatch];
+#pragma unroll
+      for (int b = 0; b < kDemapBatch; b++) {
+        const int i = j * kSubDev + s0 + 4 * b;
+        y[b] = turn ? turned(fd, sp, i, dx, dy) : sp[i];
+      }
+#pragma unroll
+      for (int b = 0; b < kDemapBatch; b++) {
+        const float e = y[b].x * y[b].x + y[b].y * y[b].y;
+        m2 = m2 + e; m4 = m4 + e * e;
+      }
     }
   }
   // (c0 + c1) + (c2 + c3)
@@ -156,16 +167,23 @@ __global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spe
   if (!live) return;
   const float k8 = s_k8[grp];
   int8_t *out = llrf + (int64_t)f * fd.subch * 2 * kSubDev + 2 * j * kSubDev;
-  for (int s = qd; s < kSubDev; s += 4) {
-    const int i = j * kSubDev + s;
-    const float2 y = turn ? turned(fd, sp, i, dx, dy) : sp[i];
-    float x = k8 * y.x, z = k8 * y.y;
-    x = x != x ? 0.0f : fminf(fmaxf(x, -80.0f), 80.0f);
-    z = z != z ? 0.0f : fminf(fmaxf(z, -80.0f), 80.0f);
-    char2 v;
-    v.x = (signed char)__float2int_rn(x);
-    v.y = (signed char)__float2int_rn(z);
-    *reinterpret_cast<char2 *>(out + 2 * s) = v;
+  for (int s0 = qd; s0 < kSubDev; s0 += 4 * kDemapBatch) {
+    float2 y[kDemapBatch];
+#pragma unroll
+    for (int b = 0; b < kDemapBatch; b++) {
+      const int i = j * kSubDev + s0 + 4 * b;
+      y[b] = turn ? turned(fd, sp, i, dx, dy) : sp[i];
+    }
+#pragma unroll
+    for (int b = 0; b < kDemapBatch; b++) {
+      float x = k8 * y[b].x, z = k8 * y[b].y;
+      x = x != x ? 0.0f : fminf(fmaxf(x, -80.0f), 80.0f);
+      z = z != z ? 0.0f : fminf(fmaxf(z, -80.0f), 80.0f);
+      char2 v;
+      v.x = (signed char)__float2int_rn(x);
+      v.y = (signed char)__float2int_rn(z);
+      *reinterpret_cast<char2 *>(out + 2 * (s0 + 4 * b)) = v;
+    }
   }
 }
 
