@@ -461,8 +461,13 @@ __global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const 
   const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
   for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
   const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
-  for (int l = 0; l < Lr; l++)
-    for (int u = tid; u < n; u += kThreads) sm.buf[l * LSTR + pad(u)] = Yf[(int64_t)l * n + u];
+  // the tile's rows into the padded lines by 8-byte asynchronous copies, all in flight at once
+  for (int t = tid; t < Lr * n; t += kThreads) {
+    const int l = t / n, u = t - l * n;
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(sm.buf + l * LSTR + pad(u));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(Yf + (int64_t)l * n + u) : "memory");
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
   fft_lines<N>(sm.buf, sm.tw, Lr);
   float2 *Cf = C + (int64_t)f * need;
