@@ -47,6 +47,9 @@ struct EncDev {
   const int32_t *rs_i0;
   const float *rs_w;
   const uint8_t *kind;
+  // per ring pixel p < q: the exact copy's picture index (rs_i0 + 2) mod n and the first tap's rs_i0 mod n (both in
+  // [0, n)); per drive pixel d < px: its border cell d / pxm
+  const int32_t *rs_cp, *rs_c0, *cellx;
 };
 
 // ---------------------------------------------------------------- blocks to coefficients
@@ -161,6 +164,11 @@ __global__ void __launch_bounds__(kEncThreads) enc_paint_kernel(EncDev e, const 
   if (in_rows)
     for (int j = 0; j < kAnchK; j++) if (dy >= e.a0[j] && dy < e.a0[j] + e.aside) aj = j;
   const float half = 0.5f * (float)e.aside;
+  // the row's terms: the picture rows it reads (the exact copy's one, the resampled intermediate's one) and its cells
+  const bool pic_row = in_rows && dy >= e.o && dy < e.o + e.q;
+  const float *crow = pic_row ? tmp + ((int64_t)f * e.n + e.rs_cp[dy - e.o]) * e.n : nullptr;
+  const float *rrow = pic_row ? tmp + ((int64_t)f * e.q + (dy - e.o)) * e.n : nullptr;
+  const uint8_t *krow = in_rows ? e.kind + (int64_t)(dy / e.pxm) * e.side : nullptr;
   for (int X = threadIdx.x; X < e.W; X += blockDim.x) {
     if (!in_rows || X < m || X >= m + e.px) {
       if (g) g[X] = 255;
@@ -170,32 +178,29 @@ __global__ void __launch_bounds__(kEncThreads) enc_paint_kernel(EncDev e, const 
     int ai = -1;
     if (aj >= 0)
       for (int i = 0; i < kAnchK; i++) if (dx >= e.a0[i] && dx < e.a0[i] + e.aside) ai = i;
+    const bool pic = pic_row && dx >= e.o && dx < e.o + e.q;
     float d;
     if (ai >= 0) {   // the anchor's pattern: light middle and rim, a dark ring (Chebyshev distance from its middle)
       const float ddx = fabsf((float)(dx - e.a0[ai]) + 0.5f - half), ddy = fabsf((float)(dy - e.a0[aj]) + 0.5f - half);
       const float r = fmaxf(ddx, ddy) / half;
       d = r < 0.25f || r >= 0.6f ? 1.0f : 0.0f;
-    } else if (e.copy && dx >= e.o && dx < e.o + e.q && dy >= e.o && dy < e.o + e.q) {
+    } else if (e.copy && pic) {
       // an exact copy: both passes' six terms are 0 x, 1 x the sample, 0 x ..., whose sums are the sample itself
-      int ry = (e.rs_i0[dy - e.o] + 2) % e.n, cx = (e.rs_i0[dx - e.o] + 2) % e.n;
-      if (ry < 0) ry += e.n;
-      if (cx < 0) cx += e.n;
-      const float v = tmp[((int64_t)f * e.n + ry) * e.n + cx];
+      const float v = crow[e.rs_cp[dx - e.o]];
       d = v < 0 ? 0.0f : v > 1 ? 1.0f : v;
-    } else if (dx >= e.o && dx < e.o + e.q && dy >= e.o && dy < e.o + e.q) {   // the picture and its guard interval
+    } else if (pic) {   // the picture and its guard interval
       const int x = dx - e.o;
-      const float *wt = e.rs_w + 6 * x, *row = tmp + ((int64_t)f * e.q + (dy - e.o)) * e.n;
-      int c = (e.rs_i0[x]) % e.n;
-      if (c < 0) c += e.n;
-      float v = wt[0] * row[c];
+      const float *wt = e.rs_w + 6 * x;
+      int c = e.rs_c0[x];
+      float v = wt[0] * rrow[c];
 #pragma unroll
       for (int t = 1; t < 6; t++) {
         c = c + 1 == e.n ? 0 : c + 1;
-        v = v + wt[t] * row[c];
+        v = v + wt[t] * rrow[c];
       }
       d = v < 0 ? 0.0f : v > 1 ? 1.0f : v;
     } else {   // the border's cell
-      d = (e.kind[(dy / e.pxm) * e.side + dx / e.pxm] & 3) == 2 ? 0.0f : 1.0f;
+      d = (krow[e.cellx[dx]] & 3) == 2 ? 0.0f : 1.0f;
     }
     if (drive) drive[((int64_t)f * e.px + dy) * e.px + dx] = d;
     if (g) {
@@ -383,6 +388,16 @@ lizg_encoder *lizg_encoder_new(int n, int subch, int span, int max_frames) {
     for (int t = 0; t < 6; t++) w[6 * p + t] = (float)(tw[t] / sum);
   }
   ok = ok && upload(x, &e.rs_i0, i0.data(), i0.size()) && upload(x, &e.rs_w, w.data(), w.size());
+  {
+    std::vector<int32_t> cp(e.q), c0(e.q), cell(e.px);
+    for (int p = 0; p < e.q; p++) {
+      int a = (i0[p] + 2) % n, b = i0[p] % n;
+      cp[p] = a < 0 ? a + n : a;
+      c0[p] = b < 0 ? b + n : b;
+    }
+    for (int d = 0; d < e.px; d++) cell[d] = d / e.pxm;
+    ok = ok && upload(x, &e.rs_cp, cp.data(), cp.size()) && upload(x, &e.rs_c0, c0.data(), c0.size()) && upload(x, &e.cellx, cell.data(), cell.size());
+  }
   e.copy = 1;
   for (int p = 0; p < e.q && e.copy; p++)
     for (int t = 0; t < 6; t++) e.copy &= w[6 * p + t] == (t == 2 ? 1.0f : 0.0f);

@@ -535,7 +535,7 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
 // The half-plane spectrum's rows (v < vrows, each along u) inverse-transformed in place: S[v][x] = sum_u S[v][u]
 // e^{+2 pi i u x / n}, as the conjugate of the forward transform of the conjugate. L rows a CTA.
 template <int N>
-__global__ void __launch_bounds__(kThreads, 2) enc_cols_kernel(EncFft e, float2 *S) {
+__global__ void __launch_bounds__(kThreads, 3) enc_cols_kernel(EncFft e, float2 *S) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int L = plan_of(N).lines, LSTR = lstride_of(N);
   float2 *buf = reinterpret_cast<float2 *>(smraw), *tw = buf + L * LSTR;
@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(kThreads, 2) enc_cols_kernel(EncFft e, float2 
 // (liblizard/src/lizard_phy.c:733-773 turn_pack). Then clipped at +-lim and mapped to 0.5 + v sc (clip_row, :775-782),
 // into pic[y][x].
 template <int N>
-__global__ void __launch_bounds__(kThreads, 2) enc_rows_kernel(EncFft e, const float2 *T, float *pic) {
+__global__ void __launch_bounds__(kThreads, 3) enc_rows_kernel(EncFft e, const float2 *T, float *pic) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int L = plan_of(N).lines, LSTR = lstride_of(N), tiles = N / (2 * L);
   float2 *buf = reinterpret_cast<float2 *>(smraw), *tw = buf + L * LSTR;
