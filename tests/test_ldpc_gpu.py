@@ -135,6 +135,16 @@ def test_chunked_host_entry_matches_device_entry(chunks):
         assert plan.transfer == in_place
         for g, w in zip(got, want):
             assert np.array_equal(g, w)
+    # page-locked but 8 bytes off a 16-byte boundary: the decoder cannot read it in place, so the batch is staged
+    big = torch.empty(plan.llr_bytes + 32, dtype=torch.int8).pin_memory()
+    off = (-big.data_ptr()) % 16 + 8
+    llr8 = big.numpy()[off:off + plan.llr_bytes]
+    llr8[:] = b["llr"]
+    plan.set_transfer(1)
+    got = plan.run(llr8, *(t.numpy() for t in pinned[1:]))
+    assert plan.transfer == 0
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
 
 
 def test_full_size_batch_properties():
