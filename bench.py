@@ -339,6 +339,21 @@ def bench_anchor(args, stream):
                     "sample": "the 64 frames once, one frame a thread (%.2f s wall)" % dt}}
 
 
+def frame_alg_bytes(fmt, H):
+    """A frame's algorithmic bytes through rows a-e on the fused path (each stage's inputs read once, outputs written
+    once): the luma footprint (the layout square's area through H, a byte a pixel), the column transforms' kept rows Y
+    written and read (8 n V B each way), the used coefficients written and read (8 B each way), their soft values
+    written and read (2 B a coefficient each way), and the decoded blocks (476 bytes, its and ok: 480 B a block)."""
+    import numpy as np
+    side = fmt.span + 30
+    c = np.array([[0, 0, 1], [side, 0, 1], [side, side, 1], [0, side, 1]], np.float64)
+    q = c @ np.asarray(H[:9], np.float64).reshape(3, 3).T
+    x, y = q[:, 0] / q[:, 2], q[:, 1] / q[:, 2]
+    area = 0.5 * abs(np.dot(x, np.roll(y, -1)) - np.dot(y, np.roll(x, -1)))
+    used = 320 * fmt.subch
+    return int(area) + 16 * fmt.n * fmt.V + 16 * used + 4 * used + 480 * fmt.blocks
+
+
 def bench_multistream(args, stream):
     """Batched multi-stream decode: 32 camera streams of 3840 x 2160 luma at a nominal 60 frames/s, picture sizes
     uneven across 384-1536 and rings mixed 64 / 128 / 256 (five formats; 10, 8, 6, 5 and 3 streams), each frame
@@ -355,6 +370,7 @@ def bench_multistream(args, stream):
     eng = lz.Engine()
     sp = stream.cuda_stream
     batches, keep, singles = [], [], []
+    tick_bytes = 0
     for i, (n, subch, span, count) in enumerate(formats):
         eng.add_format(n, subch, span, count)
         fmt = eng.formats[i]
@@ -362,6 +378,7 @@ def bench_multistream(args, stream):
         grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 700 + i), parity=i & 3)
         Hw = synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.9, 1.05))
         luma, reg = synth.capture(fmt, grey, W, Hh, H=Hw, sigma=2.0, rng=rng)
+        tick_bytes += count * frame_alg_bytes(fmt, reg)
         d_l = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(luma, (count,) + luma.shape))).cuda()
         d_r = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(reg, (count,) + reg.shape))).cuda()
         o, so = lz.rx_outputs(fmt, count)
@@ -407,6 +424,11 @@ def bench_multistream(args, stream):
            "blocks_verified": ok, "blocks": blocks, "gpu_launches_per_tick": eng.launches,
            "one_frame_a_launch": {"frames_per_s": round(streams / (ms1 / 1e3), 1), "ms_per_tick": round(ms1, 4)},
            "batched_vs_one_frame": round(ms1 / ms, 2), "identical_crc_sets": bool(same)}
+    peak, peak_src = peaks()
+    res["hbm"] = {"algorithmic_bytes_per_tick": tick_bytes, "GBps": round(tick_bytes / (ms / 1e3) / 1e9, 1),
+                  "frac": round(tick_bytes / (ms / 1e3) / 1e9 / peak, 4),
+                  "one_frame_a_launch_frac": round(tick_bytes / (ms1 / 1e3) / 1e9 / peak, 4), "peak_GBps": peak, "peak_source": peak_src,
+                  "bytes": "luma footprint + Y written and read + used coefficients and soft values written and read + blocks"}
     eng.close()
     return res
 
