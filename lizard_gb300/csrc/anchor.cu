@@ -180,12 +180,9 @@ cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, in
   a.luma = d_luma; a.skip = d_skip; a.H = d_H; a.lens = d_lens; a.out = out;
   const int W1 = a.g.W + 1;
   const size_t smem = 2 * sizeof(double) * W1 * W1 + sizeof(float) * ((size_t)a.g.W * a.g.W + (size_t)a.g.O * a.g.O);
-  static bool attr = false;
+  static SmemOptIn opt;
   cudaError_t e;
-  if (!attr) {
-    if ((e = cudaFuncSetAttribute(anchor_find_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024)) != cudaSuccess) return e;
-    attr = true;
-  }
+  if ((e = opt.set(reinterpret_cast<const void *>(anchor_find_kernel), 120 * 1024)) != cudaSuccess) return e;
   anchor_find_kernel<<<frames * kAnchK * kAnchK, 256, smem, st>>>(a);
   return cudaGetLastError();
 }

@@ -509,13 +509,11 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
   constexpr int L = plan_of(N).lines, smem = smem_bytes_of(N), tiles = N / (2 * L);
   static_assert(smem <= kFftSmemMax, "transform CTA's shared memory");
   static_assert(N % (2 * L) == 0 && L * N <= kFftPoints && kThreads % L == 0 && L <= 32, "transform plan");
-  static bool attr = false;
+  static SmemOptIn opt_cols, opt_rows;
   cudaError_t e;
-  if (!attr) {
-    if ((e = cudaFuncSetAttribute(fft_cols_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
-    if ((e = cudaFuncSetAttribute(fft_rows_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
-    attr = true;
-  }
+  if ((e = opt_cols.set(reinterpret_cast<const void *>(fft_cols_kernel<N>), smem)) != cudaSuccess ||
+      (e = opt_rows.set(reinterpret_cast<const void *>(fft_rows_kernel<N>), smem)) != cudaSuccess)
+    return e;
   (void)sms;
   const int bands = fft_hole_bands(N), rtiles = (xd.vrows + L - 1) / L;
   hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
@@ -604,13 +602,11 @@ __global__ void __launch_bounds__(kThreads, 3) enc_rows_kernel(EncFft e, const f
 template <int N>
 static cudaError_t enc_fft_launch_n(const EncFft &e, int frames, float2 *S, float *pic, cudaStream_t st) {
   constexpr int L = plan_of(N).lines, smem = (L * lstride_of(N) + N) * (int)sizeof(float2);
-  static bool attr = false;
+  static SmemOptIn opt_cols, opt_rows;
   cudaError_t err;
-  if (!attr) {
-    if ((err = cudaFuncSetAttribute(enc_cols_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return err;
-    if ((err = cudaFuncSetAttribute(enc_rows_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return err;
-    attr = true;
-  }
+  if ((err = opt_cols.set(reinterpret_cast<const void *>(enc_cols_kernel<N>), smem)) != cudaSuccess ||
+      (err = opt_rows.set(reinterpret_cast<const void *>(enc_rows_kernel<N>), smem)) != cudaSuccess)
+    return err;
   enc_cols_kernel<N><<<frames * ((e.vrows + L - 1) / L), kThreads, smem, st>>>(e, S);
   enc_rows_kernel<N><<<frames * (N / (2 * L)), kThreads, smem, st>>>(e, S, pic);
   return cudaGetLastError();

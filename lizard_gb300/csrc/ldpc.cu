@@ -736,12 +736,8 @@ static int choice_of(int code) {
 
 template <int C, int WPC, bool LOOP, bool PAIR>
 static cudaError_t launch_v(const LdpcLaunch &a, int sms, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(ldpc_decode_kernel<C, WPC, LOOP, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, cta_smem<C>());
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static SmemOptIn opt;
+  if (cudaError_t e = opt.set(reinterpret_cast<const void *>(ldpc_decode_kernel<C, WPC, LOOP, PAIR>), cta_smem<C>())) return e;
   const int need = (a.count + Code<C>::WARPS - 1) / Code<C>::WARPS;
   const int grid = need < sms ? need : sms;
   ldpc_decode_kernel<C, WPC, LOOP, PAIR><<<grid, cta_threads<C, WPC>(), cta_smem<C>(), st>>>(a);

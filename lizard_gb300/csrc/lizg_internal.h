@@ -3,10 +3,28 @@
 #define LIZG_INTERNAL_H
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <vector>
 #include "lizard_gb300.h"
 
 namespace lizg {
+
+// A kernel's opt-in to more than 48 KB of dynamic shared memory, made once a device (the attribute is the current
+// device's, so a process driving several GPUs sets it on each). Setting it twice is harmless, so a race only repeats it.
+struct SmemOptIn {
+  std::atomic<uint64_t> done{0};
+  cudaError_t set(const void *kernel, int bytes) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev >= 0 && dev < 64 ? 1ull << dev : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_release);
+    return e;
+  }
+};
+
 
 constexpr int kSubDev = 320, kTurnsDev = 4096;
 
