@@ -1,13 +1,17 @@
 // Layered normalised min-sum LDPC decoding of the four LIZARD codes plus the block's CRC-32C check, on sm_103a.
 //
-// One warp decodes one codeword. A block row (a layer) has z = 128 checks that share no bit, so lane l takes checks
-// l, l + 32, l + 64 and l + 96 of every layer and keeps their min1 / min2 / sign in registers between the layer's
-// two passes. The codeword's posteriors (int16) and check-to-bit messages (int8) live in the warp's slice of
-// shared memory for the whole decode; global memory is touched once to read the LLRs and once to write the packed
-// hard bits, so the kernel is bound by the integer pipes and shared-memory latency, not by HBM.
+// A codeword is decoded by a group of 1, 2 or 4 warps. A block row (a layer) has z = 128 checks that share no bit;
+// in the scalar form lane l of the group's warp w takes checks l + 32 t of every layer (t over the warp's share of
+// 0..3) and keeps their min1 / min2 / sign in registers between the layer's two passes; in the pair form a thread
+// takes checks i and i + 64 as the two 16-bit halves of one register (the layout is described at layer_pair). The
+// codeword's posteriors (int16) and check-to-bit messages (int8) live in the group's slice of shared memory for the
+// whole decode; global memory is touched once to read the LLRs and once to write the packed hard bits, so the
+// kernel is bound by the ALU pipe (every min/max form issues there) and shared-memory latency, not by HBM.
 //
-// Persistent grid: one CTA per SM (its shared memory holds as many codewords as fit), warps pull codeword indices
-// from a work counter, so codewords that stop early free their warp for the next one.
+// Persistent grid: one CTA per SM (its shared memory holds as many codewords as fit), groups pull codeword indices
+// from a work counter, so codewords that stop early free their group for the next one. Each code has several
+// variants (warps a codeword, registers or a loop over the row's slots, scalar or pair form), all bit-identical;
+// one per code runs, chosen by timing on the device or by hand.
 //
 // Arithmetic: the reference's four-times kernel, liblizard/src/ldpc.c:340-423 (and its NEON original, 300-328):
 // the extrinsic L - R saturated to a byte held at [-127, 127]; min1/min2 over byte magnitudes; (x * 13) >> 4 capped
