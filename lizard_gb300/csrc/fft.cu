@@ -338,7 +338,7 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, c
     h6a = __fmul_rn(H[6], mxa); h0a = __fmul_rn(H[0], mxa); h3a = __fmul_rn(H[3], mxa);
     h6b = __fmul_rn(H[6], mxb); h0b = __fmul_rn(H[0], mxb); h3b = __fmul_rn(H[3], mxb);
   }
-#pragma unroll 4
+#pragma unroll 2   // 2 of 2, 4 and 8 is the fastest on a GB300 (61.1k, 59.3k, 57.7k batch frames/s)
   for (int y = threadIdx.x / L; y < N; y += ystep) {
     const bool ysq = (ina || inb) && in_square(xd, y);
     float va, vb;
