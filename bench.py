@@ -20,6 +20,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -99,9 +100,8 @@ class ClockSampler:
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
-            self.f = open(self.path, "w")
+            fd, self.path = tempfile.mkstemp(prefix="lizg_clocks_", suffix=".csv")
+            self.f = os.fdopen(fd, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
                                        "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
@@ -129,6 +129,11 @@ class ClockSampler:
                 rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
             except ValueError:
                 continue
+        try:
+            os.remove(self.path)   # the summary is what the result line carries
+        except OSError:
+            pass
+        self.path = None
         if not rows:
             return None
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]

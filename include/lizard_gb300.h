@@ -316,14 +316,14 @@ int lizg_border_nodes_dev(int span, const uint8_t *d_luma, int w, int h, int64_t
 //
 // Gauss-Newton on the 8 homography parameters against the known pilots, measured through the receiver's own front
 // (lizg_rx_spectrum_grid_dev), the Jacobian from eight tangent pictures (forward mode); the plain registration kept
-// where the pilots' mismatch does not fall. Not in the reference: the benchmark spec's refinement step, ahead of the
-// soft stage.
+// where the pilots' mismatch does not fall. Not in the reference: a refinement of the held registration against the
+// pilots, run ahead of the soft stage.
 typedef struct lizg_gn lizg_gn;
 // The format, and the frames refined at once (chunk, 1..64: each holds 9 pictures and their spectra).
 lizg_gn *lizg_gn_new(int n, int subch, int span, int chunk);
 void lizg_gn_free(lizg_gn *g);
-// d_reg: frames x (9 + 2 nodes) registrations, H refined in place (the mesh kept). steps: Gauss-Newton steps (3 is
-// the benchmark spec's). Out (either NULL): d_loss, each frame's final mismatch; d_improved, 1 where a step was kept.
+// d_reg: frames x (9 + 2 nodes) registrations, H refined in place (the mesh kept). steps: Gauss-Newton steps (the
+// benchmark takes 3). Out (either NULL): d_loss, each frame's final mismatch; d_improved, 1 where a step was kept.
 int lizg_gn_refine_dev(lizg_gn *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int steps, float *d_loss,
                        int32_t *d_improved, void *stream);
 // The 9 pictures a step reads (the sampled picture, then its tangents in h0..h7), frames x 9 x n x n, frames <= chunk.

@@ -1,5 +1,5 @@
 """Generates tests/golden/ldpc_ref.npz: LDPC decodes by the reference itself (its C decoder compiled from its
-sources by oracle/Makefile), so the GPU decoder can be held to the reference's own outputs on the GPU machine, where the
+sources by oracle/Makefile), so the GPU decoder can be held to the reference's own outputs on a GPU host where the
 reference tree is absent.
 
 Run from the repo root where the reference is present: python tests/golden/make_ldpc_golden.py

@@ -1,5 +1,5 @@
 """Generates tests/golden/rx_ref.npz: the reference receiver's own outputs (compiled from its sources by
-oracle/Makefile) on small synthetic pictures, so the GPU receiver can be held to the reference on the GPU machine, where
+oracle/Makefile) on small synthetic pictures, so the GPU receiver can be held to the reference on a GPU host where
 the reference tree is absent.
 
 Run from the repo root where the reference is present: python tests/golden/make_rx_golden.py
