@@ -199,10 +199,11 @@ def bench_receiver(args, stream):
     # --- FFT demod batch
     sizes = [(384, 80), (768, 320), (1152, 720), (1536, 1024)]
     per = 64
-    rxs, bufs, blocks_total = [], [], 0
+    rxs, bufs, blocks_total, step_bytes = [], [], 0, 0
     for n, subch in sizes:
         rx = lz.Receiver(n, subch, 128, max_frames=per)
         luma, reg = picture_frames(rx.fmt, 8, per // 8, seed=n, sigma=3.0)
+        step_bytes += per * frame_alg_bytes(rx.fmt, reg[0], n, n)
         d_l = torch.from_numpy(luma).cuda()
         d_r = torch.from_numpy(reg).cuda()
         o, s = rx._outputs(per, torch, keep=False)
@@ -231,6 +232,10 @@ def bench_receiver(args, stream):
                               "frames_per_s": round(256 / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
                               "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
                               "gpu_launches_per_step": sum(rx.launches for rx in rxs)}
+    peak, peak_src = peaks()
+    res["fft_demod_batch"]["hbm"] = {"algorithmic_bytes_per_step": step_bytes, "GBps": round(step_bytes / (ms / 1e3) / 1e9, 1),
+                                     "frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "peak_source": peak_src,
+                                     "bytes": "luma footprint + Y written and read + used coefficients and soft values written and read + blocks"}
     # --- one frame a call (direct and captured), and a batch of frames a call, at n = 384 and n = 1536
     def capture_frames(n, subch, W, Hh, count, seed):
         rx = lz.Receiver(n, subch, 128, max_frames=count)
@@ -344,9 +349,9 @@ def bench_anchor(args, stream):
                     "sample": "the 64 frames once, one frame a thread (%.2f s wall)" % dt}}
 
 
-def frame_alg_bytes(fmt, H):
+def frame_alg_bytes(fmt, H, w, h):
     """A frame's algorithmic bytes through rows a-e on the fused path (each stage's inputs read once, outputs written
-    once): the luma footprint (the layout square's area through H, a byte a pixel), the column transforms' kept rows Y
+    once): the luma footprint (the layout square's area through H, a byte a pixel, at most the w x h frame), the column transforms' kept rows Y
     written and read (8 n V B each way), the used coefficients written and read (8 B each way), their soft values
     written and read (2 B a coefficient each way), and the decoded blocks (476 bytes, its and ok: 480 B a block)."""
     import numpy as np
@@ -356,7 +361,7 @@ def frame_alg_bytes(fmt, H):
     x, y = q[:, 0] / q[:, 2], q[:, 1] / q[:, 2]
     area = 0.5 * abs(np.dot(x, np.roll(y, -1)) - np.dot(y, np.roll(x, -1)))
     used = 320 * fmt.subch
-    return int(area) + 16 * fmt.n * fmt.V + 16 * used + 4 * used + 480 * fmt.blocks
+    return int(min(area, w * h)) + 16 * fmt.n * fmt.V + 16 * used + 4 * used + 480 * fmt.blocks
 
 
 def bench_multistream(args, stream):
@@ -383,7 +388,7 @@ def bench_multistream(args, stream):
         grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 700 + i), parity=i & 3)
         Hw = synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.9, 1.05))
         luma, reg = synth.capture(fmt, grey, W, Hh, H=Hw, sigma=2.0, rng=rng)
-        tick_bytes += count * frame_alg_bytes(fmt, reg)
+        tick_bytes += count * frame_alg_bytes(fmt, reg, W, Hh)
         d_l = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(luma, (count,) + luma.shape))).cuda()
         d_r = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(reg, (count,) + reg.shape))).cuda()
         o, so = lz.rx_outputs(fmt, count)
