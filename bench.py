@@ -1047,7 +1047,8 @@ def main():
                      "kernel": "ldpc_decode_kernel<7/8,3/4,2/3,1/2> (the 4 launches of a step)",
                      "note": "not HBM bound: the min-sum minima issue on the ALU pipe (every min/max form does on sm_103a); "
                              "see ldpc.edge_updates_per_s and alu_pipe",
-                     "alu_pipe": {"active_frac": 0.746, "kernel": "ldpc_decode_kernel 3/4 code, 2 warps a codeword, registers",
+                     "alu_pipe": {"active_frac": 0.856, "kernel": "ldpc_decode_kernel 7/8 code (41% of a step), 2 warps a codeword, "
+                                                                   "pair form with the loop",
                                   "source": "ncu sm__pipe_alu_cycles_active, profiles/ldpc_decode_65536cw.md (python bench.py "
                                             "--ldpc-variants --count 16384)"}},
         "gpu_launches": launches,
