@@ -147,6 +147,39 @@ def test_chunked_host_entry_matches_device_entry(chunks):
         assert np.array_equal(g, w)
 
 
+def test_registered_host_buffers_are_read_in_place():
+    """Buffers the caller already owns, page-locked with cudaHostRegister, take the in-place route too."""
+    torch = pytest.importorskip("torch")
+    b = synth.ldpc_batch(500, seed=6)
+    plan = lz.LdpcPlan(b["rates"], 20, 9, 0.95)
+    want = plan.run(b["llr"])
+    assert plan.transfer == 0
+    page = 1 << 16   # the largest page size a host may use: each buffer gets pages of its own
+
+    def own_pages(n, dtype):
+        nbytes = n * np.dtype(dtype).itemsize
+        raw = np.zeros(nbytes + 2 * page, np.uint8)
+        at = (-raw.ctypes.data) % page
+        return raw[at:at + nbytes].view(dtype)
+
+    bufs = [own_pages(plan.llr_bytes, np.int8), own_pages(plan.llr_bytes // 8, np.uint8), own_pages(plan.count, np.int32),
+            own_pages(plan.count, np.uint8)]
+    bufs[0][:] = b["llr"]
+    rt = torch.cuda.cudart()
+    done = []
+    try:
+        for a in bufs:
+            assert int(rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0
+            done.append(a)
+        got = plan.run(*bufs)
+        assert plan.transfer == 1
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+    finally:
+        for a in done:
+            rt.cudaHostUnregister(a.ctypes.data)
+
+
 def test_full_size_batch_properties():
     """The benchmark's batch (65,536 codewords): every decoded block is its sent codeword and passes its CRC, the
     CRC flags agree with a host CRC of the output, clean-channel codewords all decode, and a sample matches the oracle."""
