@@ -97,7 +97,9 @@ void plan_chunks(lizg_ldpc_plan *p, int k) {
   for (int j = 1; j < k; j++) {
     const int64_t target = p->llr_bytes * j / k;
     while (i < p->count && p->off[(size_t)i] < target) i++;
-    p->first[j] = std::max(i, p->first[j - 1] + 1);
+    // strictly after the previous boundary, and leaving a codeword for each chunk still to come (a large last
+    // codeword can put every offset below the target)
+    p->first[j] = std::min(std::max(i, p->first[j - 1] + 1), p->count - (k - j));
   }
   p->first[k] = p->count;
   for (int c = 0; c < 4; c++) {

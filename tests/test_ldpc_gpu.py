@@ -147,6 +147,21 @@ def test_chunked_host_entry_matches_device_entry(chunks):
         assert np.array_equal(g, w)
 
 
+@pytest.mark.parametrize("rates", [[6, 2], [2, 6, 2], [6, 6, 6, 2]])
+def test_every_chunk_holds_a_codeword(rates):
+    """Chunks split at codeword boundaries by bytes: with a large last codeword no offset reaches the last targets,
+    yet each chunk keeps a codeword and the outputs are those of one pass."""
+    b = synth.ldpc_batch(len(rates), seed=8, rates=np.array(rates, np.int32))
+    plan = lz.LdpcPlan(b["rates"], 20, 9, 0.95)
+    want = plan.run(b["llr"])
+    for k in range(2, len(rates) + 1):
+        assert plan.set_chunks(k) == k
+        got = plan.run(b["llr"])
+        assert plan.launches >= k
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+
+
 def test_registered_host_buffers_are_read_in_place():
     """Buffers the caller already owns, page-locked with cudaHostRegister, take the in-place route too."""
     torch = pytest.importorskip("torch")
