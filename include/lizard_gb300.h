@@ -24,6 +24,15 @@ enum {
   LIZG_E_STATE = -4,    // the handle is in no state for the call
 };
 
+// The receiver's picture read (lizg_rx_set_read). The reference has two: its SIMD builds' decode reads the picture in
+// integers (ob_sample_grid_pic, liblizard/src/acquire.c:5465-5480; the x86-64 form :5302-5440, called a strip of 64
+// columns at a time and once for the shading fit, liblizard/src/lizard_phy.c:1611, 1634), its portable build with
+// the exact float walk (ob_sample_grid, acquire.c:5121-5196). The two differ by up to about 1/200 of a grey level.
+enum {
+  LIZG_READ_DECODE = 0,  // the x86-64 decode's integer read, bit for bit (the default)
+  LIZG_READ_EXACT = 1,   // the exact walk, bit for bit
+};
+
 // Thread-local text of the last failure on this thread ("" if none). Replaces liz_last_error
 // (liblizard/include/lizard.h:63).
 const char *lizg_last_error(void);
@@ -145,6 +154,9 @@ int lizg_layout_nodes(int span, float *node_x, float *node_y, int32_t *nn);
 int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm);
 // Kernel launches the last finish made.
 int lizg_rx_launches(const lizg_rx *r);
+// The picture read of the handle's later finishes from captured frames (LIZG_READ_DECODE or LIZG_READ_EXACT); returns
+// the previous one, or LIZG_E_ARG. Host code.
+int lizg_rx_set_read(lizg_rx *r, int read);
 
 // Per-frame outputs, device pointers, frames x blocks entries each unless noted. Required: blocks (476 bytes a block,
 // the decoded bytes whether or not verified), ok (1 where the CRC-32C verified a decoded block), its (LDPC
@@ -180,9 +192,10 @@ int lizg_rx_spectrum_grid_dev(lizg_rx *r, const float *d_grid, int frames, float
 // frame_stride bytes apart); d_reg holds each frame's registration, 9 + 2 nx ny floats: the homography H (module
 // coordinates to image pixels, h[8] = 1, liblizard/src/internal.h:105-112) then the node mesh's (dx, dy) pixel
 // displacements row by row (liblizard/src/internal.h:123-124, what the reference's acquisition leaves held). Each
-// frame's picture is sampled on its n x n grid (liblizard/src/acquire.c:5121-5196), then as lizg_rx_finish_grid_dev.
-// d_grid (optional) receives the sampled grids (frames x n x n). The replacement for lizard_finish(f, NULL, ...) on
-// a held registration (liblizard/src/lizard_phy.c:1566-1871).
+// frame's picture is sampled on its n x n grid by the handle's read (lizg_rx_set_read), the shading fit's samples as
+// the reference's finish takes them, then as lizg_rx_finish_grid_dev. d_grid (optional) receives the sampled grids
+// (frames x n x n). The replacement for lizard_finish(f, NULL, ...) on a held registration
+// (liblizard/src/lizard_phy.c:1566-1871).
 int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
                             int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
 // lizg_rx_finish_luma_dev replayed from a CUDA graph: the first call with a given set of buffers and sizes captures

@@ -215,6 +215,7 @@ def _rx_sigs(L):
     L.lizg_rx_info.argtypes = [P, P]
     L.lizg_rx_perm.argtypes = [P, I, P]
     L.lizg_rx_launches.argtypes = [P]
+    L.lizg_rx_set_read.argtypes = [P, I]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
     L.lizg_rx_finish_grid_dev.argtypes = [P, P, I, P, P, P]
     L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
@@ -311,10 +312,14 @@ def rx_outputs(fmt, frames, keep=False):
     return o, s
 
 
-class Receiver:
-    """A receiver handle (lizg_rx_*) for one format and up to max_frames frames a call."""
+READ_DECODE, READ_EXACT = 0, 1
 
-    def __init__(self, n, subch, span=128, max_frames=1):
+
+class Receiver:
+    """A receiver handle (lizg_rx_*) for one format and up to max_frames frames a call. read: "decode" (the reference
+    decoder's integer read, the default) or "exact" (the exact float walk)."""
+
+    def __init__(self, n, subch, span=128, max_frames=1, read="decode"):
         self.fmt = Format(n, subch, span)
         L = lib()
         h = L.lizg_rx_new(n, subch, span, max_frames)
@@ -322,6 +327,13 @@ class Receiver:
             raise LizgError("lizg_rx_new: " + L.lizg_last_error().decode())
         self._h = ctypes.c_void_p(h)
         self.max_frames = max_frames
+        self.set_read(read)
+
+    def set_read(self, read):
+        """The picture read of later finishes from captured frames: "decode" or "exact"."""
+        code = {"decode": READ_DECODE, "exact": READ_EXACT}[read]
+        _check(lib().lizg_rx_set_read(self._h, code), "lizg_rx_set_read")
+        self.read = read
 
     def close(self):
         if getattr(self, "_h", None):

@@ -207,12 +207,21 @@ __device__ __forceinline__ void fft_lines(float2 *buf, const float2 *tw, int Lr)
   pass<N, P.r2, P.r0 * P.r1, P.lines>(buf, tw, Lr);
 }
 
-// A frame's picture sample (x, y): read from a supplied grid, or sampled straight from the captured frame through
-// its registration (the sampler fused into the pass that reads it).
-__device__ __forceinline__ float src_at(const SrcDev &s, int f, int x, int y) {
-  if (s.grid) return s.grid[f * s.gstride + (int64_t)y * s.sd.n + x];
+// A frame's shading-fit sample (x, y) = (8 kx, 8 ky): from the captured frame through its registration when the
+// frame is given (the decode's read as the reference's finish takes these samples, one call over every eighth row and
+// column, liblizard/src/lizard_phy.c:1611; or the exact walk), else from a supplied grid.
+__device__ __forceinline__ float shade_at(const SrcDev &s, int f, int kx, int ky) {
+  const int x = 8 * kx, y = 8 * ky;
+  if (!s.luma) return s.grid[f * s.gstride + (int64_t)y * s.sd.n + x];
   const float *H = s.reg + (int64_t)f * s.regstride;
-  return sample_xy(s.sd, s.luma + f * s.fstride, s.w, s.h, s.pitch, H, H + 9, s.sd.colt[x], s.sd.rowt[y]);
+  const uint8_t *px = s.luma + f * s.fstride;
+  const float4 ct = s.sd.colt[x], rt = s.sd.rowt[y];
+  if (s.sd.read != LIZG_READ_DECODE) return sample_xy_exact(s.sd, px, s.w, s.h, s.pitch, H, H + 9, ct, rt);
+  const RowTerms r = row_terms(H, rt);
+  const LinCol c = lin_col_shade(s.sd, H, kx);
+  LinNum n = lin_start(c, r.kw, r.ku, r.kv);
+  lin_steps(c, n, c.g);
+  return lin_point(px, s.w, s.h, s.pitch, n, lin_cell(s.sd, H + 9, ct, r.j), r.v);
 }
 
 __device__ __forceinline__ bool in_square(const FftDev &xd, int t) {
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, in
     for (int kx = lane; kx < c; kx += 32) {
       const int x = 8 * kx;
       if (ysq && in_square(xd, x)) continue;
-      const float v = src_at(src, f, x, y);
+      const float v = shade_at(src, f, kx, ky);
       s0 += v; s1 += __ldg(xd.cx + x) * v; s2 += __ldg(xd.qx + x) * v;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -290,24 +299,36 @@ __device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta
   return (float)h;
 }
 
-// The sampler's per-row quantities of a batch, worked out once a frame before the column pass reads them: for
-// picture row y and mesh cell i < nx - 1 the displacement line cell_terms gives, and at i = nx - 1 the homography's
-// row terms (kw, ku, kv). The same functions and inputs as the per-sample walk (the cell's 1 / width as the column
-// table computes it), so the column pass reads the walk's own values. A thread an entry, entries in table order.
+// The sampler's per-row quantities of a batch, worked out once a frame before the column pass reads them, with the
+// same functions and inputs as the per-sample walk (the cell's 1 / width as the column table computes it), so the
+// column pass reads the walk's own values. A thread an entry, entries in table order. The exact walk: for picture row
+// y and mesh cell i < nx - 1 the displacement line cell_terms gives, and at i = nx - 1 the homography's row terms
+// (kw, ku, kv). The decode's read: the row terms of row y at y < n, then each column x's displacement terms at mesh
+// row j (lin_cell) at n + j n + x.
 __global__ void __launch_bounds__(256) cell_table_kernel(SrcDev src, int per_frame, float4 *ctab) {
   const int f = blockIdx.y, t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= per_frame) return;
   const SampleDev &sd = src.sd;
-  const int nn = sd.nx, y = t / nn, i = t - y * nn;
   const float *H = src.reg + (int64_t)f * src.regstride;
-  const RowTerms r = row_terms(H, sd.rowt[y]);
   float4 o;
-  if (i == nn - 1) {
-    o = make_float4(r.kw, r.ku, r.kv, 0.0f);
+  if (sd.read == LIZG_READ_DECODE) {
+    if (t < sd.n) {
+      const RowTerms r = row_terms(H, sd.rowt[t]);
+      o = make_float4(r.kw, r.ku, r.kv, 0.0f);
+    } else {
+      const int j = (t - sd.n) / sd.n, x = t - sd.n - j * sd.n;
+      o = lin_cell(sd, H + 9, sd.colt[x], j);
+    }
   } else {
-    const float inv = __fdiv_rn(1.0f, __fsub_rn(sd.node_x[i + 1], sd.node_x[i]));
-    const CellTerms c = cell_terms(sd, H + 9, i, inv, r);
-    o = make_float4(c.ex, c.cx, c.ey, c.cy);
+    const int nn = sd.nx, y = t / nn, i = t - y * nn;
+    const RowTerms r = row_terms(H, sd.rowt[y]);
+    if (i == nn - 1) {
+      o = make_float4(r.kw, r.ku, r.kv, 0.0f);
+    } else {
+      const float inv = __fdiv_rn(1.0f, __fsub_rn(sd.node_x[i + 1], sd.node_x[i]));
+      const CellTerms c = cell_terms(sd, H + 9, i, inv, r);
+      o = make_float4(c.ex, c.cx, c.ey, c.cy);
+    }
   }
   ctab[(int64_t)f * per_frame + t] = o;
 }
@@ -315,8 +336,10 @@ __global__ void __launch_bounds__(256) cell_table_kernel(SrcDev src, int per_fra
 // One column tile's samples: thread t takes line l = t mod L (columns xa = x0 + l as the real part, xb = x0 + L + l as
 // the imaginary part) at rows y = t / L, t / L + kThreads / L, ...; the anchors' squares erased to the shading
 // surface as they are read. Each row's two samples are summed into the five detrend projections' raw sums, z c(x),
-// z c(y), z c(x) c(y), z q(x), z q(y) (liblizard/src/lizard_phy.c:1584-1591, 1657-1667), in p.
-template <int N, bool GRID>
+// z c(y), z c(x) c(y), z q(x), z q(y) (liblizard/src/lizard_phy.c:1584-1591, 1657-1667), in p. SRC: kSrcGrid reads a
+// supplied grid; kSrcExact and kSrcDecode sample the captured frame by the exact walk or the decode's read.
+constexpr int kSrcGrid = 0, kSrcExact = 1, kSrcDecode = 2;
+template <int N, int SRC>
 __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, const float4 *ctab, int f, int x0, const double *beta,
                                           float2 *line, float p[5]) {
   constexpr int L = plan_of(N).lines, ystep = kThreads / L;
@@ -326,8 +349,9 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, c
   float mxa = 0, mxb = 0, h6a = 0, h0a = 0, h3a = 0, h6b = 0, h0b = 0, h3b = 0;
   int ia = 0, ib = 0, nn = 1;
   const uint8_t *px = nullptr;
-  const float4 *T = nullptr;   // the frame's row and cell table, row y at T + y nn
-  if (!GRID) {
+  const float4 *T = nullptr;   // the frame's row and cell table
+  LinCol lc{};                 // the decode's read: column xa's lanes (xb shares its lane, L / 4 steps on)
+  if (SRC != kSrcGrid) {
     const float *H = src.reg + (int64_t)f * src.regstride;
     nn = src.sd.nx;
     T = ctab + (int64_t)f * N * nn;
@@ -335,17 +359,21 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, c
     const float4 ca = src.sd.colt[xa], cb = src.sd.colt[xb];
     mxa = ca.x; ia = __float_as_int(ca.y);
     mxb = cb.x; ib = __float_as_int(cb.y);
-    h6a = __fmul_rn(H[6], mxa); h0a = __fmul_rn(H[0], mxa); h3a = __fmul_rn(H[3], mxa);
-    h6b = __fmul_rn(H[6], mxb); h0b = __fmul_rn(H[0], mxb); h3b = __fmul_rn(H[3], mxb);
+    if (SRC == kSrcExact) {
+      h6a = __fmul_rn(H[6], mxa); h0a = __fmul_rn(H[0], mxa); h3a = __fmul_rn(H[3], mxa);
+      h6b = __fmul_rn(H[6], mxb); h0b = __fmul_rn(H[0], mxb); h3b = __fmul_rn(H[3], mxb);
+    } else {
+      lc = lin_col_grid(src.sd, H, xa);   // a tile's 2L columns lie in one strip of 64 (2L divides 64)
+    }
   }
 #pragma unroll 2   // 2 of 2, 4 and 8 is the fastest on a GB300 (61.1k, 59.3k, 57.7k batch frames/s)
   for (int y = threadIdx.x / L; y < N; y += ystep) {
     const bool ysq = (ina || inb) && in_square(xd, y);
     float va, vb;
-    if (GRID) {
+    if (SRC == kSrcGrid) {
       const float *g = src.grid + f * src.gstride + (int64_t)y * N;
       va = g[xa]; vb = g[xb];
-    } else {
+    } else if (SRC == kSrcExact) {
       const float4 *Ty = T + y * nn;
       const float4 rt = Ty[nn - 1], ta = Ty[ia], tb = ib == ia ? ta : Ty[ib];
       RowTerms r;
@@ -353,6 +381,15 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, c
       const CellTerms ca{ta.x, ta.y, ta.z, ta.w}, cb{tb.x, tb.y, tb.z, tb.w};
       va = sample_at(px, src.w, src.h, src.pitch, mxa, h6a, h0a, h3a, r, ca);
       vb = sample_at(px, src.w, src.h, src.pitch, mxb, h6b, h0b, h3b, r, cb);
+    } else {
+      const float4 rt = T[y], rw = __ldg(&src.sd.rowt[y]);
+      const int j = __float_as_int(rw.y);
+      const float4 ta = T[N + j * N + xa], tb = T[N + j * N + xb];
+      LinNum s = lin_start(lc, rt.x, rt.y, rt.z);
+      lin_steps(lc, s, lc.g);
+      va = lin_point(px, src.w, src.h, src.pitch, s, ta, rw.z);
+      lin_steps(lc, s, L / 4);
+      vb = lin_point(px, src.w, src.h, src.pitch, s, tb, rw.z);
     }
     if (ina && ysq) va = hole_value(xd, beta, xa, y);
     if (inb && ysq) vb = hole_value(xd, beta, xb, y);
@@ -397,8 +434,9 @@ __global__ void __launch_bounds__(kThreads, 3) fft_cols_kernel(FftDev xd, SrcDev
     }
     __syncthreads();
     float p[5] = {0, 0, 0, 0, 0};
-    if (src.grid) load_tile<N, true>(xd, src, ctab, f, x0, s_beta, line, p);
-    else load_tile<N, false>(xd, src, ctab, f, x0, s_beta, line, p);
+    if (src.grid) load_tile<N, kSrcGrid>(xd, src, ctab, f, x0, s_beta, line, p);
+    else if (src.sd.read == LIZG_READ_DECODE) load_tile<N, kSrcDecode>(xd, src, ctab, f, x0, s_beta, line, p);
+    else load_tile<N, kSrcExact>(xd, src, ctab, f, x0, s_beta, line, p);
 #pragma unroll
     for (int q = 0; q < 5; q++)
       for (int o = 16; o > 0; o >>= 1) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
@@ -518,7 +556,7 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
   const int bands = fft_hole_bands(N), rtiles = (xd.vrows + L - 1) / L;
   hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
   if (!src.grid) {
-    if (!b.ctab) return cudaErrorInvalidValue;
+    if (!b.ctab || src.sd.nx != src.sd.ny) return cudaErrorInvalidValue;
     const int per_frame = N * src.sd.nx;
     cell_table_kernel<<<dim3((per_frame + 255) / 256, frames), 256, 0, st>>>(src, per_frame, b.ctab);
   }

@@ -62,9 +62,11 @@ struct FftBufs {
   const int32_t *tpos;               // vrows x n: the pos index of spectrum point (u mod n, v), -1 where unused
   int need;                          // used coefficients a frame (subch x 320)
   float2 *C;                         // frames x need: the detrended spectrum's used coefficients in pos order
-  // frames x n x nx: for each picture row y of a frame, the mesh displacement line of each cell i < nx - 1 (ex, cx,
-  // ey, cy, as cell_terms gives them) and at i = nx - 1 the homography's row terms (kw, ku, kv, 0); filled before
-  // the column pass when the samples come straight from captured frames
+  // frames x n x nx, filled before the column pass when the samples come straight from captured frames. The exact
+  // walk: for each picture row y of a frame, the mesh displacement line of each cell i < nx - 1 (ex, cx, ey, cy, as
+  // cell_terms gives them) and at i = nx - 1 the homography's row terms (kw, ku, kv, 0). The decode's read: the
+  // homography's row terms of row y at y (n entries), then each column x's displacement terms at mesh row j
+  // (lin_cell) at n + j n + x (j < ny - 1, ny = nx)
   float4 *ctab;
 };
 
@@ -75,6 +77,7 @@ constexpr int kFftPoints = 6144;
 // The sampler's format-side inputs (row a): picture size, grid origin and step in modules, the node lattice.
 struct SampleDev {
   int n, nx, ny;
+  int read;                          // LIZG_READ_DECODE (the decode's integer read) or LIZG_READ_EXACT (the exact walk)
   float g0, step;                    // margin + 0.5 / scale, 1 / scale (floats, as the reference computes them)
   const float *node_x, *node_y;      // node centres' module coordinates
   // per picture column x: its module coordinate mx, mesh cell i and 1 / (node_x[i + 1] - node_x[i]); per row y: my,

@@ -263,6 +263,13 @@ int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm) {
 
 int lizg_rx_launches(const lizg_rx *r) { return r ? r->launches : LIZG_E_ARG; }
 
+int lizg_rx_set_read(lizg_rx *r, int read) {
+  if (!r || (read != LIZG_READ_DECODE && read != LIZG_READ_EXACT)) return lizg::record_error(LIZG_E_ARG, "lizg_rx_set_read: no handle or no such read");
+  const int was = r->sd.read;
+  r->sd.read = read;
+  return was;
+}
+
 // Rows (c), (d), (e) on a batch of spectra (spec: frame f's coefficient i, pos order, at spec[f stride + i]):
 // the pilots' fit, the soft values, the block stage, then the LDPC and CRC of every block not declined, the four
 // codes on their own streams.
@@ -317,7 +324,7 @@ static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const liz
   const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, C, r->ctab};
   cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
-  r->launches += src.grid ? 4 : 5;   // the luma source adds the sampler's row and cell table
+  r->launches += src.grid ? 4 : 5;   // sampling in the column pass adds the sampler's row and cell table
   return finish_spec(r, C, need, frames, out, st, sms);
 }
 
@@ -359,13 +366,14 @@ int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int
   r->launches = 0;
   lizg::SrcDev src{};
   src.sd = r->sd;
+  src.luma = d_luma; src.w = w; src.h = h; src.pitch = pitch; src.fstride = frame_stride; src.reg = d_reg; src.regstride = regstride;
   if (d_grid) {
+    // the grid sampled first; the transform reads it, the shading fit's samples still come from the frame as the
+    // reference's finish takes them
     cudaError_t e = lizg::sample_launch(r->sd, frames, d_luma, w, h, pitch, frame_stride, d_reg, regstride, d_grid, st);
     if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("sampler: ") + cudaGetErrorString(e)).c_str());
     r->launches = 1;
     src.grid = d_grid; src.gstride = (int64_t)r->f.n * r->f.n;
-  } else {
-    src.luma = d_luma; src.w = w; src.h = h; src.pitch = pitch; src.fstride = frame_stride; src.reg = d_reg; src.regstride = regstride;
   }
   return finish_src(r, src, frames, out, d_coef, st, sms);
 }
@@ -381,7 +389,7 @@ int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, i
   const std::vector<uintptr_t> key = {(uintptr_t)d_luma, (uintptr_t)w, (uintptr_t)h, (uintptr_t)pitch, (uintptr_t)frame_stride,
                                       (uintptr_t)d_reg, (uintptr_t)frames, (uintptr_t)out->blocks, (uintptr_t)out->ok, (uintptr_t)out->its,
                                       (uintptr_t)out->est, (uintptr_t)out->pilot, (uintptr_t)out->align, (uintptr_t)out->llrf,
-                                      (uintptr_t)out->sub_est, (uintptr_t)out->sub_rms, (uintptr_t)d_grid, (uintptr_t)d_coef};
+                                      (uintptr_t)out->sub_est, (uintptr_t)out->sub_rms, (uintptr_t)d_grid, (uintptr_t)d_coef, (uintptr_t)r->sd.read};
   cudaError_t e;
   if (!r->graph || key != r->graph_key) {
     if (r->graph) { cudaGraphExecDestroy(r->graph); r->graph = nullptr; }

@@ -1,10 +1,11 @@
-// Row (a) of the hot path on sm_103a: the picture sampler. Every sample of the n x n picture grid is read from the
-// captured luma frame through the registration: the homography H (module -> image) plus the bilinear blend of the
-// node mesh's displacements, then a bilinear luma read at gamma 1 (grey / 255), the frame edge clamped. This is the
-// reference's exact walk, liblizard/src/acquire.c:5121-5196 ob_sample_grid with internal.h:11-23 sample(), restated
-// operation for operation in float and compiled with -fmad=false, so it gives that walk's values bit for bit. (The
-// reference's decoder runs a faster integer read of the same map, ob_sample_grid_pic, which its own test holds
-// within 1/200 of grey of this walk: liblizard/test/sample_grid.c.)
+// Row (a) of the hot path on sm_103a: the picture sampler, when the grid itself is asked for (the transform's column
+// pass otherwise samples as it loads). Every sample of the n x n picture grid is read from the captured luma frame
+// through the registration: the homography H (module -> image) plus the bilinear blend of the node mesh's
+// displacements, then a bilinear luma read at gamma 1. By the receiver's read: the reference decoder's integer read
+// (ob_sample_grid_pic's x86-64 form, liblizard/src/acquire.c:5302-5440, in strips of 64 columns as
+// liblizard/src/lizard_phy.c:1634 calls it) or the exact walk (ob_sample_grid, acquire.c:5121-5196 with
+// internal.h:11-23 sample()), each restated operation for operation (sample_dev.cuh), so either gives the reference's
+// values bit for bit.
 //
 // One thread a sample, a 32 x 8 tile of samples a CTA: a warp reads a row run of 32 samples, whose luma reads are
 // neighbouring pixels of one or two image rows.
@@ -21,7 +22,7 @@ __global__ void __launch_bounds__(256) sample_kernel(SampleDev sd, const uint8_t
   const int n = sd.n;
   if (x >= n || y >= n) return;
   const float *H = reg + (int64_t)f * regstride;
-  grid[(int64_t)f * n * n + (int64_t)y * n + x] = sample_xy(sd, luma + f * fstride, w, h, pitch, H, H + 9, sd.colt[x], sd.rowt[y]);
+  grid[(int64_t)f * n * n + (int64_t)y * n + x] = sample_xy(sd, luma + f * fstride, w, h, pitch, H, H + 9, x, sd.colt[x], sd.rowt[y]);
 }
 
 __global__ void sample_tables_kernel(SampleDev sd, float4 *colt, float4 *rowt) {

@@ -212,6 +212,7 @@ def _phy_sigs(L):
     L.orc_blocks.argtypes = [P, P, P, P, P, P, I, P, P, P, P, P]
     L.orc_layout_nodes.argtypes = [I, P]
     L.orc_sample_grid.argtypes = [I, I, P, I, I, I, P, P]
+    L.orc_sample_decode.argtypes = [I, I, P, I, I, I, P, P, P]
 
 
 class Fmt:
@@ -296,6 +297,17 @@ class Fmt:
         self.L.orc_sample_grid(self.n, self.span, _p(luma), w, h, w, _p(np.ascontiguousarray(reg, np.float32)), _p(g))
         return g.reshape(self.n, self.n)
 
+    def sample_decode(self, luma, reg):
+        """The grid as the x86-64 decode samples it (strips of 64 columns, the integer read) and the shading fit's
+        samples: (grid n x n, shade n/8 x n/8)."""
+        luma = np.ascontiguousarray(luma, np.uint8)
+        h, w = luma.shape
+        g = np.zeros(self.n * self.n, np.float32)
+        c = self.n // 8
+        s = np.zeros(c * c, np.float32)
+        self.L.orc_sample_decode(self.n, self.span, _p(luma), w, h, w, _p(np.ascontiguousarray(reg, np.float32)), _p(g), _p(s))
+        return g.reshape(self.n, self.n), s.reshape(c, c)
+
     def receive(self, grid, fp64_spectrum=True):
         """The whole finish on a grid: spectrum (FP64, narrowed to float), pilots, soft values, blocks."""
         spec, _, _ = self.spectrum(grid)
@@ -329,6 +341,7 @@ class RefFmt:
             L.ref_finish_grid.argtypes = [P] + [P] * 11
             L.ref_decode_frame.argtypes = [P, P, I, I, P, P, P, P, P, P]
             L.ref_sample_grid.argtypes = [P, P, I, I, P, I, P]
+            L.ref_sample_decode.argtypes = [P, P, I, I, P, P, P]
             L._phy = True
         self.L = L
         self.h = L.ref_fmt_new(n, subch, span)
@@ -401,6 +414,18 @@ class RefFmt:
         g = np.zeros(self.n * self.n, np.float32)
         self.L.ref_sample_grid(self.h, _p(luma), iw, ih, _p(reg), int(fast), _p(g))
         return g.reshape(self.n, self.n)
+
+    def sample_decode(self, luma, H, nodes):
+        """The grid as the reference's decode samples it (strips of 64, its integer read at gamma 1) and the shading
+        fit's samples; (grid n x n, shade n/8 x n/8, lin) where lin says the integer read ran."""
+        luma = np.ascontiguousarray(luma, np.uint8)
+        ih, iw = luma.shape
+        reg = np.concatenate([np.asarray(H, np.float32).ravel(), np.asarray(nodes, np.float32).ravel()]).astype(np.float32)
+        g = np.zeros(self.n * self.n, np.float32)
+        c = self.n // 8
+        s = np.zeros(c * c, np.float32)
+        lin = self.L.ref_sample_decode(self.h, _p(luma), iw, ih, _p(reg), _p(g), _p(s))
+        return g.reshape(self.n, self.n), s.reshape(c, c), bool(lin)
 
 
 def spec_blocks(count, seed=None):

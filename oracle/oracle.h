@@ -63,6 +63,9 @@ int orc_blocks(const orc_fmt_t *f, const int8_t *llrf, const double *sub_est, co
 // The sampler's exact walk (liblizard/src/acquire.c:5121-5196): reg = H (9) then the node mesh's (dx, dy).
 int orc_layout_nodes(int side, float *pos);
 int orc_sample_grid(int n, int span, const uint8_t *luma, int w, int h, int pitch, const float *reg, float *grid);
+// The sampler as the x86-64 decode runs it (liblizard/src/acquire.c:5302-5440 with its integer read :723-779; the calls
+// of liblizard/src/lizard_phy.c:1611, 1634): the grid (n x n) in strips of 64 columns, and the shading fit's samples.
+int orc_sample_decode(int n, int span, const uint8_t *luma, int w, int h, int pitch, const float *reg, float *grid, float *shade);
 
 // The anchor search (liblizard/src/acquire.c:1876-2036, the portable build): one frame (w x h greys, rows w apart),
 // H (module -> image, 9 floats), the lens model (NULL, or K, ax, ay, R, then 11 coefficients), the anchors already

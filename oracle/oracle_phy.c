@@ -526,3 +526,83 @@ int orc_sample_grid(int n, int span, const uint8_t *luma, int w, int h, int pitc
   }
   return nn;
 }
+
+// ------------------------------------------------------------------ the sampler as the decode runs it (row a)
+
+// The decode's picture read at gamma 1 on x86-64 (liblizard/src/acquire.c:5302-5440 sample_grid_lin, reached through
+// ob_sample_grid_pic :5465-5480), restated in plain C: one call samples columns x0 .. x0 + nx - 1 of rows
+// 0 .. ny - 1 of the regular grid at (mx0 + x step, my0 + y step), in chunks of 256 columns. Per chunk and mesh row
+// every column's displacement terms D + v E (liblizard/src/acquire.c:5330-5346, the column's place u in its mesh cell
+// first, :5310-5316); per row the homography's numerators and denominator as four-column lanes stepped by four
+// columns at a time (:5348-5358: lane l starts at l (h step) + (h m0 + row terms), each step adds 4 (h step)); then
+// the point (less the half pixel, x a 512th on) read in integers (:723-779 lin_pts, lin_grey, lin_get): 16.16
+// coordinates clamped at 0 and 32767, the integer parts clamped to w - 2 and h - 2, fx the x fraction's top byte, fy
+// the y fraction's top 15 bits; each row's pair blended as 256 a + (b - a) fx, the rows' halved difference times fy
+// rounded (PMULHRSW), plus the top row's half: 128 times the grey, times 257 / 2^23 as a float. No fused operations.
+static int lin_q16(float v) {
+  if (!(v > 0)) v = 0;                 // MAXPS with 0: below 0, and NaN, read as 0
+  if (v > 32767.0f) v = 32767.0f;
+  return (int)(v * 65536.0f);          // CVTTPS2DQ: truncation; the product is exact
+}
+static float lin_read_point(const uint8_t *luma, int w, int h, int pitch, float X, float Y) {
+  const int xq = lin_q16(X), yq = lin_q16(Y);
+  int xi = xq >> 16, yi = yq >> 16;
+  if (xi > w - 2) xi = w - 2;
+  if (yi > h - 2) yi = h - 2;
+  const int fx = (xq >> 8) & 0xff, fy = (yq & 0xffff) >> 1;
+  const uint8_t *p = luma + (size_t)yi * pitch + xi;
+  const int a = p[0], b = p[1], c = p[pitch], d = p[pitch + 1];
+  const int top = 256 * a + (b - a) * fx, bot = 256 * c + (d - c) * fx;
+  const int hd = (bot - top) >> 1;                        // floor of the halved difference (PAVGW with the complement)
+  const int r = ((hd * fy + (1 << 14)) >> 15) + (top >> 1);   // PMULHRSW's rounding, plus the top row's half
+  return (float)r * (257.0f / 8388608.0f);
+}
+static void sample_lin_call(const float *node, int nn, const float *H, const float *nodes, const uint8_t *luma, int w, int h, int pitch,
+                            float mx0, float my0, float step, int x0, int nx, int y0, int ny, float *out, int opitch) {
+  for (int c0 = 0; c0 < nx; c0 += 256) {
+    const int cx0 = x0 + c0, cnx = nx - c0 < 256 ? nx - c0 : 256;
+    float tu[256];
+    int ti[256];
+    for (int k = 0; k < cnx; k++) {
+      const float mx = mx0 + (float)(cx0 + k) * step;
+      const int i = cell_of(node, nn, mx);
+      const float inv = 1.0f / (node[i + 1] - node[i]);
+      ti[k] = i;
+      tu[k] = (mx - node[i]) * inv;
+    }
+    const float m0 = mx0 + (float)cx0 * step;
+    const float hw = H[6] * step, hu = H[0] * step, hv = H[3] * step;
+    const float Cw = 4 * hw, Cu = 4 * hu, Cv = 4 * hv;
+    for (int yy = 0; yy < ny; yy++) {
+      const float my = my0 + (float)(y0 + yy) * step;
+      const int j = cell_of(node, nn, my);
+      const float vv = (my - node[j]) / (node[j + 1] - node[j]);
+      const float bw = H[6] * m0 + (H[7] * my + 1), bu = H[0] * m0 + (H[1] * my + H[2]), bv = H[3] * m0 + (H[4] * my + H[5]);
+      float nw[4], nu[4], nv[4];
+      for (int l = 0; l < 4; l++) { nw[l] = (float)l * hw + bw; nu[l] = (float)l * hu + bu; nv[l] = (float)l * hv + bv; }
+      for (int k = 0; k < cnx; k++) {
+        const int l = k & 3;
+        if (k && !l) for (int q = 0; q < 4; q++) { nw[q] = nw[q] + Cw; nu[q] = nu[q] + Cu; nv[q] = nv[q] + Cv; }
+        const float *a = nodes + 2 * (j * nn + ti[k]), *b = a + 2 * nn;
+        const float U = tu[k];
+        const float dx = (a[0] - (0.5f - 1.0f / 512)) + (a[2] - a[0]) * U, ex = (b[0] - a[0]) + ((b[2] - b[0]) - (a[2] - a[0])) * U;
+        const float dy = (a[1] - 0.5f) + (a[3] - a[1]) * U, ey = (b[1] - a[1]) + ((b[3] - b[1]) - (a[3] - a[1])) * U;
+        const float rw = 1.0f / nw[l];
+        const float X = (dx + ex * vv) + nu[l] * rw, Y = (dy + ey * vv) + nv[l] * rw;
+        out[(size_t)yy * opitch + k + c0] = lin_read_point(luma, w, h, pitch, X, Y);
+      }
+    }
+  }
+}
+
+// The picture grid as the decode samples it (liblizard/src/lizard_phy.c:1634: one call a strip of 64 columns over
+// every row) into grid (row-major n x n), and the shading fit's samples (:1611: one call over every eighth row and
+// column at eight steps) into shade ((n / 8)^2, row-major; NULL: not taken). reg = H (9) then the mesh's (dx, dy).
+int orc_sample_decode(int n, int span, const uint8_t *luma, int w, int h, int pitch, const float *reg, float *grid, float *shade) {
+  float node[40];
+  const int nn = orc_layout_nodes(span + 2 * MARGIN, node);
+  const float scale = (float)n / span, g0 = MARGIN + 0.5f / scale, step = 1.0f / scale;
+  for (int x0 = 0; x0 < n; x0 += 64) sample_lin_call(node, nn, reg, reg + 9, luma, w, h, pitch, g0, g0, step, x0, 64, 0, n, grid + x0, n);
+  if (shade) sample_lin_call(node, nn, reg, reg + 9, luma, w, h, pitch, g0, g0, 8 * step, 0, n / 8, 0, n / 8, shade, n / 8);
+  return nn;
+}

@@ -257,3 +257,27 @@ int refh_layout_kind(lizard_t *f, int fps, uint8_t *kind) {
   memcpy(kind, f->frame.kind, (size_t)f->frame.w * f->frame.h);
   return f->frame.w;
 }
+
+// The picture grid as the decode itself samples it (lizard_phy.c:1634: ob_sample_grid_pic a strip of LIZARD_STRIP
+// columns at a time) into grid (row-major n x n), and the shading fit's samples (:1611: one call over every eighth
+// row and column) into shade ((n / 8)^2, row-major, or NULL), on a given registration (H, then the nodes).
+int ref_sample_decode(lizard_t *f, const uint8_t *luma, int iw, int ih, const float *reg, float *grid, float *shade) {
+  image_t im;
+  ob_image_init(&im, luma, iw, ih, 1.0f);
+  const ob_layout_t *L = &f->frame;
+  ob_reg_t r;
+  memcpy(r.H.h, reg, 9 * sizeof(float));
+  r.nodes = calloc((size_t)L->nx * L->ny, sizeof(node_t));
+  for (int k = 0; k < L->nx * L->ny; k++) { r.nodes[k].dx = reg[9 + 2 * k]; r.nodes[k].dy = reg[10 + 2 * k]; }
+  const float g0 = f->margin + 0.5f / f->scale, step = 1.0f / f->scale;
+  const int n = f->n, sw = LIZARD_STRIP, c = n / 8;
+  float *strip = malloc((size_t)n * sw * sizeof(float));
+  for (int x0 = 0; x0 < n; x0 += sw) {
+    ob_sample_grid_pic(L, &im, &r, g0, g0, step, x0, sw, 0, n, strip, sw);
+    for (int y = 0; y < n; y++) memcpy(grid + (size_t)y * n + x0, strip + (size_t)y * sw, sw * sizeof(float));
+  }
+  if (shade) ob_sample_grid_pic(L, &im, &r, g0, g0, 8 * step, 0, c, 0, c, shade, c);
+  free(strip);
+  free(r.nodes);
+  return im.lin;
+}

@@ -1,5 +1,6 @@
-"""Row a, the picture sampler: the oracle's exact walk held to the reference's (where built here) and, on the GPU,
-the sampler kernel held to the oracle bit for bit, then rows a-e end to end from captured luma frames."""
+"""Row a, the picture sampler in its two reads: the oracle's exact walk and its restatement of the decode's integer
+read held to the reference's own (where built here) and, on the GPU, the sampler kernel and the transform's fused
+sampling held to the oracle bit for bit, then rows a-e end to end from captured luma frames."""
 import numpy as np
 import pytest
 
@@ -33,6 +34,21 @@ def test_oracle_walk_matches_reference(n, subch, W, H, warped):
     assert np.abs(r.sample_grid(luma, reg[:9], reg[9:], fast=True) - go).max() < 1 / 200
 
 
+@pytest.mark.skipif(not oracle.have_ref(), reason="the reference is not built here")
+@pytest.mark.parametrize("n,subch,W,H,warped", CASES)
+def test_oracle_decode_read_matches_reference(n, subch, W, H, warped):
+    """The decode's own read (strips of 64 columns, the integer read) and the shading fit's samples, bit for bit."""
+    f, luma, reg, _ = frame(n, subch, W, H, warped, mesh=0.6)
+    o, r = oracle.Fmt(n, subch, 128), oracle.RefFmt(n, subch, 128)
+    go, so = o.sample_decode(luma, reg)
+    gr, sr, lin = r.sample_decode(luma, reg[:9], reg[9:])
+    assert lin
+    assert np.array_equal(go.view(np.uint32), gr.view(np.uint32))
+    assert np.array_equal(so.view(np.uint32), sr.view(np.uint32))
+    # the same map as the exact walk, within the reference's own bar of 1/200 of a grey level
+    assert np.abs(go - o.sample(luma, reg)).max() < 1 / 200
+
+
 @pytest.mark.parametrize("n,subch,W,H,warped", CASES)
 def test_captures_decode_in_the_oracle(n, subch, W, H, warped):
     f, luma, reg, blocks = frame(n, subch, W, H, warped)
@@ -42,13 +58,14 @@ def test_captures_decode_in_the_oracle(n, subch, W, H, warped):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("read", ["decode", "exact"])
 @pytest.mark.parametrize("n,subch,W,H,warped", CASES)
-def test_gpu_luma_path_matches_oracle(n, subch, W, H, warped):
+def test_gpu_luma_path_matches_oracle(n, subch, W, H, warped, read):
     import torch
     f, luma, reg, blocks = frame(n, subch, W, H, warped, mesh=0.3 if warped else 0.0)
     o = oracle.Fmt(n, subch, 128)
-    go = o.sample(luma, reg)
-    rx = lz.Receiver(n, subch, 128, max_frames=2)
+    go = o.sample(luma, reg) if read == "exact" else o.sample_decode(luma, reg)[0]
+    rx = lz.Receiver(n, subch, 128, max_frames=2, read=read)
     out = rx.finish_luma(np.stack([luma, luma]), np.stack([reg, reg]))
     for k in range(2):
         assert np.array_equal(out["grid"][k], go)
