@@ -159,23 +159,65 @@ def traffic_per_step(count):
         return None
 
 
-def cpu_decode(batch, threads, sample):
-    """The CPU decoder on the first `sample` codewords: (Gbit/s, seconds, kind)."""
+def cpu_decode(batch, threads, sample, outputs=False):
+    """The CPU decoder on the first `sample` codewords: (Gbit/s, seconds, kind), and with outputs its (packed bits,
+    its, ok)."""
     import numpy as np
     import oracle
     lib, kind = (oracle.ref(), "reference") if oracle.have_ref() else (oracle.port(), "port")
     n = int(batch["offsets"][sample - 1]) + {6: 4608, 4: 5120, 3: 5760, 2: 7680}[int(batch["rates"][sample - 1])] if sample < batch["rates"].size else batch["llr"].size
     t0 = time.perf_counter()
-    oracle.ldpc_batch(lib, batch["llr"][:n], batch["offsets"][:sample], batch["rates"][:sample], MAX_ITER, STALL_IT, STALL_RATIO, threads=threads)
+    out = oracle.ldpc_batch(lib, batch["llr"][:n], batch["offsets"][:sample], batch["rates"][:sample], MAX_ITER, STALL_IT, STALL_RATIO, threads=threads)
     dt = time.perf_counter() - t0
+    if outputs:
+        return sample * 3840 / dt / 1e9, dt, kind, out
     return sample * 3840 / dt / 1e9, dt, kind
+
+
+def ref_over_port():
+    """The reference decoder's speed over the restatement's on one host (oracle/ref_vs_port.json, measured where the
+    reference compiles), or None."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "oracle", "ref_vs_port.json")))
+        return float(d["reference_over_port"]), d["host"]["machine"], d["runs"][-1]["threads"]
+    except Exception:
+        return None
+
+
+def reference_estimate(value, kind):
+    """A restatement's figure converted to the reference decoder's by the factor measured where both run."""
+    f = ref_over_port()
+    if kind != "port" or f is None:
+        return None
+    return {"value": round(value * f[0], 4), "unit": UNIT, "factor": f[0],
+            "source": "oracle/ref_vs_port.json: the reference's own ldpc_decode_stall (its SIMD layers) over the restatement, "
+                      "same batch, %d threads of an %s host; the GPU host (aarch64) has no reference tree to time it there" % (f[2], f[1]),
+            "measured": False}
+
+
+# Integer operations an edge update costs at the least in layered min-sum (liblizard/src/ldpc.c:141-192): the extrinsic
+# q = L - R, its saturation to 8 bits, |q|, the running min1 / min2 (two min/max), the sign's XOR, the message's
+# sign select, the posterior L = q + R.
+OPS_PER_EDGE = 8
+ALU_LANES_PER_SM = 64   # 4 sub-partitions x 16 lanes: one ALU warp-instruction every 2 cycles each
+
+
+def int_op_roofline(edges, launch_ms, sm_mhz, sms):
+    """The decoder's integer roofline from this run: edge updates a second x OPS_PER_EDGE against the ALU pipe's
+    peak at the run's median SM clock."""
+    if not sm_mhz:
+        return None
+    achieved = edges / (launch_ms / 1e3) * OPS_PER_EDGE / 1e12
+    peak = sms * ALU_LANES_PER_SM * sm_mhz * 1e6 / 1e12
+    return {"achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "Tops/s", "frac": round(achieved / peak, 4),
+            "ops_per_edge_update": OPS_PER_EDGE, "peak_from": "%d SMs x %d ALU lanes x the median SM clock under load (%.0f MHz)" % (sms, ALU_LANES_PER_SM, sm_mhz)}
 
 
 def picture_frames(fmt, unique, copies, seed, sigma):
     """unique painted pictures (n x n, AWGN of sigma grey levels) each repeated `copies` times, as luma frames of
     the picture alone (w = h = n), with the registration that samples them one pixel a sample."""
     import numpy as np
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     rng = np.random.default_rng(seed)
     n, scale = fmt.n, fmt.n / fmt.span
     nn = synth.layout_nodes(fmt.span).size
@@ -193,7 +235,7 @@ def bench_receiver(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     res = {}
     sp = stream.cuda_stream
     # --- FFT demod batch
@@ -294,7 +336,7 @@ def bench_anchor(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     import oracle
     span, n, subch, W, Hh, frames, distinct = 256, 1536, 1024, 1920, 1080, 64, 8
     fmt = lz.Format(n, subch, span)
@@ -374,7 +416,7 @@ def bench_multistream(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     W, Hh = 3840, 2160
     formats = [(384, 64, 128, 10), (768, 320, 128, 8), (1152, 720, 256, 6), (1536, 1024, 256, 5), (1536, 1024, 512, 3)]
     eng = lz.Engine()
@@ -543,7 +585,7 @@ def bench_border_nodes(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     import oracle
     span, n, subch, W, Hh, frames, distinct = 256, 1536, 1024, 1920, 1080, 64, 8
     fmt = lz.Format(n, subch, span)
@@ -614,7 +656,7 @@ def bench_fmt_word(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     import oracle
     span, W, Hh, frames, distinct = 256, 1280, 720, 2048, 32
     lumas, regs, words = [], [], []
@@ -689,7 +731,7 @@ def bench_encoder(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     res = {}
     for name, (n, subch, span, frames) in (("lizard1024_128ring", (1536, 1024, 256, 32)), ("lizard64_64ring", (384, 64, 128, 256))):
         fmt = lz.Format(n, subch, span)
@@ -729,7 +771,7 @@ def _render_distorted(job):
     """One distorted capture (a worker of bench_refinement's process pool): job = (index, k1, blur)."""
     import numpy as np
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     k, k1, blur = job
     fmt = lz.Format(1536, 1024, 256)
     rng = np.random.default_rng(9000 + k)
@@ -833,7 +875,7 @@ def run_reference(args, rank, ws):
     """The reference arm: the reference's CPU decoder on the host cores, same metric and workload."""
     if rank != 0:
         return
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     import oracle
     if not os.path.exists(oracle.PORT_PATH):
         oracle.build(ref=False)
@@ -852,8 +894,46 @@ def run_reference(args, rank, ws):
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8/int16",
                       "data": "synthetic", "config": workload(args.count),
                       "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": kind,
-                                       "sample": "the whole %d-codeword batch a step" % args.count},
+                                       "sample": "the whole %d-codeword batch a step" % args.count,
+                                       "reference_estimate": reference_estimate(value, kind)},
                       "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def bench_noalloc(batch, d_llr, stream):
+    """The allocation-free decode (lizg_ldpc_decode_noalloc: the four codes one after another on the caller's stream)
+    against a plan (the codes overlapped on side streams) on the batch's first LIZG_NOALLOC_MAX_CODEWORDS codewords,
+    device-resident; outputs checked identical."""
+    import ctypes
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    count = 8192
+    rates = np.ascontiguousarray(batch["rates"][:count])
+    plan = lz.LdpcPlan(rates, MAX_ITER, STALL_IT, STALL_RATIO)
+    fn = lz.lib().lizg_ldpc_decode_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float] + [ctypes.c_void_p] * 4
+    d_rate = torch.from_numpy(rates).cuda()
+    outs = [(torch.empty(plan.llr_bytes // 8, dtype=torch.uint8, device="cuda"), torch.empty(count, dtype=torch.int32, device="cuda"),
+             torch.empty(count, dtype=torch.uint8, device="cuda")) for _ in range(2)]
+    sp = stream.cuda_stream
+    calls = {"plan": lambda o: plan.run_dev(d_llr.data_ptr(), o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), sp),
+             "noalloc": lambda o: lz._check(fn(d_llr.data_ptr(), d_rate.data_ptr(), count, MAX_ITER, STALL_IT, STALL_RATIO, o[0].data_ptr(),
+                                                  o[1].data_ptr(), o[2].data_ptr(), sp), "lizg_ldpc_decode_noalloc")}
+    res = {"workload": "the first %d codewords of the batch, device-resident" % count}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for (name, call), o in zip(calls.items(), outs):
+        for _ in range(3):
+            call(o)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(20):
+            call(o)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[name + "_ms"] = round(e0.elapsed_time(e1) / 20, 4)
+    res["identical"] = all(torch.equal(a, b) for a, b in zip(outs[0], outs[1]))
+    res["noalloc_over_plan_time"] = round(res["noalloc_ms"] / res["plan_ms"], 3)
+    return res
 
 
 def bench_ldpc_variants(args, stream):
@@ -863,7 +943,7 @@ def bench_ldpc_variants(args, stream):
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     b = synth.ldpc_batch(args.count, seed=1000)
     out = {}
     for name, r in zip(("7/8", "3/4", "2/3", "1/2"), (6, 4, 3, 2)):
@@ -908,7 +988,7 @@ def main():
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     assert torch.cuda.is_available(), "bench.py needs a CUDA device"
     dev = local
     torch.cuda.set_device(dev)
@@ -1026,10 +1106,14 @@ def main():
                "staged": {"value": gbit(s_ms), "ms_per_step": round(s_ms, 3),
                           "route": "the same pinned buffers copied in and out by cudaMemcpyAsync, two chunks pipelined"}}
 
+    noalloc = bench_noalloc(batch, d_llr, stream) if rank == 0 else None
     if rank != 0:
         return
     alg_bytes = plan.llr_bytes + plan.llr_bytes // 8 + plan.count * 5
     peak, peak_src = peaks()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") if isinstance(clocks, dict) else None
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     traffic = traffic_per_step(args.count)
     out = {
@@ -1046,16 +1130,19 @@ def main():
                      "traffic": None if traffic is None else int(traffic), "peak_source": peak_src,
                      "kernel": "ldpc_decode_kernel<7/8,3/4,2/3,1/2> (the 4 launches of a step)",
                      "note": "not HBM bound: the min-sum minima issue on the ALU pipe (every min/max form does on sm_103a); "
-                             "see ldpc.edge_updates_per_s and alu_pipe",
-                     "alu_pipe": {"active_frac": 0.856, "kernel": "ldpc_decode_kernel 7/8 code (41% of a step), 2 warps a codeword, "
-                                                                   "pair form with the loop",
-                                  "source": "ncu sm__pipe_alu_cycles_active, profiles/ldpc_decode_65536cw.md (python bench.py "
-                                            "--ldpc-variants --count 16384)"}},
+                             "int_op is its roofline",
+                     "int_op": int_op_roofline(edges, launch_ms, sm_mhz, sms),
+                     "alu_pipe": {"active_frac": 0.856, "measured": False,
+                                  "kernel": "ldpc_decode_kernel 7/8 code (41% of a step), 2 warps a codeword, pair form with the loop",
+                                  "source": "imported from one ncu capture (sm__pipe_alu_cycles_active, profiles/ldpc_decode_65536cw.md, "
+                                            "python bench.py --ldpc-variants --count 16384), not measured in this run"}},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     if e2e:
         out["e2e"] = e2e
+    if noalloc:
+        out["ldpc"]["noalloc"] = noalloc
     if not args.no_receiver:
         out["receiver"] = bench_receiver(args, stream)
         out["registration"] = {"anchor_search": bench_anchor(args, stream), "refinement": bench_refinement(args, stream),
@@ -1065,9 +1152,15 @@ def main():
         out["receiver"]["multistream"] = bench_multistream(args, stream)
     if ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, dt, kind = cpu_decode(batch, threads, args.count)
+        v, dt, kind, (cb, ci, co) = cpu_decode(batch, threads, args.count, outputs=True)
         out["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": kind,
                                "sample": "the whole %d-codeword batch once (%.1f s wall on %d threads)" % (args.count, dt, threads)}
+        est = reference_estimate(v, kind)
+        if est:
+            out["cpu_baseline"]["reference_estimate"] = est
+        # the CPU decoder's outputs for every codeword of the batch against the GPU's: bits, iterations, CRC verdicts
+        out["ldpc"]["bit_exact_full_batch"] = bool(np.array_equal(ci, its) and np.array_equal(co, ok) and np.array_equal(cb, bits_dev))
+        out["ldpc"]["full_batch_checked_against"] = "the CPU decoder of cpu_baseline (%s), all %d codewords" % (kind, args.count)
     print(json.dumps(out))
 
 

@@ -102,7 +102,10 @@ int lizg_ldpc_plan_launches(const lizg_ldpc_plan *p);
 // rates); d_rate holds the count rate indices in device memory; a codeword whose rate has no code gets its = -4.
 // Queued on `stream`. The first call on a device looks up the array's address there; make that first call before
 // any stream capture. Every call shares the one array, so calls whose work overlaps on the GPU (other streams, other
-// host threads) race; serialise them. count above the maximum is refused with LIZG_E_ARG.
+// host threads) race; serialise them. count above the maximum is refused with LIZG_E_ARG. The address is kept for
+// the life of the process: do not use this entry point across a device reset (cudaDeviceReset, or the primary
+// context torn down), after which it would be stale. The four codes run one after another on `stream` (the plan API
+// overlaps them on side streams), so a mixed-rate batch takes a little longer than through a plan.
 enum { LIZG_NOALLOC_MAX_CODEWORDS = 8192 };
 int lizg_ldpc_decode_noalloc(const int8_t *d_llr, const int32_t *d_rate, int count, int max_iter, int stall_it,
                              float stall_ratio, uint8_t *d_bits, int32_t *d_its, uint8_t *d_ok, void *stream);
@@ -204,6 +207,14 @@ int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int
 // into the same buffers, where the launches would otherwise cost more than the work.
 int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg,
                               int frames, const lizg_rx_out *out, float *d_grid, float *d_coef, void *stream);
+// lizg_rx_finish_luma_dev from host memory, for a caller with no device buffers of its own (the reference's codec
+// finishing a frame it registered on the CPU): luma frames (w x h, rows pitch bytes apart, frames frame_stride apart)
+// and their registrations (frames x (9 + 2 nx ny) floats) copied to the handle's device buffers (grown to the largest
+// call), decoded on the handle's own stream, and blocks (frames x blocks x 476), ok and its (frames x blocks) written
+// before the call returns. Returns the blocks verified. The replacement for lizard_finish(f, NULL, blocks, ok, res)
+// on a held registration (liblizard/src/lizard_phy.h:236), its per-block iterations as lizard_block_stats gives them.
+int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int pitch, int64_t frame_stride, const float *reg, int frames,
+                             uint8_t *blocks, uint8_t *ok, int32_t *its);
 
 // ---------------------------------------------------------------- the multi-stream engine
 //
@@ -231,6 +242,56 @@ int lizg_engine_add_format(lizg_engine *e, int n, int subch, int span, int max_f
 lizg_rx *lizg_engine_rx(lizg_engine *e, int format);
 int lizg_engine_run_dev(lizg_engine *e, const lizg_engine_batch *b, int nb, void *stream);
 int lizg_engine_launches(const lizg_engine *e);
+
+// ---------------------------------------------------------------- the batching front (camera frames in, blocks out)
+//
+// The reference's receiver engine as the apps drive it (liz_receiver_new / _push / _batch_cap / _stats / _series /
+// _wants_luma / _free, liblizard/include/lizard.h:252-294), for frames whose registration is already held (the
+// registration front half is the caller's). A push copies the luma plane and its registration into a page-locked
+// slot of the front's, or drops the frame when every slot waits (counted), and calls release(user, tag) before it
+// returns: the caller's buffer is its own again. It never waits on the device. The front's own thread takes the
+// waiting frames in push order, up to the batch cap of one frame size at a time (a launch goes as soon as a frame
+// waits), decodes them in one lizg_rx_finish_luma_dev call on its own stream, and calls frame() for each from that
+// thread: its tag and timestamp, its verified blocks packed (count x 476 bytes, as liz_decode packs them), and every
+// block's CRC verdict and LDPC iterations. One handle is one format: n, subch, span as lizg_rx_new takes them.
+typedef struct lizg_receiver lizg_receiver;
+typedef struct {
+  int n, subch, span;      // the format of the frames pushed
+  int max_w, max_h;        // the largest luma plane a push brings
+  int batch_cap;           // the most frames a launch takes, 1 to 32 (0: 32)
+  int slots;               // frames that may wait, 1 to 128 (0: 64)
+  int read;                // LIZG_READ_DECODE or LIZG_READ_EXACT
+  void (*frame)(void *user, uint64_t tag, int64_t timestamp_ns, const uint8_t *verified, int count, const uint8_t *ok,
+                const int32_t *its, int blocks);   // NULL none; called from the front's thread
+  void (*log)(void *user, const char *line);       // NULL none; called from the front's thread
+  void *user;
+} lizg_receiver_config;
+// NULL on failure (lizg_last_error). Replaces liz_receiver_new (liblizard/include/lizard.h:270).
+lizg_receiver *lizg_receiver_new(const lizg_receiver_config *config, void (*release)(void *user, uint64_t tag));
+// Every frame pushed decoded and delivered, then the handle let go. Replaces liz_receiver_free (:271).
+void lizg_receiver_free(lizg_receiver *r);
+// One frame's luma plane (w x h, rows stride bytes apart) at timestamp_ns on the camera's clock, with its registration
+// (9 + 2 nx ny floats: H, then the node mesh, as lizg_rx_finish_luma_dev takes it). Copied or dropped, and
+// release(tag) called, before it returns. LIZG_OK, or LIZG_E_ARG. Replaces liz_receiver_push (:274), the registration
+// added.
+int lizg_receiver_push(lizg_receiver *r, const uint8_t *luma, int w, int h, int stride, int64_t timestamp_ns, uint64_t tag,
+                       const float *reg);
+// The most frames a launch takes, 1 to 32 (0: 32). Replaces liz_receiver_batch_cap (:287).
+void lizg_receiver_batch_cap(lizg_receiver *r, int frames);
+// 1: frames come as luma planes. Replaces liz_receiver_wants_luma (:279).
+int lizg_receiver_wants_luma(lizg_receiver *r);
+// A snapshot as JSON (frames in, dropped, decoded, waiting, batches and their mean size B, the cap, blocks verified and
+// new, GPU ms a frame, frames a second, goodput), valid until the next call on the handle. Replaces
+// liz_receiver_stats (:280).
+const char *lizg_receiver_stats(lizg_receiver *r);
+// The format's version (subch / 16), then 8 doubles a frame decoded after since_ms on the camera's clock, oldest
+// first: ms, verified blocks, new blocks, decoded (1, or 0 where the batch failed), the pilots' mean reading and its
+// standard error over the even blocks, then over the odd (NaN where none read). At most cap doubles; returns how many.
+// Replaces liz_receiver_series (:284).
+int lizg_receiver_series(lizg_receiver *r, double since_ms, double *out, int cap);
+// Waits until every frame pushed so far is decoded and delivered; returns the frames decoded. No counterpart in the
+// reference (its receiver only ever runs on): for a caller that must know its frames are through (a test, a shutdown).
+int lizg_receiver_flush(lizg_receiver *r);
 
 // ---------------------------------------------------------------- registration assist: the anchor search
 //

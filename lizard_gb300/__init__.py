@@ -216,6 +216,7 @@ def _rx_sigs(L):
     L.lizg_rx_perm.argtypes = [P, I, P]
     L.lizg_rx_launches.argtypes = [P]
     L.lizg_rx_set_read.argtypes = [P, I]
+    L.lizg_layout_nodes.argtypes = [I, P, P, P]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
     L.lizg_rx_finish_grid_dev.argtypes = [P, P, I, P, P, P]
     L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
@@ -546,8 +547,7 @@ def border_nodes(span, luma, H, lens=None, stream=None):
         lu = lu[None]
     frames, h, w = lu.shape
     Hf = np.ascontiguousarray(np.asarray(H, np.float32).reshape(frames, -1))
-    from . import synth
-    nn = synth.layout_nodes(span).size
+    nn = int(lib().lizg_layout_nodes(span, None, None, None))
     d_l, d_h = torch.from_numpy(lu).cuda(), torch.from_numpy(Hf).cuda()
     d_lens = None if lens is None else torch.from_numpy(np.ascontiguousarray(np.asarray(lens, np.float64).reshape(frames, 15))).cuda()
     d_n = torch.zeros((frames, nn, nn, 4), dtype=torch.float32, device="cuda")

@@ -2,6 +2,7 @@
 // and the order the receive kernels run in. Host C++.
 #include "lizard_gb300.h"
 #include "format.h"
+#include "lizard_codes.h"
 #include "lizg_internal.h"
 #include <cuda_runtime.h>
 #include <cmath>
@@ -47,6 +48,15 @@ struct lizg_rx {
   cudaGraphExec_t graph = nullptr;
   std::vector<uintptr_t> graph_key;
   int graph_launches = 0;
+  // lizg_rx_finish_luma_host's device copies of its inputs and outputs, grown to the largest call, and its stream
+  struct Staged {
+    uint8_t *luma = nullptr, *blocks = nullptr, *ok = nullptr;
+    float *reg = nullptr;
+    int32_t *its = nullptr;
+    size_t luma_bytes = 0;
+    int frames = 0;
+    cudaStream_t st = nullptr;
+  } hs;
 };
 
 namespace {
@@ -200,6 +210,8 @@ void lizg_rx_free(lizg_rx *r) {
   if (r->fork) cudaEventDestroy(r->fork);
   if (r->graph) cudaGraphExecDestroy(r->graph);
   if (r->cap) cudaStreamDestroy(r->cap);
+  cudaFree(r->hs.luma); cudaFree(r->hs.reg); cudaFree(r->hs.blocks); cudaFree(r->hs.ok); cudaFree(r->hs.its);
+  if (r->hs.st) cudaStreamDestroy(r->hs.st);
   delete r;
 }
 
@@ -412,6 +424,51 @@ int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, i
     return lizg::record_error(LIZG_E_CUDA, (std::string("graph launch: ") + cudaGetErrorString(e)).c_str());
   r->launches = r->graph_launches;
   return 0;
+}
+
+// Rows (a) to (e) from frames and registrations in host memory: copied to the handle's device buffers (grown to the
+// largest call), decoded as lizg_rx_finish_luma_dev on the handle's own stream, the blocks, verdicts and iterations
+// copied back before the call returns.
+int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int pitch, int64_t frame_stride, const float *reg, int frames,
+                             uint8_t *blocks, uint8_t *ok, int32_t *its) {
+  if (!r || !luma || !reg || !blocks || !ok || !its) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_luma_host: NULL argument");
+  if (frames < 1 || frames > r->max_frames) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_luma_host: frames out of 1..max_frames");
+  if (w < 2 || h < 2 || pitch < w || frame_stride < (int64_t)pitch * h) return lizg::record_error(LIZG_E_ARG, "lizg_rx_finish_luma_host: bad frame geometry");
+  int sms = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  auto &hs = r->hs;
+  const size_t lb = (size_t)w * h * frames, nb = (size_t)r->f.blocks * frames, rs = 9 + 2 * (size_t)r->sd.nx * r->sd.ny;
+  cudaError_t e = cudaSuccess;
+  auto fail = [&](const char *what) { return lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_finish_luma_host: ") + what + ": " + cudaGetErrorString(e)).c_str()); };
+  if (!hs.st && (e = cudaStreamCreateWithFlags(&hs.st, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream");
+  if (lb > hs.luma_bytes) {
+    cudaFree(hs.luma); hs.luma = nullptr; hs.luma_bytes = 0;
+    if ((e = cudaMalloc(&hs.luma, lb)) != cudaSuccess) return lizg::record_error(LIZG_E_NOMEM, "lizg_rx_finish_luma_host: device memory");
+    hs.luma_bytes = lb;
+  }
+  if (frames > hs.frames) {
+    cudaFree(hs.reg); cudaFree(hs.blocks); cudaFree(hs.ok); cudaFree(hs.its);
+    hs.reg = nullptr; hs.blocks = hs.ok = nullptr; hs.its = nullptr; hs.frames = 0;
+    if (cudaMalloc(&hs.reg, rs * sizeof(float) * frames) != cudaSuccess || cudaMalloc(&hs.blocks, nb * LIZG_BLOCK_BYTES) != cudaSuccess ||
+        cudaMalloc(&hs.ok, nb) != cudaSuccess || cudaMalloc(&hs.its, nb * sizeof(int32_t)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_NOMEM, "lizg_rx_finish_luma_host: device memory");
+    hs.frames = frames;
+  }
+  if (pitch == w && frame_stride == (int64_t)w * h) e = cudaMemcpyAsync(hs.luma, luma, lb, cudaMemcpyHostToDevice, hs.st);
+  else
+    for (int k = 0; k < frames && e == cudaSuccess; k++)
+      e = cudaMemcpy2DAsync(hs.luma + (size_t)k * w * h, w, luma + k * frame_stride, pitch, w, h, cudaMemcpyHostToDevice, hs.st);
+  if (e != cudaSuccess || (e = cudaMemcpyAsync(hs.reg, reg, rs * sizeof(float) * frames, cudaMemcpyHostToDevice, hs.st)) != cudaSuccess) return fail("copy in");
+  const lizg_rx_out out{hs.blocks, hs.ok, hs.its, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (int rc = lizg_rx_finish_luma_dev(r, hs.luma, w, h, w, (int64_t)w * h, hs.reg, frames, &out, nullptr, nullptr, hs.st)) return rc;
+  if ((e = cudaMemcpyAsync(blocks, hs.blocks, nb * LIZG_BLOCK_BYTES, cudaMemcpyDeviceToHost, hs.st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(ok, hs.ok, nb, cudaMemcpyDeviceToHost, hs.st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(its, hs.its, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, hs.st)) != cudaSuccess)
+    return fail("copy out");
+  if ((e = cudaStreamSynchronize(hs.st)) != cudaSuccess) return fail("decode");
+  int verified = 0;
+  for (size_t i = 0; i < nb; i++) verified += ok[i] != 0;
+  return verified;
 }
 
 }  // extern "C"

@@ -8,7 +8,7 @@ the 7/8 code's never-sent bits fed as known zeros, +127 (liblizard/src/lizard_ph
 """
 import numpy as np
 
-from . import BLOCK_BYTES, CODE_K, CODE_N, CODE_NT, INFO_BITS, SUB, crc32c, ldpc_encode_many
+from lizard_gb300 import BLOCK_BYTES, CODE_K, CODE_N, CODE_NT, INFO_BITS, SUB, crc32c, ldpc_encode_many
 
 # Rate mix of the batch by count (the format's profile: 39% 7/8, 26% 3/4, 15% 2/3, 20% 1/2) and the Eb/N0 sweep.
 MIX = ((6, 0.39), (4, 0.26), (3, 0.15), (2, 0.20))
@@ -169,7 +169,7 @@ def grids(fmt, frames, seed=0, sigma=3.0, shift=None):
 
 def layout_nodes(span):
     """The registration mesh's node centres (module coordinates) of a ring of span modules."""
-    from . import lib, _ptr
+    from lizard_gb300 import lib, _ptr
     import ctypes
     nx = np.zeros(40, np.float32)
     nn = np.zeros(2, np.int32)

@@ -15,7 +15,10 @@ PORT_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
 REF_SCALAR_PATH = os.path.join(HERE, "_ref", "libref_scalar.so")
 REF_DEVELOP_PATH = os.path.join(HERE, "_ref", "libref_develop.so")
-REF_SRC = "/root/reference/liblizard/src"
+# The reference tree's root is LIZARD_REF (default /root/reference); the tests pinned to the reference skip where it
+# is absent or not built.
+REF_ROOT = os.environ.get("LIZARD_REF", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "liblizard", "src")
 
 _port = None
 _ref = None
@@ -32,7 +35,7 @@ def build(ref=True):
     """make the restatement, and the reference where its sources are present."""
     subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
     if ref and os.path.isdir(REF_SRC):
-        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", "LIZARD_REF=" + REF_ROOT], check=True)
 
 
 def port():

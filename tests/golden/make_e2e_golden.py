@@ -25,7 +25,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
-from lizard_gb300 import synth  # noqa: E402
+from lizard_gb300_testing import synth  # noqa: E402
 
 QUIET = 2   # the painted square's quiet margin, modules a side
 

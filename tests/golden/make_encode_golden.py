@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 import lizard_gb300 as lz  # noqa: E402
-from lizard_gb300 import synth  # noqa: E402
+from lizard_gb300_testing import synth  # noqa: E402
 from test_encode_oracle import _ref, golden_crops, ref_page  # noqa: E402
 
 

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 import oracle  # noqa: E402
-from lizard_gb300 import synth  # noqa: E402
+from lizard_gb300_testing import synth  # noqa: E402
 from test_fmt_oracle import capture_cases, random_q  # noqa: E402
 
 

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 import lizard_gb300 as lz  # noqa: E402
-from lizard_gb300 import synth  # noqa: E402
+from lizard_gb300_testing import synth  # noqa: E402
 
 
 def main():

@@ -102,7 +102,7 @@ def test_no_gpu_fails_loudly():
 
 
 def test_synth_batch_shapes():
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     b = synth.ldpc_batch(40, seed=1)
     n = sum(lz.CODE_N[int(r)] for r in b["rates"])
     assert b["llr"].size == n and b["offsets"][0] == 0

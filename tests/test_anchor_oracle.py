@@ -8,7 +8,7 @@ import pytest
 
 import lizard_gb300 as lz
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 FIELDS = ("ok", "peak", "dx", "dy", "u", "v")

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import lizard_gb300 as lz
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 from test_encode_oracle import DRIVE_TOL, FORMATS, GOLDEN, GREY_FRACTION, golden_crops
 
 pytestmark = pytest.mark.gpu

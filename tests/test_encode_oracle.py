@@ -10,7 +10,7 @@ import pytest
 
 import lizard_gb300 as lz
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "encode_ref.npz")
 # (n, subch, span): the 64 ring at exact copy, the 128 ring resampled (1.5 samples a module onto 2 pixels), n = 768 in

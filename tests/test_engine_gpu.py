@@ -6,7 +6,7 @@ import pytest
 import torch
 
 import lizard_gb300 as lz
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 pytestmark = pytest.mark.gpu
 

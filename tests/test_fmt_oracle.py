@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "fmt_ref.npz")
 SPANS = (128, 256, 512)

@@ -7,7 +7,7 @@ import pytest
 
 import lizard_gb300 as lz
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 pytestmark = pytest.mark.gpu
 

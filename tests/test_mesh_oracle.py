@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "mesh_ref.npz")
 

@@ -87,7 +87,7 @@ def test_oracle_matches_reference_golden(tag, mi, si, ratio):
 @pytest.mark.skipif(not oracle.have_ref(), reason="the reference is not built here")
 def test_oracle_batch_matches_reference_batch():
     """The port and the reference on a fresh seeded mixed-rate batch across the Eb/N0 sweep, every bit and return."""
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     b = synth.ldpc_batch(600, seed=11)
     for mi, si, ratio in [(20, 9, 0.95), (30, 9, 0.95), (12, 0, 0.0)]:
         pb, pi, po = oracle.ldpc_batch(oracle.port(), b["llr"], b["offsets"], b["rates"], mi, si, ratio, threads=8)

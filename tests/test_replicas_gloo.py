@@ -26,7 +26,7 @@ def worker(rank, ws, port, out):
     import torch.distributed as dist
     import bench
     import oracle
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     dist.init_process_group("gloo", rank=rank, world_size=ws)
     # each replica decodes its own shard of one batch with the CPU decoder (the oracle stands in for a GPU here)
     b = synth.ldpc_batch(64, seed=9)
@@ -43,7 +43,7 @@ def worker(rank, ws, port, out):
 @pytest.mark.timeout(300)
 def test_two_replicas_over_gloo():
     import oracle
-    from lizard_gb300 import synth
+    from lizard_gb300_testing import synth
     ctx = mp.get_context("spawn")
     mgr = ctx.Manager()
     out = mgr.dict()

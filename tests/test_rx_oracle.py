@@ -9,7 +9,7 @@ import pytest
 
 import lizard_gb300 as lz
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 FORMATS = [(384, 64), (384, 80), (512, 256), (768, 320), (1024, 1024), (1152, 720), (1280, 880), (1536, 1024)]

@@ -6,7 +6,7 @@ import pytest
 
 import lizard_gb300 as lz
 import oracle
-from lizard_gb300 import synth
+from lizard_gb300_testing import synth
 
 CASES = [(384, 64, 1280, 720, False), (384, 64, 1280, 720, True), (768, 320, 1920, 1080, True), (1536, 1024, 3840, 2160, True)]
 
