@@ -217,6 +217,7 @@ def _rx_sigs(L):
     L.lizg_rx_launches.argtypes = [P]
     L.lizg_rx_set_read.argtypes = [P, I]
     L.lizg_layout_nodes.argtypes = [I, P, P, P]
+    L.lizg_rx_finish_luma_host.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
     L.lizg_rx_finish_grid_dev.argtypes = [P, P, I, P, P, P]
     L.lizg_rx_finish_luma_dev.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P, P]
@@ -416,6 +417,99 @@ class Receiver:
             out["grid"] = g.cpu().numpy()
         out["coef"] = c.cpu().numpy()
         return out
+
+    def finish_luma_host(self, luma, reg):
+        """lizg_rx_finish_luma_host: frames x h x w uint8 and frames x (9 + 2 nx ny) float32 from host memory;
+        (blocks, ok, its, verified)."""
+        lu = np.ascontiguousarray(luma, np.uint8)
+        rg = np.ascontiguousarray(reg, np.float32)
+        frames, h, w = lu.shape
+        nb = frames * self.fmt.blocks
+        blocks = np.zeros((frames, self.fmt.blocks, BLOCK_BYTES), np.uint8)
+        ok = np.zeros((frames, self.fmt.blocks), np.uint8)
+        its = np.zeros((frames, self.fmt.blocks), np.int32)
+        v = _check(lib().lizg_rx_finish_luma_host(self._h, _ptr(lu), w, h, w, h * w, _ptr(rg), frames, _ptr(blocks), _ptr(ok), _ptr(its)),
+                   "lizg_rx_finish_luma_host")
+        assert ok.size == nb
+        return blocks, ok, its, v
+
+
+FRAME_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint8), ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int32), ctypes.c_int)
+LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p)
+RELEASE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64)
+
+
+class FrontConfig(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("subch", ctypes.c_int), ("span", ctypes.c_int), ("max_w", ctypes.c_int), ("max_h", ctypes.c_int),
+                ("batch_cap", ctypes.c_int), ("slots", ctypes.c_int), ("read", ctypes.c_int), ("frame", FRAME_FN), ("log", LOG_FN),
+                ("user", ctypes.c_void_p)]
+
+
+class FrontReceiver:
+    """The batching front (lizg_receiver_*): frames pushed from host memory with their registrations, decoded in
+    batches on the front's own thread. on_frame(tag, ts_ns, verified bytes, ok, its) and on_release(tag) are called
+    from C (the front's thread, or inside push)."""
+
+    def __init__(self, n, subch, span, max_w, max_h, batch_cap=0, slots=0, read="decode", on_frame=None, on_release=None, on_log=None):
+        L = lib()
+        if not hasattr(L, "_front"):
+            P, I = ctypes.c_void_p, ctypes.c_int
+            L.lizg_receiver_new.argtypes = [ctypes.POINTER(FrontConfig), RELEASE_FN]
+            L.lizg_receiver_new.restype = P
+            L.lizg_receiver_free.argtypes = [P]
+            L.lizg_receiver_push.argtypes = [P, P, I, I, I, ctypes.c_int64, ctypes.c_uint64, P]
+            L.lizg_receiver_batch_cap.argtypes = [P, I]
+            L.lizg_receiver_wants_luma.argtypes = [P]
+            L.lizg_receiver_flush.argtypes = [P]
+            L.lizg_receiver_stats.argtypes = [P]
+            L.lizg_receiver_stats.restype = ctypes.c_char_p
+            L.lizg_receiver_series.argtypes = [P, ctypes.c_double, P, I]
+            L._front = True
+
+        def frame(user, tag, ts, verified, count, ok, its, blocks):
+            if on_frame:
+                on_frame(int(tag), int(ts), bytes(ctypes.string_at(verified, count * BLOCK_BYTES)) if count else b"",
+                         np.ctypeslib.as_array(ok, (blocks,)).copy(), np.ctypeslib.as_array(its, (blocks,)).copy())
+
+        self._frame = FRAME_FN(frame)
+        self._log = LOG_FN(lambda user, line: on_log(line.decode()) if on_log else None)
+        self._release = RELEASE_FN(lambda user, tag: on_release(int(tag)) if on_release else None)
+        cfg = FrontConfig(n, subch, span, max_w, max_h, batch_cap, slots, {"decode": READ_DECODE, "exact": READ_EXACT}[read],
+                          self._frame, self._log, None)
+        h = L.lizg_receiver_new(ctypes.byref(cfg), self._release)
+        if not h:
+            raise LizgError("lizg_receiver_new: " + L.lizg_last_error().decode())
+        self._h = ctypes.c_void_p(h)
+
+    def push(self, luma, ts_ns, tag, reg):
+        lu = np.ascontiguousarray(luma, np.uint8)
+        rg = np.ascontiguousarray(reg, np.float32)
+        h, w = lu.shape
+        return _check(lib().lizg_receiver_push(self._h, _ptr(lu), w, h, w, int(ts_ns), int(tag), _ptr(rg)), "lizg_receiver_push")
+
+    def batch_cap(self, frames):
+        lib().lizg_receiver_batch_cap(self._h, frames)
+
+    def flush(self):
+        return _check(lib().lizg_receiver_flush(self._h), "lizg_receiver_flush")
+
+    def stats(self):
+        import json
+        return json.loads(lib().lizg_receiver_stats(self._h).decode())
+
+    def series(self, since_ms=-1e300, cap=1 << 16):
+        out = np.zeros(cap, np.float64)
+        k = _check(lib().lizg_receiver_series(self._h, since_ms, _ptr(out), cap), "lizg_receiver_series")
+        return out[:k]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lizg_receiver_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 class AnchorOut(ctypes.Structure):
