@@ -213,18 +213,26 @@ def int_op_roofline(edges, launch_ms, sm_mhz, sms):
             "ops_per_edge_update": OPS_PER_EDGE, "peak_from": "%d SMs x %d ALU lanes x the median SM clock under load (%.0f MHz)" % (sms, ALU_LANES_PER_SM, sm_mhz)}
 
 
-def picture_frames(fmt, unique, copies, seed, sigma):
-    """unique painted pictures (n x n, AWGN of sigma grey levels) each repeated `copies` times, as luma frames of
-    the picture alone (w = h = n), with the registration that samples them one pixel a sample."""
+def picture_frames(fmt, count, seed, sigma):
+    """count distinct pictures painted by the sender (the library's GPU encoder at the 64 ring's exact-copy scale, so
+    the picture's region of the page is the picture itself), each seeded blocks, AWGN of sigma grey levels: luma frames
+    of the picture alone (w = h = n) on the device, and the registration that samples them one pixel a sample."""
     import numpy as np
-    from lizard_gb300_testing import synth
-    rng = np.random.default_rng(seed)
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300_testing import render, synth
     n, scale = fmt.n, fmt.n / fmt.span
     nn = synth.layout_nodes(fmt.span).size
     reg = np.concatenate([np.array([scale, 0, -15 * scale, 0, scale, -15 * scale, 0, 0, 1], np.float32), np.zeros(2 * nn * nn, np.float32)])
-    pics = [synth.noisy(synth.picture(fmt, synth.random_blocks(fmt.blocks, seed * 100 + u), parity=u & 3), sigma, rng) for u in range(unique)]
-    luma = np.stack([pics[i % unique] for i in range(unique * copies)])
-    return luma, np.tile(reg, (unique * copies, 1))
+    blocks = np.stack([synth.random_blocks(fmt.blocks, seed * 1000 + u) for u in range(count)])
+    pg, pxm = render.pages(lz, n, fmt.subch, fmt.span, blocks, 1)
+    assert pxm * fmt.span == n, "an exact-copy scale"
+    o = (render.QUIET + 15) * pxm
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    pic = pg[:, o:o + n, o:o + n].to(torch.float32)
+    luma = torch.clamp(torch.round(pic + sigma * torch.randn(pic.shape, generator=gen, device="cuda")), 0, 255).to(torch.uint8)
+    return luma.contiguous(), np.tile(reg, (count, 1))
 
 
 def bench_receiver(args, stream):
@@ -244,9 +252,8 @@ def bench_receiver(args, stream):
     rxs, bufs, blocks_total, step_bytes = [], [], 0, 0
     for n, subch in sizes:
         rx = lz.Receiver(n, subch, 128, max_frames=per)
-        luma, reg = picture_frames(rx.fmt, 8, per // 8, seed=n, sigma=3.0)
+        d_l, reg = picture_frames(rx.fmt, per, seed=n, sigma=3.0)
         step_bytes += per * frame_alg_bytes(rx.fmt, reg[0], n, n)
-        d_l = torch.from_numpy(luma).cuda()
         d_r = torch.from_numpy(reg).cuda()
         o, s = rx._outputs(per, torch, keep=False)
         rxs.append(rx)
@@ -270,7 +277,8 @@ def bench_receiver(args, stream):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / K
-    res["fft_demod_batch"] = {"workload": "256 pictures, 64 each at n=384/768/1152/1536 (LIZARD-80/320/720/1024), 64 ring, AWGN 3 DN, rows a-e, one call per size",
+    res["fft_demod_batch"] = {"workload": "256 distinct pictures, 64 each at n=384/768/1152/1536 (LIZARD-80/320/720/1024), 64 ring, painted by the sender, "
+                                          "AWGN 3 DN, rows a-e, one call per size",
                               "frames_per_s": round(256 / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
                               "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
                               "gpu_launches_per_step": sum(rx.launches for rx in rxs)}
@@ -324,7 +332,86 @@ def bench_receiver(args, stream):
     res["n1536_one_frame"] = receiver_line(1536, 1024, 3840, 2160, 1, False, 50, "LIZARD-1024, n=1536, 64 ring, 3840x2160 luma, AWGN 2 DN, one frame a call")
     res["n1536_batched_graph"] = receiver_line(1536, 1024, 3840, 2160, 32, True, 5, "the same, 32 frames a call replayed from a CUDA graph")
     res["n1536_batched_vs_one_frame"] = round(res["n1536_batched_graph"]["frames_per_s"] / res["n1536_one_frame"]["frames_per_s"], 2)
+    res["n1536_batched_refined"] = batched_refined_line(rx_frames=capture_frames, timed=timed, stream=stream, one_frame=res["n1536_one_frame"])
     return res
+
+
+def batched_refined_line(rx_frames, timed, stream, one_frame):
+    """Batched and refined against the plain receiver one frame a launch, at n = 1536 on clean inputs (the same
+    frames as n1536_one_frame): 32 frames a call decoded, the frames the decode left blocks unverified in refined by
+    the adjoint refinement (lizg_field_refine_dev, gated on them; anchors measured through the registration) and
+    decoded again. Also the refinement's cost with the gate open on every frame (the outputs then checked
+    unchanged: a registration already right stays right)."""
+    import torch
+    import lizard_gb300 as lz
+    frames, W, Hh = 32, 3840, 2160
+    rx, d_l, d_r = rx_frames(1536, 1024, W, Hh, frames, seed=1536)
+    fmt = rx.fmt
+    sp = stream.cuda_stream
+    stride = d_r.shape[1]
+    d_g = torch.empty_like(d_r)
+    o, s = rx._outputs(frames, torch, keep=False)
+    o0, s0 = rx._outputs(frames, torch, keep=False)
+    d_gate = torch.zeros(frames, dtype=torch.uint8, device="cuda")
+    ao = {"ok": torch.zeros((frames, 49), dtype=torch.uint8, device="cuda")}
+    for key in ("peak", "dx", "dy", "u", "v"):
+        ao[key] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
+    a_out = lz.AnchorOut(*[ao[key].data_ptr() for key in ("ok", "peak", "dx", "dy", "u", "v")])
+    fld = lz.FieldRefiner(1536, 1024, 128, chunk=32)
+
+    def finish(d_reg, so):
+        lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W, W * Hh, lz.ctypes.c_void_p(d_reg.data_ptr()),
+                                                   frames, lz.ctypes.byref(so), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
+
+    def call(force=False):
+        d_g.copy_(d_r)
+        finish(d_g, s)
+        if force:
+            d_gate.fill_(1)
+        else:
+            d_gate.copy_((o["ok"].sum(dim=1) < fmt.blocks).to(torch.uint8))
+            if not bool(d_gate.any().item()):   # every frame verified: nothing to refine
+                return
+        lz._check(lz.lib().lizg_anchor_find_dev(128, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W * Hh, lz.ctypes.c_void_p(d_g.data_ptr()), stride,
+                                                None, None, frames, lz.ctypes.byref(a_out), lz.ctypes.c_void_p(sp)), "anchor_find")
+        fld.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_g.data_ptr(), frames, 3, a_out, d_gate.data_ptr(), None, None, sp)
+        finish(d_g, s)
+
+    finish(d_r, s0)   # the plain registration's outputs, to compare
+    ms = timed(call, 10)
+    same = bool(torch.equal(o["ok"], o0["ok"]) and torch.equal(o["its"], o0["its"]) and torch.equal(o["blocks"], o0["blocks"]))
+    refined = int(d_gate.sum().item())
+    ms_forced = timed(lambda: call(True), 3)
+    same_forced = bool(torch.equal(o["ok"], o0["ok"]))
+    fld.close()
+    fps = frames / (ms / 1e3)
+    return {"workload": "LIZARD-1024, n=1536, 3840x2160 clean captures (as n1536_one_frame), 32 frames a call: decode, the frames with "
+                        "unverified blocks refined by the adjoint refinement (3 steps, anchors measured) and decoded again",
+            "frames_per_s": round(fps, 1), "ms_per_call": round(ms, 4), "frames_refined": refined,
+            "vs_plain_one_frame_a_launch": round(fps / one_frame["frames_per_s"], 2), "identical_decoded_output": same,
+            "gate_open_on_every_frame": {"frames_per_s": round(frames / (ms_forced / 1e3), 1), "ms_per_call": round(ms_forced, 4),
+                                         "identical_crc_sets": same_forced}}
+
+
+def warped_frames(n, subch, span, W, Hh, count, seed0, scale):
+    """count distinct captures (W x Hh luma on the device): seeded blocks painted by the sender (the library's GPU
+    encoder, the page with its border), each under its own warp (synth.warp: rotation up to 15 degrees, a little
+    perspective, scale x the page's pixels a module), AWGN 3 DN, rendered on the GPU. Also the warps (3 x 3 each)."""
+    import numpy as np
+    import torch
+    import lizard_gb300 as lz
+    from lizard_gb300_testing import render, synth
+    fmt = lz.Format(n, subch, span)
+    blocks = np.stack([synth.random_blocks(fmt.blocks, seed0 + k) for k in range(count)])
+    pg, pxm = render.pages(lz, n, subch, span, blocks, 1)
+    d_l = torch.empty((count, Hh, W), dtype=torch.uint8, device="cuda")
+    Hws = []
+    for k in range(count):
+        rng = np.random.default_rng(seed0 + k)
+        Hw = np.asarray(synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=scale), np.float64).reshape(3, 3)
+        d_l[k] = render.capture(pg[k], pxm, W, Hh, Hw, 0.0, 0.0, 3.0, seed0 + k)
+        Hws.append(Hw)
+    return d_l, Hws
 
 
 def bench_anchor(args, stream):
@@ -338,22 +425,18 @@ def bench_anchor(args, stream):
     import lizard_gb300 as lz
     from lizard_gb300_testing import synth
     import oracle
-    span, n, subch, W, Hh, frames, distinct = 256, 1536, 1024, 1920, 1080, 64, 8
-    fmt = lz.Format(n, subch, span)
-    lumas, Hs = [], []
-    for k in range(distinct):
-        rng = np.random.default_rng(500 + k)
-        grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 500 + k), parity=k & 3)
-        Hw = synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.42, 0.45))
-        luma, reg = synth.capture(fmt, grey, W, Hh, H=Hw, sigma=3.0, rng=rng)
-        H = reg[:9].copy()
+    span, n, subch, W, Hh, frames = 256, 1536, 1024, 1920, 1080, 64
+    d_l, Hws = warped_frames(n, subch, span, W, Hh, frames, 500, (0.42, 0.45))
+    lumas = list(d_l.cpu().numpy())
+    Hs = []
+    for k in range(frames):
+        rng = np.random.default_rng(10500 + k)
+        H = (Hws[k] / Hws[k][2, 2]).astype(np.float32).ravel()
         H[2] += np.float32(rng.uniform(-1, 1) * 2.6)
         H[5] += np.float32(rng.uniform(-1, 1) * 2.6)
-        lumas.append(luma)
         Hs.append(H)
-    luma = np.stack([lumas[k % distinct] for k in range(frames)])
-    Hf = np.stack([Hs[k % distinct] for k in range(frames)]).astype(np.float32)
-    d_l, d_h = torch.from_numpy(luma).cuda(), torch.from_numpy(Hf).cuda()
+    Hf = np.stack(Hs).astype(np.float32)
+    d_h = torch.from_numpy(Hf).cuda()
     o = {"ok": torch.zeros((frames, 49), dtype=torch.uint8, device="cuda")}
     for key in ("peak", "dx", "dy", "u", "v"):
         o[key] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
@@ -381,10 +464,11 @@ def bench_anchor(args, stream):
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     with concurrent.futures.ThreadPoolExecutor(threads) as ex:
-        cpu = list(ex.map(lambda k: oracle.anchor_find(oracle.port(), "orc_anchor_find", span, lumas[k % distinct], Hs[k % distinct]), range(frames)))
+        cpu = list(ex.map(lambda k: oracle.anchor_find(oracle.port(), "orc_anchor_find", span, lumas[k], Hs[k]), range(frames)))
     dt = time.perf_counter() - t0
-    same = all(np.array_equal(cpu[k]["ok"], o["ok"][k].cpu().numpy()) and np.array_equal(cpu[k]["dx"], o["dx"][k].cpu().numpy()) for k in range(distinct))
-    return {"workload": "anchor search, 64 frames of 1920x1080, LIZARD-1024 (n=1536) in the 128 ring at ~2.6 px a module, rotation up to 15 deg, H up to a module off, AWGN 3 DN",
+    same = all(np.array_equal(cpu[k]["ok"], o["ok"][k].cpu().numpy()) and np.array_equal(cpu[k]["dx"], o["dx"][k].cpu().numpy()) for k in range(frames))
+    return {"workload": "anchor search, 64 distinct frames of 1920x1080, LIZARD-1024 (n=1536) in the 128 ring painted by the sender at ~2.6 px a module, "
+                        "rotation up to 15 deg, H up to a module off, AWGN 3 DN",
             "frames_per_s": round(frames / (ms / 1e3), 1), "anchors_per_s": round(49 * frames / (ms / 1e3), 1), "ms_per_call": round(ms, 4),
             "anchors_found": found, "anchors": 49 * frames, "gpu_launches_per_call": 1, "identical_to_host": bool(same),
             "cpu": {"frames_per_s": round(frames / dt, 1), "cores": threads, "kind": "port",
@@ -407,48 +491,65 @@ def frame_alg_bytes(fmt, H, w, h):
 
 
 def bench_multistream(args, stream):
-    """Batched multi-stream decode: 32 camera streams of 3840 x 2160 luma at a nominal 60 frames/s, picture sizes
-    uneven across 384-1536 and rings mixed 64 / 128 / 256 (five formats; 10, 8, 6, 5 and 3 streams), each frame
-    warped (rotation up to 15 degrees, perspective, scale 0.9-1.05) and registered by its true map. A tick (one frame
-    of every stream) runs through the multi-stream engine: one batch per format, each on its own stream from its own
-    CUDA graph. Beside it the same frames one frame a launch (lizg_rx_finish_luma_dev per frame). Device-timed; the
-    two paths' CRC-passing block sets are checked identical."""
+    """Batched multi-stream decode with device registration: 32 camera streams of 3840 x 2160 luma at a nominal 60
+    frames/s, picture sizes uneven across 384-1536 and rings mixed 64 / 128 / 256 (five formats; 10, 8, 6, 5 and 3
+    streams), each stream's frame painted by the sender and seen as the distorted full receiver's frames are (rotation
+    U(+-15 deg), tilt U(+-20 deg), the layout's side 1700 px x U(0.8, 1.1), radial k1 U(+-0.05), blur U(0.5, 2.0) px in
+    linear light, AWGN 3 DN), registered from a finder's corners. A tick (one frame of every stream): the anchors'
+    registration (3 rounds of the anchor search and the lens model, lizg_refine_dev) one batch a format, then the
+    multi-stream engine: one receiver batch a format, each on its own stream from its own CUDA graph. Beside it the same
+    frames one frame a launch (lizg_refine_dev and lizg_rx_finish_luma_dev a frame). Device-timed; the two paths'
+    CRC-passing block sets are checked identical."""
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    from lizard_gb300_testing import synth
+    from lizard_gb300_testing import render, synth
     W, Hh = 3840, 2160
     formats = [(384, 64, 128, 10), (768, 320, 128, 8), (1152, 720, 256, 6), (1536, 1024, 256, 5), (1536, 1024, 512, 3)]
     eng = lz.Engine()
     sp = stream.cuda_stream
     batches, keep, singles = [], [], []
     tick_bytes = 0
+    rng = np.random.default_rng(700)
     for i, (n, subch, span, count) in enumerate(formats):
         eng.add_format(n, subch, span, count)
         fmt = eng.formats[i]
-        rng = np.random.default_rng(700 + i)
-        grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 700 + i), parity=i & 3)
-        Hw = synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.9, 1.05))
-        luma, reg = synth.capture(fmt, grey, W, Hh, H=Hw, sigma=2.0, rng=rng)
-        tick_bytes += count * frame_alg_bytes(fmt, reg, W, Hh)
-        d_l = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(luma, (count,) + luma.shape))).cuda()
-        d_r = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(reg, (count,) + reg.shape))).cuda()
+        seeds = [7000 + 100 * i + k for k in range(count)]
+        dist = [(float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for _ in range(count)]
+        vs = render.views(n, span, W, Hh, seeds, 1700.0)
+        pg, pxm = render.pages(lz, n, subch, span, np.stack([synth.random_blocks(fmt.blocks, s) for s in seeds]), 1)
+        d_l = torch.empty((count, Hh, W), dtype=torch.uint8, device="cuda")
+        for k in range(count):
+            d_l[k] = render.capture(pg[k], pxm, W, Hh, vs[k], dist[k][0], dist[k][1], 3.0, seeds[k])
+        del pg
+        plain = np.stack([render.registration(span, vs[k], dist[k][0], W, Hh) for k in range(count)])
+        tick_bytes += sum(frame_alg_bytes(fmt, plain[k], W, Hh) for k in range(count))
+        d_p = torch.from_numpy(plain).cuda()
+        d_r = torch.empty_like(d_p)
         o, so = lz.rx_outputs(fmt, count)
-        keep.append((d_l, d_r, o))
+        refiner = lz.Refiner(span, count)
+        keep.append((d_l, d_r, o, d_p, refiner, count))
         batches.append((i, d_l.data_ptr(), W, Hh, W, W * Hh, d_r.data_ptr(), count, so))
         rx1 = lz.Receiver(n, subch, span, max_frames=1)
+        ref1 = lz.Refiner(span, 1)
+        d_r1 = torch.empty_like(d_p)
         o1 = [lz.rx_outputs(fmt, 1) for _ in range(count)]
-        singles.append((rx1, d_l, d_r, o1))
+        singles.append((rx1, ref1, d_l, d_p, d_r1, o1))
     streams = sum(f[3] for f in formats)
 
     def tick():
+        for d_l, d_r, o, d_p, refiner, count in keep:
+            d_r.copy_(d_p)
+            refiner.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_r.data_ptr(), count, 3, None, None, sp)
         eng.run_dev(batches, sp)
 
     def tick_single():
-        for rx1, d_l, d_r, o1 in singles:
+        for rx1, ref1, d_l, d_p, d_r1, o1 in singles:
+            d_r1.copy_(d_p)
             for k, (o, so) in enumerate(o1):
+                ref1.refine_dev(d_l[k].data_ptr(), W, Hh, W * Hh, d_r1[k].data_ptr(), 1, 3, None, None, sp)
                 lz._check(lz.lib().lizg_rx_finish_luma_dev(rx1._h, lz.ctypes.c_void_p(d_l[k].data_ptr()), W, Hh, W, W * Hh,
-                                                           lz.ctypes.c_void_p(d_r[k].data_ptr()), 1, lz.ctypes.byref(so), None, None,
+                                                           lz.ctypes.c_void_p(d_r1[k].data_ptr()), 1, lz.ctypes.byref(so), None, None,
                                                            lz.ctypes.c_void_p(sp)), "finish_luma")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -465,22 +566,29 @@ def bench_multistream(args, stream):
     K = max(5, args.steps // 3)
     ms = timed(tick, K)
     ms1 = timed(tick_single, max(3, K // 2))
-    ok = sum(int(o["ok"].sum().item()) for _, _, o in keep)
+    ok = sum(int(o["ok"].sum().item()) for _, _, o, _, _, _ in keep)
     blocks = sum(f[3] * eng.formats[i].blocks for i, f in enumerate(formats))
     same = all(np.array_equal(o["ok"][k].cpu().numpy(), o1[k][0]["ok"][0].cpu().numpy())
-               for (_, _, o), (_, _, _, o1) in zip(keep, singles) for k in range(len(o1)))
+               for (_, _, o, _, _, _), (_, _, _, _, _, o1) in zip(keep, singles) for k in range(len(o1)))
     res = {"workload": "32 streams of 3840x2160 luma at nominal 60 fps; formats n/subch/span 384/64/128 x10, 768/320/128 x8, "
-                       "1152/720/256 x6, 1536/1024/256 x5, 1536/1024/512 x3; warped (15 deg, perspective, 0.9-1.05), AWGN 2 DN, true maps",
+                       "1152/720/256 x6, 1536/1024/256 x5, 1536/1024/512 x3; painted by the sender; rotation 15 deg, tilt 20 deg, "
+                       "scale 0.8-1.1 x 1700 px, radial k1 U(+-0.05), blur U(0.5, 2.0) px, AWGN 3 DN; registered on the device "
+                       "from a finder's corners (3 rounds of anchors and lens model) inside the tick",
            "streams": streams, "frames_per_s": round(streams / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
            "ms_per_tick": round(ms, 4), "realtime_60fps_streams": round(streams / (ms / 1e3) / 60, 1),
-           "blocks_verified": ok, "blocks": blocks, "gpu_launches_per_tick": eng.launches,
+           "blocks_verified": ok, "blocks": blocks, "block_pass_rate": round(ok / blocks, 4), "gpu_launches_per_tick": eng.launches,
            "one_frame_a_launch": {"frames_per_s": round(streams / (ms1 / 1e3), 1), "ms_per_tick": round(ms1, 4)},
            "batched_vs_one_frame": round(ms1 / ms, 2), "identical_crc_sets": bool(same)}
     peak, peak_src = peaks()
     res["hbm"] = {"algorithmic_bytes_per_tick": tick_bytes, "GBps": round(tick_bytes / (ms / 1e3) / 1e9, 1),
                   "frac": round(tick_bytes / (ms / 1e3) / 1e9 / peak, 4),
                   "one_frame_a_launch_frac": round(tick_bytes / (ms1 / 1e3) / 1e9 / peak, 4), "peak_GBps": peak, "peak_source": peak_src,
-                  "bytes": "luma footprint + Y written and read + used coefficients and soft values written and read + blocks"}
+                  "bytes": "luma footprint + Y written and read + used coefficients and soft values written and read + blocks (the "
+                           "registration's reads not counted)"}
+    for _, _, _, _, refiner, _ in keep:
+        refiner.close()
+    for _, ref1, _, _, _, _ in singles:
+        ref1.close()
     eng.close()
     return res
 
@@ -576,8 +684,8 @@ def bench_ingest(args, stream):
 
 
 def bench_border_nodes(args, stream):
-    """The registration's border nodes (lizg_border_nodes_dev): refine_node over the border lattice of 64 captured
-    1920 x 1080 frames (8 distinct), each LIZARD-1024 (n = 1536) in the 128 ring at about 2.6 pixels a module, rotated
+    """The registration's border nodes (lizg_border_nodes_dev): refine_node over the border lattice of 64 distinct captured
+    1920 x 1080 frames, each LIZARD-1024 (n = 1536) in the 128 ring at about 2.6 pixels a module, rotated
     up to 15 degrees, H put up to a pixel off. Device-timed with CUDA events; every distinct frame's nodes checked
     identical to the oracle's (the reference's portable build, restated); beside it the oracle on the host cores, a
     frame a thread."""
@@ -587,24 +695,18 @@ def bench_border_nodes(args, stream):
     import lizard_gb300 as lz
     from lizard_gb300_testing import synth
     import oracle
-    span, n, subch, W, Hh, frames, distinct = 256, 1536, 1024, 1920, 1080, 64, 8
-    fmt = lz.Format(n, subch, span)
+    span, n, subch, W, Hh, frames = 256, 1536, 1024, 1920, 1080, 64
     nn = synth.layout_nodes(span).size
-    lumas, Hs = [], []
-    for k in range(distinct):
-        rng = np.random.default_rng(800 + k)
-        grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 800 + k), parity=k & 3)
-        pxm = synth.pxm_for(n, span)
-        drive = synth.border_drive(span, pxm, synth.fmt_word(subch // 16, 0, span), picture=grey)
-        Hw = np.asarray(synth.warp(fmt, W, Hh, rng, rot_deg=15, scale=(0.42, 0.45)), np.float64).reshape(3, 3)
-        luma = synth.render_drive(drive, pxm, W, Hh, Hw, sigma=3.0, rng=rng)
-        H = (Hw / Hw[2, 2]).astype(np.float32).ravel()
+    d_l, Hws = warped_frames(n, subch, span, W, Hh, frames, 800, (0.42, 0.45))
+    lumas = list(d_l.cpu().numpy())
+    Hs = []
+    for k in range(frames):
+        rng = np.random.default_rng(10800 + k)
+        H = (Hws[k] / Hws[k][2, 2]).astype(np.float32).ravel()
         H[2] += np.float32(rng.uniform(-1, 1))
         H[5] += np.float32(rng.uniform(-1, 1))
-        lumas.append(luma)
         Hs.append(H)
-    d_l = torch.from_numpy(np.stack([lumas[k % distinct] for k in range(frames)])).cuda()
-    d_h = torch.from_numpy(np.stack([Hs[k % distinct] for k in range(frames)])).cuda()
+    d_h = torch.from_numpy(np.stack(Hs)).cuda()
     d_n = torch.zeros((frames, nn, nn, 4), dtype=torch.float32, device="cuda")
     sp = stream.cuda_stream
 
@@ -629,21 +731,22 @@ def bench_border_nodes(args, stream):
         out = np.zeros(4 * nn * nn, np.float32)
         P.orc_border_nodes(span, oracle._p(lumas[k]), W, Hh, oracle._p(Hs[k]), None, oracle._p(out))
         return out.reshape(nn, nn, 4)
-    same = all(np.array_equal(got[k].view(np.uint32), host(k).view(np.uint32)) for k in range(distinct))
+    same = all(np.array_equal(got[k].view(np.uint32), host(k).view(np.uint32)) for k in range(frames))
     marked = 4 * (nn - 2)
     held = int((got[..., 2] >= 0.35).sum())
     threads = os.cpu_count() or 1
     done, t0 = 0, time.perf_counter()
     with concurrent.futures.ThreadPoolExecutor(threads) as ex:
         while time.perf_counter() - t0 < 2.0:
-            list(ex.map(host, range(distinct)))
-            done += distinct
+            list(ex.map(host, range(frames)))
+            done += frames
     dt = time.perf_counter() - t0
-    return {"workload": "border nodes (refine_node over the 128 ring's border lattice, %d nodes a frame), 64 frames of 1920x1080, LIZARD-1024 at ~2.6 px a module, rotation up to 15 deg, H up to a pixel off, AWGN 3 DN" % marked,
+    return {"workload": "border nodes (refine_node over the 128 ring's border lattice, %d nodes a frame), 64 distinct frames of 1920x1080, LIZARD-1024 "
+                        "painted by the sender at ~2.6 px a module, rotation up to 15 deg, H up to a pixel off, AWGN 3 DN" % marked,
             "frames_per_s": round(frames / (ms / 1e3), 1), "nodes_per_s": round(frames * marked / (ms / 1e3), 1), "ms_per_call": round(ms, 4),
             "nodes_held": held, "nodes": frames * marked, "gpu_launches_per_call": 1, "identical_to_oracle": bool(same),
             "cpu": {"frames_per_s": round(done / dt, 1), "cores": threads, "kind": "port",
-                    "sample": "the 8 distinct frames repeatedly for %.1f s, a frame a thread" % dt}}
+                    "sample": "the 64 frames repeatedly for %.1f s, a frame a thread" % dt}}
 
 
 def bench_fmt_word(args, stream):
@@ -767,107 +870,120 @@ def bench_encoder(args, stream):
     return res
 
 
-def _render_distorted(job):
-    """One distorted capture (a worker of bench_refinement's process pool): job = (index, k1, blur)."""
-    import numpy as np
-    import lizard_gb300 as lz
-    from lizard_gb300_testing import synth
-    k, k1, blur = job
-    fmt = lz.Format(1536, 1024, 256)
-    rng = np.random.default_rng(9000 + k)
-    grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 9000 + k), parity=k & 3)
-    view = synth.distorted_view(fmt, 1920, 1080, rng, base_side=1000.0)
-    return synth.distorted_capture(fmt, grey, 1920, 1080, view, k1=k1, blur=blur, sigma=3.0, rng=rng)
-
-
 def bench_refinement(args, stream):
-    """The full receiver on distorted captures, plain against refined registration: 1920 x 1080 frames, one
-    LIZARD-1024 (n = 1536) symbol in the 128 ring, rotation U(+-15 deg), tilt U(+-20 deg) about a random in-plane axis,
-    scale U(0.8, 1.1) x a 1000-pixel layout side, radial k1 about the frame centre, Gaussian blur in linear light
-    (gamma 2.2), AWGN 3 DN, seed = frame index. Plain: the homography through the layout's four corners as the camera
-    sees them (a finder's corners), no lens. Refined: plus three rounds of the anchor search and the lens model the
-    anchors give, written into the node mesh (lizg_refine_dev). Refined with pilots: plus three Gauss-Newton steps on H
-    against the known pilots (lizg_gn_refine_dev). Three sets: the configuration's spread (k1 U(+-0.05),
-    blur U(0.5, 2.0)), the point blur 1.5 / k1 0.03, and mild blur (k1 U(+-0.05), blur 0.5). Device-timed."""
-    import concurrent.futures
-    import multiprocessing
+    """The full receiver on distorted captures (the distorted full receiver's configuration): 1920 x 1080 frames, one
+    LIZARD-1024 (n = 1536) symbol in the 128 ring painted by the sender (the library's GPU encoder: the reference's
+    page with its border and the picture's cyclic guard), seen through rotation U(+-15 deg), tilt U(+-20 deg) about a
+    random in-plane axis, the layout's side 1000 px x U(0.8, 1.1), radial k1 about the frame centre, Gaussian blur in
+    linear light (gamma 2.2), AWGN 3 DN, a seed a frame (lizard_gb300_testing.render, on the GPU). Registrations:
+    corners = the homography through the layout's four corners as the camera sees them (a finder's), no lens; plain
+    (the configuration's: homography + anchors) = + three rounds of the anchor search and the lens model the anchors
+    give, written into the node mesh (lizg_refine_dev); refined = the plain registration's decode, then the frames it
+    left blocks unverified in refined by three Gauss-Newton steps of the adjoint refinement (H and the 7 x 7 anchor
+    field against the pilots, the timing track and the anchors' centres, lizg_field_refine_dev) and decoded again;
+    bound = the camera's true map at every node (no registration can do better). Three sets:
+    the configuration's 1024 frames (k1 U(+-0.05), blur U(0.5, 2.0)), blur 1.5 px / k1 0.03, blur 0.5 px / k1 U(+-0.05).
+    Device-timed."""
     import numpy as np
     import torch
     import lizard_gb300 as lz
-    sets = []
+    from lizard_gb300_testing import render, synth
+    n, subch, span, W, Hh = 1536, 1024, 256, 1920, 1080
+    fmt = lz.Format(n, subch, span)
     rng = np.random.default_rng(123)
-    sets.append(("spread", [(k, float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for k in range(256)]))   # 256 of the 1024
-    sets.append(("blur1.5_k1_0.03", [(100 + k, 0.03, 1.5) for k in range(16)]))
-    sets.append(("mild_blur0.5", [(200 + k, float(rng.uniform(-0.05, 0.05)), 0.5) for k in range(32)]))
-    jobs = [j for _, js in sets for j in js]
-    with concurrent.futures.ProcessPoolExecutor(max_workers=os.cpu_count() or 4, mp_context=multiprocessing.get_context("spawn")) as ex:
-        caps = list(ex.map(_render_distorted, jobs, chunksize=2))
+    sets = [("spread", [(9000 + k, float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for k in range(1024)]),
+            ("blur1.5_k1_0.03", [(9100 + k, 0.03, 1.5) for k in range(64)]),
+            ("mild_blur0.5", [(9200 + k, float(rng.uniform(-0.05, 0.05)), 0.5) for k in range(64)])]
     sp = stream.cuda_stream
-    res = {"workload": "1920x1080, LIZARD-1024 (n=1536) in the 128 ring, rotation 15 deg, tilt 20 deg, scale 0.8-1.1 x 1000 px, "
-                       "radial k1, blur in linear light, AWGN 3 DN, a seed a frame (the spread: 256 frames of the configuration's 1024); "
-                       "plain = corners' homography, refined = + 3 rounds of anchors and lens model"}
-    at = 0
+    res = {"workload": "1920x1080, LIZARD-1024 (n=1536) in the 128 ring painted by the sender (border, cyclic guard), rotation 15 deg, "
+                       "tilt 20 deg, scale 0.8-1.1 x 1000 px, radial k1, blur in linear light, AWGN 3 DN, a seed a frame; corners = a finder's "
+                       "homography; plain = + 3 rounds of anchors and lens model (homography + anchors); refined = + 3 Gauss-Newton steps "
+                       "against the pilots; bound = the true map at every node"}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rx = lz.Receiver(n, subch, span, max_frames=1024)
+    ref = lz.Refiner(span, 1024)
+    fld = lz.FieldRefiner(n, subch, span, chunk=32)
     for name, js in sets:
         frames = len(js)
-        luma = np.stack([caps[at + i][0] for i in range(frames)])
-        reg = np.stack([caps[at + i][1] for i in range(frames)])
-        at += frames
-        rx = lz.Receiver(1536, 1024, 256, max_frames=frames)
-        ref = lz.Refiner(256, frames)
-        d_l = torch.from_numpy(luma).cuda()
-        d_plain = torch.from_numpy(reg).cuda()
-        d_ref = torch.empty_like(d_plain)
+        seeds = [j[0] for j in js]
+        vs = render.views(n, span, W, Hh, seeds, 1000.0)
+        blocks = np.stack([synth.random_blocks(fmt.blocks, s) for s in seeds])
+        pg, pxm = render.pages(lz, n, subch, span, blocks, 1)
+        d_l = torch.empty((frames, Hh, W), dtype=torch.uint8, device="cuda")
+        for k, (s, k1, blur) in enumerate(js):
+            d_l[k] = render.capture(pg[k], pxm, W, Hh, vs[k], k1, blur, 3.0, s)
+        del pg
+        d_plain = torch.from_numpy(np.stack([render.registration(span, vs[k], js[k][1], W, Hh) for k in range(frames)])).cuda()
+        d_true = torch.from_numpy(np.stack([render.registration(span, vs[k], js[k][1], W, Hh, true_mesh=True) for k in range(frames)])).cuda()
+        stride = d_plain.shape[1]
+        d_a = torch.empty_like(d_plain)
+        d_g = torch.empty_like(d_plain)
         d_found = torch.zeros(frames, dtype=torch.int32, device="cuda")
-        o_p, s_p = rx._outputs(frames, torch, keep=False)
-        o_r, s_r = rx._outputs(frames, torch, keep=False)
-        o_g, s_g = rx._outputs(frames, torch, keep=False)
-        gn = lz.PilotRefiner(1536, 1024, 256, chunk=16)
-        d_gn = torch.empty_like(d_plain)
+        d_lens = torch.zeros((frames, 15), dtype=torch.float64, device="cuda")
+        d_gate = torch.zeros(frames, dtype=torch.uint8, device="cuda")
         d_imp = torch.zeros(frames, dtype=torch.int32, device="cuda")
+        ao = {"ok": torch.zeros((frames, 49), dtype=torch.uint8, device="cuda")}
+        for key in ("peak", "dx", "dy", "u", "v"):
+            ao[key] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
+        a_out = lz.AnchorOut(*[ao[key].data_ptr() for key in ("ok", "peak", "dx", "dy", "u", "v")])
+        outs = {t: rx._outputs(frames, torch, keep=False) for t in ("corners", "plain", "first", "refined", "bound")}
+        d_union = torch.zeros((frames, fmt.blocks), dtype=torch.uint8, device="cuda")
 
-        def plain():
-            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
-                                                       lz.ctypes.c_void_p(d_plain.data_ptr()), frames, lz.ctypes.byref(s_p), None, None,
-                                                       lz.ctypes.c_void_p(sp)), "finish_luma")
+        def finish(d_reg, tag):
+            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W, W * Hh, lz.ctypes.c_void_p(d_reg.data_ptr()),
+                                                       frames, lz.ctypes.byref(outs[tag][1]), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
+
+        def anchors(d_reg):
+            d_reg.copy_(d_plain)
+            ref.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_reg.data_ptr(), frames, 3, d_found.data_ptr(), d_lens.data_ptr(), sp)
 
         def refined():
-            d_ref.copy_(d_plain)
-            ref.refine_dev(d_l.data_ptr(), 1920, 1080, 1920 * 1080, d_ref.data_ptr(), frames, 3, d_found.data_ptr(), None, sp)
-            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
-                                                       lz.ctypes.c_void_p(d_ref.data_ptr()), frames, lz.ctypes.byref(s_r), None, None,
-                                                       lz.ctypes.c_void_p(sp)), "finish_luma")
-        def refined_pilots():   # the anchors' refinement, then 3 Gauss-Newton steps on H against the pilots
-            d_gn.copy_(d_plain)
-            ref.refine_dev(d_l.data_ptr(), 1920, 1080, 1920 * 1080, d_gn.data_ptr(), frames, 3, d_found.data_ptr(), None, sp)
-            lz._check(lz.lib().lizg_gn_refine_dev(gn._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920 * 1080, lz.ctypes.c_void_p(d_gn.data_ptr()),
-                                                  frames, 3, None, lz.ctypes.c_void_p(d_imp.data_ptr()), lz.ctypes.c_void_p(sp)), "gn_refine")
-            lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), 1920, 1080, 1920, 1920 * 1080,
-                                                       lz.ctypes.c_void_p(d_gn.data_ptr()), frames, lz.ctypes.byref(s_g), None, None,
-                                                       lz.ctypes.c_void_p(sp)), "finish_luma")
+            # the plain registration and decode; then the frames it left blocks unverified in, refined by the adjoint
+            # (H and the anchor field against the pilots, the track and the anchors' centres) and decoded again; a
+            # block verified by either decode is the frame's (the CRC-32C decides, as a receiver keeps any block it
+            # verifies)
+            anchors(d_g)
+            finish(d_g, "first")
+            d_gate.copy_((outs["first"][0]["ok"].sum(dim=1) < fmt.blocks).to(torch.uint8))
+            lz._check(lz.lib().lizg_anchor_find_dev(span, lz.ctypes.c_void_p(d_l.data_ptr()), W, Hh, W * Hh, lz.ctypes.c_void_p(d_g.data_ptr()), stride,
+                                                    lz.ctypes.c_void_p(d_lens.data_ptr()), None, frames, lz.ctypes.byref(a_out), lz.ctypes.c_void_p(sp)),
+                      "anchor_find")
+            fld.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_g.data_ptr(), frames, 3, a_out, d_gate.data_ptr(), None, d_imp.data_ptr(), sp)
+            finish(d_g, "refined")
+            torch.maximum(outs["refined"][0]["ok"], outs["first"][0]["ok"], out=d_union)
+
+        paths = {"corners": lambda: finish(d_plain, "corners"),
+                 "plain": lambda: (anchors(d_a), finish(d_a, "plain")),
+                 "refined": refined,
+                 "bound": lambda: finish(d_true, "bound")}
         out = {"frames": frames}
-        for tag, fn, o in (("plain", plain, o_p), ("refined", refined, o_r), ("refined_pilots", refined_pilots, o_g)):
-            for _ in range(2):
-                fn()
+        for tag, fn in paths.items():
+            fn()
             torch.cuda.synchronize()
-            reps = 3
+            reps = 2 if tag == "refined" else 3
             e0.record(stream)
             for _ in range(reps):
                 fn()
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
-            ok = o["ok"].cpu().numpy()
-            out[tag] = {"blocks_verified": int(ok.sum()), "blocks": int(ok.size), "block_pass_rate": round(float(ok.mean()), 4),
+            def rates(ok):
+                return {"blocks_verified": int(ok.sum()), "blocks": int(ok.size), "block_pass_rate": round(float(ok.mean()), 4),
                         "frames_with_a_block": int((ok.sum(axis=1) > 0).sum()), "frames_all_blocks": int(ok.all(axis=1).sum()),
                         "frames_per_s": round(frames / (ms / 1e3), 1)}
+            out[tag] = rates((d_union if tag == "refined" else outs[tag][0]["ok"]).cpu().numpy())
+            if tag == "refined":
+                out["refined_registration_alone"] = rates(outs["refined"][0]["ok"].cpu().numpy())
         out["anchors_found_mean"] = round(float(d_found.float().mean().item()), 1)
-        out["block_pass_points_gained"] = round(100 * (out["refined"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
-        out["pilot_steps_kept_frames"] = int(d_imp.sum().item())
-        out["pilot_points_gained_over_plain"] = round(100 * (out["refined_pilots"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
-        del gn
+        out["refined_frames"] = int(d_gate.sum().item())
+        out["refined_steps_kept_frames"] = int(d_imp.sum().item())
+        out["plain_points_over_corners"] = round(100 * (out["plain"]["block_pass_rate"] - out["corners"]["block_pass_rate"]), 2)
+        out["refined_points_over_plain"] = round(100 * (out["refined"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
+        out["bound_points_over_plain"] = round(100 * (out["bound"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
         res[name] = out
-        ref.close()
+        del d_l
+    ref.close()
+    fld.close()
     return res
 
 

@@ -423,6 +423,36 @@ void lizg_refiner_free(lizg_refiner *r);
 int lizg_refine_dev(lizg_refiner *r, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int rounds,
                     int32_t *d_found, double *d_lens, void *stream);
 
+// ---------------------------------------------------------------- registration refined by its adjoint (H and the anchor field)
+//
+// No reference counterpart: a refinement of the held registration before the soft stage, Gauss-Newton over the 8
+// homography parameters and a 7 x 7 field of displacements at the anchors' centres (carried into the mesh as the
+// reference's interior fill carries its anchors' readings, liblizard/src/acquire.c:2199-2217, 2335-2385: cubic
+// Hermite knots at the node lattice's ends, held at zero, and at the anchors' centres), against three terms: the
+// known pilots as the receiver's own front measures them, the timing track's cells, and the anchors' centres where
+// the anchor search found them. The gradient comes from one adjoint pass (the pilots' residuals inverse-transformed
+// to every picture sample, the warp recomputed at each sample); the step's normal equations take the pilots' J^T J
+// from the tangents' own Gram scaled by the pilots' share of the picture's energy, the track's and the anchors'
+// exactly. Each step is kept where the weighted mismatch falls, halved from the best registration otherwise; the
+// registration given is the baseline and the fallback. chunk: frames a pass (1..64).
+// d_reg: frames x (9 + 2 nx ny), refined in place (H and the mesh). anchors (may be NULL: no anchor term): the anchor
+// search's outputs through the same registration (lizg_anchor_find_dev, frames x 49 each). d_gate (frames bytes, may
+// be NULL): 0 leaves a frame's registration as it is and spends nothing on it (for instance the frames whose plain
+// decode verified every block). d_loss, d_improved (frames, may be NULL): the weighted mismatch at the registration
+// kept, and 1 where a step was kept.
+enum { LIZG_FIELD_PARAMS = 8 + 2 * 49 };
+typedef struct lizg_field lizg_field;
+lizg_field *lizg_field_new(int n, int subch, int span, int chunk);
+void lizg_field_free(lizg_field *g);
+int lizg_field_refine_dev(lizg_field *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int steps,
+                          const lizg_anchor_out *anchors, const uint8_t *d_gate, float *d_loss, int32_t *d_improved, void *stream);
+// The three terms at given parameters, unweighted, for checks: d_theta frames x LIZG_FIELD_PARAMS (H[0..7], then the
+// field's (x, y) a knot, row by row, pixels) about the registration d_reg (its mesh the field is added to); d_terms
+// frames x 3 x (1 + LIZG_FIELD_PARAMS) doubles: per term (pilots, track, anchors) its loss (a sum of squares) then
+// its gradient in the parameters. frames at most the chunk.
+int lizg_field_terms_dev(lizg_field *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_reg, const float *d_theta,
+                         int frames, const lizg_anchor_out *anchors, double *d_terms, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -738,6 +738,87 @@ class Engine:
             pass
 
 
+FIELD_PARAMS = 8 + 2 * 49
+
+
+class FieldRefiner:
+    """The registration refined by its adjoint (lizg_field_*): Gauss-Newton over H and the 7 x 7 anchor field against
+    the pilots, the timing track and the anchors' centres, chunk frames a pass."""
+
+    def __init__(self, n, subch, span, chunk=8):
+        L = lib()
+        if not hasattr(L, "_field"):
+            P, I = ctypes.c_void_p, ctypes.c_int
+            L.lizg_field_new.argtypes = [I, I, I, I]
+            L.lizg_field_new.restype = P
+            L.lizg_field_free.argtypes = [P]
+            L.lizg_field_refine_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, I, P, P, P, P, P]
+            L.lizg_field_terms_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, P, I, P, P, P]
+            L._field = True
+        self._h = L.lizg_field_new(n, subch, span, chunk)
+        if not self._h:
+            raise LizgError("lizg_field_new: " + L.lizg_last_error().decode())
+        self._h = ctypes.c_void_p(self._h)
+        self.n, self.span, self.chunk = n, span, chunk
+
+    def refine_dev(self, d_luma, w, h, frame_stride, d_reg, frames, steps=3, anchors=None, d_gate=None, d_loss=None, d_improved=None, stream=0):
+        """Device pointers; anchors: an AnchorOut of device pointers (frames x 49) or None."""
+        _check(lib().lizg_field_refine_dev(self._h, ctypes.c_void_p(d_luma), w, h, frame_stride, ctypes.c_void_p(d_reg), frames, steps,
+                                           None if anchors is None else ctypes.byref(anchors), None if d_gate is None else ctypes.c_void_p(d_gate),
+                                           None if d_loss is None else ctypes.c_void_p(d_loss),
+                                           None if d_improved is None else ctypes.c_void_p(d_improved), ctypes.c_void_p(stream)),
+               "lizg_field_refine_dev")
+
+    def terms(self, luma, reg, theta, anchors=None):
+        """The three terms (pilots, track, anchors) at parameters theta (frames x FIELD_PARAMS) about reg: frames x 3 x
+        (1 + FIELD_PARAMS) float64, each term's loss then its gradient. anchors: a dict of numpy ok, u, v (frames x 49)."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        frames, h, w = lu.shape
+        d_l = torch.from_numpy(lu).cuda()
+        d_r = torch.from_numpy(np.ascontiguousarray(reg, np.float32).reshape(frames, -1)).cuda()
+        d_t = torch.from_numpy(np.ascontiguousarray(theta, np.float32).reshape(frames, FIELD_PARAMS)).cuda()
+        d_o = torch.zeros((frames, 3, 1 + FIELD_PARAMS), dtype=torch.float64, device="cuda")
+        keep = None
+        if anchors is not None:
+            keep = {k: torch.from_numpy(np.ascontiguousarray(anchors[k], np.uint8 if k == "ok" else np.float32)).cuda() for k in ("ok", "u", "v")}
+            z = keep["u"]
+            ao = AnchorOut(keep["ok"].data_ptr(), z.data_ptr(), z.data_ptr(), z.data_ptr(), keep["u"].data_ptr(), keep["v"].data_ptr())
+        _check(lib().lizg_field_terms_dev(self._h, ctypes.c_void_p(d_l.data_ptr()), w, h, h * w, ctypes.c_void_p(d_r.data_ptr()),
+                                          ctypes.c_void_p(d_t.data_ptr()), frames, None if keep is None else ctypes.byref(ao),
+                                          ctypes.c_void_p(d_o.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), "lizg_field_terms_dev")
+        torch.cuda.synchronize()
+        return d_o.cpu().numpy()
+
+    def refine(self, luma, reg, steps=3, anchors=None, gate=None):
+        """luma frames x h x w uint8, reg frames x (9 + 2 nodes): (refined reg, loss, improved)."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        frames, h, w = lu.shape
+        d_l = torch.from_numpy(lu).cuda()
+        d_r = torch.from_numpy(np.ascontiguousarray(reg, np.float32).reshape(frames, -1).copy()).cuda()
+        d_loss = torch.zeros(frames, dtype=torch.float32, device="cuda")
+        d_imp = torch.zeros(frames, dtype=torch.int32, device="cuda")
+        d_g = None if gate is None else torch.from_numpy(np.ascontiguousarray(gate, np.uint8)).cuda()
+        keep = None
+        if anchors is not None:
+            keep = {k: torch.from_numpy(np.ascontiguousarray(anchors[k], np.uint8 if k == "ok" else np.float32)).cuda() for k in ("ok", "u", "v")}
+            z = keep["u"]
+            keep["out"] = AnchorOut(keep["ok"].data_ptr(), z.data_ptr(), z.data_ptr(), z.data_ptr(), keep["u"].data_ptr(), keep["v"].data_ptr())
+        self.refine_dev(d_l.data_ptr(), w, h, h * w, d_r.data_ptr(), frames, steps, None if keep is None else keep["out"],
+                        None if d_g is None else d_g.data_ptr(), d_loss.data_ptr(), d_imp.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return d_r.cpu().numpy(), d_loss.cpu().numpy(), d_imp.cpu().numpy()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lizg_field_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 class Refiner:
     """The registration's refinement from the anchors (lizg_refine_*) for frames of one ring span."""
 

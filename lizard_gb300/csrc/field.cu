@@ -1,0 +1,876 @@
+// The registration refined by its adjoint on sm_103a (include/lizard_gb300.h lizg_field_*): Gauss-Newton over the
+// 8 homography parameters and a 7 x 7 field of anchor displacements, against the known pilots, the timing track and
+// the anchors' measured centres. No reference counterpart: a refinement of the held registration before the soft
+// stage.
+//
+// The parameters. H[0..7] (H[8] = 1), and a displacement (x, y, pixels) at each of the 7 x 7 anchors' centres. The
+// field reaches the mesh as the reference's interior fill carries its anchors' readings inward
+// (liblizard/src/acquire.c:2199-2217 anch_herm4, 2335-2385): knots on each axis at the node lattice's two ends (held
+// at zero: the border holds the map there) and at the 7 anchors' centres between; each node's displacement gains
+// the 4 x 4 cubic Hermite blend of its knots, on top of the registration's own mesh. The sampler then blends the
+// nodes bilinearly, so every sample's position is affine in the field.
+//
+// The mismatch, three terms:
+//  - pilots: every block tail's coefficients measured by the receiver's own front (sampling through the registration
+//    by the exact walk, the anchors' erase, the detrend, the 2D transform), each against its known symbol times a
+//    real gain a radius band and block parity (the gains fitted afresh at every evaluation);
+//  - the timing track: the border's track cells (2 x 2 modules, dark or light by the layout's track bits) sampled at
+//    their centres, each against the frame's dark or light level;
+//  - the anchors' centres: where the registration maps each anchor's centre against where the anchor search found it.
+// Each term is weighted to unit mean square at the starting registration, and the field has a Gaussian prior of
+// 0.25 pixels a knot (so its 98 knots do not follow the residuals' noise).
+//
+// The adjoint (reverse mode). The pilots' residuals r are scattered into a half-plane spectrum and one inverse
+// transform (the sender's, enc_fft_launch) gives the mismatch's gradient in every picture sample,
+// g(x, y) = 2 Re sum_p r_p e^{+2 pi i (u_p x + v_p y) / n}, less the detrend's share (the surface's projections, taken
+// exactly; the anchors' erased squares are held constant). One pass over the samples recomputes the warp (H, the mesh
+// with the field in it) and the bilinear read's gradient at every sample, and sums g times each parameter's tangent:
+// the mismatch's full gradient J^T r in the 106 parameters. Gauss-Newton needs J^T J as well, which the adjoint
+// does not give; this one uses, for the pilots, the tangent pictures' own Gram matrix (over H, exact) and their
+// energies (over the field, the diagonal) scaled by the share of the picture's energy the pilots carry (Parseval: a
+// tangent picture's spectrum takes the picture's shape), plus the track's and the anchors' exact J^T J. Each step is
+// solved in double (the columns scaled, a Levenberg damping), kept where the weighted mismatch falls, halved from the
+// best registration otherwise. The registration the caller gave is the baseline and the fallback.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+#include "format.h"
+#include "lizard_gb300.h"
+#include "lizg_internal.h"
+#include "sample_dev.cuh"
+
+namespace lizg {
+
+constexpr int kFK = 9;                          // knots an axis: the two ends and the 7 anchors
+constexpr int kFP = LIZG_FIELD_PARAMS;          // 8 + 2 x 49
+constexpr int kFThreads = 256, kFRows = 8;      // the gradient pass: a warp a picture row, 8 rows a CTA
+constexpr int kFBins = 8, kFGroups = 2 * kFBins;
+constexpr int kFHs = 8 + 36 + 2;                // a CTA's H sums: g t (8), the tangents' Gram (36), sum z, sum z^2
+constexpr int kFFs = 2 * kFK * kFK * 2;         // and the field's: g t and t^2 at each knot, two components
+constexpr int kFPart = kFHs + kFFs;
+constexpr int kFMaxTrack = 1024;
+constexpr double kFieldSigma = 0.25;            // the field's prior, pixels a knot
+
+struct FieldArgs {
+  int n, nn, w, h, reg_stride, npilot, need, vrows, ntrack;
+  int64_t fstride;
+  float g0, step;
+  float pos[40];
+  float anc[7];                    // the anchors' centres along an axis (module coordinates)
+  int elo[7], ehi[7];
+  double sx2, sq2;
+  const uint8_t *luma;
+  const float *cx, *qx;            // the detrend basis, n each
+  const float2 *x1, *x2;           // its DFTs
+  const float *wk;                 // nn x kFK: node i's Hermite weight on knot a
+  const int32_t *pilot;            // pos index of each pilot
+  const int16_t *puv;              // its (u, v)
+  const float2 *shat;              // its symbol for a count bit of 0
+  const uint8_t *group;            // parity * kFBins + radius band
+  const float4 *track;             // a track cell's centre (mx, my) and 1 where dark
+};
+
+struct FieldState {
+  float theta[kFP];                // the evaluation in hand
+  float best[kFP];
+  float delta[kFP];                // the step from best
+  double loss_best, wp, wa, wt;
+  float scale;
+  int evals, improved;
+};
+
+// Per frame and evaluation, from the pilots' pass: the pilots' loss, the detrend's adjoint constants K1..K5, the
+// pilots' energy.
+struct PilotTerms {
+  double loss, k[5], energy;
+};
+
+// The warp at module point (mx, my): H, then the mesh's bilinear displacement from the frame's registration reg;
+// the node cell (i, j) and the place (uu, vv) in it.
+struct WarpAt {
+  float u, v, wd, U, V;
+  int i, j;
+  float uu, vv;
+};
+__device__ __forceinline__ int cell_of(const float *pos, int nn, float m) {
+  int lo = 0, hi = nn - 2;
+  while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (m >= pos[mid]) lo = mid; else hi = mid - 1; }
+  return lo;
+}
+__device__ __forceinline__ WarpAt warp_at(const FieldArgs &a, const float *reg, float mx, float my) {
+  WarpAt o;
+  o.i = cell_of(a.pos, a.nn, mx);
+  o.j = cell_of(a.pos, a.nn, my);
+  o.uu = (mx - a.pos[o.i]) / (a.pos[o.i + 1] - a.pos[o.i]);
+  o.vv = (my - a.pos[o.j]) / (a.pos[o.j + 1] - a.pos[o.j]);
+  const float *n00 = reg + 9 + 2 * (o.j * a.nn + o.i), *n10 = n00 + 2, *n01 = n00 + 2 * a.nn, *n11 = n01 + 2;
+  const float mdx = (n00[0] * (1 - o.uu) + n10[0] * o.uu) * (1 - o.vv) + (n01[0] * (1 - o.uu) + n11[0] * o.uu) * o.vv;
+  const float mdy = (n00[1] * (1 - o.uu) + n10[1] * o.uu) * (1 - o.vv) + (n01[1] * (1 - o.uu) + n11[1] * o.uu) * o.vv;
+  const float *h = reg;
+  o.wd = h[6] * mx + h[7] * my + 1;
+  o.U = (h[0] * mx + h[1] * my + h[2]) / o.wd;
+  o.V = (h[3] * mx + h[4] * my + h[5]) / o.wd;
+  o.u = o.U + mdx;
+  o.v = o.V + mdy;
+  return o;
+}
+// The bilinear read at gamma 1 at pixel point (u, v) (sample()'s clamp) and its gradient in u and v (zero along an
+// axis the clamp holds: past the frame's edge the read no longer moves with the point).
+__device__ __forceinline__ float read_grad(const uint8_t *px, int w, int h, float u, float v, float *Iu, float *Iv) {
+  float sx = u - 0.5f, sy = v - 0.5f;
+  const float xm = (float)w - 1.001f, ym = (float)h - 1.001f;
+  const bool hx = !(sx >= 0 && sx <= xm), hy = !(sy >= 0 && sy <= ym);
+  if (sx < 0) sx = 0; else if (sx > xm) sx = xm;
+  if (sy < 0) sy = 0; else if (sy > ym) sy = ym;
+  const int xi = sx >= 0 ? (int)sx : 0, yi = sy >= 0 ? (int)sy : 0;
+  const float fx = sx - (float)xi, fy = sy - (float)yi;
+  const uint8_t *p = px + (int64_t)yi * w + xi;
+  const float A = grey_of(p[0]), B = grey_of(p[1]), C = grey_of(p[w]), D = grey_of(p[w + 1]);
+  *Iu = hx ? 0.0f : (B - A) * (1 - fy) + (D - C) * fy;
+  *Iv = hy ? 0.0f : (C - A) * (1 - fx) + (D - B) * fx;
+  return (A + (B - A) * fx) * (1 - fy) + (C + (D - C) * fx) * fy;
+}
+// The warp's derivative in h0..h7 at (mx, my): du[q], dv[q].
+__device__ __forceinline__ void dwarp_dh(const WarpAt &o, float mx, float my, float du[8], float dv[8]) {
+  const float iw = 1.0f / o.wd;
+  du[0] = mx * iw; du[1] = my * iw; du[2] = iw; du[3] = 0; du[4] = 0; du[5] = 0; du[6] = -o.U * mx * iw; du[7] = -o.U * my * iw;
+  dv[0] = 0; dv[1] = 0; dv[2] = 0; dv[3] = mx * iw; dv[4] = my * iw; dv[5] = iw; dv[6] = -o.V * mx * iw; dv[7] = -o.V * my * iw;
+}
+// A point's weight on knot a along one axis: the bilinear blend of its cell's two nodes' Hermite weights.
+__device__ __forceinline__ float knot_w(const FieldArgs &a, int i, float uu, int k) {
+  return (1 - uu) * a.wk[i * kFK + k] + uu * a.wk[(i + 1) * kFK + k];
+}
+__device__ __forceinline__ bool in_sq(const FieldArgs &a, int t) {
+  bool in = false;
+#pragma unroll
+  for (int q = 0; q < 7; q++) in |= t >= a.elo[q] && t <= a.ehi[q];
+  return in;
+}
+
+// The registration the parameters give: H from theta, the base registration's mesh plus the field's Hermite blend
+// at every node. A CTA a frame.
+__global__ void __launch_bounds__(256) field_mesh_kernel(FieldArgs a, const FieldState *st, int use_best, const float *base, float *out) {
+  const int f = blockIdx.x;
+  const float *th = use_best ? st[f].best : st[f].theta;
+  const float *b = base + (int64_t)f * a.reg_stride;
+  float *o = out + (int64_t)f * a.reg_stride;
+  if (threadIdx.x < 9) o[threadIdx.x] = threadIdx.x < 8 ? th[threadIdx.x] : 1.0f;
+  for (int t = threadIdx.x; t < a.nn * a.nn; t += blockDim.x) {
+    const int j = t / a.nn, i = t - j * a.nn;
+    float dx = b[9 + 2 * t], dy = b[10 + 2 * t];
+    for (int kb = 1; kb < kFK - 1; kb++) {
+      const float wy = a.wk[j * kFK + kb];
+      if (wy == 0) continue;
+      for (int ka = 1; ka < kFK - 1; ka++) {
+        const float ww = wy * a.wk[i * kFK + ka];
+        const int q = 8 + 2 * ((kb - 1) * 7 + (ka - 1));
+        dx += ww * th[q];
+        dy += ww * th[q + 1];
+      }
+    }
+    o[9 + 2 * t] = dx;
+    o[10 + 2 * t] = dy;
+  }
+}
+
+// Sums a double over the CTA in a fixed order (a warp's tree, then the warps in turn).
+__device__ double fblock_sum(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+  return t;
+}
+
+// The pilots: the gains, the residuals (into the half-plane spectrum R, pilots only, R zero elsewhere), the loss, the
+// detrend's adjoint constants and the pilots' energy. A CTA a frame.
+__global__ void __launch_bounds__(kFThreads) field_pilot_kernel(FieldArgs a, const float2 *coef, const uint8_t *skip, float2 *R, PilotTerms *pt) {
+  __shared__ double red[kFThreads / 32], gain[kFGroups];
+  const int f = blockIdx.x, tid = threadIdx.x, n = a.n;
+  if (skip && skip[f]) return;
+  const float2 *C = coef + (int64_t)f * a.need;
+  for (int g = 0; g < kFGroups; g++) {
+    double num = 0, den = 0;
+    for (int k = tid; k < a.npilot; k += blockDim.x) {
+      if (a.group[k] != g) continue;
+      const float2 s = a.shat[k], c = C[a.pilot[k]];
+      num += (double)s.x * c.x + (double)s.y * c.y;
+      den += (double)s.x * s.x + (double)s.y * s.y;
+    }
+    num = fblock_sum(num, red);
+    den = fblock_sum(den, red);
+    if (tid == 0) gain[g] = den > 0 ? num / den : 0.0;
+  }
+  __syncthreads();
+  double loss = 0, en = 0, k1 = 0, k2 = 0, k3 = 0, k4 = 0, k5 = 0;
+  float2 *Rf = R + (int64_t)f * a.vrows * n;
+  for (int k = tid; k < a.npilot; k += blockDim.x) {
+    const float2 s = a.shat[k], c = C[a.pilot[k]];
+    const double gk = gain[a.group[k]];
+    const double rx = c.x - gk * s.x, ry = c.y - gk * s.y;
+    loss += rx * rx + ry * ry;
+    en += (double)c.x * c.x + (double)c.y * c.y;
+    const int u = a.puv[2 * k], v = a.puv[2 * k + 1], um = (u + n) % n;
+    Rf[(int64_t)v * n + um] = make_float2((float)rx, (float)ry);
+    // Re(conj(r) z) = rx zx + ry zy
+    const float2 xu = a.x1[um], xv = a.x1[v];
+    const double pr = (double)xu.x * xv.x - (double)xu.y * xv.y, pi = (double)xu.x * xv.y + (double)xu.y * xv.x;
+    k1 += rx * pr + ry * pi;
+    if (v == 0) { const float2 yu = a.x2[um]; k2 += rx * xu.x + ry * xu.y; k3 += rx * yu.x + ry * yu.y; }
+    if (u == 0) { const float2 yv = a.x2[v]; k4 += rx * xv.x + ry * xv.y; k5 += rx * yv.x + ry * yv.y; }
+  }
+  loss = fblock_sum(loss, red);
+  en = fblock_sum(en, red);
+  k1 = fblock_sum(k1, red); k2 = fblock_sum(k2, red); k3 = fblock_sum(k3, red); k4 = fblock_sum(k4, red); k5 = fblock_sum(k5, red);
+  if (tid == 0) {
+    PilotTerms &p = pt[f];
+    p.loss = loss; p.energy = en;
+    p.k[0] = 2 * k1 / (a.sx2 * a.sx2); p.k[1] = 2 * k2 / a.sx2; p.k[2] = 2 * k3 / a.sq2; p.k[3] = 2 * k4 / a.sx2; p.k[4] = 2 * k5 / a.sq2;
+  }
+}
+
+// The adjoint pass over the samples. A CTA takes kFRows picture rows of a frame, a warp a row, lanes along x. G: the
+// inverse transform of the residuals (0.5 + g from the sender's transform). Out, a CTA's partial sums (floats, in a
+// fixed order): H's g t (8), the H tangents' Gram (36, upper triangle), sum z, sum z^2, then per knot pair (b, a)
+// and component the field's g t (kFK^2 x 2) and t^2 (kFK^2 x 2).
+__global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, const float *regs, const float *G, const PilotTerms *pt,
+                                                               const uint8_t *skip, float *part) {
+  const int blocks = a.n / kFRows, f = blockIdx.x / blocks, blk = blockIdx.x - f * blocks;
+  if (skip && skip[f]) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, y = blk * kFRows + warp, n = a.n;
+  const float *reg = regs + (int64_t)f * a.reg_stride;
+  const uint8_t *px = a.luma + f * a.fstride;
+  const float *Gf = G + (int64_t)f * n * n + (int64_t)y * n;
+  __shared__ float s_pq[kFRows][kFK][4];   // a row's field sums: g t x, g t y, t x^2, t y^2 at each knot a
+  __shared__ float s_wy[kFRows][kFK];
+  __shared__ float s_h[kFThreads / 32][kFHs];
+  const double *K = pt[f].k;
+  const float my = a.g0 + (float)y * a.step;
+  const float cy = a.cx[y], qy = a.qx[y];
+  const bool ysq = in_sq(a, y);
+  float hs[kFHs];
+#pragma unroll
+  for (int q = 0; q < kFHs; q++) hs[q] = 0;
+  float pq[kFK][4];
+#pragma unroll
+  for (int k = 0; k < kFK; k++) pq[k][0] = pq[k][1] = pq[k][2] = pq[k][3] = 0;
+  int jrow = 0;
+  float vrow = 0;
+  for (int x = lane; x < n; x += 32) {
+    const float mx = a.g0 + (float)x * a.step;
+    const WarpAt o = warp_at(a, reg, mx, my);
+    jrow = o.j; vrow = o.vv;
+    float Iu, Iv;
+    const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
+    hs[44] += z; hs[45] += z * z;
+    if (ysq && in_sq(a, x)) continue;   // erased: the shading surface, held constant
+    const float cxx = a.cx[x], qxx = a.qx[x];
+    const float g = Gf[x] - 0.5f - (float)(K[0] * cxx * cy + K[1] * cxx + K[2] * qxx + K[3] * cy + K[4] * qy);
+    float du[8], dv[8];
+    dwarp_dh(o, mx, my, du, dv);
+    float t[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) { t[q] = Iu * du[q] + Iv * dv[q]; hs[q] += g * t[q]; }
+    int e = 8;
+#pragma unroll
+    for (int p = 0; p < 8; p++)
+#pragma unroll
+      for (int q = p; q < 8; q++) hs[e++] += t[p] * t[q];
+#pragma unroll
+    for (int k = 0; k < kFK; k++) {
+      const float wx = knot_w(a, o.i, o.uu, k);
+      const float tx = Iu * wx, ty = Iv * wx;
+      pq[k][0] += g * tx; pq[k][1] += g * ty; pq[k][2] += tx * tx; pq[k][3] += ty * ty;
+    }
+  }
+  // the row's field sums over the warp, then weighted by the row's knot weights across the CTA's rows in order
+#pragma unroll
+  for (int k = 0; k < kFK; k++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      float v = pq[k][c];
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+      if (lane == 0) s_pq[warp][k][c] = v;
+    }
+  if (lane < kFK) s_wy[warp][lane] = knot_w(a, jrow, vrow, lane);
+#pragma unroll
+  for (int q = 0; q < kFHs; q++) {
+    float v = hs[q];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+    if (lane == 0) s_h[warp][q] = v;
+  }
+  __syncthreads();
+  float *out = part + ((int64_t)f * blocks + blk) * kFPart;
+  for (int q = threadIdx.x; q < kFHs; q += blockDim.x) {
+    float acc = 0;
+    for (int r = 0; r < kFRows; r++) acc += s_h[r][q];
+    out[q] = acc;
+  }
+  for (int e = threadIdx.x; e < kFK * kFK * 2; e += blockDim.x) {   // (b, a, c): g t and t^2
+    const int c = e & 1, ka = (e >> 1) % kFK, kb = (e >> 1) / kFK;
+    float gt = 0, tt = 0;
+    for (int r = 0; r < kFRows; r++) {
+      const float wy = s_wy[r][kb];
+      gt += wy * s_pq[r][ka][c];
+      tt += wy * wy * s_pq[r][ka][2 + c];
+    }
+    out[kFHs + e] = gt;
+    out[kFHs + kFK * kFK * 2 + e] = tt;
+  }
+}
+
+// A point's Jacobian row in one image axis (0: u, 1: v) for module point (mx, my): H's 8 (du or dv), then the field's
+// knots around it (that axis's component); with axis < 0, a sample's row: the image gradient (scale_u, scale_v) times
+// the warp's derivative, both components of each knot.
+constexpr int kRowNz = 8 + 2 * 25;   // H, and at most 5 x 5 knots about a point, both components
+__device__ __forceinline__ int point_row(const FieldArgs &a, const WarpAt &o, float mx, float my, int axis, float scale_u, float scale_v,
+                                         uint8_t *idx, float *J) {
+  float du[8], dv[8];
+  dwarp_dh(o, mx, my, du, dv);
+  int nz = 0;
+  for (int q = 0; q < 8; q++) { idx[nz] = (uint8_t)q; J[nz++] = scale_u * du[q] + scale_v * dv[q]; }
+  for (int kb = 1; kb < kFK - 1; kb++) {
+    const float wy = knot_w(a, o.j, o.vv, kb);
+    if (wy == 0) continue;
+    for (int ka = 1; ka < kFK - 1; ka++) {
+      const float ww = wy * knot_w(a, o.i, o.uu, ka);
+      if (ww == 0 || nz + 2 > kRowNz) continue;
+      const int q = 8 + 2 * ((kb - 1) * 7 + (ka - 1));
+      if (axis < 0) {
+        idx[nz] = (uint8_t)q; J[nz++] = scale_u * ww;
+        idx[nz] = (uint8_t)(q + 1); J[nz++] = scale_v * ww;
+      } else {
+        idx[nz] = (uint8_t)(q + axis); J[nz++] = ww;
+      }
+    }
+  }
+  return nz;
+}
+
+// The normal equations of the three terms at the evaluation in hand, the loss, and the step (kept or halved). A CTA a
+// frame; A (kFP x kFP doubles) in dynamic shared memory. The track's and the anchors' residual rows are staged
+// kRowBatch at a time (a thread a row) and added into A and the gradients in row order by every thread at once, so
+// the sums are the same on every run. With terms set (the checks' call), the three terms' raw losses and gradients
+// are written there instead (frames x 3 x (1 + kFP)) and no step is taken.
+constexpr int kRowBatch = 128;
+__global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const float *regs, const float *part, const PilotTerms *pt,
+                                                          const float *anc_u, const float *anc_v, const uint8_t *anc_ok,
+                                                          const uint8_t *skip, FieldState *st, int last, double *terms) {
+  extern __shared__ double smA[];
+  __shared__ double bv[3][kFP], red[8], s_sum[kFPart], s_lvl[2], s_loss[3], s_cnt[3];
+  __shared__ double x[kFP], sc[kFP];
+  __shared__ uint8_t r_idx[kRowBatch][kRowNz];
+  __shared__ float r_J[kRowBatch][kRowNz], r_r[kRowBatch];
+  __shared__ int r_nz[kRowBatch], r_term[kRowBatch];
+  __shared__ int s_ok;
+  const int f = blockIdx.x, tid = threadIdx.x, blocks = a.n / kFRows;
+  if (skip && skip[f]) return;
+  const float *reg = regs + (int64_t)f * a.reg_stride;
+  const uint8_t *px = a.luma + f * a.fstride;
+  FieldState &S = st[f];
+  // the adjoint pass's partial sums, in block order
+  for (int q = tid; q < kFPart; q += blockDim.x) {
+    double acc = 0;
+    const float *p = part + (int64_t)f * blocks * kFPart + q;
+    for (int b = 0; b < blocks; b++) acc += p[(int64_t)b * kFPart];
+    s_sum[q] = acc;
+  }
+  for (int q = tid; q < 3 * kFP; q += blockDim.x) bv[q / kFP][q % kFP] = 0;
+  for (int q = tid; q < kFP * kFP; q += blockDim.x) smA[q] = 0;
+  __syncthreads();
+  // the track's levels: the dark cells' and the light cells' mean sample
+  double ld = 0, ll = 0, nd = 0, nl = 0;
+  for (int t = tid; t < a.ntrack; t += blockDim.x) {
+    const float4 c = a.track[t];
+    const WarpAt o = warp_at(a, reg, c.x, c.y);
+    float Iu, Iv;
+    const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
+    if (c.z > 0) { ld += z; nd += 1; } else { ll += z; nl += 1; }
+  }
+  ld = fblock_sum(ld, red); ll = fblock_sum(ll, red); nd = fblock_sum(nd, red); nl = fblock_sum(nl, red);
+  if (tid == 0) { s_lvl[0] = nd > 0 ? ld / nd : 0; s_lvl[1] = nl > 0 ? ll / nl : 0; }
+  __syncthreads();
+  // the track's and the anchors' losses
+  double lt = 0, la = 0, na = 0;
+  for (int t = tid; t < a.ntrack; t += blockDim.x) {
+    const float4 c = a.track[t];
+    const WarpAt o = warp_at(a, reg, c.x, c.y);
+    float Iu, Iv;
+    const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
+    const double r = z - (c.z > 0 ? s_lvl[0] : s_lvl[1]);
+    lt += r * r;
+  }
+  if (anc_ok)
+    for (int k = tid; k < 49; k += blockDim.x) {
+      if (!anc_ok[f * 49 + k]) continue;
+      const WarpAt o = warp_at(a, reg, a.anc[k % 7], a.anc[k / 7]);
+      const double ru = o.u - anc_u[f * 49 + k], rv = o.v - anc_v[f * 49 + k];
+      la += ru * ru + rv * rv;
+      na += 1;
+    }
+  lt = fblock_sum(lt, red); la = fblock_sum(la, red); na = fblock_sum(na, red);
+  if (tid == 0) {
+    s_loss[0] = pt[f].loss; s_loss[1] = lt; s_loss[2] = la; s_cnt[0] = a.npilot; s_cnt[1] = a.ntrack; s_cnt[2] = na;
+    // the terms' weights, fixed at the first evaluation: each term's residuals at unit mean square there (an anchor's
+    // reading under blur is far noisier than its 0.15 px on a sharp capture, so its spread is measured, not assumed)
+    if (!terms && S.evals == 0) {
+      S.wp = s_loss[0] > 0 ? s_cnt[0] / s_loss[0] : 0;
+      S.wt = s_loss[1] > 0 ? s_cnt[1] / s_loss[1] : 0;
+      S.wa = s_loss[2] > 0 ? 2 * s_cnt[2] / s_loss[2] : 0;
+    }
+  }
+  __syncthreads();
+  const double wt = terms ? 0.0 : S.wt, wa = terms ? 0.0 : S.wa;
+  // the track's rows (term 1), then the anchors' two rows each (term 2)
+  const int rows = a.ntrack + (anc_ok ? 98 : 0);
+  for (int base = 0; base < rows; base += kRowBatch) {
+    if (tid < kRowBatch) {
+      const int t = base + tid;
+      int nz = 0, term = 1;
+      float r = 0;
+      if (t < a.ntrack) {
+        const float4 c = a.track[t];
+        const WarpAt o = warp_at(a, reg, c.x, c.y);
+        float Iu, Iv;
+        const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
+        r = (float)(z - (c.z > 0 ? s_lvl[0] : s_lvl[1]));
+        nz = point_row(a, o, c.x, c.y, -1, Iu, Iv, r_idx[tid], r_J[tid]);
+      } else if (t < rows) {
+        const int k = (t - a.ntrack) >> 1, ax = (t - a.ntrack) & 1;
+        term = 2;
+        if (anc_ok[f * 49 + k]) {
+          const float X = a.anc[k % 7], Y = a.anc[k / 7];
+          const WarpAt o = warp_at(a, reg, X, Y);
+          r = ax == 0 ? o.u - anc_u[f * 49 + k] : o.v - anc_v[f * 49 + k];
+          nz = point_row(a, o, X, Y, ax, ax == 0 ? 1.0f : 0.0f, ax == 1 ? 1.0f : 0.0f, r_idx[tid], r_J[tid]);
+        }
+      }
+      r_nz[tid] = nz; r_term[tid] = term; r_r[tid] = r;
+    }
+    __syncthreads();
+    const int nrow = min(kRowBatch, rows - base);
+    for (int k = 0; k < nrow; k++) {
+      const int nz = r_nz[k], term = r_term[k];
+      const double w = term == 1 ? wt : wa;
+      if (w != 0)
+        for (int e = tid; e < nz * nz; e += blockDim.x) {
+          const int p = e / nz, q = e - p * nz;
+          smA[r_idx[k][p] * kFP + r_idx[k][q]] += w * r_J[k][p] * r_J[k][q];
+        }
+      if (tid < nz) bv[term][r_idx[k][tid]] += (double)r_J[k][tid] * r_r[k];
+      __syncthreads();
+    }
+  }
+  // the pilots' gradient: the adjoint pass's g t is d(loss)/d(theta), twice J^T r
+  for (int q = tid; q < kFP; q += blockDim.x) {
+    if (q < 8) bv[0][q] = 0.5 * s_sum[q];
+    else {
+      const int e = (q - 8) >> 1, c = (q - 8) & 1, kb = e / 7 + 1, ka = e % 7 + 1;
+      bv[0][q] = 0.5 * s_sum[kFHs + (kb * kFK + ka) * 2 + c];
+    }
+  }
+  __syncthreads();
+  if (terms) {   // the checks: raw losses and gradients (2 J^T r) of the three terms
+    double *o = terms + (int64_t)f * 3 * (1 + kFP);
+    for (int q = tid; q < 3 * (1 + kFP); q += blockDim.x) {
+      const int term = q / (1 + kFP), e = q % (1 + kFP);
+      o[q] = e == 0 ? s_loss[term] : 2.0 * bv[term][e - 1];
+    }
+    return;
+  }
+  const double wp = S.wp;
+  // the field's prior: each knot's displacement a zero-mean Gaussian of kFieldSigma pixels (the field carries what
+  // the registration's own mesh left, which is small where the anchors and the lens model already fit), so 98 knots
+  // cannot follow the residuals' noise
+  double fprior = 0;
+  for (int q = 8 + tid; q < kFP; q += blockDim.x) fprior += (double)S.theta[q] * S.theta[q];
+  fprior = fblock_sum(fprior, red) / (kFieldSigma * kFieldSigma);
+  // the pilots' J^T J: the tangents' Gram over H, their energies on the field's diagonal, times the pilots' share of
+  // the picture's energy; the prior's diagonal
+  const double npx = (double)a.n * a.n, mean = s_sum[44] / npx, ez = s_sum[45] - npx * mean * mean;
+  const double rho = ez > 0 ? pt[f].energy / ez : 0;
+  for (int e = tid; e < 64; e += blockDim.x) {
+    const int p = e >> 3, q = e & 7, lo = min(p, q), hi = max(p, q);
+    const int g = 8 + lo * 8 - lo * (lo - 1) / 2 + (hi - lo);   // (lo, hi) in the upper triangle, row by row
+    smA[p * kFP + q] += wp * rho * s_sum[g];
+  }
+  for (int q = 8 + tid; q < kFP; q += blockDim.x) {
+    const int e = (q - 8) >> 1, c = (q - 8) & 1, kb = e / 7 + 1, ka = e % 7 + 1;
+    smA[q * kFP + q] += wp * rho * s_sum[kFHs + kFK * kFK * 2 + (kb * kFK + ka) * 2 + c] + 1.0 / (kFieldSigma * kFieldSigma);
+  }
+  __syncthreads();
+  const double loss = wp * s_loss[0] + wt * s_loss[1] + wa * s_loss[2] + fprior;
+  // the right-hand side, the columns scaled, a Levenberg damping
+  for (int q = tid; q < kFP; q += blockDim.x) {
+    const double d = smA[q * kFP + q];
+    sc[q] = d > 0 ? sqrt(d) : 1.0;
+    x[q] = -(wp * bv[0][q] + wt * bv[1][q] + wa * bv[2][q] + (q >= 8 ? S.theta[q] / (kFieldSigma * kFieldSigma) : 0.0));
+  }
+  __syncthreads();
+  for (int e = tid; e < kFP * kFP; e += blockDim.x) {
+    const int p = e / kFP, q = e % kFP;
+    smA[e] /= sc[p] * sc[q];
+    if (p == q) smA[e] = smA[e] * 1.001 + 1e-9;
+  }
+  for (int q = tid; q < kFP; q += blockDim.x) x[q] /= sc[q];
+  if (tid == 0) s_ok = 1;
+  __syncthreads();
+  // Cholesky (the system is symmetric positive definite: J^T J, the prior and the damping), the lower triangle in
+  // place column by column across the CTA, then the two triangular solves
+  for (int c = 0; c < kFP; c++) {
+    if (tid == 0) {
+      const double d = smA[c * kFP + c];
+      if (!(d > 1e-300)) s_ok = 0;
+      else smA[c * kFP + c] = sqrt(d);
+    }
+    __syncthreads();
+    if (!s_ok) break;
+    const double l = smA[c * kFP + c];
+    for (int r = c + 1 + tid; r < kFP; r += blockDim.x) smA[r * kFP + c] /= l;
+    __syncthreads();
+    const int m = kFP - c - 1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int r = c + 1 + e / m, q = c + 1 + e % m;
+      if (q <= r) smA[r * kFP + q] -= smA[r * kFP + c] * smA[q * kFP + c];
+    }
+    __syncthreads();
+  }
+  if (tid != 0) return;
+  if (s_ok) {
+    for (int r = 0; r < kFP; r++) {   // L y = b
+      double v = x[r];
+      for (int q = 0; q < r; q++) v -= smA[r * kFP + q] * x[q];
+      x[r] = v / smA[r * kFP + r];
+    }
+    for (int r = kFP - 1; r >= 0; r--) {   // L^T z = y
+      double v = x[r];
+      for (int q = r + 1; q < kFP; q++) v -= smA[q * kFP + r] * x[q];
+      x[r] = v / smA[r * kFP + r];
+    }
+  }
+  float delta[kFP];
+  for (int q = 0; q < kFP; q++) delta[q] = s_ok && isfinite(x[q] / sc[q]) ? (float)(x[q] / sc[q]) : 0.0f;
+  if (S.evals == 0 || loss < S.loss_best) {
+    if (S.evals > 0) S.improved = 1;
+    S.loss_best = loss;
+    for (int q = 0; q < kFP; q++) { S.best[q] = S.theta[q]; S.delta[q] = delta[q]; }
+    S.scale = 1.0f;
+  } else {
+    S.scale *= 0.5f;
+  }
+  S.evals++;
+  for (int q = 0; q < kFP; q++) S.theta[q] = last ? S.best[q] : S.best[q] + S.scale * S.delta[q];
+}
+
+__global__ void field_load_kernel(const float *reg, int reg_stride, const float *theta, int frames, FieldState *st) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= frames) return;
+  FieldState &S = st[f];
+  for (int q = 0; q < kFP; q++) {
+    const float v = theta ? theta[(int64_t)f * kFP + q] : (q < 8 ? reg[(int64_t)f * reg_stride + q] : 0.0f);
+    S.theta[q] = S.best[q] = v;
+    S.delta[q] = 0;
+  }
+  S.loss_best = 0; S.wp = S.wa = S.wt = 0; S.scale = 1.0f; S.evals = 0; S.improved = 0;
+}
+
+__global__ void field_store_kernel(const FieldState *st, const uint8_t *skip, int frames, float *loss_out, int32_t *improved_out) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= frames) return;
+  const bool s = skip && skip[f];
+  if (loss_out) loss_out[f] = s ? 0.0f : (float)st[f].loss_best;
+  if (improved_out) improved_out[f] = s ? 0 : st[f].improved;
+}
+
+// The refined registration written back: the best parameters' H and mesh, frames the gate skips untouched.
+__global__ void field_copy_kernel(const float *src, const uint8_t *skip, int frames, int reg_stride, float *dst) {
+  const int f = blockIdx.y;
+  if (f >= frames || (skip && skip[f])) return;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < reg_stride; t += gridDim.x * blockDim.x) dst[(int64_t)f * reg_stride + t] = src[(int64_t)f * reg_stride + t];
+}
+
+}  // namespace lizg
+
+struct lizg_field {
+  lizg::Format f;
+  lizg::FieldArgs a{};
+  lizg_rx *rx = nullptr;
+  int chunk = 0;
+  lizg::EncFft enc{};
+  float *eff = nullptr, *G = nullptr, *part = nullptr, *base = nullptr;
+  float2 *coef = nullptr, *R = nullptr;
+  lizg::FieldState *state = nullptr;
+  lizg::PilotTerms *pt = nullptr;
+  uint8_t *skip = nullptr;
+  std::vector<void *> owned;
+};
+
+namespace {
+
+// A cubic Hermite's weights on its knots at x (the knots' slopes from their neighbours, one-sided at the ends): the
+// value is sum w[q] v[b + q], q = 0..3 (liblizard/src/acquire.c:2199-2217, the interior fill's mesh).
+void herm4(const double *t, int n, double x, int *b, double w[4]) {
+  int i = 0;
+  while (i < n - 2 && x >= t[i + 1]) i++;
+  const double hc = t[i + 1] - t[i], s = (x - t[i]) / hc, s2 = s * s, s3 = s2 * s;
+  const double h00 = 2 * s3 - 3 * s2 + 1, h01 = -2 * s3 + 3 * s2, A = (s3 - 2 * s2 + s) * hc, Bc = (s3 - s2) * hc;
+  w[0] = w[3] = 0; w[1] = h00; w[2] = h01;
+  if (i > 0) { const double d = t[i + 1] - t[i - 1]; w[0] -= A / d; w[2] += A / d; } else { w[1] -= A / hc; w[2] += A / hc; }
+  if (i + 2 < n) { const double d = t[i + 2] - t[i]; w[1] -= Bc / d; w[3] += Bc / d; } else { w[1] -= Bc / hc; w[2] += Bc / hc; }
+  *b = i - 1;
+}
+
+int track_bit(int side, int j) {   // liblizard/src/layout.c:57-61
+  uint32_t v = (uint32_t)(side * 4099 + (j >> 1)) * 2654435761u + 40503u;
+  v ^= v >> 15;
+  v *= 2246822519u;
+  v ^= v >> 13;
+  return (int)((v ^ (uint32_t)j) & 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+lizg_field *lizg_field_new(int n, int subch, int span, int chunk) {
+  using namespace lizg;
+  if (chunk < 1 || chunk > 64) { record_error(LIZG_E_ARG, "lizg_field_new: chunk must be 1..64"); return nullptr; }
+  int sms = 0;
+  if (device_ready(&sms)) return nullptr;
+  lizg_field *g = new (std::nothrow) lizg_field();
+  if (!g) { record_error(LIZG_E_NOMEM, "lizg_field_new: out of host memory"); return nullptr; }
+  if (format_build(n, subch, span, g->f)) { delete g; record_error(LIZG_E_ARG, "lizg_field_new: no such format"); return nullptr; }
+  const Format &f = g->f;
+  FieldArgs &a = g->a;
+  a.n = n; a.need = subch * kSub;
+  a.g0 = kMargin + 0.5f / f.scale; a.step = 1.0f / f.scale;
+  a.nn = layout_nodes(span + 2 * kMargin, a.pos);
+  a.reg_stride = 9 + 2 * a.nn * a.nn;
+  a.sx2 = f.sx2; a.sq2 = f.sq2;
+  for (int i = 0; i < 7; i++) { a.elo[i] = f.elo[i]; a.ehi[i] = f.ehi[i]; }
+  const int aside = span / 64;
+  for (int i = 0; i < 7; i++) a.anc[i] = (float)((int)std::floor(kMargin + (double)span * (i + 0.5) / 7 - aside / 2.0 + 0.5) + aside / 2.0);
+  // the pilots: their symbols (count bit 0), groups (block parity, radius band by quantile), (u, v)
+  std::vector<int32_t> pk;
+  std::vector<int16_t> puv;
+  std::vector<float2> shat;
+  std::vector<int> par;
+  std::vector<double> rho;
+  const float qa = 0.70710678f;
+  int vmax = 0;
+  for (size_t k = 0; k < f.uv.size() / 2; k++) vmax = std::max<int>(vmax, f.uv[2 * k + 1]);
+  for (int b = 0; b < f.blocks; b++) {
+    const Tier &tr = f.tier[f.block_tier[b]];
+    const int first = f.block_slot[b] / 2;
+    for (int s = tr.nt / 2; s < tr.slots / 2; s++) {
+      const int k = first + s;
+      pk.push_back(k);
+      puv.push_back(f.uv[2 * k]); puv.push_back(f.uv[2 * k + 1]);
+      shat.push_back(make_float2(f.white[2 * k] ? -qa : qa, f.white[2 * k + 1] ? -qa : qa));
+      par.push_back(b & 1);
+      rho.push_back(std::hypot((double)f.uv[2 * k], (double)f.uv[2 * k + 1]));
+    }
+  }
+  const int np = (int)pk.size();
+  std::vector<double> sorted = rho;
+  std::sort(sorted.begin(), sorted.end());
+  std::vector<uint8_t> grp(np);
+  for (int k = 0; k < np; k++) {
+    int bin = 0;
+    for (int q = 1; q < kFBins; q++) if (np && rho[k] > sorted[(size_t)((double)q * (np - 1) / kFBins)]) bin = q;
+    grp[k] = (uint8_t)(par[k] * kFBins + bin);
+  }
+  a.npilot = np;
+  a.vrows = vmax + 1;
+  // the Hermite weights of every node on the knots (the lattice's ends and the anchors' centres)
+  double kn[kFK];
+  const double X0 = a.pos[0], SX = a.pos[a.nn - 1] - a.pos[0];
+  kn[0] = 0; kn[kFK - 1] = 1;
+  for (int i = 0; i < 7; i++) kn[i + 1] = (a.anc[i] - X0) / SX;
+  std::vector<float> wk((size_t)a.nn * kFK, 0.0f);
+  for (int i = 0; i < a.nn; i++) {
+    int b;
+    double w[4];
+    herm4(kn, kFK, (a.pos[i] - X0) / SX, &b, w);
+    for (int q = 0; q < 4; q++) if (b + q >= 0 && b + q < kFK) wk[(size_t)i * kFK + b + q] += (float)w[q];
+  }
+  // the timing track's cells: 2 x 2 modules at depth 5..6 on every side, the even runs of 4 (layout.c:57-61, 69-141)
+  std::vector<float4> track;
+  {
+    const int side = span + 2 * kMargin, reserve = 15;
+    for (int sd = 0; sd < 4; sd++)
+      for (int cell = 0; reserve + 2 * cell + 1 < side - reserve; cell++) {
+        if ((cell / 4) & 1) continue;
+        const float along = (float)(reserve + 2 * cell + 1), depth = 6.0f;
+        const float dark = (float)track_bit(sd, cell / 4 / 2 * 4 + cell % 4);
+        float mx, my;
+        if (sd == 0) { mx = along; my = depth; }
+        else if (sd == 2) { mx = along; my = (float)side - depth; }
+        else if (sd == 3) { mx = depth; my = along; }
+        else { mx = (float)side - depth; my = along; }
+        if ((int)track.size() < kFMaxTrack) track.push_back(make_float4(mx, my, dark, 0.0f));
+      }
+  }
+  a.ntrack = (int)track.size();
+  // the detrend basis and its DFTs, the sender's transform's twiddles
+  std::vector<float2> x1(n), x2(n);
+  for (int t = 0; t < n; t++) { x1[t] = make_float2(f.x1r[t], f.x1i[t]); x2[t] = make_float2(f.x2r[t], f.x2i[t]); }
+  int rad[3], lines;
+  if (fft_plan(n, rad, &lines)) { delete g; record_error(LIZG_E_ARG, "lizg_field_new: no transform plan"); return nullptr; }
+  std::vector<float2> tws(n);
+  for (int s = 0, ns = 1; s < 3; ns *= rad[s], s++)
+    for (int q = 1; q < rad[s]; q++)
+      for (int k = 0; k < ns; k++) {
+        const double th = -2.0 * 3.14159265358979323846 * q * k / ((double)ns * rad[s]);
+        tws[ns + (q - 1) * ns + k] = make_float2((float)std::cos(th), (float)std::sin(th));
+      }
+  g->chunk = chunk;
+  bool ok = np >= 16;
+  auto up = [&](const void *src, size_t bytes) -> void * {
+    void *d = nullptr;
+    if (!ok || cudaMalloc(&d, std::max<size_t>(bytes, 1)) != cudaSuccess) { ok = false; return nullptr; }
+    g->owned.push_back(d);
+    if (src && bytes && cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) ok = false;
+    return d;
+  };
+  a.pilot = static_cast<int32_t *>(up(pk.data(), pk.size() * 4));
+  a.puv = static_cast<int16_t *>(up(puv.data(), puv.size() * 2));
+  a.shat = static_cast<float2 *>(up(shat.data(), shat.size() * sizeof(float2)));
+  a.group = static_cast<uint8_t *>(up(grp.data(), grp.size()));
+  a.wk = static_cast<float *>(up(wk.data(), wk.size() * 4));
+  a.track = static_cast<float4 *>(up(track.data(), track.size() * sizeof(float4)));
+  a.cx = static_cast<float *>(up(f.cx.data(), f.cx.size() * 4));
+  a.qx = static_cast<float *>(up(f.qx.data(), f.qx.size() * 4));
+  a.x1 = static_cast<float2 *>(up(x1.data(), x1.size() * sizeof(float2)));
+  a.x2 = static_cast<float2 *>(up(x2.data(), x2.size() * sizeof(float2)));
+  g->enc.n = n; g->enc.vrows = a.vrows; g->enc.lim = 3.0e38f; g->enc.sc = 1.0f;
+  g->enc.tws = static_cast<float2 *>(up(tws.data(), tws.size() * sizeof(float2)));
+  const size_t C = (size_t)chunk;
+  g->eff = static_cast<float *>(up(nullptr, C * a.reg_stride * 4));
+  g->base = static_cast<float *>(up(nullptr, C * a.reg_stride * 4));
+  g->G = static_cast<float *>(up(nullptr, C * n * n * 4));
+  g->part = static_cast<float *>(up(nullptr, C * (n / kFRows) * kFPart * 4));
+  g->coef = static_cast<float2 *>(up(nullptr, C * a.need * sizeof(float2)));
+  g->R = static_cast<float2 *>(up(nullptr, C * a.vrows * n * sizeof(float2)));
+  g->state = static_cast<FieldState *>(up(nullptr, C * sizeof(FieldState)));
+  g->pt = static_cast<PilotTerms *>(up(nullptr, C * sizeof(PilotTerms)));
+  g->skip = static_cast<uint8_t *>(up(nullptr, C));
+  if (ok) {
+    g->rx = lizg_rx_new(n, subch, span, chunk);
+    ok = g->rx != nullptr;
+    if (ok) lizg_rx_set_read(g->rx, LIZG_READ_EXACT);   // the refinement's forward model: the float walk it differentiates
+  }
+  if (!ok) {
+    lizg_field_free(g);
+    record_error(LIZG_E_NOMEM, np < 16 ? "lizg_field_new: the format has too few pilots" : "lizg_field_new: device allocation failed");
+    return nullptr;
+  }
+  static SmemOptIn opt;
+  if (opt.set(reinterpret_cast<const void *>(field_solve_kernel), kFP * kFP * (int)sizeof(double)) != cudaSuccess) {
+    lizg_field_free(g);
+    record_error(LIZG_E_CUDA, "lizg_field_new: shared memory opt-in");
+    return nullptr;
+  }
+  return g;
+}
+
+void lizg_field_free(lizg_field *g) {
+  if (!g) return;
+  if (g->rx) lizg_rx_free(g->rx);
+  for (void *p : g->owned) cudaFree(p);
+  delete g;
+}
+
+}  // extern "C"
+
+namespace {
+
+// One evaluation of a chunk of fc frames (luma and base registrations at frame f0 of the call): the registration the
+// parameters give, the spectrum, the pilots, the adjoint transform and pass, then the step (or, with terms, the raw
+// terms).
+int field_eval(lizg_field *g, const lizg::FieldArgs &a, const float *base, int fc, const lizg_anchor_out *anchors, int f0, int last,
+               double *terms, cudaStream_t st) {
+  using namespace lizg;
+  field_mesh_kernel<<<fc, 256, 0, st>>>(a, g->state, 0, base, g->eff);
+  if (int rc = rx_spectrum_luma(g->rx, a.luma, a.w, a.h, a.w, a.fstride, g->eff, fc, reinterpret_cast<float *>(g->coef), st)) return rc;
+  cudaMemsetAsync(g->R, 0, sizeof(float2) * (size_t)fc * a.vrows * a.n, st);
+  field_pilot_kernel<<<fc, kFThreads, 0, st>>>(a, g->coef, g->skip, g->R, g->pt);
+  if (enc_fft_launch(g->enc, fc, g->R, g->G, st) != cudaSuccess) return record_error(LIZG_E_CUDA, "lizg_field: adjoint transform launch");
+  field_grad_kernel<<<fc * (a.n / kFRows), kFThreads, 0, st>>>(a, g->eff, g->G, g->pt, g->skip, g->part);
+  const float *au = anchors ? anchors->u + (int64_t)f0 * 49 : nullptr, *av = anchors ? anchors->v + (int64_t)f0 * 49 : nullptr;
+  const uint8_t *ao = anchors ? anchors->ok + (int64_t)f0 * 49 : nullptr;
+  field_solve_kernel<<<fc, 256, kFP * kFP * sizeof(double), st>>>(a, g->eff, g->part, g->pt, au, av, ao, g->skip, g->state, last, terms);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : record_error(LIZG_E_CUDA, (std::string("lizg_field: ") + cudaGetErrorString(e)).c_str());
+}
+
+int check_frames(const lizg_field *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const void *d_reg, int frames, const char *who) {
+  if (!g || !d_luma || !d_reg || frames < 1 || w < 2 || h < 2 || (frames > 1 && frame_stride < (int64_t)w * h))
+    return lizg::record_error(LIZG_E_ARG, (std::string(who) + ": NULL argument, empty batch or frame under 2 x 2").c_str());
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lizg_field_refine_dev(lizg_field *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int steps,
+                          const lizg_anchor_out *anchors, const uint8_t *d_gate, float *d_loss, int32_t *d_improved, void *stream) {
+  using namespace lizg;
+  if (int rc = check_frames(g, d_luma, w, h, frame_stride, d_reg, frames, "lizg_field_refine_dev")) return rc;
+  if (steps < 0 || steps > 16) return record_error(LIZG_E_ARG, "lizg_field_refine_dev: steps outside 0..16");
+  if (anchors && (!anchors->ok || !anchors->u || !anchors->v)) return record_error(LIZG_E_ARG, "lizg_field_refine_dev: anchors without ok, u, v");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the gate on the host: only runs of frames it lets through are worked on
+  std::vector<uint8_t> gate(frames, 1);
+  if (d_gate && (cudaMemcpyAsync(gate.data(), d_gate, frames, cudaMemcpyDeviceToHost, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess))
+    return record_error(LIZG_E_CUDA, "lizg_field_refine_dev: reading the gate");
+  for (int f0 = 0; f0 < frames;) {
+    if (!gate[f0]) { f0++; continue; }
+    int fc = 0;
+    while (f0 + fc < frames && fc < g->chunk && gate[f0 + fc]) fc++;
+    FieldArgs a = g->a;
+    a.w = w; a.h = h; a.fstride = frame_stride;
+    a.luma = d_luma + (int64_t)f0 * frame_stride;
+    float *reg = d_reg + (int64_t)f0 * a.reg_stride;
+    cudaMemsetAsync(g->skip, 0, fc, st);
+    cudaMemcpyAsync(g->base, reg, sizeof(float) * fc * a.reg_stride, cudaMemcpyDeviceToDevice, st);
+    field_load_kernel<<<(fc + 127) / 128, 128, 0, st>>>(g->base, a.reg_stride, nullptr, fc, g->state);
+    for (int e = 0; e <= steps; e++)   // steps + 1 evaluations: the baseline, then each step's
+      if (int rc = field_eval(g, a, g->base, fc, anchors, f0, e == steps, nullptr, st)) return rc;
+    field_mesh_kernel<<<fc, 256, 0, st>>>(a, g->state, 1, g->base, g->eff);
+    field_copy_kernel<<<dim3(1, fc), 256, 0, st>>>(g->eff, g->skip, fc, a.reg_stride, reg);
+    field_store_kernel<<<(fc + 127) / 128, 128, 0, st>>>(g->state, g->skip, fc, d_loss ? d_loss + f0 : nullptr, d_improved ? d_improved + f0 : nullptr);
+    f0 += fc;
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : record_error(LIZG_E_CUDA, (std::string("lizg_field_refine_dev: ") + cudaGetErrorString(e)).c_str());
+}
+
+int lizg_field_terms_dev(lizg_field *g, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_reg, const float *d_theta,
+                         int frames, const lizg_anchor_out *anchors, double *d_terms, void *stream) {
+  using namespace lizg;
+  if (int rc = check_frames(g, d_luma, w, h, frame_stride, d_reg, frames, "lizg_field_terms_dev")) return rc;
+  if (!d_theta || !d_terms || frames > g->chunk) return record_error(LIZG_E_ARG, "lizg_field_terms_dev: NULL theta or terms, or frames over the chunk");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  FieldArgs a = g->a;
+  a.w = w; a.h = h; a.fstride = frame_stride; a.luma = d_luma;
+  cudaMemsetAsync(g->skip, 0, frames, st);
+  cudaMemcpyAsync(g->base, d_reg, sizeof(float) * frames * a.reg_stride, cudaMemcpyDeviceToDevice, st);
+  field_load_kernel<<<(frames + 127) / 128, 128, 0, st>>>(g->base, a.reg_stride, d_theta, frames, g->state);
+  return field_eval(g, a, g->base, frames, anchors, 0, 0, d_terms, st);
+}
+
+}  // extern "C"

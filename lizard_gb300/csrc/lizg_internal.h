@@ -162,6 +162,11 @@ cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, in
                                const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
+// Row (b) alone from captured frames: the handle's read through each frame's registration, the anchors' erase, the
+// detrend and the 2D transform, the used coefficients into d_coef (frames x subch x 320 complex, pos order); no soft
+// stage. For the registration's refinements, which measure their mismatch where the receiver measures it.
+int rx_spectrum_luma(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
+                     float *d_coef, cudaStream_t st);
 
 }  // namespace lizg
 

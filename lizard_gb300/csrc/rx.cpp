@@ -390,6 +390,25 @@ int lizg_rx_finish_luma_dev(lizg_rx *r, const uint8_t *d_luma, int w, int h, int
   return finish_src(r, src, frames, out, d_coef, st, sms);
 }
 
+}  // extern "C"
+
+int lizg::rx_spectrum_luma(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
+                           float *d_coef, cudaStream_t st) {
+  if (!r || !d_luma || !d_reg || !d_coef || frames < 1 || frames > r->max_frames || w < 2 || h < 2 || pitch < w)
+    return lizg::record_error(LIZG_E_ARG, "spectrum from frames: bad arguments");
+  int sms = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  lizg::SrcDev src{};
+  src.sd = r->sd;
+  src.luma = d_luma; src.w = w; src.h = h; src.pitch = pitch; src.fstride = frame_stride; src.reg = d_reg;
+  src.regstride = 9 + 2 * r->sd.nx * r->sd.ny;
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, r->f.subch * lizg::kSub, reinterpret_cast<float2 *>(d_coef), r->ctab};
+  const cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
+  return e == cudaSuccess ? 0 : lizg::record_error(LIZG_E_CUDA, (std::string("spectrum from frames: ") + cudaGetErrorString(e)).c_str());
+}
+
+extern "C" {
+
 // The same call as lizg_rx_finish_luma_dev, replayed from a CUDA graph: the first call with a given set of buffers
 // and sizes captures the whole per-frame pipeline (its 10 to 12 kernels, the per-code fork and join) on the handle's
 // own stream; later calls with the same arguments launch the captured graph on `stream` in one call. Different
