@@ -235,6 +235,43 @@ def picture_frames(fmt, count, seed, sigma):
     return luma.contiguous(), np.tile(reg, (count, 1))
 
 
+def fft_error_table():
+    """The transform's error per picture size on the FFT demod batch's sizes (n = 384, 768, 1152, 1536 at their top
+    versions): the GPU's spectrum against the reference's own FP32 one (tests/golden/fft_ref.npz, made by the reference
+    compiled from its sources; every eighth coefficient) and against the FP64 oracle (every coefficient), max and rms
+    relative to the spectrum's rms; the reference's own FP32 against FP64 beside them."""
+    import hashlib
+    import numpy as np
+    import lizard_gb300 as lz
+    import oracle
+    from lizard_gb300_testing import synth
+    if not os.path.exists(oracle.PORT_PATH):
+        oracle.build(ref=False)
+    z = np.load(os.path.join(ROOT, "tests", "golden", "fft_ref.npz"))
+    table = {}
+    for n in (384, 768, 1152, 1536):
+        n_, subch, span = (int(v) for v in z["n%d_fmt" % n])
+        f = lz.Format(n_, subch, span)
+        g, _ = synth.grids(f, 1, seed=31 * n, sigma=3.0, shift=(0.15, -0.1))
+        if hashlib.sha256(np.rint(g[0] * 255.0).astype(np.uint8).tobytes()).digest() != z["n%d_sha256" % n].tobytes():
+            table[n] = {"error": "the grid made here differs from the fixture's"}
+            continue
+        c = lz.Receiver(n_, subch, span, max_frames=1).finish_grid(g)["coef"][0]
+        c = c[0::2] + 1j * c[1::2]
+        r = z["n%d_ref" % n]
+        ref = r[:, 0].astype(np.float64) + 1j * r[:, 1]
+        fp64, _, _ = oracle.Fmt(n_, subch, span).spectrum(g[0])
+        idx = np.arange(0, c.size, 8)
+
+        def err(a, b):
+            rms = np.sqrt(np.mean(np.abs(b) ** 2))
+            e = np.abs(a - b)
+            return {"max": float("%.3g" % (e.max() / rms)), "rms": float("%.3g" % (np.sqrt(np.mean(e ** 2)) / rms))}
+        table[n] = {"vs_reference_fp32": err(c[idx], ref), "vs_fp64": err(c, fp64), "reference_fp32_vs_fp64": err(ref, fp64[idx]),
+                    "bar": 1e-4}
+    return table
+
+
 def bench_receiver(args, stream):
     """The frame receiver, rows a-e (sampler, erase, detrend, 2D FFT, pilots, demap, LDPC, CRC), on two workloads:
     the FFT demod batch (256 pictures: 64 each at n = 384, 768, 1152, 1536 at their top versions, 64 ring, AWGN 3
@@ -283,6 +320,7 @@ def bench_receiver(args, stream):
                               "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
                               "gpu_launches_per_step": sum(rx.launches for rx in rxs)}
     peak, peak_src = peaks()
+    res["fft_demod_batch"]["error_per_n"] = fft_error_table()
     res["fft_demod_batch"]["hbm"] = {"algorithmic_bytes_per_step": step_bytes, "GBps": round(step_bytes / (ms / 1e3) / 1e9, 1),
                                      "frac": round(step_bytes / (ms / 1e3) / 1e9 / peak, 4), "peak_source": peak_src,
                                      "bytes": "luma footprint + Y written and read + used coefficients and soft values written and read + blocks"}
