@@ -157,6 +157,9 @@ int lizg_layout_nodes(int span, float *node_x, float *node_y, int32_t *nn);
 int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm);
 // Kernel launches the last finish made.
 int lizg_rx_launches(const lizg_rx *r);
+// 1 where one of the handle's passes gave up a bounded wait (the row pass's wait for its bulk tensor copies, which
+// complete in microseconds; the pass then leaves its tile), else 0. Waits for the device. Host code.
+int lizg_rx_fault(lizg_rx *r);
 // The picture read of the handle's later finishes from captured frames (LIZG_READ_DECODE or LIZG_READ_EXACT); returns
 // the previous one, or LIZG_E_ARG. Host code.
 int lizg_rx_set_read(lizg_rx *r, int read);

@@ -216,6 +216,7 @@ def _rx_sigs(L):
     L.lizg_rx_perm.argtypes = [P, I, P]
     L.lizg_rx_launches.argtypes = [P]
     L.lizg_rx_set_read.argtypes = [P, I]
+    L.lizg_rx_fault.argtypes = [P]
     L.lizg_layout_nodes.argtypes = [I, P, P, P]
     L.lizg_rx_finish_luma_host.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
@@ -348,6 +349,10 @@ class Receiver:
     @property
     def launches(self):
         return int(lib().lizg_rx_launches(self._h))
+
+    def fault(self):
+        """1 where a pass's bounded wait gave up (never expected), else 0."""
+        return _check(lib().lizg_rx_fault(self._h), "lizg_rx_fault")
 
     def _outputs(self, frames, torch, keep):
         return rx_outputs(self.fmt, frames, keep)

@@ -23,6 +23,8 @@
 // read or written, fall on distinct banks within a half-warp) and lines 16 / L (mod 16) slots apart; the passes'
 // twiddles sit beside the lines, per pass [r - 1][k], so a warp reads consecutive entries. FP32 throughout, as the
 // reference's; the twiddles and the surface factors are worked out in double.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "lizg_internal.h"
@@ -486,26 +488,73 @@ __global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const do
   }
 }
 
+// A bounded wait on an mbarrier's phase (try_wait blocks a while in hardware before it answers): false when the
+// limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit) {
+  for (int i = 0; i < limit; i++) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // The row pass: a CTA takes (frame f, rows v0 .. v0 + L - 1), transforms them along x and takes the surface's
 // spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0. The used
 // coefficients go straight to their place in pos order: C[f][tpos[v][u]] (tpos -1 where (u, v) is not used).
+// The tile's rows come in by the tensor memory accelerator: bulk tensor copies of 128 complex points of a row each,
+// issued by one thread, landing densely at the start of each line's slots (at a 128-byte boundary) and counted on an
+// mbarrier; then every thread moves its points from the dense rows to the padded lines (all read, then all written).
 template <int N>
-__global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const float2 *fac, const float2 *Y, const int32_t *tpos,
-                                                               int need, float2 *C) {
+__global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const float2 *fac, const __grid_constant__ CUtensorMap ymap,
+                                                               const int32_t *tpos, int need, float2 *C, int *err) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N);
+  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), SEGS = N / 128, PER = (L * N + kThreads - 1) / kThreads;
+  static_assert(LSTR >= N + 16, "a line's slots hold its dense row at a 128-byte boundary");
+  __shared__ __align__(8) uint64_t s_bar;
   const SmemMap sm = smem_map<N>(smraw);
   const int tid = threadIdx.x, tiles = (xd.vrows + L - 1) / L;
   const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
-  for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
-  const float2 *Yf = Y + ((int64_t)f * xd.vrows + v0) * n;
-  // the tile's rows into the padded lines by 8-byte asynchronous copies, all in flight at once
-  for (int t = tid; t < Lr * n; t += kThreads) {
-    const int l = t / n, u = t - l * n;
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(sm.buf + l * LSTR + pad(u));
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(Yf + (int64_t)l * n + u) : "memory");
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+  // line l's dense row: at the first 128-byte boundary of its slots (room: a line's slots exceed n by 16 or more)
+  auto dense = [&](int l) { return (uint32_t)(((uint32_t)__cvta_generic_to_shared(sm.buf + l * LSTR) + 127u) & ~127u); };
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"((uint32_t)(Lr * N * 8)) : "memory");
+    const int y0 = f * xd.vrows + v0;
+    for (int l = 0; l < Lr; l++)
+      for (int s = 0; s < SEGS; s++)
+        asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n"
+                     ::"r"(dense(l) + 1024u * s), "l"(&ymap), "r"(256 * s), "r"(y0 + l), "r"(bar) : "memory");
+  }
+  for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
+  if (!mbar_wait(bar, 0, 1 << 22)) {   // never expected: record it, wait for the copies once more, leave the tile
+    atomicOr(err, 1);
+    mbar_wait(bar, 0, 1 << 22);
+    return;
+  }
+  // dense rows to padded lines: thread t takes points t, t + kThreads, ... of the tile (line-major), all read first
+  float2 v[PER];
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const int p = tid + k * kThreads, l = p / N, u = p - l * N;
+    if (p < L * N && l < Lr) {
+      float2 t;
+      asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(t.x), "=f"(t.y) : "r"(dense(l) + 8u * u));
+      v[k] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const int p = tid + k * kThreads, l = p / N, u = p - l * N;
+    if (p < L * N && l < Lr) sm.buf[l * LSTR + pad(u)] = v[k];
+  }
   __syncthreads();
   fft_lines<N>(sm.buf, sm.tw, Lr);
   float2 *Cf = C + (int64_t)f * need;
@@ -542,6 +591,21 @@ int fft_plan(int n, int radix[3], int *lines) {
 
 int fft_hole_bands(int n) { return (n / 8 + kHoleBand - 1) / kHoleBand; }
 
+int fft_y_map(CUtensorMap *map, float2 *Y, int n, int64_t rows) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess || !fn) return -1;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)2 * n, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)2 * n * sizeof(float)};
+  const cuuint32_t box[2] = {256, 1}, estr[2] = {1, 1};
+  return (int)encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, Y, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
 template <int N>
 static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st) {
   constexpr int L = plan_of(N).lines, smem = smem_bytes_of(N), tiles = N / (2 * L);
@@ -562,7 +626,8 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
   }
   fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, b.ctab, bands, b.hole, b.part, b.Y);
   fac_kernel<<<frames, 256, 0, st>>>(xd, tiles, b.part, b.fac);
-  fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, b.Y, b.tpos, b.need, b.C);
+  if (!b.ymap || !b.err) return cudaErrorInvalidValue;
+  fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, *b.ymap, b.tpos, b.need, b.C, b.err);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,7 @@
 // Internal declarations shared by the host shim (api.cpp) and the kernels (*.cu). Not part of the C ABI.
 #ifndef LIZG_INTERNAL_H
 #define LIZG_INTERNAL_H
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <atomic>
@@ -68,7 +69,13 @@ struct FftBufs {
   // homography's row terms of row y at y (n entries), then each column x's displacement terms at mesh row j
   // (lin_cell) at n + j n + x (j < ny - 1, ny = nx)
   float4 *ctab;
+  // Y as a 2D tensor (rows frames x vrows, each n complex as 2n floats; boxes of 128 complex by one row) for the row
+  // pass's bulk tensor loads, and a device word the passes set when a bounded wait gave up
+  const CUtensorMap *ymap;
+  int *err;
 };
+// Encodes the tensor map of a Y buffer of `rows` rows of n complex points (the row pass's loads). 0, or a CUresult.
+int fft_y_map(CUtensorMap *map, float2 *Y, int n, int64_t rows);
 
 // The transform CTA's dynamic shared memory bound and the complex points its lines hold at most.
 constexpr int kFftSmemMax = 96 * 1024;

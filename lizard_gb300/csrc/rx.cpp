@@ -38,6 +38,8 @@ struct lizg_rx {
   float2 *Y = nullptr, *C = nullptr;   // column transforms' kept rows; the spectrum's used coefficients in pos order
   float4 *ctab = nullptr;              // the sampler's row and mesh-cell terms, frames x n x nx
   int32_t *tpos = nullptr;             // vrows x n: the pos index of each kept spectrum point, -1 where unused
+  CUtensorMap ymap;                    // Y as the row pass's bulk tensor loads see it
+  int *dev_err = nullptr;              // set by a pass whose bounded wait gave up
   // per-tier streams, forked from and joined to the caller's
   cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -175,6 +177,9 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
   ok(dev_alloc(r, &r->fac, F * (2 * (size_t)n + r->xd.vrows)));
   ok(dev_alloc(r, &r->part, F * (size_t)(n / 2) * 5));   // column tiles (at most n / 2) x 5
   ok(dev_alloc(r, &r->Y, F * (size_t)r->xd.vrows * n));
+  ok(dev_alloc(r, &r->dev_err, 1));
+  if (e == cudaSuccess) e = cudaMemset(r->dev_err, 0, sizeof(int));
+  if (e == cudaSuccess && lizg::fft_y_map(&r->ymap, r->Y, n, F * (int64_t)r->xd.vrows)) e = cudaErrorInvalidValue;
   ok(dev_alloc(r, &r->ctab, F * n * (size_t)r->sd.nx));
   ok(dev_alloc(r, &r->C, F * need));
   {
@@ -275,6 +280,13 @@ int lizg_rx_perm(const lizg_rx *r, int tier, int16_t *perm) {
 
 int lizg_rx_launches(const lizg_rx *r) { return r ? r->launches : LIZG_E_ARG; }
 
+int lizg_rx_fault(lizg_rx *r) {
+  if (!r) return lizg::record_error(LIZG_E_ARG, "lizg_rx_fault: NULL handle");
+  int v = 0;
+  const cudaError_t e = cudaMemcpy(&v, r->dev_err, sizeof(int), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? v : lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_fault: ") + cudaGetErrorString(e)).c_str());
+}
+
 int lizg_rx_set_read(lizg_rx *r, int read) {
   if (!r || (read != LIZG_READ_DECODE && read != LIZG_READ_EXACT)) return lizg::record_error(LIZG_E_ARG, "lizg_rx_set_read: no handle or no such read");
   const int was = r->sd.read;
@@ -333,7 +345,7 @@ int lizg_rx_finish_coef_dev(lizg_rx *r, const float *d_coef, int frames, const l
 static int finish_src(lizg_rx *r, const lizg::SrcDev &src, int frames, const lizg_rx_out *out, float *d_coef, cudaStream_t st, int sms) {
   const int need = r->f.subch * lizg::kSub;
   float2 *C = d_coef ? reinterpret_cast<float2 *>(d_coef) : r->C;   // the caller's spectrum buffer when given
-  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, C, r->ctab};
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, C, r->ctab, &r->ymap, r->dev_err};
   cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("transform: ") + cudaGetErrorString(e)).c_str());
   r->launches += src.grid ? 4 : 5;   // sampling in the column pass adds the sampler's row and cell table
@@ -359,7 +371,7 @@ int lizg_rx_spectrum_grid_dev(lizg_rx *r, const float *d_grid, int frames, float
   lizg::SrcDev src{};
   src.grid = d_grid; src.gstride = (int64_t)r->f.n * r->f.n; src.sd = r->sd;
   const int need = r->f.subch * lizg::kSub;
-  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, reinterpret_cast<float2 *>(d_coef), r->ctab};
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, need, reinterpret_cast<float2 *>(d_coef), r->ctab, &r->ymap, r->dev_err};
   cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, static_cast<cudaStream_t>(stream));
   r->launches = 4;
   return e == cudaSuccess ? 0 : lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_spectrum_grid_dev: ") + cudaGetErrorString(e)).c_str());
@@ -402,7 +414,7 @@ int lizg::rx_spectrum_luma(lizg_rx *r, const uint8_t *d_luma, int w, int h, int 
   src.sd = r->sd;
   src.luma = d_luma; src.w = w; src.h = h; src.pitch = pitch; src.fstride = frame_stride; src.reg = d_reg;
   src.regstride = 9 + 2 * r->sd.nx * r->sd.ny;
-  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, r->f.subch * lizg::kSub, reinterpret_cast<float2 *>(d_coef), r->ctab};
+  const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, r->f.subch * lizg::kSub, reinterpret_cast<float2 *>(d_coef), r->ctab, &r->ymap, r->dev_err};
   const cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   return e == cudaSuccess ? 0 : lizg::record_error(LIZG_E_CUDA, (std::string("spectrum from frames: ") + cudaGetErrorString(e)).c_str());
 }
