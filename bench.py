@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--fmt-only", action="store_true", help="time only the format word and the border nodes (profiling)")
     ap.add_argument("--encode-only", action="store_true", help="time only the sender on the GPU (profiling)")
     ap.add_argument("--refine-only", action="store_true", help="time only the distorted captures' registration comparison")
+    ap.add_argument("--refine-frames", type=int, default=0, help="with --refine-only: the first K frames of the spread set alone "
+                    "(profiling; 0: the configuration's three sets)")
     ap.add_argument("--ldpc-variants", action="store_true", help="time every decoder kernel variant of every code on the "
                     "workload's codewords of that code (device-resident), outputs checked identical across variants")
     return ap.parse_args()
@@ -932,6 +934,8 @@ def bench_refinement(args, stream):
     sets = [("spread", [(9000 + k, float(rng.uniform(-0.05, 0.05)), float(rng.uniform(0.5, 2.0))) for k in range(1024)]),
             ("blur1.5_k1_0.03", [(9100 + k, 0.03, 1.5) for k in range(64)]),
             ("mild_blur0.5", [(9200 + k, float(rng.uniform(-0.05, 0.05)), 0.5) for k in range(64)])]
+    if getattr(args, "refine_frames", 0):
+        sets = [("spread", sets[0][1][:args.refine_frames])]
     sp = stream.cuda_stream
     res = {"workload": "1920x1080, LIZARD-1024 (n=1536) in the 128 ring painted by the sender (border, cyclic guard), rotation 15 deg, "
                        "tilt 20 deg, scale 0.8-1.1 x 1000 px, radial k1, blur in linear light, AWGN 3 DN, a seed a frame; corners = a finder's "

@@ -94,7 +94,7 @@ struct PilotTerms {
 // The warp at module point (mx, my): H, then the mesh's bilinear displacement from the frame's registration reg;
 // the node cell (i, j) and the place (uu, vv) in it.
 struct WarpAt {
-  float u, v, wd, U, V;
+  float u, v, wd, iw, U, V;
   int i, j;
   float uu, vv;
 };
@@ -103,22 +103,27 @@ __device__ __forceinline__ int cell_of(const float *pos, int nn, float m) {
   while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (m >= pos[mid]) lo = mid; else hi = mid - 1; }
   return lo;
 }
-__device__ __forceinline__ WarpAt warp_at(const FieldArgs &a, const float *reg, float mx, float my) {
+// The warp at (mx, my) in node cell (i, j) at place (uu, vv).
+__device__ __forceinline__ WarpAt warp_in(const FieldArgs &a, const float *reg, float mx, float my, int i, int j, float uu, float vv) {
   WarpAt o;
-  o.i = cell_of(a.pos, a.nn, mx);
-  o.j = cell_of(a.pos, a.nn, my);
-  o.uu = (mx - a.pos[o.i]) / (a.pos[o.i + 1] - a.pos[o.i]);
-  o.vv = (my - a.pos[o.j]) / (a.pos[o.j + 1] - a.pos[o.j]);
+  o.i = i; o.j = j; o.uu = uu; o.vv = vv;
   const float *n00 = reg + 9 + 2 * (o.j * a.nn + o.i), *n10 = n00 + 2, *n01 = n00 + 2 * a.nn, *n11 = n01 + 2;
   const float mdx = (n00[0] * (1 - o.uu) + n10[0] * o.uu) * (1 - o.vv) + (n01[0] * (1 - o.uu) + n11[0] * o.uu) * o.vv;
   const float mdy = (n00[1] * (1 - o.uu) + n10[1] * o.uu) * (1 - o.vv) + (n01[1] * (1 - o.uu) + n11[1] * o.uu) * o.vv;
   const float *h = reg;
   o.wd = h[6] * mx + h[7] * my + 1;
-  o.U = (h[0] * mx + h[1] * my + h[2]) / o.wd;
-  o.V = (h[3] * mx + h[4] * my + h[5]) / o.wd;
+  o.iw = 1.0f / o.wd;
+  o.U = (h[0] * mx + h[1] * my + h[2]) * o.iw;
+  o.V = (h[3] * mx + h[4] * my + h[5]) * o.iw;
   o.u = o.U + mdx;
   o.v = o.V + mdy;
   return o;
+}
+// pos, inv: the node positions (a.pos) and each cell's 1 / width, in the caller's CTA's shared memory (lanes search
+// them at different places, which a kernel parameter would serve one address at a time).
+__device__ __forceinline__ WarpAt warp_at(const FieldArgs &a, const float *pos, const float *inv, const float *reg, float mx, float my) {
+  const int i = cell_of(pos, a.nn, mx), j = cell_of(pos, a.nn, my);
+  return warp_in(a, reg, mx, my, i, j, (mx - pos[i]) * inv[i], (my - pos[j]) * inv[j]);
 }
 // The bilinear read at gamma 1 at pixel point (u, v) (sample()'s clamp) and its gradient in u and v (zero along an
 // axis the clamp holds: past the frame's edge the read no longer moves with the point).
@@ -138,13 +143,27 @@ __device__ __forceinline__ float read_grad(const uint8_t *px, int w, int h, floa
 }
 // The warp's derivative in h0..h7 at (mx, my): du[q], dv[q].
 __device__ __forceinline__ void dwarp_dh(const WarpAt &o, float mx, float my, float du[8], float dv[8]) {
-  const float iw = 1.0f / o.wd;
+  const float iw = o.iw;
   du[0] = mx * iw; du[1] = my * iw; du[2] = iw; du[3] = 0; du[4] = 0; du[5] = 0; du[6] = -o.U * mx * iw; du[7] = -o.U * my * iw;
   dv[0] = 0; dv[1] = 0; dv[2] = 0; dv[3] = mx * iw; dv[4] = my * iw; dv[5] = iw; dv[6] = -o.V * mx * iw; dv[7] = -o.V * my * iw;
 }
 // A point's weight on knot a along one axis: the bilinear blend of its cell's two nodes' Hermite weights.
-__device__ __forceinline__ float knot_w(const FieldArgs &a, int i, float uu, int k) {
-  return (1 - uu) * a.wk[i * kFK + k] + uu * a.wk[(i + 1) * kFK + k];
+// wk: the knot weights (a.wk) in shared memory.
+__device__ __forceinline__ float knot_w(const float *wk, int i, float uu, int k) {
+  return (1 - uu) * wk[i * kFK + k] + uu * wk[(i + 1) * kFK + k];
+}
+// The node positions and knot weights a CTA reads at every point, staged in its shared memory.
+struct FieldShared {
+  float pos[40], inv[40];
+  float wk[40 * kFK];
+};
+__device__ __forceinline__ void stage_shared(const FieldArgs &a, FieldShared &s) {
+  for (int t = threadIdx.x; t < a.nn; t += blockDim.x) {
+    s.pos[t] = a.pos[t];
+    s.inv[t] = t + 1 < a.nn ? 1.0f / (a.pos[t + 1] - a.pos[t]) : 0.0f;
+  }
+  for (int t = threadIdx.x; t < a.nn * kFK; t += blockDim.x) s.wk[t] = a.wk[t];
+  __syncthreads();
 }
 __device__ __forceinline__ bool in_sq(const FieldArgs &a, int t) {
   bool in = false;
@@ -196,46 +215,49 @@ __device__ double fblock_sum(double v, double *red) {
 // detrend's adjoint constants and the pilots' energy. A CTA a frame.
 __global__ void __launch_bounds__(kFThreads) field_pilot_kernel(FieldArgs a, const float2 *coef, const uint8_t *skip, float2 *R, PilotTerms *pt) {
   __shared__ double red[kFThreads / 32], gain[kFGroups];
+  __shared__ float s_acc[kFGroups * 2][kFThreads];   // each thread's own column: its pilots' sums by group
   const int f = blockIdx.x, tid = threadIdx.x, n = a.n;
   if (skip && skip[f]) return;
   const float2 *C = coef + (int64_t)f * a.need;
-  for (int g = 0; g < kFGroups; g++) {
-    double num = 0, den = 0;
-    for (int k = tid; k < a.npilot; k += blockDim.x) {
-      if (a.group[k] != g) continue;
-      const float2 s = a.shat[k], c = C[a.pilot[k]];
-      num += (double)s.x * c.x + (double)s.y * c.y;
-      den += (double)s.x * s.x + (double)s.y * s.y;
-    }
-    num = fblock_sum(num, red);
-    den = fblock_sum(den, red);
-    if (tid == 0) gain[g] = den > 0 ? num / den : 0.0;
+  // the gains: each group's sum s.c over s.s, a thread's pilots summed in float in its own slots, then the slots in
+  // thread order in double (FP64 is a narrow pipe on this part: the per-pilot work stays in float)
+  for (int q = 0; q < 2 * kFGroups; q++) s_acc[q][tid] = 0.0f;
+  for (int k = tid; k < a.npilot; k += blockDim.x) {
+    const float2 s = a.shat[k], c = C[a.pilot[k]];
+    const int g = a.group[k];
+    s_acc[2 * g][tid] += s.x * c.x + s.y * c.y;
+    s_acc[2 * g + 1][tid] += s.x * s.x + s.y * s.y;
   }
   __syncthreads();
-  double loss = 0, en = 0, k1 = 0, k2 = 0, k3 = 0, k4 = 0, k5 = 0;
+  if (tid < kFGroups) {
+    double num = 0, den = 0;
+    for (int t = 0; t < (int)blockDim.x; t++) { num += s_acc[2 * tid][t]; den += s_acc[2 * tid + 1][t]; }
+    gain[tid] = den > 0 ? num / den : 0.0;
+  }
+  __syncthreads();
+  float loss = 0, en = 0, k1 = 0, k2 = 0, k3 = 0, k4 = 0, k5 = 0;
   float2 *Rf = R + (int64_t)f * a.vrows * n;
   for (int k = tid; k < a.npilot; k += blockDim.x) {
     const float2 s = a.shat[k], c = C[a.pilot[k]];
-    const double gk = gain[a.group[k]];
-    const double rx = c.x - gk * s.x, ry = c.y - gk * s.y;
+    const float gk = (float)gain[a.group[k]];
+    const float rx = c.x - gk * s.x, ry = c.y - gk * s.y;
     loss += rx * rx + ry * ry;
-    en += (double)c.x * c.x + (double)c.y * c.y;
+    en += c.x * c.x + c.y * c.y;
     const int u = a.puv[2 * k], v = a.puv[2 * k + 1], um = (u + n) % n;
-    Rf[(int64_t)v * n + um] = make_float2((float)rx, (float)ry);
+    Rf[(int64_t)v * n + um] = make_float2(rx, ry);
     // Re(conj(r) z) = rx zx + ry zy
     const float2 xu = a.x1[um], xv = a.x1[v];
-    const double pr = (double)xu.x * xv.x - (double)xu.y * xv.y, pi = (double)xu.x * xv.y + (double)xu.y * xv.x;
+    const float pr = xu.x * xv.x - xu.y * xv.y, pi = xu.x * xv.y + xu.y * xv.x;
     k1 += rx * pr + ry * pi;
     if (v == 0) { const float2 yu = a.x2[um]; k2 += rx * xu.x + ry * xu.y; k3 += rx * yu.x + ry * yu.y; }
     if (u == 0) { const float2 yv = a.x2[v]; k4 += rx * xv.x + ry * xv.y; k5 += rx * yv.x + ry * yv.y; }
   }
-  loss = fblock_sum(loss, red);
-  en = fblock_sum(en, red);
-  k1 = fblock_sum(k1, red); k2 = fblock_sum(k2, red); k3 = fblock_sum(k3, red); k4 = fblock_sum(k4, red); k5 = fblock_sum(k5, red);
+  const double lossd = fblock_sum(loss, red), end = fblock_sum(en, red);
+  const double k1d = fblock_sum(k1, red), k2d = fblock_sum(k2, red), k3d = fblock_sum(k3, red), k4d = fblock_sum(k4, red), k5d = fblock_sum(k5, red);
   if (tid == 0) {
     PilotTerms &p = pt[f];
-    p.loss = loss; p.energy = en;
-    p.k[0] = 2 * k1 / (a.sx2 * a.sx2); p.k[1] = 2 * k2 / a.sx2; p.k[2] = 2 * k3 / a.sq2; p.k[3] = 2 * k4 / a.sx2; p.k[4] = 2 * k5 / a.sq2;
+    p.loss = lossd; p.energy = end;
+    p.k[0] = 2 * k1d / (a.sx2 * a.sx2); p.k[1] = 2 * k2d / a.sx2; p.k[2] = 2 * k3d / a.sq2; p.k[3] = 2 * k4d / a.sx2; p.k[4] = 2 * k5d / a.sq2;
   }
 }
 
@@ -251,10 +273,13 @@ __global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, cons
   const float *reg = regs + (int64_t)f * a.reg_stride;
   const uint8_t *px = a.luma + f * a.fstride;
   const float *Gf = G + (int64_t)f * n * n + (int64_t)y * n;
+  __shared__ FieldShared fs;
+  stage_shared(a, fs);
   __shared__ float s_pq[kFRows][kFK][4];   // a row's field sums: g t x, g t y, t x^2, t y^2 at each knot a
   __shared__ float s_wy[kFRows][kFK];
   __shared__ float s_h[kFThreads / 32][kFHs];
-  const double *K = pt[f].k;
+  // the detrend's adjoint constants in float: the gradient's share of them needs no more (FP64 is a narrow pipe here)
+  const float K0 = (float)pt[f].k[0], K1 = (float)pt[f].k[1], K2 = (float)pt[f].k[2], K3 = (float)pt[f].k[3], K4 = (float)pt[f].k[4];
   const float my = a.g0 + (float)y * a.step;
   const float cy = a.cx[y], qy = a.qx[y];
   const bool ysq = in_sq(a, y);
@@ -264,18 +289,20 @@ __global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, cons
   float pq[kFK][4];
 #pragma unroll
   for (int k = 0; k < kFK; k++) pq[k][0] = pq[k][1] = pq[k][2] = pq[k][3] = 0;
-  int jrow = 0;
-  float vrow = 0;
+  // the row's mesh row once; each lane's cell found onwards from its last (x rises along the row)
+  const int jrow = cell_of(fs.pos, a.nn, my);
+  const float vrow = (my - fs.pos[jrow]) * fs.inv[jrow];
+  int icell = 0;
   for (int x = lane; x < n; x += 32) {
     const float mx = a.g0 + (float)x * a.step;
-    const WarpAt o = warp_at(a, reg, mx, my);
-    jrow = o.j; vrow = o.vv;
+    while (icell < a.nn - 2 && mx >= fs.pos[icell + 1]) icell++;
+    const WarpAt o = warp_in(a, reg, mx, my, icell, jrow, (mx - fs.pos[icell]) * fs.inv[icell], vrow);
     float Iu, Iv;
     const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
     hs[44] += z; hs[45] += z * z;
     if (ysq && in_sq(a, x)) continue;   // erased: the shading surface, held constant
     const float cxx = a.cx[x], qxx = a.qx[x];
-    const float g = Gf[x] - 0.5f - (float)(K[0] * cxx * cy + K[1] * cxx + K[2] * qxx + K[3] * cy + K[4] * qy);
+    const float g = Gf[x] - 0.5f - (K0 * cxx * cy + K1 * cxx + K2 * qxx + K3 * cy + K4 * qy);
     float du[8], dv[8];
     dwarp_dh(o, mx, my, du, dv);
     float t[8];
@@ -288,7 +315,7 @@ __global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, cons
       for (int q = p; q < 8; q++) hs[e++] += t[p] * t[q];
 #pragma unroll
     for (int k = 0; k < kFK; k++) {
-      const float wx = knot_w(a, o.i, o.uu, k);
+      const float wx = knot_w(fs.wk, o.i, o.uu, k);
       const float tx = Iu * wx, ty = Iv * wx;
       pq[k][0] += g * tx; pq[k][1] += g * ty; pq[k][2] += tx * tx; pq[k][3] += ty * ty;
     }
@@ -303,7 +330,7 @@ __global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, cons
       for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
       if (lane == 0) s_pq[warp][k][c] = v;
     }
-  if (lane < kFK) s_wy[warp][lane] = knot_w(a, jrow, vrow, lane);
+  if (lane < kFK) s_wy[warp][lane] = knot_w(fs.wk, jrow, vrow, lane);
 #pragma unroll
   for (int q = 0; q < kFHs; q++) {
     float v = hs[q];
@@ -331,61 +358,71 @@ __global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, cons
   }
 }
 
-// A point's Jacobian row in one image axis (0: u, 1: v) for module point (mx, my): H's 8 (du or dv), then the field's
-// knots around it (that axis's component); with axis < 0, a sample's row: the image gradient (scale_u, scale_v) times
-// the warp's derivative, both components of each knot.
-constexpr int kRowNz = 8 + 2 * 25;   // H, and at most 5 x 5 knots about a point, both components
-__device__ __forceinline__ int point_row(const FieldArgs &a, const WarpAt &o, float mx, float my, int axis, float scale_u, float scale_v,
-                                         uint8_t *idx, float *J) {
+// A point's Jacobian row in one image axis (0: u, 1: v) for module point (mx, my), written into a dense row of kFPad
+// floats the caller zeroed: H's 8 (du or dv), then the field's knots around it (that axis's component); with axis < 0,
+// a sample's row: the image gradient (scale_u, scale_v) times the warp's derivative, both components of each knot.
+constexpr int kFPad = (kFP + 3) / 4 * 4;   // a staged row's stride, floats: whole 16-byte groups
+__device__ __forceinline__ void point_row(const FieldShared &fs, const WarpAt &o, float mx, float my, int axis, float scale_u,
+                                          float scale_v, float *row) {
   float du[8], dv[8];
   dwarp_dh(o, mx, my, du, dv);
-  int nz = 0;
-  for (int q = 0; q < 8; q++) { idx[nz] = (uint8_t)q; J[nz++] = scale_u * du[q] + scale_v * dv[q]; }
+  for (int q = 0; q < 8; q++) row[q] = scale_u * du[q] + scale_v * dv[q];
   for (int kb = 1; kb < kFK - 1; kb++) {
-    const float wy = knot_w(a, o.j, o.vv, kb);
+    const float wy = knot_w(fs.wk, o.j, o.vv, kb);
     if (wy == 0) continue;
     for (int ka = 1; ka < kFK - 1; ka++) {
-      const float ww = wy * knot_w(a, o.i, o.uu, ka);
-      if (ww == 0 || nz + 2 > kRowNz) continue;
+      const float ww = wy * knot_w(fs.wk, o.i, o.uu, ka);
+      if (ww == 0) continue;
       const int q = 8 + 2 * ((kb - 1) * 7 + (ka - 1));
       if (axis < 0) {
-        idx[nz] = (uint8_t)q; J[nz++] = scale_u * ww;
-        idx[nz] = (uint8_t)(q + 1); J[nz++] = scale_v * ww;
+        row[q] = scale_u * ww;
+        row[q + 1] = scale_v * ww;
       } else {
-        idx[nz] = (uint8_t)(q + axis); J[nz++] = ww;
+        row[q + axis] = ww;
       }
     }
   }
-  return nz;
 }
 
 // The normal equations of the three terms at the evaluation in hand, the loss, and the step (kept or halved). A CTA a
-// frame; A (kFP x kFP doubles) in dynamic shared memory. The track's and the anchors' residual rows are staged
-// kRowBatch at a time (a thread a row) and added into A and the gradients in row order by every thread at once, so
-// the sums are the same on every run. With terms set (the checks' call), the three terms' raw losses and gradients
+// frame; A (kFP x kFP doubles) in dynamic shared memory, then the staged rows. The track's and the anchors' residual
+// rows are staged kRowBatch at a time as dense rows (a thread a row); each thread then sums a 4 x 4 tile of the upper
+// triangle of J^T W J over the batch in float and adds it into A (double), and the terms' J^T r a parameter a thread,
+// so every sum runs in a fixed order. With terms set (the checks' call), the three terms' raw losses and gradients
 // are written there instead (frames x 3 x (1 + kFP)) and no step is taken.
 constexpr int kRowBatch = 128;
-__global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const float *regs, const float *part, const PilotTerms *pt,
+constexpr int kFTiles = kFPad / 4, kFTileCount = kFTiles * (kFTiles + 1) / 2;
+constexpr size_t kSolveSmem = sizeof(double) * kFP * kFP + sizeof(float) * kRowBatch * kFPad;
+static_assert((sizeof(double) * kFP * kFP) % 16 == 0, "the staged rows start on a 16-byte boundary");
+__global__ void __launch_bounds__(256, 1) field_solve_kernel(FieldArgs a, const float *regs, const float *part, const PilotTerms *pt,
                                                           const float *anc_u, const float *anc_v, const uint8_t *anc_ok,
                                                           const uint8_t *skip, FieldState *st, int last, double *terms) {
-  extern __shared__ double smA[];
+  extern __shared__ __align__(16) double smA[];
+  float *Jd = reinterpret_cast<float *>(smA + kFP * kFP);   // kRowBatch x kFPad
   __shared__ double bv[3][kFP], red[8], s_sum[kFPart], s_lvl[2], s_loss[3], s_cnt[3];
-  __shared__ double x[kFP], sc[kFP];
-  __shared__ uint8_t r_idx[kRowBatch][kRowNz];
-  __shared__ float r_J[kRowBatch][kRowNz], r_r[kRowBatch];
-  __shared__ int r_nz[kRowBatch], r_term[kRowBatch];
-  __shared__ int s_ok;
+  __shared__ double x[kFP], sc[kFP], isc[kFP], s_inv[kFP];
+  __shared__ float r_w[kRowBatch], r_r[kRowBatch];
+  __shared__ int r_term[kRowBatch];
+  __shared__ FieldShared fs;
   const int f = blockIdx.x, tid = threadIdx.x, blocks = a.n / kFRows;
   if (skip && skip[f]) return;
+  stage_shared(a, fs);
   const float *reg = regs + (int64_t)f * a.reg_stride;
   const uint8_t *px = a.luma + f * a.fstride;
   FieldState &S = st[f];
-  // the adjoint pass's partial sums, in block order
+  // the adjoint pass's partial sums, in block order within each of 8 interleaved sums (8 loads in flight a thread),
+  // the 8 then added pairwise (blocks is a multiple of 8 for every picture size; any rest is summed after)
   for (int q = tid; q < kFPart; q += blockDim.x) {
-    double acc = 0;
     const float *p = part + (int64_t)f * blocks * kFPart + q;
-    for (int b = 0; b < blocks; b++) acc += p[(int64_t)b * kFPart];
-    s_sum[q] = acc;
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int b = 0;
+    for (; b + 8 <= blocks; b += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) acc[u] += p[(int64_t)(b + u) * kFPart];
+    }
+    double tail = 0;
+    for (; b < blocks; b++) tail += p[(int64_t)b * kFPart];
+    s_sum[q] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])) + tail;
   }
   for (int q = tid; q < 3 * kFP; q += blockDim.x) bv[q / kFP][q % kFP] = 0;
   for (int q = tid; q < kFP * kFP; q += blockDim.x) smA[q] = 0;
@@ -394,7 +431,7 @@ __global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const flo
   double ld = 0, ll = 0, nd = 0, nl = 0;
   for (int t = tid; t < a.ntrack; t += blockDim.x) {
     const float4 c = a.track[t];
-    const WarpAt o = warp_at(a, reg, c.x, c.y);
+    const WarpAt o = warp_at(a, fs.pos, fs.inv, reg, c.x, c.y);
     float Iu, Iv;
     const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
     if (c.z > 0) { ld += z; nd += 1; } else { ll += z; nl += 1; }
@@ -406,7 +443,7 @@ __global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const flo
   double lt = 0, la = 0, na = 0;
   for (int t = tid; t < a.ntrack; t += blockDim.x) {
     const float4 c = a.track[t];
-    const WarpAt o = warp_at(a, reg, c.x, c.y);
+    const WarpAt o = warp_at(a, fs.pos, fs.inv, reg, c.x, c.y);
     float Iu, Iv;
     const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
     const double r = z - (c.z > 0 ? s_lvl[0] : s_lvl[1]);
@@ -415,7 +452,7 @@ __global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const flo
   if (anc_ok)
     for (int k = tid; k < 49; k += blockDim.x) {
       if (!anc_ok[f * 49 + k]) continue;
-      const WarpAt o = warp_at(a, reg, a.anc[k % 7], a.anc[k / 7]);
+      const WarpAt o = warp_at(a, fs.pos, fs.inv, reg, a.anc[k % 7], a.anc[k / 7]);
       const double ru = o.u - anc_u[f * 49 + k], rv = o.v - anc_v[f * 49 + k];
       la += ru * ru + rv * rv;
       na += 1;
@@ -433,45 +470,81 @@ __global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const flo
   }
   __syncthreads();
   const double wt = terms ? 0.0 : S.wt, wa = terms ? 0.0 : S.wa;
+  const bool need_a = wt != 0 || wa != 0;
   // the track's rows (term 1), then the anchors' two rows each (term 2)
   const int rows = a.ntrack + (anc_ok ? 98 : 0);
   for (int base = 0; base < rows; base += kRowBatch) {
-    if (tid < kRowBatch) {
+    const int nrow = min(kRowBatch, rows - base);
+    for (int e = tid; e < kRowBatch * kFPad / 4; e += blockDim.x) reinterpret_cast<float4 *>(Jd)[e] = make_float4(0, 0, 0, 0);
+    __syncthreads();
+    if (tid < nrow) {
       const int t = base + tid;
-      int nz = 0, term = 1;
+      float *row = Jd + tid * kFPad;
+      int term = 1;
       float r = 0;
       if (t < a.ntrack) {
         const float4 c = a.track[t];
-        const WarpAt o = warp_at(a, reg, c.x, c.y);
+        const WarpAt o = warp_at(a, fs.pos, fs.inv, reg, c.x, c.y);
         float Iu, Iv;
         const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
         r = (float)(z - (c.z > 0 ? s_lvl[0] : s_lvl[1]));
-        nz = point_row(a, o, c.x, c.y, -1, Iu, Iv, r_idx[tid], r_J[tid]);
-      } else if (t < rows) {
+        point_row(fs, o, c.x, c.y, -1, Iu, Iv, row);
+      } else {
         const int k = (t - a.ntrack) >> 1, ax = (t - a.ntrack) & 1;
         term = 2;
         if (anc_ok[f * 49 + k]) {
           const float X = a.anc[k % 7], Y = a.anc[k / 7];
-          const WarpAt o = warp_at(a, reg, X, Y);
+          const WarpAt o = warp_at(a, fs.pos, fs.inv, reg, X, Y);
           r = ax == 0 ? o.u - anc_u[f * 49 + k] : o.v - anc_v[f * 49 + k];
-          nz = point_row(a, o, X, Y, ax, ax == 0 ? 1.0f : 0.0f, ax == 1 ? 1.0f : 0.0f, r_idx[tid], r_J[tid]);
+          point_row(fs, o, X, Y, ax, ax == 0 ? 1.0f : 0.0f, ax == 1 ? 1.0f : 0.0f, row);
         }
       }
-      r_nz[tid] = nz; r_term[tid] = term; r_r[tid] = r;
+      r_term[tid] = term; r_r[tid] = r; r_w[tid] = (float)(term == 1 ? wt : wa);
     }
     __syncthreads();
-    const int nrow = min(kRowBatch, rows - base);
-    for (int k = 0; k < nrow; k++) {
-      const int nz = r_nz[k], term = r_term[k];
-      const double w = term == 1 ? wt : wa;
-      if (w != 0)
-        for (int e = tid; e < nz * nz; e += blockDim.x) {
-          const int p = e / nz, q = e - p * nz;
-          smA[r_idx[k][p] * kFP + r_idx[k][q]] += w * r_J[k][p] * r_J[k][q];
+    if (need_a)
+      for (int t = tid; t < kFTileCount; t += blockDim.x) {
+        int ti = 0, rem = t;   // tile row ti holds the tiles tj = ti .. kFTiles - 1
+        while (rem >= kFTiles - ti) { rem -= kFTiles - ti; ti++; }
+        const int tj = ti + rem;
+        float acc[4][4];
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc[p][q] = 0;
+        for (int r = 0; r < nrow; r++) {
+          const float w = r_w[r];
+          const float4 va = *reinterpret_cast<const float4 *>(Jd + r * kFPad + 4 * ti);
+          const float4 vb = *reinterpret_cast<const float4 *>(Jd + r * kFPad + 4 * tj);
+          const float pa[4] = {w * va.x, w * va.y, w * va.z, w * va.w}, pb[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+          for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[p][q] += pa[p] * pb[q];
         }
-      if (tid < nz) bv[term][r_idx[k][tid]] += (double)r_J[k][tid] * r_r[k];
-      __syncthreads();
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const int i = 4 * ti + p, j = 4 * tj + q;
+            if (i < kFP && j < kFP) smA[i * kFP + j] += acc[p][q];
+          }
+      }
+    for (int i = tid; i < kFP; i += blockDim.x) {
+      float g1 = 0, g2 = 0;
+      for (int r = 0; r < nrow; r++) {
+        const float v = Jd[r * kFPad + i] * r_r[r];
+        if (r_term[r] == 1) g1 += v; else g2 += v;
+      }
+      bv[1][i] += g1;
+      bv[2][i] += g2;
     }
+    __syncthreads();
+  }
+  // the upper triangle mirrored into the lower
+  for (int e = tid; e < kFP * kFP; e += blockDim.x) {
+    const int p = e / kFP, q = e - p * kFP;
+    if (p > q) smA[e] = smA[q * kFP + p];
   }
   // the pilots' gradient: the adjoint pass's g t is d(loss)/d(theta), twice J^T r
   for (int q = tid; q < kFP; q += blockDim.x) {
@@ -516,52 +589,60 @@ __global__ void __launch_bounds__(256) field_solve_kernel(FieldArgs a, const flo
   for (int q = tid; q < kFP; q += blockDim.x) {
     const double d = smA[q * kFP + q];
     sc[q] = d > 0 ? sqrt(d) : 1.0;
+    isc[q] = 1.0 / sc[q];
     x[q] = -(wp * bv[0][q] + wt * bv[1][q] + wa * bv[2][q] + (q >= 8 ? S.theta[q] / (kFieldSigma * kFieldSigma) : 0.0));
   }
   __syncthreads();
   for (int e = tid; e < kFP * kFP; e += blockDim.x) {
     const int p = e / kFP, q = e % kFP;
-    smA[e] /= sc[p] * sc[q];
+    smA[e] *= isc[p] * isc[q];
     if (p == q) smA[e] = smA[e] * 1.001 + 1e-9;
   }
-  for (int q = tid; q < kFP; q += blockDim.x) x[q] /= sc[q];
-  if (tid == 0) s_ok = 1;
+  for (int q = tid; q < kFP; q += blockDim.x) x[q] *= isc[q];
   __syncthreads();
-  // Cholesky (the system is symmetric positive definite: J^T J, the prior and the damping), the lower triangle in
-  // place column by column across the CTA, then the two triangular solves
+  if (tid == 0) s_inv[0] = 1.0 / smA[0];
+  __syncthreads();
+  // L D L^T (the system is symmetric positive definite: J^T J, the prior and the damping) in the lower triangle, in
+  // place, a column a step across the CTA (16 x 16 threads over the trailing rows and columns); a column's entries
+  // become L's one step later, once nothing reads them. Every thread reads the same pivot, so all stop together; the
+  // thread that finishes the next pivot takes its reciprocal (one double division a column).
+  const int tx = tid & 15, ty = tid >> 4;
+  bool ok = true;
   for (int c = 0; c < kFP; c++) {
-    if (tid == 0) {
-      const double d = smA[c * kFP + c];
-      if (!(d > 1e-300)) s_ok = 0;
-      else smA[c * kFP + c] = sqrt(d);
+    const double d = smA[c * kFP + c];
+    if (!(d > 1e-300)) { ok = false; break; }
+    if (c > 0) {
+      const double ip = s_inv[c - 1];
+      for (int r = c + tid; r < kFP; r += blockDim.x) smA[r * kFP + c - 1] *= ip;
     }
-    __syncthreads();
-    if (!s_ok) break;
-    const double l = smA[c * kFP + c];
-    for (int r = c + 1 + tid; r < kFP; r += blockDim.x) smA[r * kFP + c] /= l;
-    __syncthreads();
-    const int m = kFP - c - 1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int r = c + 1 + e / m, q = c + 1 + e % m;
-      if (q <= r) smA[r * kFP + q] -= smA[r * kFP + c] * smA[q * kFP + c];
+    const double id = s_inv[c];
+    for (int r = c + 1 + ty; r < kFP; r += 16) {
+      const double lr = smA[r * kFP + c] * id;
+      for (int q = c + 1 + tx; q <= r; q += 16) smA[r * kFP + q] -= lr * smA[q * kFP + c];
     }
+    if (tid == 0 && c + 1 < kFP) s_inv[c + 1] = 1.0 / smA[(c + 1) * kFP + c + 1];   // this thread's own last update
     __syncthreads();
   }
+  // L y = b, D z = y, L^T w = z: one warp, a column a step
+  if (ok && tid < 32) {
+    for (int c = 0; c < kFP; c++) {
+      __syncwarp();
+      const double yc = x[c];
+      for (int r = c + 1 + tid; r < kFP; r += 32) x[r] -= smA[r * kFP + c] * yc;
+    }
+    __syncwarp();
+    for (int q = tid; q < kFP; q += 32) x[q] *= s_inv[q];
+    for (int c = kFP - 1; c >= 0; c--) {
+      __syncwarp();
+      const double zc = x[c];
+      for (int r = tid; r < c; r += 32) x[r] -= smA[c * kFP + r] * zc;
+    }
+  }
+  __syncthreads();
   if (tid != 0) return;
-  if (s_ok) {
-    for (int r = 0; r < kFP; r++) {   // L y = b
-      double v = x[r];
-      for (int q = 0; q < r; q++) v -= smA[r * kFP + q] * x[q];
-      x[r] = v / smA[r * kFP + r];
-    }
-    for (int r = kFP - 1; r >= 0; r--) {   // L^T z = y
-      double v = x[r];
-      for (int q = r + 1; q < kFP; q++) v -= smA[q * kFP + r] * x[q];
-      x[r] = v / smA[r * kFP + r];
-    }
-  }
+  const bool s_ok = ok;
   float delta[kFP];
-  for (int q = 0; q < kFP; q++) delta[q] = s_ok && isfinite(x[q] / sc[q]) ? (float)(x[q] / sc[q]) : 0.0f;
+  for (int q = 0; q < kFP; q++) delta[q] = s_ok && isfinite(x[q] * isc[q]) ? (float)(x[q] * isc[q]) : 0.0f;
   if (S.evals == 0 || loss < S.loss_best) {
     if (S.evals > 0) S.improved = 1;
     S.loss_best = loss;
@@ -778,7 +859,7 @@ lizg_field *lizg_field_new(int n, int subch, int span, int chunk) {
     return nullptr;
   }
   static SmemOptIn opt;
-  if (opt.set(reinterpret_cast<const void *>(field_solve_kernel), kFP * kFP * (int)sizeof(double)) != cudaSuccess) {
+  if (opt.set(reinterpret_cast<const void *>(field_solve_kernel), (int)kSolveSmem) != cudaSuccess) {
     lizg_field_free(g);
     record_error(LIZG_E_CUDA, "lizg_field_new: shared memory opt-in");
     return nullptr;
@@ -811,7 +892,7 @@ int field_eval(lizg_field *g, const lizg::FieldArgs &a, const float *base, int f
   field_grad_kernel<<<fc * (a.n / kFRows), kFThreads, 0, st>>>(a, g->eff, g->G, g->pt, g->skip, g->part);
   const float *au = anchors ? anchors->u + (int64_t)f0 * 49 : nullptr, *av = anchors ? anchors->v + (int64_t)f0 * 49 : nullptr;
   const uint8_t *ao = anchors ? anchors->ok + (int64_t)f0 * 49 : nullptr;
-  field_solve_kernel<<<fc, 256, kFP * kFP * sizeof(double), st>>>(a, g->eff, g->part, g->pt, au, av, ao, g->skip, g->state, last, terms);
+  field_solve_kernel<<<fc, 256, kSolveSmem, st>>>(a, g->eff, g->part, g->pt, au, av, ao, g->skip, g->state, last, terms);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : record_error(LIZG_E_CUDA, (std::string("lizg_field: ") + cudaGetErrorString(e)).c_str());
 }

@@ -31,7 +31,6 @@ struct lizg_rx {
   int *counters = nullptr;
   double *hole = nullptr, *part = nullptr;
   float2 *fac = nullptr;
-  float *grid = nullptr;              // sampled pictures (luma input)
   lizg::SampleDev sd{};
   float *node_xy = nullptr;
   float4 *sample_t = nullptr;
@@ -172,7 +171,6 @@ lizg_rx *lizg_rx_new(int n, int subch, int span, int max_frames) {
     }
   }
   const size_t F = (size_t)max_frames;
-  ok(dev_alloc(r, &r->grid, F * n * n));
   ok(dev_alloc(r, &r->hole, F * lizg::fft_hole_bands(n) * 6));
   ok(dev_alloc(r, &r->fac, F * (2 * (size_t)n + r->xd.vrows)));
   ok(dev_alloc(r, &r->part, F * (size_t)(n / 2) * 5));   // column tiles (at most n / 2) x 5
