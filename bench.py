@@ -304,23 +304,37 @@ def bench_receiver(args, stream):
             lz._check(lz.lib().lizg_rx_finish_luma_dev(rx._h, lz.ctypes.c_void_p(d_l.data_ptr()), n, n, n, n * n, lz.ctypes.c_void_p(d_r.data_ptr()),
                                                          per, lz.ctypes.byref(s), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
 
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
-    ok = sum(int(b[2]["ok"].sum().item()) for b in bufs)
     K = max(1, args.steps // 3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(K):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / K
+
+    def timed():
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(K):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
+
+    # the device's LDPC variants (tuned on large batches of one code), then each handle's own per-tier choice timed
+    # on its batch (lizg_rx_autotune: per picture size and code rate)
+    ms_global = timed()
+    ok_global = [b[2]["ok"].clone() for b in bufs]
+    choices = {}
+    for rx, (d_l, d_r, o, s, n) in zip(rxs, bufs):
+        choices[str(n)] = rx.autotune_dev(d_l.data_ptr(), n, n, n, n * n, d_r.data_ptr(), per, sp)[:rx.fmt.tiers]
+    ms = timed()
+    ok = sum(int(b[2]["ok"].sum().item()) for b in bufs)
+    same = all(bool(torch.equal(a, b[2]["ok"])) for a, b in zip(ok_global, bufs))
     res["fft_demod_batch"] = {"workload": "256 distinct pictures, 64 each at n=384/768/1152/1536 (LIZARD-80/320/720/1024), 64 ring, painted by the sender, "
                                           "AWGN 3 DN, rows a-e, one call per size",
                               "frames_per_s": round(256 / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
                               "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
-                              "gpu_launches_per_step": sum(rx.launches for rx in rxs)}
+                              "gpu_launches_per_step": sum(rx.launches for rx in rxs),
+                              "ldpc_per_n_and_rate": {"variants_per_tier": choices, "frames_per_s_device_choice": round(256 / (ms_global / 1e3), 1),
+                                                      "identical_verdicts": same}}
     peak, peak_src = peaks()
     res["fft_demod_batch"]["error_per_n"] = fft_error_table()
     res["fft_demod_batch"]["hbm"] = {"algorithmic_bytes_per_step": step_bytes, "GBps": round(step_bytes / (ms / 1e3) / 1e9, 1),

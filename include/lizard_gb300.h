@@ -163,6 +163,19 @@ int lizg_rx_fault(lizg_rx *r);
 // The picture read of the handle's later finishes from captured frames (LIZG_READ_DECODE or LIZG_READ_EXACT); returns
 // the previous one, or LIZG_E_ARG. Host code.
 int lizg_rx_set_read(lizg_rx *r, int read);
+// The handle's LDPC kernel variant for each of its tiers (tier t's code: lizg_rx_info), chosen by timing on the
+// caller's own frames: one lizg_rx_finish_luma_dev of the batch (d_luma, d_reg as that call takes them) for the
+// soft values, then every variant of each tier's code timed on them in the receiver's own form (a codeword per block,
+// the batch's frames x the tier's blocks); the fastest is kept by the handle for its later finishes (its format and
+// batch size: the choice per picture size and code rate). All variants decode bit for bit alike, so the blocks never
+// change; the global choice of lizg_ldpc_autotune, tuned on large batches of one code, is what the handle uses
+// without it. choice (may be NULL): 4 entries, each tier's variant index (lizg_ldpc_variant's numbering), -1 past the
+// format's tiers. Synchronises the stream. No counterpart in the reference (one decoder form a build).
+int lizg_rx_autotune(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
+                     int32_t *choice, void *stream);
+// Tier t's LDPC kernel variant as the handle's finishes launch it: its own after lizg_rx_autotune, else the device's
+// (lizg_ldpc_variant). Host code.
+int lizg_rx_variant(const lizg_rx *r, int tier);
 
 // Per-frame outputs, device pointers, frames x blocks entries each unless noted. Required: blocks (476 bytes a block,
 // the decoded bytes whether or not verified), ok (1 where the CRC-32C verified a decoded block), its (LDPC

@@ -217,6 +217,8 @@ def _rx_sigs(L):
     L.lizg_rx_launches.argtypes = [P]
     L.lizg_rx_set_read.argtypes = [P, I]
     L.lizg_rx_fault.argtypes = [P]
+    L.lizg_rx_autotune.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P]
+    L.lizg_rx_variant.argtypes = [P, I]
     L.lizg_layout_nodes.argtypes = [I, P, P, P]
     L.lizg_rx_finish_luma_host.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
@@ -353,6 +355,20 @@ class Receiver:
     def fault(self):
         """1 where a pass's bounded wait gave up (never expected), else 0."""
         return _check(lib().lizg_rx_fault(self._h), "lizg_rx_fault")
+
+    def autotune_dev(self, d_luma, w, h, pitch, frame_stride, d_reg, frames, stream=None):
+        """lizg_rx_autotune on device buffers (pointers): each tier's LDPC kernel variant timed on these frames and
+        kept by the handle. Returns the 4 choices (-1 past the format's tiers)."""
+        import torch
+        choice = np.full(4, -1, np.int32)
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _check(lib().lizg_rx_autotune(self._h, ctypes.c_void_p(d_luma), w, h, pitch, frame_stride, ctypes.c_void_p(d_reg), frames,
+                                      _ptr(choice), ctypes.c_void_p(st)), "lizg_rx_autotune")
+        return [int(c) for c in choice]
+
+    def variant(self, tier):
+        """Tier's LDPC kernel variant as the handle's finishes launch it (its own after autotune, else the device's)."""
+        return _check(lib().lizg_rx_variant(self._h, tier), "lizg_rx_variant")
 
     def _outputs(self, frames, torch, keep):
         return rx_outputs(self.fmt, frames, keep)

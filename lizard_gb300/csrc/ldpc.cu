@@ -782,6 +782,15 @@ cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st)
   return launch_variant(code, choice_of(code), a, sms, st);
 }
 
+int ldpc_variant_count(int code) { return code >= 0 && code <= 3 ? variant_count(code) : 0; }
+int ldpc_choice(int code) { return code >= 0 && code <= 3 ? choice_of(code) : 0; }
+
+cudaError_t ldpc_launch_variant(int code, int v, const LdpcLaunch &a, int sms, cudaStream_t st) {
+  if (a.count <= 0) return cudaSuccess;
+  if (code < 0 || code > 3 || v < 0 || v >= variant_count(code)) return cudaErrorInvalidValue;
+  return launch_variant(code, v, a, sms, st);
+}
+
 }  // namespace lizg
 
 extern "C" {

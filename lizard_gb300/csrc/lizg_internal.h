@@ -169,6 +169,10 @@ cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, in
                                const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
+// The decoder's kernel variants of a code (all bit for bit alike), and a launch of variant v of them.
+int ldpc_variant_count(int code);
+int ldpc_choice(int code);   // the device's choice for the code (lizg_ldpc_autotune, lizg_ldpc_set_variant)
+cudaError_t ldpc_launch_variant(int code, int v, const LdpcLaunch &a, int sms, cudaStream_t st);
 // Row (b) alone from captured frames: the handle's read through each frame's registration, the anchors' erase, the
 // detrend and the 2D transform, the used coefficients into d_coef (frames x subch x 320 complex, pos order); no soft
 // stage. For the registration's refinements, which measure their mismatch where the receiver measures it.

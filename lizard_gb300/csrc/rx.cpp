@@ -43,6 +43,7 @@ struct lizg_rx {
   cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
   int launches = 0;
+  int variant[4] = {-1, -1, -1, -1};   // each tier's LDPC kernel variant (lizg_rx_autotune), -1: the global choice
   std::vector<void *> owned;
   // the captured pipeline of lizg_rx_finish_luma_graph and the call it was captured for
   cudaStream_t cap = nullptr;
@@ -318,7 +319,8 @@ static int finish_spec(lizg_rx *r, const float2 *spec, int64_t stride, int frame
     a.rx.llrf = llrf; a.rx.decl = r->decl; a.rx.blocks = out->blocks; a.rx.llr_stride = 2 * need;
     a.fd = fd; a.tier = t;
     if ((e = cudaStreamWaitEvent(r->side[t], r->fork, 0)) != cudaSuccess ||
-        (e = lizg::ldpc_launch(f.tier[t].code, a, sms, r->side[t])) != cudaSuccess ||
+        (e = (r->variant[t] >= 0 ? lizg::ldpc_launch_variant(f.tier[t].code, r->variant[t], a, sms, r->side[t])
+                                 : lizg::ldpc_launch(f.tier[t].code, a, sms, r->side[t]))) != cudaSuccess ||
         (e = cudaEventRecord(r->join[t], r->side[t])) != cudaSuccess || (e = cudaStreamWaitEvent(st, r->join[t], 0)) != cudaSuccess)
       return lizg::record_error(LIZG_E_CUDA, (std::string("rx LDPC: ") + cudaGetErrorString(e)).c_str());
     r->launches++;
@@ -430,7 +432,9 @@ int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, i
   const std::vector<uintptr_t> key = {(uintptr_t)d_luma, (uintptr_t)w, (uintptr_t)h, (uintptr_t)pitch, (uintptr_t)frame_stride,
                                       (uintptr_t)d_reg, (uintptr_t)frames, (uintptr_t)out->blocks, (uintptr_t)out->ok, (uintptr_t)out->its,
                                       (uintptr_t)out->est, (uintptr_t)out->pilot, (uintptr_t)out->align, (uintptr_t)out->llrf,
-                                      (uintptr_t)out->sub_est, (uintptr_t)out->sub_rms, (uintptr_t)d_grid, (uintptr_t)d_coef, (uintptr_t)r->sd.read};
+                                      (uintptr_t)out->sub_est, (uintptr_t)out->sub_rms, (uintptr_t)d_grid, (uintptr_t)d_coef, (uintptr_t)r->sd.read,
+                                      (uintptr_t)(r->variant[0] + 1), (uintptr_t)(r->variant[1] + 1), (uintptr_t)(r->variant[2] + 1),
+                                      (uintptr_t)(r->variant[3] + 1)};
   cudaError_t e;
   if (!r->graph || key != r->graph_key) {
     if (r->graph) { cudaGraphExecDestroy(r->graph); r->graph = nullptr; }
@@ -498,6 +502,72 @@ int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int 
   int verified = 0;
   for (size_t i = 0; i < nb; i++) verified += ok[i] != 0;
   return verified;
+}
+
+int lizg_rx_variant(const lizg_rx *r, int tier) {
+  if (!r || tier < 0 || tier >= r->f.tiers) return lizg::record_error(LIZG_E_ARG, "lizg_rx_variant: no handle or no such tier");
+  return r->variant[tier] >= 0 ? r->variant[tier] : lizg::ldpc_choice(r->f.tier[tier].code);
+}
+
+int lizg_rx_autotune(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
+                     int32_t *choice, void *stream) {
+  if (!r || !d_luma || !d_reg) return lizg::record_error(LIZG_E_ARG, "lizg_rx_autotune: NULL argument");
+  if (frames < 1 || frames > r->max_frames) return lizg::record_error(LIZG_E_ARG, "lizg_rx_autotune: frames out of 1..max_frames");
+  int sms = 0;
+  if (int rc = lizg::device_ready(&sms)) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const lizg::Format &f = r->f;
+  const size_t nb = (size_t)f.blocks * frames;
+  uint8_t *blocks = nullptr, *ok = nullptr;
+  int32_t *its = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&blocks, nb * LIZG_BLOCK_BYTES);
+  if (e == cudaSuccess) e = cudaMalloc(&ok, nb);
+  if (e == cudaSuccess) e = cudaMalloc(&its, nb * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  int rc = 0;
+  int best[4] = {-1, -1, -1, -1};
+  if (e == cudaSuccess) {
+    // the soft values of the batch, in the handle's own buffers
+    for (int t = 0; t < 4; t++) r->variant[t] = -1;
+    const lizg_rx_out out{blocks, ok, its, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    rc = lizg_rx_finish_luma_dev(r, d_luma, w, h, pitch, frame_stride, d_reg, frames, &out, nullptr, nullptr, stream);
+    const lizg::FmtDev fd = fmt_dev(r, frames);
+    for (int t = 0; t < f.tiers && !rc && e == cudaSuccess; t++) {
+      lizg::LdpcLaunch a{};
+      a.its = its; a.ok = ok;
+      a.count = frames * f.tier[t].blocks; a.counter = r->counters + t;
+      a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // as finish_spec launches it
+      a.rx.llrf = r->llrf; a.rx.decl = r->decl; a.rx.blocks = blocks; a.rx.llr_stride = 2 * (int64_t)f.subch * lizg::kSub;
+      a.fd = fd; a.tier = t;
+      float best_ms = 0;
+      for (int v = 0; v < lizg::ldpc_variant_count(f.tier[t].code) && e == cudaSuccess; v++) {
+        float ms_min = 0;
+        for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {   // the first run warms up
+          if ((e = cudaMemsetAsync(r->counters + t, 0, sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(e0, st)) != cudaSuccess ||
+              (e = lizg::ldpc_launch_variant(f.tier[t].code, v, a, sms, st)) != cudaSuccess || (e = cudaEventRecord(e1, st)) != cudaSuccess ||
+              (e = cudaEventSynchronize(e1)) != cudaSuccess)
+            break;
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (rep == 1 || (rep > 1 && ms < ms_min)) ms_min = ms;
+        }
+        if (e == cudaSuccess && (best[t] < 0 || ms_min < best_ms)) { best[t] = v; best_ms = ms_min; }
+      }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  cudaFree(blocks); cudaFree(ok); cudaFree(its);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("lizg_rx_autotune: ") + cudaGetErrorString(e)).c_str());
+  for (int t = 0; t < 4; t++) {
+    r->variant[t] = t < f.tiers ? best[t] : -1;
+    if (choice) choice[t] = r->variant[t];
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -83,3 +83,28 @@ def test_gpu_luma_path_matches_oracle(n, subch, W, H, warped, read):
     for k in ("coef", "llrf", "its", "ok", "blocks", "align"):
         assert np.array_equal(fused[k], out[k]), k
     assert rx.launches == 5 + 3 + f.tiers
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,subch,W,H,warped", [CASES[0], CASES[3]])
+def test_gpu_autotune_keeps_every_block(n, subch, W, H, warped):
+    """The receiver's per-tier LDPC choice (lizg_rx_autotune) times every kernel variant of each tier's code on the
+    batch; the variants decode bit for bit alike, so the blocks, verdicts and iterations stay the same, directly and
+    from a captured graph."""
+    import torch
+    f, luma, reg, blocks = frame(n, subch, W, H, warped, mesh=0.3)
+    frames = 3
+    rx = lz.Receiver(n, subch, 128, max_frames=frames)
+    before = rx.finish_luma(np.stack([luma] * frames), np.stack([reg] * frames), grid=False)
+    d_l = torch.from_numpy(np.stack([luma] * frames)).cuda()
+    d_r = torch.from_numpy(np.stack([reg] * frames)).cuda()
+    choice = rx.autotune_dev(d_l.data_ptr(), W, H, W, W * H, d_r.data_ptr(), frames)
+    for t in range(4):
+        if t < f.tiers:
+            assert 0 <= choice[t] < lz.lib().lizg_ldpc_variants(f.tier[t][0]) and rx.variant(t) == choice[t]
+        else:
+            assert choice[t] == -1
+    after = rx.finish_luma(np.stack([luma] * frames), np.stack([reg] * frames), grid=False)
+    for k in ("blocks", "ok", "its", "llrf", "coef"):
+        assert np.array_equal(after[k], before[k]), k
+    assert after["ok"].all() and np.array_equal(after["blocks"][0], blocks)
