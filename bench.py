@@ -932,7 +932,9 @@ def bench_refinement(args, stream):
     linear light (gamma 2.2), AWGN 3 DN, a seed a frame (lizard_gb300_testing.render, on the GPU). Registrations:
     corners = the homography through the layout's four corners as the camera sees them (a finder's), no lens; plain
     (the configuration's: homography + anchors) = + three rounds of the anchor search and the lens model the anchors
-    give, written into the node mesh (lizg_refine_dev); refined = the plain registration's decode, then the frames it
+    give, written into the node mesh (lizg_refine_dev); anchor_register = the reference's whole registration from the
+    anchors (lizg_anchor_register_dev: up to six rounds, H refitted from the anchors each round, the robust model, the
+    corners judged and searched again, H made again, the model about H); refined = the plain registration's decode, then the frames it
     left blocks unverified in refined by three Gauss-Newton steps of the adjoint refinement (H and the 7 x 7 anchor
     field against the pilots, the timing track and the anchors' centres, lizg_field_refine_dev) and decoded again;
     bound = the camera's true map at every node (no registration can do better). Three sets:
@@ -982,7 +984,8 @@ def bench_refinement(args, stream):
         for key in ("peak", "dx", "dy", "u", "v"):
             ao[key] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
         a_out = lz.AnchorOut(*[ao[key].data_ptr() for key in ("ok", "peak", "dx", "dy", "u", "v")])
-        outs = {t: rx._outputs(frames, torch, keep=False) for t in ("corners", "plain", "first", "refined", "bound")}
+        outs = {t: rx._outputs(frames, torch, keep=False) for t in ("corners", "plain", "anchor_register", "first", "refined", "bound")}
+        d_ar = torch.empty_like(d_plain)
         d_union = torch.zeros((frames, fmt.blocks), dtype=torch.uint8, device="cuda")
 
         def finish(d_reg, tag):
@@ -992,6 +995,13 @@ def bench_refinement(args, stream):
         def anchors(d_reg):
             d_reg.copy_(d_plain)
             ref.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_reg.data_ptr(), frames, 3, d_found.data_ptr(), d_lens.data_ptr(), sp)
+
+        def registered():
+            # the reference's own registration from the anchors (anchor_register: H refitted each round, the robust
+            # model, the corners judged and searched again, H made again), then the decode
+            d_ar.copy_(d_plain)
+            ref.register_dev(d_l.data_ptr(), W, Hh, W * Hh, d_ar.data_ptr(), frames, stream=sp)
+            finish(d_ar, "anchor_register")
 
         def refined():
             # the plain registration and decode; then the frames it left blocks unverified in, refined by the adjoint
@@ -1010,6 +1020,7 @@ def bench_refinement(args, stream):
 
         paths = {"corners": lambda: finish(d_plain, "corners"),
                  "plain": lambda: (anchors(d_a), finish(d_a, "plain")),
+                 "anchor_register": registered,
                  "refined": refined,
                  "bound": lambda: finish(d_true, "bound")}
         out = {"frames": frames}
@@ -1036,6 +1047,7 @@ def bench_refinement(args, stream):
         out["plain_points_over_corners"] = round(100 * (out["plain"]["block_pass_rate"] - out["corners"]["block_pass_rate"]), 2)
         out["refined_points_over_plain"] = round(100 * (out["refined"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
         out["bound_points_over_plain"] = round(100 * (out["bound"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
+        out["anchor_register_points_over_plain"] = round(100 * (out["anchor_register"]["block_pass_rate"] - out["plain"]["block_pass_rate"]), 2)
         res[name] = out
         del d_l
     ref.close()

@@ -427,9 +427,9 @@ int lizg_gn_pictures_dev(lizg_gn *g, const uint8_t *d_luma, int w, int h, int64_
 // anchors not yet found (lizg_anchor_find_dev's search, through H and, after the first round, the lens model so
 // far) and fits the lens model the found anchors give about H: the reference's anchor_model
 // (liblizard/src/acquire.c:2038-2055: the four corner nodes with no displacement and the anchors found, the model of
-// 8 + K terms, K = 0..3 chosen by AICc, lensm_fit's first round 1630-1669), in double. The reference's registration
-// goes on from there (anchor_homo's homography re-fit, the corners' outliers, node refinement: 2128-2200); this
-// refinement keeps H and writes the model's displacement at every node into the mesh (zeros where no model fits).
+// 8 + K terms, K = 0..3 chosen by AICc, lensm_fit's first round 1630-1669), in double. This refinement keeps H and
+// writes the model's displacement at every node into the mesh (zeros where no model fits); lizg_anchor_register_dev
+// below runs the reference's whole registration from the anchors (H refitted, the corners judged).
 // d_reg: frames x (9 + 2 nx ny) floats, H kept, the mesh overwritten. d_found (frames, may be NULL): anchors found;
 // d_lens (frames x 15, may be NULL): the model (K, ax, ay, R, 11 coefficients). The handle keeps the anchors'
 // device buffers for up to max_frames frames of one ring span (128, 256 or 512).
@@ -438,6 +438,23 @@ lizg_refiner *lizg_refiner_new(int span, int max_frames);
 void lizg_refiner_free(lizg_refiner *r);
 int lizg_refine_dev(lizg_refiner *r, const uint8_t *d_luma, int w, int h, int64_t frame_stride, float *d_reg, int frames, int rounds,
                     int32_t *d_found, double *d_lens, void *stream);
+// The reference's own registration from the anchors (liblizard/src/acquire.c:2128-2197 anchor_register, its portable
+// build) for a batch of frames whose H a finder's four corners gave: up to six rounds of the anchor search through the
+// homography the anchors found so far say (anchor_homo, :2062-2094, refitted each round) and the lens model they say
+// about it, held to the robust rule (anchor_model_free, :2101-2118: a reading further from the model than half a
+// module or three robust spreads is no longer found), until a round finds nothing new; then each corner judged by
+// that map: one further than 3 modules from where the anchors put it searched again (the border node search on the
+// corner, d_rim, through the corners' H and the joint model of the anchors and the kept corners), kept where it
+// correlates 0.35 or more, else the model's place, and H made again from the four (homography, :611-654); then the
+// anchors' model about H (anchor_model). It holds where 12 or more anchors and a model remain. d_reg: frames x
+// (9 + 2 nx ny) floats: in, the corners' H; out, the registration's H and the model's displacement at every node
+// (zeros where it did not hold). d_rim: the border search's image (the frame's border blur as the reference's
+// acquisition makes it, or NULL: d_luma itself), frames as d_luma. d_quad (frames x 8, may be NULL: the corner nodes
+// through H): the corners in the image, out as moved; pixels a module are their sides over the lattice's. d_held
+// (frames, may be NULL): 1 where it held. d_lens (frames x 15, may be NULL): the model about H. anchors (may be NULL):
+// each frame's 49 anchors (ok, peak, dx and dy about H, u, v).
+int lizg_anchor_register_dev(lizg_refiner *r, const uint8_t *d_luma, const uint8_t *d_rim, int w, int h, int64_t frame_stride, float *d_reg,
+                             float *d_quad, int frames, int32_t *d_held, double *d_lens, const lizg_anchor_out *anchors, void *stream);
 
 // ---------------------------------------------------------------- registration refined by its adjoint (H and the anchor field)
 //

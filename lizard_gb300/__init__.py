@@ -240,6 +240,7 @@ def _rx_sigs(L):
     L.lizg_refiner_new.restype = P
     L.lizg_refiner_free.argtypes = [P]
     L.lizg_refine_dev.argtypes = [P, P, I, I, ctypes.c_int64, P, I, I, P, P, P]
+    L.lizg_anchor_register_dev.argtypes = [P, P, P, I, I, ctypes.c_int64, P, P, I, P, P, P, P]
     L.lizg_encoder_new.argtypes = [I, I, I, I]
     L.lizg_encoder_new.restype = P
     L.lizg_encoder_free.argtypes = [P]
@@ -868,6 +869,43 @@ class Refiner:
                         torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         return d_r.cpu().numpy(), d_f.cpu().numpy(), d_lens.cpu().numpy()
+
+    def register_dev(self, d_luma, w, h, frame_stride, d_reg, frames, d_rim=None, d_quad=None, d_held=None, d_lens=None, anchors=None, stream=0):
+        """lizg_anchor_register_dev on device pointers; anchors: an AnchorOut or None."""
+        p = lambda x: None if x is None else ctypes.c_void_p(x)
+        _check(lib().lizg_anchor_register_dev(self._h, ctypes.c_void_p(d_luma), p(d_rim), w, h, frame_stride, ctypes.c_void_p(d_reg), p(d_quad),
+                                              frames, p(d_held), p(d_lens), None if anchors is None else ctypes.byref(anchors),
+                                              ctypes.c_void_p(stream)), "lizg_anchor_register_dev")
+
+    def register(self, luma, reg, quad=None, rim=None):
+        """The reference's registration from the anchors for frames x h x w uint8 and their registrations (H the corners';
+        frames x (9 + 2 nx ny)): a dict of reg, quad, held, lens and the anchors' ok, peak, dx, dy, u, v."""
+        import torch
+        lu = np.ascontiguousarray(luma, np.uint8)
+        if lu.ndim == 2:
+            lu = lu[None]
+        frames, h, w = lu.shape
+        d_l = torch.from_numpy(lu).cuda()
+        d_rim = None if rim is None else torch.from_numpy(np.ascontiguousarray(rim, np.uint8).reshape(lu.shape)).cuda()
+        d_r = torch.from_numpy(np.ascontiguousarray(np.asarray(reg, np.float32).reshape(frames, -1))).cuda()
+        d_q = torch.from_numpy(np.ascontiguousarray(np.asarray(quad, np.float32).reshape(frames, 8))).cuda() if quad is not None else \
+            torch.zeros((frames, 8), dtype=torch.float32, device="cuda")
+        d_held = torch.zeros(frames, dtype=torch.int32, device="cuda")
+        d_lens = torch.zeros((frames, 15), dtype=torch.float64, device="cuda")
+        ao = {"ok": torch.zeros((frames, 49), dtype=torch.uint8, device="cuda")}
+        for k in ("peak", "dx", "dy", "u", "v"):
+            ao[k] = torch.zeros((frames, 49), dtype=torch.float32, device="cuda")
+        out = AnchorOut(*[ao[k].data_ptr() for k in ("ok", "peak", "dx", "dy", "u", "v")])
+        # with no quad given the corners come from H; the buffer then only receives them
+        self.register_dev(d_l.data_ptr(), w, h, w * h, d_r.data_ptr(), frames, None if d_rim is None else d_rim.data_ptr(),
+                          d_q.data_ptr() if quad is not None else None, d_held.data_ptr(), d_lens.data_ptr(), out,
+                          torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        res = {"reg": d_r.cpu().numpy(), "held": d_held.cpu().numpy(), "lens": d_lens.cpu().numpy()}
+        res["quad"] = d_q.cpu().numpy() if quad is not None else None
+        for k, v in ao.items():
+            res[k] = v.cpu().numpy()
+        return res
 
     def close(self):
         if self._h:

@@ -49,6 +49,8 @@ struct AnchArgs {
   const uint8_t *luma, *skip;
   const float *H;
   const double *lens;
+  const int *lens_on;       // frames: 0 where frame f searches through H alone (NULL: every frame through lens)
+  const uint8_t *active;    // frames: 0 where frame f is not searched at all (NULL: every frame)
   lizg_anchor_out out;
 };
 
@@ -61,6 +63,7 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
   const int f = blockIdx.x / (kAnchK * kAnchK), k = blockIdx.x % (kAnchK * kAnchK), i = k % kAnchK, j = k / kAnchK;
   const int64_t o = (int64_t)f * kAnchK * kAnchK + k;
   if (a.skip && a.skip[o]) return;   // found before: left as it is
+  if (a.active && !a.active[f]) return;
   const AnchGeom g = a.g;
   const int r = g.r, W = g.W, O = g.O, W1 = W + 1, tid = threadIdx.x;
   const float hs = g.hs, ah = (float)g.a * 0.5f;
@@ -70,7 +73,8 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
   __shared__ double s_lens[kLensStride];
   __shared__ int s_r25[2], s_r6[2], s_bi[256];
   if (tid < 9) s_h[tid] = a.H[(int64_t)f * a.hstride + tid];
-  if (a.lens && tid < kLensStride) s_lens[tid] = a.lens[(int64_t)f * kLensStride + tid];
+  const bool use_lens = a.lens && (!a.lens_on || a.lens_on[f]);
+  if (use_lens && tid < kLensStride) s_lens[tid] = a.lens[(int64_t)f * kLensStride + tid];
   if (tid == 0) {
     // the pattern's mean and norm in the reference's order, and its squares' ranges along an axis
     float tm = 0, tn = 0;
@@ -97,7 +101,7 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
     s_r25[0] = i25; s_r25[1] = j25; s_r6[0] = i6; s_r6[1] = j6;
   }
   __syncthreads();
-  const double *lens = a.lens ? s_lens : nullptr;
+  const double *lens = use_lens ? s_lens : nullptr;
   const float x0 = (float)a.m0[i], y0 = (float)a.m0[j], X = x0 + ah, Y = y0 + ah;
   const uint8_t *px = a.luma + (int64_t)f * a.fstride;
   // the window
@@ -172,8 +176,10 @@ __global__ void __launch_bounds__(256) anchor_find_kernel(AnchArgs a) {
 
 // Queues the search for a batch of frames (arguments as lizg_anchor_find_dev's, already checked).
 cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
-                               const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st) {
+                               const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st,
+                               const int *d_lens_on, const uint8_t *d_active) {
   AnchArgs a{};
+  a.lens_on = d_lens_on; a.active = d_active;
   a.span = span; a.w = w; a.h = h; a.frames = frames; a.hstride = h_stride; a.fstride = frame_stride;
   a.g = anch_geom(span);
   for (int i = 0; i < kAnchK; i++) a.m0[i] = (int)floor(kMarginM + (double)span * (i + 0.5) / kAnchK - a.g.a / 2.0 + 0.5);

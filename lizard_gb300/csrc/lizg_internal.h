@@ -165,8 +165,16 @@ cudaError_t sample_tables_launch(SampleDev sd, float4 *colt, float4 *rowt, cudaS
 // The node lattice of a layout of side modules (liblizard/src/layout.c:110-117): returns nx (= ny).
 int layout_nodes(int side, float *pos);
 // The anchor search for a batch of frames (arguments as lizg_anchor_find_dev's, already checked).
+// The border node search on the four corners alone (refine_node, the anchors' registration's second look at the
+// corners it disagrees with): frame f's corner c searched where d_redo[4 f + c], through H and (where d_lens_on) the
+// lens model; d_nodes frames x nn^2 x (dx, dy, score, done) as lizg_border_nodes_dev writes them.
+cudaError_t border_corners_launch(int span, const uint8_t *d_rim, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
+                                  const double *d_lens, const int *d_lens_on, const uint8_t *d_redo, int frames, float *d_nodes, cudaStream_t st);
+// d_lens_on (frames, may be NULL): 0 where a frame searches through H alone; d_active (frames, may be NULL): 0 where a
+// frame is not searched.
 cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
-                               const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st);
+                               const double *d_lens, const uint8_t *d_skip, int frames, const lizg_anchor_out &out, cudaStream_t st,
+                               const int *d_lens_on = nullptr, const uint8_t *d_active = nullptr);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
 // The decoder's kernel variants of a code (all bit for bit alike), and a launch of variant v of them.

@@ -33,6 +33,8 @@ struct MeshArgs {
   const uint8_t *luma, *kind;
   const float *H;
   const double *lens;   // frames x kLensStride, or NULL
+  const int *lens_on;   // frames: 0 where frame f has no model (NULL: every frame has lens's)
+  const uint8_t *redo;  // frames x 4: the corners searched again (the anchors' registration); NULL: the border pass
   const int16_t *order;
   float *nodes;         // frames x nn^2 x (dx, dy, score, done)
 };
@@ -73,17 +75,19 @@ __global__ void __launch_bounds__(kMeshThreads) border_nodes_kernel(MeshArgs a) 
   float *nodes = reinterpret_cast<float *>(smraw + ((sizeof(MeshShared) + 15) & ~(size_t)15));   // nn^2 x 4
   const int f = blockIdx.x, tid = threadIdx.x, nn = a.nn;
   const uint8_t *px = a.luma + f * a.fstride;
-  const bool have_lens = a.lens != nullptr;
+  const bool have_lens = a.lens != nullptr && (!a.lens_on || a.lens_on[f]);
   if (tid < 9) m.h[tid] = a.H[(int64_t)f * a.hstride + tid];
   if (have_lens && tid < kLensStride) m.lens[tid] = a.lens[(int64_t)f * kLensStride + tid];
   for (int k = tid; k < nn * nn; k += blockDim.x) {
     const int i = k % nn, j = k / nn, corner = (i == 0 || i == nn - 1) && (j == 0 || j == nn - 1);
-    nodes[4 * k] = 0; nodes[4 * k + 1] = 0; nodes[4 * k + 2] = 0; nodes[4 * k + 3] = corner ? 1.0f : 0.0f;
+    const int c = j == 0 ? (i == 0 ? 0 : 1) : (i == 0 ? 3 : 2);   // corners in the layout's order
+    const bool again = corner && a.redo && a.redo[(int64_t)f * 4 + c];
+    nodes[4 * k] = 0; nodes[4 * k + 1] = 0; nodes[4 * k + 2] = 0; nodes[4 * k + 3] = corner && !again ? 1.0f : 0.0f;
   }
   __syncthreads();
   const float *H = m.h;
   for (int ko = 0; ko < a.no; ko++) {
-    const int idx = a.order[ko];
+    const int idx = a.redo ? ((ko >= 2 ? nn - 1 : 0) * nn + ((ko == 1 || ko == 2) ? nn - 1 : 0)) : a.order[ko];
     if (nodes[4 * idx + 3] != 0.0f) continue;   // uniform: read after the last barrier
     const int i = idx % nn, j = idx / nn, cx0 = (int)a.pos[i], cy0 = (int)a.pos[j];
     if (tid == 0) {
@@ -296,6 +300,22 @@ static cudaError_t mesh_ready(int span, MeshSpan **out) {
   }
   *out = &ms;
   return cudaSuccess;
+}
+
+cudaError_t border_corners_launch(int span, const uint8_t *d_rim, int w, int h, int64_t frame_stride, const float *d_H, int h_stride,
+                                  const double *d_lens, const int *d_lens_on, const uint8_t *d_redo, int frames, float *d_nodes, cudaStream_t st) {
+  MeshSpan *ms = nullptr;
+  cudaError_t e = mesh_ready(span, &ms);
+  if (e != cudaSuccess) return e;
+  MeshArgs a{};
+  a.span = span; a.side = span + 2 * kMargin; a.nn = ms->nn; a.no = 4; a.w = w; a.h = h; a.hstride = h_stride;
+  a.fstride = frame_stride;
+  for (int k = 0; k < kMaxNodes; k++) a.pos[k] = k < ms->nn ? ms->pos[k] : 0.0f;
+  a.luma = d_rim; a.kind = ms->kind; a.H = d_H; a.lens = d_lens; a.lens_on = d_lens_on; a.redo = d_redo; a.order = ms->order; a.nodes = d_nodes;
+  const size_t smem = ((sizeof(MeshShared) + 15) & ~(size_t)15) + (size_t)ms->nn * ms->nn * 4 * sizeof(float);
+  if ((e = cudaFuncSetAttribute(border_nodes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) return e;
+  border_nodes_kernel<<<frames, kMeshThreads, smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 }  // namespace lizg

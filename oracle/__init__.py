@@ -55,6 +55,7 @@ def port():
         L.orc_ldpc_batch.argtypes = [P, P, P, I, I, I, F, P, P, P, I]
         L.orc_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
         L.orc_lens_fit.argtypes = [I, I, I, P, P, P, P, P]
+        L.orc_anchor_register.argtypes = [I, P, P, I, I, P, P, F, P, P, P, P, P, P, P]
         U = ctypes.c_uint32
         L.orc_ingest_pixels.argtypes = [P, I, I, I, I, P]
         L.orc_gamma_lut.argtypes = [P]
@@ -92,6 +93,7 @@ def ref_scalar():
         P, I = ctypes.c_void_p, ctypes.c_int
         L.refs_anchor_find.argtypes = [I, P, I, I, P, P, P, P, P, P, P, P, P]
         L.refs_anchor_model.argtypes = [I, I, I, P, P, P, P, P]
+        L.refs_anchor_register.argtypes = [I, P, P, I, I, P, P, ctypes.c_float, P, P, P, P, P, P, P]
         _ref_scalar = L
     return _ref_scalar
 
@@ -144,6 +146,21 @@ def anchor_find(lib, fn, span, luma, H, lens=None, ok_in=None):
         out[k] = np.zeros(49, np.float32)
     out["found"] = getattr(lib, fn)(span, _p(luma), w, h, _p(Hf), None if ln is None else _p(ln), None if oi is None else _p(oi),
                                     _p(out["ok"]), _p(out["peak"]), _p(out["dx"]), _p(out["dy"]), _p(out["u"]), _p(out["v"]))
+    return out
+
+
+def anchor_register(lib, fn, span, luma, H, quad, mpx, rim=None):
+    """The code registered from the anchors through lib.fn (the oracle's orc_anchor_register or the reference's
+    refs_anchor_register): a dict with held, H (9), quad (8), lens (15) and the 49-entry arrays ok, peak, dx, dy, u, v."""
+    luma = np.ascontiguousarray(luma, np.uint8)
+    h, w = luma.shape
+    rm = None if rim is None else np.ascontiguousarray(rim, np.uint8)
+    out = {"H": np.ascontiguousarray(H, np.float32).ravel()[:9].copy(), "quad": np.ascontiguousarray(quad, np.float32).ravel()[:8].copy(),
+           "lens": np.zeros(15, np.float64), "ok": np.zeros(49, np.uint8)}
+    for k in ("peak", "dx", "dy", "u", "v"):
+        out[k] = np.zeros(49, np.float32)
+    out["held"] = getattr(lib, fn)(span, _p(luma), None if rm is None else _p(rm), w, h, _p(out["H"]), _p(out["quad"]), float(mpx), _p(out["ok"]),
+                                   _p(out["peak"]), _p(out["dx"]), _p(out["dy"]), _p(out["u"]), _p(out["v"]), _p(out["lens"]))
     return out
 
 

@@ -78,6 +78,12 @@ int orc_lens_fit(int span, int iw, int ih, const float *H, const uint8_t *ok, co
 // The registration's border nodes (acquire.c:1242-1374 refine_node, 5044-5058 the pass): nn * nn x (dx, dy, score,
 // done) out. Returns nn.
 int orc_border_nodes(int span, const uint8_t *px, int w, int h, const float *H, const double *lens, float *nodes_out);
+// The code registered from the anchors (liblizard/src/acquire.c:2128-2197 anchor_register): px the frame, rim the border
+// search's image (the frame, or its border blur), H the corners' homography (in) and the registration's (out), quad
+// the corners in the image (in, out as moved), mpx pixels a module. Out per anchor: ok, peak, dx, dy, u, v; lens the
+// model about H. Returns 1 where it holds, 0 where not, -1 on no memory.
+int orc_anchor_register(int span, const uint8_t *px, const uint8_t *rim, int w, int h, float *H, float *quad, float mpx, uint8_t *ok,
+                        float *peak, float *dx, float *dy, float *u, float *v, double *lens);
 
 // Camera-format ingest (liblizard/api/codec.cpp:128-140; liblizard/core/ingest/develop.cpp): a frame's pixels in one of
 // liz_pixfmt's formats to tight luma rows, and the develop of P010 / RAW16 / RAW10 / RAW12 (ImageFormat values).

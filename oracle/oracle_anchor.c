@@ -468,3 +468,249 @@ int orc_border_nodes(int span, const uint8_t *px, int w, int h, const float *H, 
   free(kind); free(nodes);
   return nn;
 }
+
+// ---------------------------------------------------------------- the anchors' registration (acquire.c:2039-2197)
+
+// lensm_fit (liblizard/src/acquire.c:1630-1694) about the axis (ax, ay) and scale R: the normal equations over the
+// points not dropped, summed once in the points' order; every model of 0..3 radial terms solved, the least AICc
+// kept. With isb (the points the robust rule judges), up to three more rounds: each judged point's distance from the
+// model, tau = max(tau_floor, 3 x 1.4826 x their median), a point further than tau dropped, the model fitted again
+// until no verdict changes. lens out as lens_at takes it. Returns 1 where a model fitted.
+static int cmp_dbl(const void *a, const void *b) { const double x = *(const double *)a, y = *(const double *)b; return (x > y) - (x < y); }
+static int lensm_fit_o(int np, const double *qx, const double *qy, const double *dx, const double *dy, const unsigned char *isb,
+                       unsigned char *drop, double tau_floor, double ax, double ay, double R, double *lens) {
+  int ok = 0;
+  lens[1] = ax; lens[2] = ay; lens[3] = R;
+  for (int round = 0; round < 4; round++) {
+    double A3[LENSP][LENSP + 1], rx[LENSP], ry[LENSP], best = INFINITY, tb[LENSP] = {0};
+    memset(A3, 0, sizeof A3);
+    int n = 0, K = -1;
+    for (int i = 0; i < np; i++) {
+      if (drop[i]) continue;
+      n++;
+      lens_rows(qx[i], qy[i], 3, rx, ry);
+      for (int p = 0; p < LENSP; p++) {
+        for (int q = p; q < LENSP; q++) A3[p][q] += rx[p] * rx[q] + ry[p] * ry[q];
+        A3[p][LENSP] += rx[p] * dx[i] + ry[p] * dy[i];
+      }
+    }
+    for (int p = 1; p < LENSP; p++) for (int q = 0; q < p; q++) A3[p][q] = A3[q][p];
+    for (int k = 0; k <= 3; k++) {
+      const int p = 8 + k;
+      double A[LENSP][LENSP + 1];
+      memcpy(A, A3, sizeof A);
+      for (int c = 0; c < p; c++) A[c][c] += 1e-12;
+      if (2 * n - p - 1 <= 0 || !solve_lens(A, p)) continue;
+      double t[LENSP] = {0}, rss = 0;
+      for (int c = 0; c < p; c++) t[c] = A[c][LENSP] / A[c][c];
+      for (int i = 0; i < np; i++) {
+        if (drop[i]) continue;
+        lens_rows(qx[i], qy[i], k, rx, ry);
+        double fx = 0, fy = 0;
+        for (int c = 0; c < p; c++) { fx += t[c] * rx[c]; fy += t[c] * ry[c]; }
+        rss += (dx[i] - fx) * (dx[i] - fx) + (dy[i] - fy) * (dy[i] - fy);
+      }
+      const double n2 = 2.0 * n, aicc = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
+      if (aicc < best) { best = aicc; K = k; memcpy(tb, t, sizeof tb); }
+    }
+    if (K < 0) break;
+    lens[0] = K;
+    for (int c = 0; c < LENSP; c++) lens[4 + c] = tb[c];
+    ok = 1;
+    if (!isb || round == 3) break;
+    double res[ANK * ANK + 4], srt[ANK * ANK + 4];
+    int nb = 0, changed = 0;
+    for (int i = 0; i < np; i++) {
+      if (!isb[i]) continue;
+      float fx, fy;
+      lens_at(lens, qx[i] * R + ax, qy[i] * R + ay, &fx, &fy);
+      res[nb++] = hypot(dx[i] - fx, dy[i] - fy);
+    }
+    if (!nb) break;
+    memcpy(srt, res, (size_t)nb * sizeof(double));
+    qsort(srt, (size_t)nb, sizeof(double), cmp_dbl);
+    const double tau = fmax(tau_floor, 3 * 1.4826 * srt[nb / 2]);
+    for (int i = 0, b = 0; i < np; i++) {
+      if (!isb[i]) continue;
+      const unsigned char bad = res[b++] > tau;
+      if (bad != drop[i]) { drop[i] = bad; changed++; }
+    }
+    if (!changed) break;
+  }
+  return ok;
+}
+
+// The homography through the anchors found (liblizard/src/acquire.c:2062-2094 anchor_homo): least squares with
+// h33 = 1 on coordinates centred and scaled by their mean distance over sqrt 2; 0 where fewer than eight anchors or
+// fewer than three of the grid's rows or columns hold them.
+static int anchor_homo_o(int span, const uint8_t *ok, const float *u, const float *v, float *H) {
+  const int a = span / 64;
+  int n = 0, rows = 0, cols = 0, rm = 0, cm = 0;
+  double mx = 0, my = 0, mu = 0, mv = 0;
+  float X[ANK * ANK], Y[ANK * ANK];
+  for (int k = 0; k < ANK * ANK; k++) {
+    X[k] = (float)anchor_m0(span, k % ANK) + a * 0.5f; Y[k] = (float)anchor_m0(span, k / ANK) + a * 0.5f;
+    if (ok[k]) { n++; mx += X[k]; my += Y[k]; mu += u[k]; mv += v[k]; rm |= 1 << (k / ANK); cm |= 1 << (k % ANK); }
+  }
+  for (int b = 0; b < ANK; b++) { rows += (rm >> b) & 1; cols += (cm >> b) & 1; }
+  if (n < 8 || rows < 3 || cols < 3) return 0;
+  mx /= n; my /= n; mu /= n; mv /= n;
+  double sx = 0, su = 0;
+  for (int k = 0; k < ANK * ANK; k++) if (ok[k]) { sx += hypot(X[k] - mx, Y[k] - my); su += hypot(u[k] - mu, v[k] - mv); }
+  sx = sx / n / 1.4142135623730951; su = su / n / 1.4142135623730951;
+  if (!(sx > 0) || !(su > 0)) return 0;
+  double M[LENSP][LENSP + 1];
+  memset(M, 0, sizeof M);
+  for (int k = 0; k < ANK * ANK; k++) {
+    if (!ok[k]) continue;
+    const double x = (X[k] - mx) / sx, y = (Y[k] - my) / sx, uu = (u[k] - mu) / su, vv = (v[k] - mv) / su;
+    const double r0[8] = {x, y, 1, 0, 0, 0, -uu * x, -uu * y}, r1[8] = {0, 0, 0, x, y, 1, -vv * x, -vv * y};
+    for (int p = 0; p < 8; p++) { for (int q = 0; q < 8; q++) M[p][q] += r0[p] * r0[q] + r1[p] * r1[q]; M[p][LENSP] += r0[p] * uu + r1[p] * vv; }
+  }
+  if (!solve_lens(M, 8)) return 0;
+  double g[9];
+  for (int p = 0; p < 8; p++) g[p] = M[p][LENSP] / M[p][p];
+  g[8] = 1;
+  const double tx[9] = {1 / sx, 0, -mx / sx, 0, 1 / sx, -my / sx, 0, 0, 1}, ti[9] = {su, 0, mu, 0, su, mv, 0, 0, 1};
+  double gt[9], h[9];
+  for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) { gt[3 * r + c] = 0; for (int k = 0; k < 3; k++) gt[3 * r + c] += g[3 * r + k] * tx[3 * k + c]; }
+  for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) { h[3 * r + c] = 0; for (int k = 0; k < 3; k++) h[3 * r + c] += ti[3 * r + k] * gt[3 * k + c]; }
+  if (!(fabs(h[8]) > 1e-12)) return 0;
+  for (int k = 0; k < 9; k++) H[k] = (float)(h[k] / h[8]);
+  return 1;
+}
+
+// The homography through four point pairs (liblizard/src/acquire.c:611-654 solve8 / homography, the portable form).
+static int homography_o(const float *src, const float *dst, float *H) {
+  double A[8][9];
+  for (int i = 0; i < 4; i++) {
+    const double x = src[2 * i], y = src[2 * i + 1], u = dst[2 * i], v = dst[2 * i + 1];
+    const double r0[9] = {x, y, 1, 0, 0, 0, -u * x, -u * y, u}, r1[9] = {0, 0, 0, x, y, 1, -v * x, -v * y, v};
+    memcpy(A[2 * i], r0, sizeof r0); memcpy(A[2 * i + 1], r1, sizeof r1);
+  }
+  for (int c = 0; c < 8; c++) {
+    int p = c;
+    for (int r = c + 1; r < 8; r++) if (fabs(A[r][c]) > fabs(A[p][c])) p = r;
+    if (fabs(A[p][c]) < 1e-12) return 0;
+    for (int k = 0; k < 9; k++) { const double t = A[c][k]; A[c][k] = A[p][k]; A[p][k] = t; }
+    for (int r = 0; r < 8; r++) {
+      if (r == c) continue;
+      const double f = A[r][c] / A[c][c];
+      for (int k = c; k < 9; k++) A[r][k] -= f * A[c][k];
+    }
+  }
+  for (int i = 0; i < 8; i++) H[i] = (float)(A[i][8] / A[i][i]);
+  H[8] = 1;
+  return 1;
+}
+
+// The code registered from the anchors (liblizard/src/acquire.c:2128-2197 anchor_register): rounds of the anchor
+// search (at most six) through the homography the anchors found so far say (anchor_homo) and the lens model they say
+// about it, held to the robust rule (anchor_model_free, :2101-2118: a reading further from the model than half a
+// module, mpx / 2 px, or three robust spreads, no longer found), until a round finds nothing new; then each corner
+// judged by that map (further than 3 modules off, searched again through the border node search on rim from where
+// the joint model of the anchors and the kept corners puts it, kept where it correlates 0.35 or more, else the
+// model's place, and H made again from the four); then the anchors' model about H (anchor_model). px: the frame
+// (the anchor search's), rim: the border search's image (the frame, or its border blur; NULL: the frame), both w x h. H: in the
+// corners' homography, out the registration's; quad: the corners as the finder measured them (in, and out as moved);
+// mpx: pixels a module. Out per anchor: ok, peak, dx, dy (about H), u, v; lens: the model about H. Returns 1 where
+// the registration holds (OB_ANCH_MIN = 12 anchors or more and a model), else 0 (H, quad unchanged).
+int orc_anchor_register(int span, const uint8_t *px, const uint8_t *rim, int w, int h, float *H, float *quad, float mpx, uint8_t *ok,
+                        float *peak, float *adx, float *ady, float *au, float *av, double *lens) {
+  enum { NA = ANK * ANK, ROUNDS = 6, AMIN = 12, CORNER = 3 };
+  const int side = span + 2 * MARGIN;
+  float pos[NMAXN];
+  const int nn = orc_layout_nodes(side, pos);
+  const double ax = w * 0.5f, ay = h * 0.5f;
+  double R = 0;
+  for (int c = 0; c < 4; c++) { const double d = hypot((c & 1 ? w : 0) - ax, (c & 2 ? h : 0) - ay); if (d > R) R = d; }
+  if (!(R > 0)) R = 1;
+  float Ha[9], H0[9];
+  memcpy(Ha, H, sizeof Ha); memcpy(H0, H, sizeof H0);
+  double mf[4 + LENSP];
+  int have = 0, nf = 0;
+  for (int k = 0; k < NA; k++) { ok[k] = 0; peak[k] = adx[k] = ady[k] = au[k] = av[k] = 0; }
+  const int a = span / 64;
+  float X[NA], Y[NA];
+  for (int k = 0; k < NA; k++) { X[k] = (float)anchor_m0(span, k % ANK) + a * 0.5f; Y[k] = (float)anchor_m0(span, k / ANK) + a * 0.5f; }
+  for (int round = 0; round < ROUNDS; round++) {
+    uint8_t ok_in[NA], ok2[NA];
+    float pk2[NA], dx2[NA], dy2[NA], u2[NA], v2[NA];
+    memcpy(ok_in, ok, NA);
+    const int now = orc_anchor_find(span, px, w, h, Ha, have ? mf : NULL, ok_in, ok2, pk2, dx2, dy2, u2, v2);
+    for (int k = 0; k < NA; k++)
+      if (!ok_in[k]) { ok[k] = ok2[k]; peak[k] = pk2[k]; adx[k] = dx2[k]; ady[k] = dy2[k]; au[k] = u2[k]; av[k] = v2[k]; }
+    if (now == nf || now < 4) break;
+    nf = now;
+    float Hn[9];
+    if (anchor_homo_o(span, ok, au, av, Hn)) memcpy(Ha, Hn, sizeof Ha);
+    // anchor_model_free: the anchors' displacements about Ha, the robust rule at half a module
+    double qx[NA], qy[NA], dx[NA], dy[NA];
+    unsigned char drop[NA] = {0}, isb[NA];
+    int np = 0, at[NA];
+    memset(isb, 1, sizeof isb);
+    for (int k = 0; k < NA; k++) {
+      if (!ok[k]) continue;
+      float hu, hv;
+      project(Ha, X[k], Y[k], &hu, &hv);
+      adx[k] = au[k] - hu; ady[k] = av[k] - hv;
+      qx[np] = (hu - ax) / R; qy[np] = (hv - ay) / R; dx[np] = adx[k]; dy[np] = ady[k]; at[np] = k; np++;
+    }
+    have = np >= 4 && lensm_fit_o(np, qx, qy, dx, dy, isb, drop, 0.5 * mpx, ax, ay, R, mf);
+    if (!have) break;
+    for (int i = 0; i < np; i++) if (drop[i]) ok[at[i]] = 0;
+    nf = 0;
+    for (int k = 0; k < NA; k++) nf += ok[k];
+  }
+  if (!have || nf < AMIN) return 0;
+  // the anchors and the corners about the corners' H; each corner judged by the anchors' own map
+  double qx[NA + 4], qy[NA + 4], dx[NA + 4], dy[NA + 4], mc[4 + LENSP];
+  unsigned char drop[NA + 4] = {0};
+  int np = 4;
+  for (int c = 0; c < 4; c++) {
+    float u, v;
+    project(H0, pos[(c == 1 || c == 2) ? nn - 1 : 0], pos[c >= 2 ? nn - 1 : 0], &u, &v);
+    qx[c] = (u - ax) / R; qy[c] = (v - ay) / R; dx[c] = dy[c] = 0;
+  }
+  for (int k = 0; k < NA; k++) {
+    if (!ok[k]) continue;
+    float hu, hv;
+    project(H0, X[k], Y[k], &hu, &hv);
+    qx[np] = (hu - ax) / R; qy[np] = (hv - ay) / R; dx[np] = au[k] - hu; dy[np] = av[k] - hv; np++;
+  }
+  for (int c = 0; c < 4; c++) {
+    float pu, pv, mu, mv;
+    project(Ha, pos[(c == 1 || c == 2) ? nn - 1 : 0], pos[c >= 2 ? nn - 1 : 0], &pu, &pv);
+    lens_at(mf, pu, pv, &mu, &mv);
+    drop[c] = hypotf(pu + mu - quad[2 * c], pv + mv - quad[2 * c + 1]) > CORNER * mpx;
+  }
+  const int fit = lensm_fit_o(np, qx, qy, dx, dy, NULL, drop, 0, ax, ay, R, mc);
+  const float src[8] = {pos[0], pos[0], pos[nn - 1], pos[0], pos[nn - 1], pos[nn - 1], pos[0], pos[nn - 1]};
+  int moved = 0;
+  if (fit) {
+    unsigned char *kind = malloc((size_t)side * side);
+    onode_t *nodes = calloc((size_t)nn * nn, sizeof(onode_t));
+    if (!kind || !nodes) { free(kind); free(nodes); return -1; }
+    mesh_kind(span, kind);
+    const omesh_t M = {kind, side, nn, pos};
+    for (int c = 0; c < 4; c++) nodes[((c >= 2) ? nn - 1 : 0) * nn + ((c == 1 || c == 2) ? nn - 1 : 0)].done = 1;
+    for (int c = 0; c < 4; c++) {
+      if (!drop[c]) continue;
+      const int i = (c == 1 || c == 2) ? nn - 1 : 0, j = c >= 2 ? nn - 1 : 0;
+      float hu, hv, mu, mv;
+      project(H0, pos[i], pos[j], &hu, &hv);
+      lens_at(mc, hu, hv, &mu, &mv);
+      onode_t *nd = &nodes[j * nn + i];
+      nd->done = 0;
+      refine_node(&M, rim ? rim : px, w, h, H0, i, j, nodes, mc);
+      if (nd->score >= 0.35f) { quad[2 * c] = hu + nd->dx; quad[2 * c + 1] = hv + nd->dy; }
+      else { quad[2 * c] = hu + mu; quad[2 * c + 1] = hv + mv; }
+      moved++;
+    }
+    free(kind); free(nodes);
+  }
+  float Hc[9];
+  if (moved && homography_o(src, quad, Hc)) memcpy(H, Hc, 9 * sizeof(float));
+  for (int k = 0; k < NA; k++) if (ok[k]) { float hu, hv; project(H, X[k], Y[k], &hu, &hv); adx[k] = au[k] - hu; ady[k] = av[k] - hv; }
+  return orc_lens_fit(span, w, h, H, ok, adx, ady, lens);
+}

@@ -105,3 +105,40 @@ int refs_border_nodes(int span, const uint8_t *px, int w, int h, const float *H9
   ob_layout_free(&L);
   return nx;
 }
+
+// The code registered from the anchors as the reference's acquisition runs it (liblizard/src/acquire.c:2128-2197
+// anchor_register) after its corners' step (:5028-5037: the four corners done, no displacement): px the frame, rim
+// the border search's image (NULL: the frame), H9 the corners' homography (in; out the registration's), quad the
+// corners in the image (in; out as moved), mpx pixels a module. Out per anchor: ok, peak, dx, dy, u, v; lens the
+// model about H (K, ax, ay, R, coefficients). Returns anchor_register's result (1 held, 0 not), or -1.
+int refs_anchor_register(int span, const uint8_t *px, const uint8_t *rim_px, int w, int h, float *H9, float *quad, float mpx, uint8_t *ok,
+                         float *peak, float *dx, float *dy, float *u, float *v, double *lens) {
+  ob_layout_t L;
+  if (ob_layout_init(&L, span + 2 * OB_MARGIN)) return -1;
+  uint8_t cw[OB_FMT_BYTES_MAX];
+  memset(cw, 0, sizeof cw);
+  ob_layout_set_fmt(&L, cw);
+  image_t im, rim;
+  ob_image_init(&im, px, w, h, 1.0f);
+  ob_image_init(&rim, rim_px ? rim_px : px, w, h, 1.0f);
+  homo_t H;
+  memcpy(H.h, H9, sizeof H.h);
+  const int nx = L.nx, ny = L.ny;
+  node_t *nodes = calloc((size_t)nx * ny, sizeof(node_t));
+  if (!nodes) { ob_layout_free(&L); return -1; }
+  for (int c = 0; c < 4; c++) nodes[((c >= 2) ? ny - 1 : 0) * nx + ((c == 1 || c == 2) ? nx - 1 : 0)].done = 1;
+  anchor_t A[OB_ANCH_K * OB_ANCH_K];
+  memset(A, 0, sizeof A);
+  lensm_t m;
+  memset(&m, 0, sizeof m);
+  const int held = anchor_register(&L, &im, &rim, &H, w, h, mpx, quad, nodes, A, &m);
+  memcpy(H9, H.h, sizeof H.h);
+  for (int k = 0; k < OB_ANCH_K * OB_ANCH_K; k++) {
+    ok[k] = (uint8_t)A[k].ok; peak[k] = A[k].peak; dx[k] = A[k].dx; dy[k] = A[k].dy; u[k] = A[k].u; v[k] = A[k].v;
+  }
+  lens[0] = m.K; lens[1] = m.ax; lens[2] = m.ay; lens[3] = m.R;
+  for (int k = 0; k < LENS_P; k++) lens[4 + k] = m.t[k];
+  free(nodes);
+  ob_layout_free(&L);
+  return held;
+}

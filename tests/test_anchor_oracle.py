@@ -82,3 +82,43 @@ def test_lens_fit_matches_reference(seed, k1):
     f2, l2 = oracle.lens_fit(oracle.ref_scalar(), "refs_anchor_model", 256, 1920, 1080, reg[:9], a["ok"], a["dx"], a["dy"])
     assert f1 == f2 == 1
     assert np.array_equal(l1.view(np.uint64), l2.view(np.uint64)), (l1, l2)
+
+
+def registration_case(seed, k1, blur, moved):
+    """A distorted capture of LIZARD-1024 in the 128 ring (1920 x 1080) and what a finder hands the registration: the
+    corners in the image (quad; with moved = c + 1, corner c placed 15 modules off, past the 3 the rule allows),
+    the homography through them and the pixels a module, as the reference's acquisition forms them."""
+    fmt = lz.Format(1536, 1024, 256)
+    rng = np.random.default_rng(seed)
+    grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, seed), parity=seed & 3)
+    Hv = synth.distorted_view(fmt, 1920, 1080, rng, base_side=1000)
+    luma, reg = synth.distorted_capture(fmt, grey, 1920, 1080, Hv, k1=k1, blur=blur, sigma=3.0, rng=rng)
+    nodes = synth.layout_nodes(256)
+    lo, hi = float(nodes[0]), float(nodes[-1])
+    src = np.array([[lo, lo], [hi, lo], [hi, hi], [lo, hi]], np.float64)
+    H0 = reg[:9].astype(np.float64).reshape(3, 3)
+    q = H0 @ np.column_stack([src, np.ones(4)]).T
+    quad = np.stack([q[0] / q[2], q[1] / q[2]], 1).astype(np.float32)
+    sides = [np.hypot(*(quad[(k + 1) % 4] - quad[k])) / np.hypot(*(src[(k + 1) % 4] - src[k])) for k in range(4)]
+    mpx = np.float32(sum(np.float32(s) / np.float32(4) for s in sides))
+    if moved:
+        quad[moved - 1] += np.float32(15 * mpx) * np.float32([0.6, 0.8])
+    H = synth.homography_4(src, quad.astype(np.float64)).astype(np.float32).ravel()
+    return luma, H, quad.ravel(), float(mpx)
+
+
+@pytest.mark.skipif(oracle.ref_scalar() is None, reason="the reference's portable build is not here")
+@pytest.mark.parametrize("seed,k1,blur,moved", [(1, 0.0, 1.0, 0), (2, 0.03, 1.5, 0), (3, -0.04, 0.8, 1), (4, 0.05, 1.0, 3)])
+def test_anchor_register_matches_reference(seed, k1, blur, moved):
+    """The code registered from the anchors (anchor_register: rounds through the anchors' own homography and robust
+    model, each corner judged by their map and searched again where it disagrees, H made again, the model about H),
+    the oracle against the reference's portable build, bit for bit."""
+    luma, H, quad, mpx = registration_case(seed, k1, blur, moved)
+    a = oracle.anchor_register(oracle.port(), "orc_anchor_register", 256, luma, H, quad, mpx)
+    b = oracle.anchor_register(oracle.ref_scalar(), "refs_anchor_register", 256, luma, H, quad, mpx)
+    assert a["held"] == b["held"] == 1
+    for k in ("H", "quad", "lens") + FIELDS:
+        assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(b[k]).view(np.uint8)), k
+    assert a["ok"].sum() >= 30
+    if moved:   # the corner put 15 modules off comes back
+        assert not np.array_equal(a["quad"], quad)

@@ -79,3 +79,30 @@ def test_refined_decodes_what_plain_cannot():
     refined = rx.finish_luma(luma, reg3, keep=False, grid=False)
     print("blocks verified: plain %d refined %d of %d" % (plain["ok"].sum(), refined["ok"].sum(), plain["ok"].size))
     assert refined["ok"].sum() >= plain["ok"].sum() + 4 * 25
+
+
+def test_anchor_register_matches_oracle():
+    """The reference's whole registration from the anchors on the GPU (lizg_anchor_register_dev: rounds through the
+    anchors' own homography and robust model, the corners judged and searched again, H made again, the model about H)
+    against the oracle's restatement (itself held to the reference's portable build on the same cases), four frames
+    in one call: held, H, the corners, the model and every anchor bit for bit, the mesh the model at the nodes."""
+    import test_anchor_oracle as tao
+    cases = [tao.registration_case(seed, k1, blur, moved) for seed, k1, blur, moved in
+             [(1, 0.0, 1.0, 0), (2, 0.03, 1.5, 0), (3, -0.04, 0.8, 1), (4, 0.05, 1.0, 3), (5, 0.02, 1.2, 2)]]
+    nn = synth.layout_nodes(256).size
+    luma = np.stack([c[0] for c in cases])
+    reg = np.zeros((len(cases), 9 + 2 * nn * nn), np.float32)
+    for f, c in enumerate(cases):
+        reg[f, :9] = c[1]
+    quad = np.stack([c[2] for c in cases])
+    rf = lz.Refiner(256, len(cases))
+    got = rf.register(luma, reg, quad=quad)
+    for f, (lu, Hc, q, mpx) in enumerate(cases):
+        want = oracle.anchor_register(oracle.port(), "orc_anchor_register", 256, lu, Hc, q, mpx)
+        assert got["held"][f] == want["held"] == 1, f
+        assert np.array_equal(got["reg"][f, :9].view(np.uint32), want["H"].view(np.uint32)), f
+        assert np.array_equal(got["quad"][f].view(np.uint32), want["quad"].view(np.uint32)), f
+        assert np.array_equal(got["lens"][f].view(np.uint64), want["lens"].view(np.uint64)), f
+        for k in ("ok", "peak", "dx", "dy", "u", "v"):
+            assert np.array_equal(np.asarray(got[k][f]).view(np.uint8), np.asarray(want[k]).view(np.uint8)), (f, k)
+        assert np.array_equal(got["reg"][f, 9:], mesh_expected(got["reg"][f], got["lens"][f], 256)), f
