@@ -52,6 +52,84 @@ struct FitArgs {
   const int *gate;                 // frames, may be NULL: 0 where no model is fitted (have 0)
 };
 
+// Gauss-Jordan with partial pivoting on the first p rows of A (the right-hand side in column kLP) across a warp, the
+// reference's solve_lens (liblizard/src/acquire.c:1491-1504) operation for operation: lane 0 finds the pivot (the
+// first largest magnitude), the lanes swap the two rows, take each row's factor from its pivot-column entry, then
+// update every (row, column) entry, each with the product and subtraction the serial loop makes. Returns (on every
+// lane) 0 where a pivot falls under thresh.
+__device__ bool warp_gj(double (*A)[kLP + 1], int p, double thresh, double *s_f, int *s_piv) {
+  const int lane = threadIdx.x & 31;
+  for (int c = 0; c < p; c++) {
+    if (lane == 0) {
+      int pv = c;
+      for (int r = c + 1; r < p; r++) if (fabs(A[r][c]) > fabs(A[pv][c])) pv = r;
+      s_piv[0] = pv;
+      s_piv[1] = fabs(A[pv][c]) < thresh;
+    }
+    __syncwarp();
+    if (s_piv[1]) return false;
+    const int pv = s_piv[0];
+    if (pv != c)
+      for (int k = lane; k <= kLP; k += 32) { const double t = A[c][k]; A[c][k] = A[pv][k]; A[pv][k] = t; }
+    __syncwarp();
+    for (int r = lane; r < p; r += 32) s_f[r] = r == c ? 0.0 : A[r][c] / A[c][c];
+    __syncwarp();
+    const int ncol = kLP + 1 - c;
+    for (int e = lane; e < p * ncol; e += 32) {
+      const int r = e / ncol, k = c + (e - r * ncol);
+      if (r != c) A[r][k] -= s_f[r] * A[c][k];
+    }
+    __syncwarp();
+  }
+  return true;
+}
+
+// lensm_fit's models over the points (liblizard/src/acquire.c:1651-1668) on a warp, from its summed normal equations
+// sA (upper triangle and right side; n of the np points not dropped): for K = 0..3 radial terms the system of 8 + K
+// unknowns solved (warp_gj), each point's model value on its own lane, the residuals' sum over the points in order on
+// lane 0, AICc; the least kept. Out (shared): tb the coefficients, K (-1 where none solved).
+__device__ void warp_models(int np, int n, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const uint8_t *drop, double (*sA)[kLP + 1],
+                            double (*A)[kLP + 1], double *s_f, double *s_t, double *s_tb, double (*s_pt)[2], int *s_piv, int *s_K) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    for (int p = 1; p < kLP; p++) for (int q = 0; q < p; q++) sA[p][q] = sA[q][p];
+    *s_K = -1;
+    for (int c = 0; c < kLP; c++) s_tb[c] = 0;
+  }
+  __syncwarp();
+  double best = INFINITY;   // lane 0's
+  for (int k = 0; k <= 3; k++) {
+    const int p = 8 + k;
+    for (int e = lane; e < kLP * (kLP + 1); e += 32) {
+      const int r = e / (kLP + 1), c = e - r * (kLP + 1);
+      A[r][c] = sA[r][c] + (r == c && c < p ? 1e-12 : 0.0);
+    }
+    __syncwarp();
+    if (2 * n - p - 1 <= 0) continue;
+    if (!warp_gj(A, p, 1e-14, s_f, s_piv)) continue;
+    for (int c = lane; c < kLP; c += 32) s_t[c] = c < p ? A[c][kLP] / A[c][c] : 0.0;
+    __syncwarp();
+    for (int i = lane; i < np; i += 32) {
+      if (drop && drop[i]) continue;
+      double fx = 0, fy = 0;
+      for (int c = 0; c < p; c++) { fx += s_t[c] * rx[i][c]; fy += s_t[c] * ry[i][c]; }
+      s_pt[i][0] = fx; s_pt[i][1] = fy;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double rss = 0;
+      for (int i = 0; i < np; i++) {
+        if (drop && drop[i]) continue;
+        const double fx = s_pt[i][0], fy = s_pt[i][1];
+        rss += (d[i][0] - fx) * (d[i][0] - fx) + (d[i][1] - fy) * (d[i][1] - fy);
+      }
+      const double n2 = 2.0 * n, aicc = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
+      if (aicc < best) { best = aicc; *s_K = k; for (int c = 0; c < kLP; c++) s_tb[c] = s_t[c]; }
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void __launch_bounds__(32) lens_fit_kernel(FitArgs a) {
   const int f = blockIdx.x, lane = threadIdx.x;
   if (a.gate && !a.gate[f]) {
@@ -98,40 +176,13 @@ __global__ void __launch_bounds__(32) lens_fit_kernel(FitArgs a) {
     s_A[p][q] = acc;
   }
   __syncwarp();
+  __shared__ double s_f[kLP], s_t[kLP], s_tb[kLP], s_pt[kMaxPts][2];
+  __shared__ int s_piv[2], s_K;
+  warp_models(np, np, s_rx, s_ry, s_d, nullptr, s_A, A, s_f, s_t, s_tb, s_pt, s_piv, &s_K);
   if (lane != 0) return;
-  for (int p = 1; p < kLP; p++) for (int q = 0; q < p; q++) s_A[p][q] = s_A[q][p];
-  double best = INFINITY, tb[kLP];
-  for (int c = 0; c < kLP; c++) tb[c] = 0;
-  int K = -1;
-  for (int k = 0; k <= 3; k++) {
-    const int p = 8 + k;
-    for (int r = 0; r < kLP; r++) for (int c = 0; c <= kLP; c++) A[r][c] = s_A[r][c];
-    for (int c = 0; c < p; c++) A[c][c] += 1e-12;
-    if (2 * np - p - 1 <= 0) continue;
-    bool solved = true;
-    for (int c = 0; c < p && solved; c++) {
-      int pv = c;
-      for (int r = c + 1; r < p; r++) if (fabs(A[r][c]) > fabs(A[pv][c])) pv = r;
-      if (fabs(A[pv][c]) < 1e-14) { solved = false; break; }
-      for (int kk = 0; kk <= kLP; kk++) { const double t = A[c][kk]; A[c][kk] = A[pv][kk]; A[pv][kk] = t; }
-      for (int r = 0; r < p; r++) {
-        if (r == c) continue;
-        const double fr = A[r][c] / A[c][c];
-        for (int kk = c; kk <= kLP; kk++) A[r][kk] -= fr * A[c][kk];
-      }
-    }
-    if (!solved) continue;
-    double t[kLP], rss = 0;
-    for (int c = 0; c < kLP; c++) t[c] = 0;
-    for (int c = 0; c < p; c++) t[c] = A[c][kLP] / A[c][c];
-    for (int i = 0; i < np; i++) {
-      double fx = 0, fy = 0;
-      for (int c = 0; c < p; c++) { fx += t[c] * s_rx[i][c]; fy += t[c] * s_ry[i][c]; }
-      rss += (s_d[i][0] - fx) * (s_d[i][0] - fx) + (s_d[i][1] - fy) * (s_d[i][1] - fy);
-    }
-    const double n2 = 2.0 * np, aicc = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
-    if (aicc < best) { best = aicc; K = k; for (int c = 0; c < kLP; c++) tb[c] = t[c]; }
-  }
+  const int K = s_K;
+  double tb[kLP];
+  for (int c = 0; c < kLP; c++) tb[c] = s_tb[c];
   double *L = a.lens + (int64_t)f * kLStride;
   if (K < 0) {   // no model: no displacement
     L[0] = 0; L[1] = ax; L[2] = ay; L[3] = R;
@@ -217,14 +268,16 @@ struct RegArgs {
 
 // lensm_fit (liblizard/src/acquire.c:1630-1694) over np points whose rows (lens_rows at K = 3) are rx, ry, residuals
 // d, places qx, qy, on one warp: every lane takes entries of the normal equations (upper triangle and right side),
-// each summed over the points not dropped in their order; lane 0 solves each model of 0..3 radial terms, keeps the
-// least AICc, and (robust) judges every point by the robust rule and goes round again while a verdict changes (at
-// most four rounds). lens (shared, 15) receives the model (K, ax, ay, R, coefficients). Returns (on every lane) 1
-// where a model fitted.
+// each summed over the points not dropped in their order; the models as warp_models fits them; with robust, every
+// point's distance from the model on its own lane, their median by ranks (each lane places its distances in the sorted
+// order), the verdicts on lane 0, and round again while a verdict changes (at most four rounds). lens (shared, 15)
+// receives the model (K, ax, ay, R, coefficients). Returns (on every lane) 1 where a model fitted.
 __device__ int warp_lensm_fit(int np, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const double *qx, const double *qy, uint8_t *drop,
                               bool robust, double tau_floor, double ax, double ay, double R, double *lens, double (*sA)[kLP + 1],
                               double (*A)[kLP + 1], double *res, int *s_flag) {
   const int lane = threadIdx.x & 31;
+  __shared__ double s_f[kLP], s_t[kLP], s_tb[kLP], s_pt[kMaxPts][2], s_srt[kMaxPts];
+  __shared__ int s_piv[2], s_K;
   int ok = 0;
   for (int round = 0; round < 4; round++) {
     int n = 0;
@@ -239,77 +292,39 @@ __device__ int warp_lensm_fit(int np, double (*rx)[kLP], double (*ry)[kLP], doub
       sA[p][q] = acc;
     }
     __syncwarp();
+    warp_models(np, n, rx, ry, d, drop, sA, A, s_f, s_t, s_tb, s_pt, s_piv, &s_K);
+    const int K = s_K;
+    if (K < 0) break;
     if (lane == 0) {
-      for (int p = 1; p < kLP; p++) for (int q = 0; q < p; q++) sA[p][q] = sA[q][p];
-      double best = INFINITY, tb[kLP];
-      for (int c = 0; c < kLP; c++) tb[c] = 0;
-      int K = -1;
-      for (int k = 0; k <= 3; k++) {
-        const int p = 8 + k;
-        for (int r = 0; r < kLP; r++) for (int c = 0; c <= kLP; c++) A[r][c] = sA[r][c];
-        for (int c = 0; c < p; c++) A[c][c] += 1e-12;
-        if (2 * n - p - 1 <= 0) continue;
-        bool solved = true;
-        for (int c = 0; c < p && solved; c++) {
-          int pv = c;
-          for (int r = c + 1; r < p; r++) if (fabs(A[r][c]) > fabs(A[pv][c])) pv = r;
-          if (fabs(A[pv][c]) < 1e-14) { solved = false; break; }
-          for (int kk = 0; kk <= kLP; kk++) { const double t = A[c][kk]; A[c][kk] = A[pv][kk]; A[pv][kk] = t; }
-          for (int r = 0; r < p; r++) {
-            if (r == c) continue;
-            const double fr = A[r][c] / A[c][c];
-            for (int kk = c; kk <= kLP; kk++) A[r][kk] -= fr * A[c][kk];
-          }
-        }
-        if (!solved) continue;
-        double t[kLP], rss = 0;
-        for (int c = 0; c < kLP; c++) t[c] = 0;
-        for (int c = 0; c < p; c++) t[c] = A[c][kLP] / A[c][c];
-        for (int i = 0; i < np; i++) {
-          if (drop[i]) continue;
-          double fx = 0, fy = 0;
-          for (int c = 0; c < p; c++) { fx += t[c] * rx[i][c]; fy += t[c] * ry[i][c]; }
-          rss += (d[i][0] - fx) * (d[i][0] - fx) + (d[i][1] - fy) * (d[i][1] - fy);
-        }
-        const double n2 = 2.0 * n, aicc = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
-        if (aicc < best) { best = aicc; K = k; for (int c = 0; c < kLP; c++) tb[c] = t[c]; }
-      }
-      int go = 0;
-      if (K >= 0) {
-        lens[0] = K; lens[1] = ax; lens[2] = ay; lens[3] = R;
-        for (int c = 0; c < kLP; c++) lens[4 + c] = tb[c];
-        ok = 1;
-        if (robust && round < 3) {
-          // the robust rule: every point's distance from the model, tau from their median, the verdicts again
-          int nb = 0;
-          for (int i = 0; i < np; i++) {
-            float fx, fy;
-            lens_at(lens, qx[i] * R + ax, qy[i] * R + ay, &fx, &fy);
-            res[nb++] = hypot(d[i][0] - fx, d[i][1] - fy);
-          }
-          if (nb) {
-            double srt[kMaxPts];
-            for (int i = 0; i < nb; i++) {   // insertion sort, ascending
-              const double x = res[i];
-              int j = i;
-              while (j > 0 && srt[j - 1] > x) { srt[j] = srt[j - 1]; j--; }
-              srt[j] = x;
-            }
-            const double tau = fmax(tau_floor, 3 * 1.4826 * srt[nb / 2]);
-            int changed = 0;
-            for (int i = 0; i < np; i++) {
-              const uint8_t bad = res[i] > tau;
-              if (bad != drop[i]) { drop[i] = bad; changed++; }
-            }
-            go = changed > 0;
-          }
-        }
-      }
-      s_flag[0] = ok;
-      s_flag[1] = go;
+      lens[0] = K; lens[1] = ax; lens[2] = ay; lens[3] = R;
+      for (int c = 0; c < kLP; c++) lens[4 + c] = s_tb[c];
+    }
+    ok = 1;
+    __syncwarp();
+    if (!robust || round == 3) break;
+    // the robust rule: every point's distance from the model, tau from their median, the verdicts again
+    for (int i = lane; i < np; i += 32) {
+      float fx, fy;
+      lens_at(lens, qx[i] * R + ax, qy[i] * R + ay, &fx, &fy);
+      res[i] = hypot(d[i][0] - fx, d[i][1] - fy);
     }
     __syncwarp();
-    ok = s_flag[0];
+    for (int i = lane; i < np; i += 32) {   // the ascending order, ties by index: the sort's array
+      int rank = 0;
+      for (int j = 0; j < np; j++) rank += res[j] < res[i] || (res[j] == res[i] && j < i);
+      s_srt[rank] = res[i];
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const double tau = fmax(tau_floor, 3 * 1.4826 * s_srt[np / 2]);
+      int changed = 0;
+      for (int i = 0; i < np; i++) {
+        const uint8_t bad = res[i] > tau;
+        if (bad != drop[i]) { drop[i] = bad; changed++; }
+      }
+      s_flag[1] = changed > 0;
+    }
+    __syncwarp();
     if (!s_flag[1]) break;
   }
   return ok;
