@@ -550,8 +550,9 @@ def bench_multistream(args, stream):
     streams), each stream's frame painted by the sender and seen as the distorted full receiver's frames are (rotation
     U(+-15 deg), tilt U(+-20 deg), the layout's side 1700 px x U(0.8, 1.1), radial k1 U(+-0.05), blur U(0.5, 2.0) px in
     linear light, AWGN 3 DN), registered from a finder's corners. A tick (one frame of every stream): the anchors'
-    registration (3 rounds of the anchor search and the lens model, lizg_refine_dev) one batch a format, then the
-    multi-stream engine: one receiver batch a format, each on its own stream from its own CUDA graph. Beside it the same
+    registration (3 rounds of the anchor search and the lens model, lizg_refine_dev) one batch a format, each format on
+    its own stream, then the multi-stream engine: one receiver batch a format, each on its own stream from its own CUDA
+    graph. Beside it the same
     frames one frame a launch (lizg_refine_dev and lizg_rx_finish_luma_dev a frame). Device-timed; the two paths'
     CRC-passing block sets are checked identical."""
     import numpy as np
@@ -591,10 +592,20 @@ def bench_multistream(args, stream):
         singles.append((rx1, ref1, d_l, d_p, d_r1, o1))
     streams = sum(f[3] for f in formats)
 
+    # each format's registration on its own stream, forked from the tick's stream and joined back before the engine
+    # (the formats' frames are independent; the engine overlaps their receivers the same way)
+    sides = [torch.cuda.Stream() for _ in keep]
+    fork, joins = torch.cuda.Event(), [torch.cuda.Event() for _ in keep]
+
     def tick():
-        for d_l, d_r, o, d_p, refiner, count in keep:
-            d_r.copy_(d_p)
-            refiner.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_r.data_ptr(), count, 3, None, None, sp)
+        fork.record(stream)
+        for (d_l, d_r, o, d_p, refiner, count), side, join in zip(keep, sides, joins):
+            side.wait_event(fork)
+            with torch.cuda.stream(side):
+                d_r.copy_(d_p)
+            refiner.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_r.data_ptr(), count, 3, None, None, side.cuda_stream)
+            join.record(side)
+            stream.wait_event(join)
         eng.run_dev(batches, sp)
 
     def tick_single():

@@ -106,3 +106,34 @@ def test_anchor_register_matches_oracle():
         for k in ("ok", "peak", "dx", "dy", "u", "v"):
             assert np.array_equal(np.asarray(got[k][f]).view(np.uint8), np.asarray(want[k]).view(np.uint8)), (f, k)
         assert np.array_equal(got["reg"][f, 9:], mesh_expected(got["reg"][f], got["lens"][f], 256)), f
+
+
+def test_anchor_register_defaults():
+    """lizg_anchor_register_dev with no corners given (the corner nodes through H) and the frame itself given as the
+    border search's image: the oracle's results with the corners H gives; the same frames with rim omitted agree."""
+    import test_anchor_oracle as tao
+    luma, Hc, _, _ = tao.registration_case(6, 0.02, 1.0, 0)
+    nn = synth.layout_nodes(256).size
+    reg = np.zeros((1, 9 + 2 * nn * nn), np.float32)
+    reg[0, :9] = Hc
+    rf = lz.Refiner(256, 1)
+    a = rf.register(luma[None], reg)
+    b = rf.register(luma[None], reg, rim=luma[None])
+    assert a["quad"] is None
+    for k in ("reg", "held", "lens", "ok", "u", "v"):
+        assert np.array_equal(a[k], b[k]), k
+    # the corners the device took: the corner nodes through H, as float projections
+    nodes = synth.layout_nodes(256).astype(np.float32)
+    lo, hi = nodes[0], nodes[-1]
+    h = Hc.astype(np.float32)
+    quad = []
+    for x, y in ((lo, lo), (hi, lo), (hi, hi), (lo, hi)):
+        w = h[6] * x + h[7] * y + np.float32(1)
+        quad += [(h[0] * x + h[1] * y + h[2]) / w, (h[3] * x + h[4] * y + h[5]) / w]
+    quad = np.array(quad, np.float32)
+    sides = [np.float32(np.hypot(*(quad[2 * ((k + 1) % 4):2 * ((k + 1) % 4) + 2] - quad[2 * k:2 * k + 2]))) for k in range(4)]
+    assert a["held"][0] == 1 and a["ok"][0].sum() >= 30
+    want = oracle.anchor_register(oracle.port(), "orc_anchor_register", 256, luma, Hc, quad,
+                                  float(sum(np.float32(s) / np.float32(hi - lo) / np.float32(4) for s in sides)))
+    assert want["held"] == 1
+    assert np.array_equal(a["ok"][0], want["ok"])
