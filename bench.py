@@ -365,9 +365,14 @@ def bench_receiver(args, stream):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / K
 
-    def receiver_line(n, subch, W, Hh, frames, graph, K, label):
+    def receiver_line(n, subch, W, Hh, frames, graph, K, label, tune=False):
         rx, d_l, d_r = capture_frames(n, subch, W, Hh, frames, seed=n)
         o, s = rx._outputs(frames, torch, keep=False)
+        choice = None
+        if tune:   # the handle's own decode: each tier's variant and one launch across the tiers or a launch a tier
+            choice = rx.autotune_dev(d_l.data_ptr(), W, Hh, W, W * Hh, d_r.data_ptr(), frames, sp)[:rx.fmt.tiers]
+            mixed = rx.set_ldpc_mixed(0)
+            rx.set_ldpc_mixed(mixed)
         fn = lz.lib().lizg_rx_finish_luma_graph if graph else lz.lib().lizg_rx_finish_luma_dev
 
         def call():
@@ -375,14 +380,19 @@ def bench_receiver(args, stream):
                          lz.ctypes.byref(s), None, None, lz.ctypes.c_void_p(sp)), "finish_luma")
         ms = timed(call, K)
         okb = int(o["ok"].sum().item())
-        return {"workload": label, "frames_per_call": frames, "graph": graph, "frames_per_s": round(frames / (ms / 1e3), 1),
+        line = {"workload": label, "frames_per_call": frames, "graph": graph, "frames_per_s": round(frames / (ms / 1e3), 1),
                 "payload_MBps": round(okb * 472 / (ms / 1e3) / 1e6, 3), "ms_per_call": round(ms, 4),
                 "blocks_verified": okb, "blocks": frames * rx.fmt.blocks, "gpu_launches_per_call": rx.launches}
+        if tune:
+            line["ldpc_decode"] = {"variants_per_tier": choice, "one_launch_across_tiers": bool(mixed)}
+        return line
 
     if args.batch_only:
         return res
     res["plain_one_frame"] = receiver_line(384, 64, 1280, 720, 1, False, 200, "LIZARD-64, n=384, 64 ring, 1280x720 luma, AWGN 2 DN, axis-aligned, one frame a call")
     res["plain_one_frame_graph"] = receiver_line(384, 64, 1280, 720, 1, True, 400, "the same, the call replayed from a CUDA graph")
+    res["plain_one_frame_graph_tuned"] = receiver_line(384, 64, 1280, 720, 1, True, 400, "the same from a graph, the handle's decode "
+                                                       "tuned on the frame (lizg_rx_autotune)", tune=True)
     res["n1536_one_frame"] = receiver_line(1536, 1024, 3840, 2160, 1, False, 50, "LIZARD-1024, n=1536, 64 ring, 3840x2160 luma, AWGN 2 DN, one frame a call")
     res["n1536_batched_graph"] = receiver_line(1536, 1024, 3840, 2160, 32, True, 5, "the same, 32 frames a call replayed from a CUDA graph")
     res["n1536_batched_vs_one_frame"] = round(res["n1536_batched_graph"]["frames_per_s"] / res["n1536_one_frame"]["frames_per_s"], 2)

@@ -169,10 +169,17 @@ int lizg_rx_set_read(lizg_rx *r, int read);
 // the batch's frames x the tier's blocks); the fastest is kept by the handle for its later finishes (its format and
 // batch size: the choice per picture size and code rate). All variants decode bit for bit alike, so the blocks never
 // change; the global choice of lizg_ldpc_autotune, tuned on large batches of one code, is what the handle uses
-// without it. choice (may be NULL): 4 entries, each tier's variant index (lizg_ldpc_variant's numbering), -1 past the
-// format's tiers. Synchronises the stream. No counterpart in the reference (one decoder form a build).
+// without it. Then the whole decode stage with those variants, a launch a tier on forked streams, against one
+// persistent launch across the tiers (lizg_rx_set_ldpc_mixed); the faster is kept too. choice (may be NULL): 4
+// entries, each tier's variant index (lizg_ldpc_variant's numbering), -1 past the format's tiers. Synchronises the
+// stream. No counterpart in the reference (one decoder form a build).
 int lizg_rx_autotune(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
                      int32_t *choice, void *stream);
+// The handle's decode stage: 0, a launch a tier on the tiers' own streams (the default); 1, every tier's blocks in one
+// persistent launch (a queue of (tier, block) items, the longer codes first, each decoded by its code's form in a slice
+// sized for the longest code: fewer launches and no tail a tier, for small batches). The blocks are the same either
+// way. Returns the previous setting, or LIZG_E_ARG. Host code.
+int lizg_rx_set_ldpc_mixed(lizg_rx *r, int mixed);
 // Tier t's LDPC kernel variant as the handle's finishes launch it: its own after lizg_rx_autotune, else the device's
 // (lizg_ldpc_variant). Host code.
 int lizg_rx_variant(const lizg_rx *r, int tier);

@@ -219,6 +219,7 @@ def _rx_sigs(L):
     L.lizg_rx_fault.argtypes = [P]
     L.lizg_rx_autotune.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P]
     L.lizg_rx_variant.argtypes = [P, I]
+    L.lizg_rx_set_ldpc_mixed.argtypes = [P, I]
     L.lizg_layout_nodes.argtypes = [I, P, P, P]
     L.lizg_rx_finish_luma_host.argtypes = [P, P, I, I, I, ctypes.c_int64, P, I, P, P, P]
     L.lizg_rx_finish_coef_dev.argtypes = [P, P, I, P, P]
@@ -366,6 +367,10 @@ class Receiver:
         _check(lib().lizg_rx_autotune(self._h, ctypes.c_void_p(d_luma), w, h, pitch, frame_stride, ctypes.c_void_p(d_reg), frames,
                                       _ptr(choice), ctypes.c_void_p(st)), "lizg_rx_autotune")
         return [int(c) for c in choice]
+
+    def set_ldpc_mixed(self, mixed):
+        """The decode stage: 0 a launch a tier (the default), 1 one persistent launch across the tiers; the previous."""
+        return _check(lib().lizg_rx_set_ldpc_mixed(self._h, int(mixed)), "lizg_rx_set_ldpc_mixed")
 
     def variant(self, tier):
         """Tier's LDPC kernel variant as the handle's finishes launch it (its own after autotune, else the device's)."""

@@ -538,20 +538,139 @@ __device__ __forceinline__ int lpos(int v) {
   return T::K + (c % T::MB) * 128 + c / T::MB;
 }
 
+// One codeword (item `item` of the launch: a codeword of the batch's list, or in receiver mode block `item` of tier
+// `tier` across the frames) decoded by the calling thread's group of WPC warps in its slice of shared memory (the
+// posteriors, then the messages); red: the group's WPC slots for the unsatisfied-check count. Ends with the group
+// synchronised (a declined block returns at once, having touched nothing of the group's).
 template <int C, int WPC, bool LOOP, bool PAIR>
-__global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(LdpcLaunch a) {
+__device__ __forceinline__ void decode_item(const LdpcLaunch &a, int tier, int item, uint8_t *slice, const uint32_t *crc_tab,
+                                            const uint32_t *crc_k, int *red, int g) {
   using T = Code<C>;
   constexpr int CPL = 4 / WPC, GT = WPC * 32, NP = PAIR ? 2 / WPC : 1;
   static_assert(!PAIR || WPC <= 2, "the pair form runs 64 check pairs a layer on one or two warps");
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, sub = warp % WPC, tg = sub * 32 + lane, t0 = sub * CPL;
+  int16_t *L = reinterpret_cast<int16_t *>(slice);
+  int8_t *R = reinterpret_cast<int8_t *>(L + T::N);
+  int cw, gi = 0;
+  int64_t off = 0;
+  if (a.rx.llrf) {
+    // Receiver mode: item -> (frame, block) of this tier. A declined block is not tried (its -2). Otherwise its
+    // slots' soft values go through the bit map into codeword order, whitening taken off by sign, the never-sent
+    // bits at 0 and the 7/8 code's known zeros past the block's 3840 bits at 127
+    // (liblizard/src/lizard_phy.c:156-192, 1818-1823).
+    const int f = item / a.fd.tier_blocks[tier], b = a.fd.tier_first[tier] + item % a.fd.tier_blocks[tier];
+    gi = f * a.fd.blocks + b;
+    cw = gi;
+    if (a.rx.decl[gi]) {
+      if (tg == 0) { a.its[gi] = -2; a.ok[gi] = 0; }
+      return;
+    }
+    const int s0 = a.fd.block_slot[b], nt = a.fd.tier_nt[tier];
+    const int8_t *sl = a.rx.llrf + f * a.rx.llr_stride + s0;
+    const uint8_t *wh = a.fd.white + s0;
+    const int16_t *perm = a.fd.perm[tier];
+    for (int i = tg; i < nt; i += GT) {
+      const int v = perm[i];
+      const int8_t x = sl[i];
+      const int8_t y = wh[i] ? (int8_t)(-x) : x;
+      L[lpos<C, PAIR>(v)] = y;
+    }
+    for (int v = LIZG_INFO_BITS + tg; v < T::K; v += GT) L[lpos<C, PAIR>(v)] = 127;
+  } else {
+    cw = a.list[item];
+    off = a.off[cw];
+    // LLRs in: data bits in code order, parity bit k + c (c = i mb + r) at [r][i].
+    const int4 *src = reinterpret_cast<const int4 *>(a.llr + off);
+    for (int t = tg; t < T::N / 16; t += GT) {
+      const int4 w = __ldg(src + t);
+      const int8_t *bb = reinterpret_cast<const int8_t *>(&w);
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        L[lpos<C, PAIR>(t * 16 + j)] = bb[j];
+      }
+    }
+  }
+  // messages cleared
+  int4 *rz = reinterpret_cast<int4 *>(R);
+  for (int t = tg; t < slots<C>() * 128 / 16; t += GT) rz[t] = make_int4(0, 0, 0, 0);
+  group_sync<WPC>(g);
+
+  int used = -1, first = 0;
+  for (int it = 0; it < a.max_iter; it++) {
+    for (int step = 0; step < T::MB; step++) {
+      const int r = (it & 1) ? T::MB - 1 - step : step;
+      if (PAIR && LOOP) layer_pair_loop<C, NP>(L, R, r, lane, sub * NP);
+      else if (PAIR) layer_pair<C, NP>(L, R, r, lane, sub * NP);
+      else if (LOOP) layer_loop<C, CPL>(L, R, r, lane, t0);
+      else layer<C, CPL>(L, R, r, lane, t0);
+      group_sync<WPC>(g);
+    }
+    // the count only where the stall rule reads it (after the first iteration and at stall_it), else a clear test
+    const bool counted = a.stall_it > 1 && (it == 0 || it == a.stall_it - 1);
+    int bad = PAIR ? unsat_pair<C, NP>(L, lane, sub * NP, counted, it & 1) : unsat<C, CPL>(L, lane, t0, counted, it & 1);
+    if (WPC > 1) {
+      if (lane == 0) red[sub] = bad;
+      group_sync<WPC>(g);
+      bad = 0;
+#pragma unroll
+      for (int w = 0; w < WPC; w++) bad += red[w];
+      group_sync<WPC>(g);
+    }
+    if (bad == 0) { used = it + 1; break; }
+    if (a.stall_it > 1 && it == a.stall_it - 1) {
+      if ((float)bad > __fmul_rn(a.stall_ratio, (float)first)) { used = -3; break; }
+    } else if (it == 0 && a.stall_it > 1) first = bad;
+  }
+
+  // Hard bits packed MSB first into the message area (no longer needed), then the CRC over the block's bytes.
+  uint8_t *pk = reinterpret_cast<uint8_t *>(R);
+  for (int j = tg; j < T::N / 8; j += GT) {
+    int byte = 0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const int v = 8 * j + t;
+      const int16_t x = L[lpos<C, PAIR>(v)];
+      byte = (byte << 1) | (x < 0);
+    }
+    pk[j] = (uint8_t)byte;
+  }
+  group_sync<WPC>(g);
+  if (sub == 0) {
+    const int s0 = 15 * lane, s1 = min(s0 + 15, kBlockBytes);
+    uint32_t c = 0;
+    for (int j = s0; j < s1; j++) c = crc_tab[(c ^ pk[j]) & 255u] ^ (c >> 8);
+    c = gf_mul(c, crc_k[lane]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c ^= __shfl_xor_sync(0xffffffffu, c, o);
+    const uint32_t crc = ~(c ^ crc_k[32]);
+    const uint32_t want = (uint32_t)pk[476] << 24 | (uint32_t)pk[477] << 16 | (uint32_t)pk[478] << 8 | pk[479];
+    // the batch reports the CRC of whatever was decided; the receiver verifies only decoded blocks (its > 0)
+    if (lane == 0) { a.its[cw] = used; a.ok[cw] = (a.rx.llrf ? used > 0 : true) && crc == want; }
+  }
+  if (a.rx.llrf) {
+    // the block's 476 bytes, verified or not (ok says which)
+    uint8_t *dst = a.rx.blocks + (int64_t)gi * kBlockBytes;
+    for (int t = tg; t < kBlockBytes; t += GT) dst[t] = pk[t];
+  } else {
+    int4 *dst = reinterpret_cast<int4 *>(a.bits + off / 8);
+    const int4 *pv = reinterpret_cast<const int4 *>(pk);
+    for (int t = tg; t < T::N / 128; t += GT) dst[t] = pv[t];
+  }
+  group_sync<WPC>(g);
+}
+
+// The per-code persistent kernel: every group pulls codewords of the launch's code from its work counter.
+template <int C, int WPC, bool LOOP, bool PAIR>
+__global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(LdpcLaunch a) {
+  using T = Code<C>;
   static_assert(cta_threads<C, WPC>() <= 1024, "a CTA of at most 1024 threads");
   static_assert(T::WARPS <= 15, "one named barrier a codeword");
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int s_item[T::WARPS], s_red[T::WARPS][WPC];
   uint32_t *crc_tab = reinterpret_cast<uint32_t *>(smem);
   uint32_t *crc_k = crc_tab + 256;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = warp / WPC, sub = warp % WPC, tg = sub * 32 + lane, t0 = sub * CPL;
-  int16_t *L = reinterpret_cast<int16_t *>(smem + kCrcBytes + g * warp_bytes<C>());
-  int8_t *R = reinterpret_cast<int8_t *>(L + T::N);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = warp / WPC, sub = warp % WPC, tg = sub * 32 + lane;
+  uint8_t *slice = smem + kCrcBytes + g * warp_bytes<C>();
   for (int t = threadIdx.x; t < 256; t += blockDim.x) {
     uint32_t c = (uint32_t)t;
     for (int k = 0; k < 8; k++) c = (c >> 1) ^ (kCrcPoly & (0u - (c & 1u)));
@@ -559,120 +678,57 @@ __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(L
   }
   for (int t = threadIdx.x; t < 33; t += blockDim.x) crc_k[t] = c_crc_shift[t];
   __syncthreads();
+  (void)lane;
   const int count = a.count_dev ? *a.count_dev : a.count;
-
   for (;;) {
     if (tg == 0) s_item[g] = atomicAdd(a.counter, 1);
     group_sync<WPC>(g);
     const int item = s_item[g];
     group_sync<WPC>(g);   // every warp of the codeword has read it before its next write
     if (item >= count) break;
-    int cw, gi = 0;
-    int64_t off = 0;
-    if (a.rx.llrf) {
-      // Receiver mode: item -> (frame, block) of this tier. A declined block is not tried (its -2). Otherwise its
-      // slots' soft values go through the bit map into codeword order, whitening taken off by sign, the never-sent
-      // bits at 0 and the 7/8 code's known zeros past the block's 3840 bits at 127
-      // (liblizard/src/lizard_phy.c:156-192, 1818-1823).
-      const int f = item / a.fd.tier_blocks[a.tier], b = a.fd.tier_first[a.tier] + item % a.fd.tier_blocks[a.tier];
-      gi = f * a.fd.blocks + b;
-      cw = gi;
-      if (a.rx.decl[gi]) {
-        if (tg == 0) { a.its[gi] = -2; a.ok[gi] = 0; }
-        continue;
-      }
-      const int s0 = a.fd.block_slot[b], nt = a.fd.tier_nt[a.tier];
-      const int8_t *sl = a.rx.llrf + f * a.rx.llr_stride + s0;
-      const uint8_t *wh = a.fd.white + s0;
-      const int16_t *perm = a.fd.perm[a.tier];
-      for (int i = tg; i < nt; i += GT) {
-        const int v = perm[i];
-        const int8_t x = sl[i];
-        const int8_t y = wh[i] ? (int8_t)(-x) : x;
-        L[lpos<C, PAIR>(v)] = y;
-      }
-      for (int v = LIZG_INFO_BITS + tg; v < T::K; v += GT) L[lpos<C, PAIR>(v)] = 127;
-    } else {
-      cw = a.list[item];
-      off = a.off[cw];
-      // LLRs in: data bits in code order, parity bit k + c (c = i mb + r) at [r][i].
-      const int4 *src = reinterpret_cast<const int4 *>(a.llr + off);
-      for (int t = tg; t < T::N / 16; t += GT) {
-        const int4 w = __ldg(src + t);
-        const int8_t *bb = reinterpret_cast<const int8_t *>(&w);
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-          L[lpos<C, PAIR>(t * 16 + j)] = bb[j];
-        }
-      }
-    }
-    // messages cleared
-    int4 *rz = reinterpret_cast<int4 *>(R);
-    for (int t = tg; t < slots<C>() * 128 / 16; t += GT) rz[t] = make_int4(0, 0, 0, 0);
-    group_sync<WPC>(g);
+    decode_item<C, WPC, LOOP, PAIR>(a, a.tier, item, slice, crc_tab, crc_k, s_red[g], g);
+  }
+}
 
-    int used = -1, first = 0;
-    for (int it = 0; it < a.max_iter; it++) {
-      for (int step = 0; step < T::MB; step++) {
-        const int r = (it & 1) ? T::MB - 1 - step : step;
-        if (PAIR && LOOP) layer_pair_loop<C, NP>(L, R, r, lane, sub * NP);
-        else if (PAIR) layer_pair<C, NP>(L, R, r, lane, sub * NP);
-        else if (LOOP) layer_loop<C, CPL>(L, R, r, lane, t0);
-        else layer<C, CPL>(L, R, r, lane, t0);
-        group_sync<WPC>(g);
-      }
-      // the count only where the stall rule reads it (after the first iteration and at stall_it), else a clear test
-      const bool counted = a.stall_it > 1 && (it == 0 || it == a.stall_it - 1);
-      int bad = PAIR ? unsat_pair<C, NP>(L, lane, sub * NP, counted, it & 1) : unsat<C, CPL>(L, lane, t0, counted, it & 1);
-      if (WPC > 1) {
-        if (lane == 0) s_red[g][sub] = bad;
-        group_sync<WPC>(g);
-        bad = 0;
-#pragma unroll
-        for (int w = 0; w < WPC; w++) bad += s_red[g][w];
-        group_sync<WPC>(g);
-      }
-      if (bad == 0) { used = it + 1; break; }
-      if (a.stall_it > 1 && it == a.stall_it - 1) {
-        if ((float)bad > __fmul_rn(a.stall_ratio, (float)first)) { used = -3; break; }
-      } else if (it == 0 && a.stall_it > 1) first = bad;
+// The receiver's decode in one persistent launch across its tiers (every code): a queue of (tier, block) items, the
+// tiers of the longer codes first, pulled by groups of two warps, each item decoded by its code's form (the pair form
+// with the loop for 7/8, messages in registers for the others) in a slice sized for the longest code. One launch in
+// place of a launch a tier on forked streams: for the small batches where the launches and their tails are the cost.
+constexpr int cmax(int x, int y) { return x > y ? x : y; }
+constexpr int kMixSlice = cmax(cmax(warp_bytes<0>(), warp_bytes<1>()), cmax(warp_bytes<2>(), warp_bytes<3>()));
+constexpr int kMixWpc = 2, kMixGroups = (227 * 1024 - kCrcBytes) / kMixSlice, kMixThreads = kMixGroups * kMixWpc * 32;
+static_assert(kMixGroups >= 1 && kMixGroups <= 15, "groups of the mixed launch");
+__global__ void __launch_bounds__(kMixThreads, 1) ldpc_mixed_kernel(LdpcMix m) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int s_item[kMixGroups], s_red[kMixGroups][kMixWpc];
+  uint32_t *crc_tab = reinterpret_cast<uint32_t *>(smem);
+  uint32_t *crc_k = crc_tab + 256;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = warp / kMixWpc, sub = warp % kMixWpc, tg = sub * 32 + lane;
+  uint8_t *slice = smem + kCrcBytes + g * kMixSlice;
+  for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+    uint32_t c = (uint32_t)t;
+    for (int k = 0; k < 8; k++) c = (c >> 1) ^ (kCrcPoly & (0u - (c & 1u)));
+    crc_tab[t] = c;
+  }
+  for (int t = threadIdx.x; t < 33; t += blockDim.x) crc_k[t] = c_crc_shift[t];
+  __syncthreads();
+  (void)lane;
+  const int total = m.first[4];
+  for (;;) {
+    if (tg == 0) s_item[g] = atomicAdd(m.counter, 1);
+    group_sync<kMixWpc>(g);
+    const int item = s_item[g];
+    group_sync<kMixWpc>(g);
+    if (item >= total) break;
+    int seg = 0;
+    while (seg < 3 && item >= m.first[seg + 1]) seg++;
+    const int tier = m.tier[seg], local = item - m.first[seg];
+    switch (m.code[seg]) {
+      case 0: decode_item<0, kMixWpc, true, true>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      case 1: decode_item<1, kMixWpc, false, false>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      case 2: decode_item<2, kMixWpc, false, false>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      default: decode_item<3, kMixWpc, false, false>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
     }
-
-    // Hard bits packed MSB first into the message area (no longer needed), then the CRC over the block's bytes.
-    uint8_t *pk = reinterpret_cast<uint8_t *>(R);
-    for (int j = tg; j < T::N / 8; j += GT) {
-      int byte = 0;
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        const int v = 8 * j + t;
-        const int16_t x = L[lpos<C, PAIR>(v)];
-        byte = (byte << 1) | (x < 0);
-      }
-      pk[j] = (uint8_t)byte;
-    }
-    group_sync<WPC>(g);
-    if (sub == 0) {
-      const int s0 = 15 * lane, s1 = min(s0 + 15, kBlockBytes);
-      uint32_t c = 0;
-      for (int j = s0; j < s1; j++) c = crc_tab[(c ^ pk[j]) & 255u] ^ (c >> 8);
-      c = gf_mul(c, crc_k[lane]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) c ^= __shfl_xor_sync(0xffffffffu, c, o);
-      const uint32_t crc = ~(c ^ crc_k[32]);
-      const uint32_t want = (uint32_t)pk[476] << 24 | (uint32_t)pk[477] << 16 | (uint32_t)pk[478] << 8 | pk[479];
-      // the batch reports the CRC of whatever was decided; the receiver verifies only decoded blocks (its > 0)
-      if (lane == 0) { a.its[cw] = used; a.ok[cw] = (a.rx.llrf ? used > 0 : true) && crc == want; }
-    }
-    if (a.rx.llrf) {
-      // the block's 476 bytes, verified or not (ok says which)
-      uint8_t *dst = a.rx.blocks + (int64_t)gi * kBlockBytes;
-      for (int t = tg; t < kBlockBytes; t += GT) dst[t] = pk[t];
-    } else {
-      int4 *dst = reinterpret_cast<int4 *>(a.bits + off / 8);
-      const int4 *pv = reinterpret_cast<const int4 *>(pk);
-      for (int t = tg; t < T::N / 128; t += GT) dst[t] = pv[t];
-    }
-    group_sync<WPC>(g);
   }
 }
 
@@ -783,6 +839,17 @@ cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st)
 }
 
 int ldpc_variant_count(int code) { return code >= 0 && code <= 3 ? variant_count(code) : 0; }
+
+cudaError_t ldpc_mixed_launch(const LdpcMix &m, int sms, cudaStream_t st) {
+  if (m.first[4] <= 0) return cudaSuccess;
+  static SmemOptIn opt;
+  constexpr int smem = kCrcBytes + kMixGroups * kMixSlice;
+  static_assert(smem <= 227 * 1024, "the mixed launch's slices fit");
+  if (cudaError_t e = opt.set(reinterpret_cast<const void *>(ldpc_mixed_kernel), smem)) return e;
+  const int need = (m.first[4] + kMixGroups - 1) / kMixGroups;
+  ldpc_mixed_kernel<<<need < sms ? need : sms, kMixThreads, smem, st>>>(m);
+  return cudaGetLastError();
+}
 int ldpc_choice(int code) { return code >= 0 && code <= 3 ? choice_of(code) : 0; }
 
 cudaError_t ldpc_launch_variant(int code, int v, const LdpcLaunch &a, int sms, cudaStream_t st) {

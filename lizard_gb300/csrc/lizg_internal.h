@@ -177,6 +177,15 @@ cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, in
                                const int *d_lens_on = nullptr, const uint8_t *d_active = nullptr);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
+// The receiver's decode of every tier in one persistent launch: a queue of segments, segment s items
+// [first[s], first[s + 1]) of tier tier[s] (code code[s]); a's receiver fields (its, ok, rx, fd, the stop rule) as a
+// tier's launch takes them (its count, counter and tier unused); counter zero at launch.
+struct LdpcMix {
+  LdpcLaunch a;
+  int first[5], tier[4], code[4];
+  int *counter;
+};
+cudaError_t ldpc_mixed_launch(const LdpcMix &m, int sms, cudaStream_t st);
 // The decoder's kernel variants of a code (all bit for bit alike), and a launch of variant v of them.
 int ldpc_variant_count(int code);
 int ldpc_choice(int code);   // the device's choice for the code (lizg_ldpc_autotune, lizg_ldpc_set_variant)

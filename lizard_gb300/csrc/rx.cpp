@@ -44,6 +44,7 @@ struct lizg_rx {
   cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
   int launches = 0;
   int variant[4] = {-1, -1, -1, -1};   // each tier's LDPC kernel variant (lizg_rx_autotune), -1: the global choice
+  int mixed = 0;                        // 1: every tier's decode in one persistent launch (lizg_rx_set_ldpc_mixed)
   std::vector<void *> owned;
   // the captured pipeline of lizg_rx_finish_luma_graph and the call it was captured for
   cudaStream_t cap = nullptr;
@@ -293,6 +294,53 @@ int lizg_rx_set_read(lizg_rx *r, int read) {
   return was;
 }
 
+// Row (d) and (e) on a batch's soft values: the LDPC decode and CRC of every block not declined, a launch a tier on
+// the tiers' own streams (forked from st, joined back), or every tier in one persistent launch (r->mixed).
+static int rx_ldpc(lizg_rx *r, const lizg::FmtDev &fd, int frames, int8_t *llrf, const lizg_rx_out *out, cudaStream_t st, int sms) {
+  const lizg::Format &f = r->f;
+  const int64_t need = (int64_t)f.subch * lizg::kSub;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(r->counters, 0, 4 * sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(r->fork, st)) != cudaSuccess)
+    return lizg::record_error(LIZG_E_CUDA, (std::string("rx fork: ") + cudaGetErrorString(e)).c_str());
+  if (r->mixed) {
+    // every tier in one launch on the caller's stream, the longer codes' tiers first
+    lizg::LdpcMix m{};
+    m.a.its = out->its; m.a.ok = out->ok;
+    m.a.max_iter = 30; m.a.stall_it = 9; m.a.stall_ratio = 0.95f;
+    m.a.rx.llrf = llrf; m.a.rx.decl = r->decl; m.a.rx.blocks = out->blocks; m.a.rx.llr_stride = 2 * need;
+    m.a.fd = fd;
+    int order[4], no = 0;
+    for (int c = 3; c >= 0; c--)
+      for (int t = 0; t < f.tiers; t++) if (f.tier[t].code == c) order[no++] = t;
+    m.first[0] = 0;
+    for (int sgm = 0; sgm < 4; sgm++) {
+      const int t = sgm < no ? order[sgm] : -1;
+      m.tier[sgm] = t < 0 ? 0 : t; m.code[sgm] = t < 0 ? 0 : f.tier[t].code;
+      m.first[sgm + 1] = m.first[sgm] + (t < 0 ? 0 : frames * f.tier[t].blocks);
+    }
+    m.counter = r->counters;
+    if ((e = lizg::ldpc_mixed_launch(m, sms, st)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_CUDA, (std::string("rx LDPC: ") + cudaGetErrorString(e)).c_str());
+    r->launches++;
+    return 0;
+  }
+  for (int t = 0; t < f.tiers; t++) {
+    lizg::LdpcLaunch a{};
+    a.its = out->its; a.ok = out->ok;
+    a.count = frames * f.tier[t].blocks; a.counter = r->counters + t;
+    a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // the receiver's (liblizard/src/lizard_phy.c:80-82, 1824)
+    a.rx.llrf = llrf; a.rx.decl = r->decl; a.rx.blocks = out->blocks; a.rx.llr_stride = 2 * need;
+    a.fd = fd; a.tier = t;
+    if ((e = cudaStreamWaitEvent(r->side[t], r->fork, 0)) != cudaSuccess ||
+        (e = (r->variant[t] >= 0 ? lizg::ldpc_launch_variant(f.tier[t].code, r->variant[t], a, sms, r->side[t])
+                                 : lizg::ldpc_launch(f.tier[t].code, a, sms, r->side[t]))) != cudaSuccess ||
+        (e = cudaEventRecord(r->join[t], r->side[t])) != cudaSuccess || (e = cudaStreamWaitEvent(st, r->join[t], 0)) != cudaSuccess)
+      return lizg::record_error(LIZG_E_CUDA, (std::string("rx LDPC: ") + cudaGetErrorString(e)).c_str());
+    r->launches++;
+  }
+  return 0;
+}
+
 // Rows (c), (d), (e) on a batch of spectra (spec: frame f's coefficient i, pos order, at spec[f stride + i]):
 // the pilots' fit, the soft values, the block stage, then the LDPC and CRC of every block not declined, the four
 // codes on their own streams.
@@ -309,23 +357,7 @@ static int finish_spec(lizg_rx *r, const float2 *spec, int64_t stride, int frame
   cudaError_t e = lizg::demap_launch(fd, spec, stride, align, llrf, sub_est, sub_rms, est, pilot, r->decl, st);
   if (e != cudaSuccess) return lizg::record_error(LIZG_E_CUDA, (std::string("demap: ") + cudaGetErrorString(e)).c_str());
   r->launches += 3;
-  if ((e = cudaMemsetAsync(r->counters, 0, 4 * sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(r->fork, st)) != cudaSuccess)
-    return lizg::record_error(LIZG_E_CUDA, (std::string("rx fork: ") + cudaGetErrorString(e)).c_str());
-  for (int t = 0; t < f.tiers; t++) {
-    lizg::LdpcLaunch a{};
-    a.its = out->its; a.ok = out->ok;
-    a.count = frames * f.tier[t].blocks; a.counter = r->counters + t;
-    a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // the receiver's (liblizard/src/lizard_phy.c:80-82, 1824)
-    a.rx.llrf = llrf; a.rx.decl = r->decl; a.rx.blocks = out->blocks; a.rx.llr_stride = 2 * need;
-    a.fd = fd; a.tier = t;
-    if ((e = cudaStreamWaitEvent(r->side[t], r->fork, 0)) != cudaSuccess ||
-        (e = (r->variant[t] >= 0 ? lizg::ldpc_launch_variant(f.tier[t].code, r->variant[t], a, sms, r->side[t])
-                                 : lizg::ldpc_launch(f.tier[t].code, a, sms, r->side[t]))) != cudaSuccess ||
-        (e = cudaEventRecord(r->join[t], r->side[t])) != cudaSuccess || (e = cudaStreamWaitEvent(st, r->join[t], 0)) != cudaSuccess)
-      return lizg::record_error(LIZG_E_CUDA, (std::string("rx LDPC: ") + cudaGetErrorString(e)).c_str());
-    r->launches++;
-  }
-  return 0;
+  return rx_ldpc(r, fd, frames, llrf, out, st, sms);
 }
 
 static int check_call(lizg_rx *r, const void *in, int frames, const lizg_rx_out *out, const char *who, int *sms) {
@@ -434,7 +466,7 @@ int lizg_rx_finish_luma_graph(lizg_rx *r, const uint8_t *d_luma, int w, int h, i
                                       (uintptr_t)out->est, (uintptr_t)out->pilot, (uintptr_t)out->align, (uintptr_t)out->llrf,
                                       (uintptr_t)out->sub_est, (uintptr_t)out->sub_rms, (uintptr_t)d_grid, (uintptr_t)d_coef, (uintptr_t)r->sd.read,
                                       (uintptr_t)(r->variant[0] + 1), (uintptr_t)(r->variant[1] + 1), (uintptr_t)(r->variant[2] + 1),
-                                      (uintptr_t)(r->variant[3] + 1)};
+                                      (uintptr_t)(r->variant[3] + 1), (uintptr_t)r->mixed};
   cudaError_t e;
   if (!r->graph || key != r->graph_key) {
     if (r->graph) { cudaGraphExecDestroy(r->graph); r->graph = nullptr; }
@@ -504,6 +536,13 @@ int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int 
   return verified;
 }
 
+int lizg_rx_set_ldpc_mixed(lizg_rx *r, int mixed) {
+  if (!r || (mixed != 0 && mixed != 1)) return lizg::record_error(LIZG_E_ARG, "lizg_rx_set_ldpc_mixed: no handle, or not 0 or 1");
+  const int was = r->mixed;
+  r->mixed = mixed;
+  return was;
+}
+
 int lizg_rx_variant(const lizg_rx *r, int tier) {
   if (!r || tier < 0 || tier >= r->f.tiers) return lizg::record_error(LIZG_E_ARG, "lizg_rx_variant: no handle or no such tier");
   return r->variant[tier] >= 0 ? r->variant[tier] : lizg::ldpc_choice(r->f.tier[tier].code);
@@ -531,6 +570,7 @@ int lizg_rx_autotune(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch,
   if (e == cudaSuccess) {
     // the soft values of the batch, in the handle's own buffers
     for (int t = 0; t < 4; t++) r->variant[t] = -1;
+    r->mixed = 0;
     const lizg_rx_out out{blocks, ok, its, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     rc = lizg_rx_finish_luma_dev(r, d_luma, w, h, pitch, frame_stride, d_reg, frames, &out, nullptr, nullptr, stream);
     const lizg::FmtDev fd = fmt_dev(r, frames);
@@ -556,8 +596,26 @@ int lizg_rx_autotune(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch,
         if (e == cudaSuccess && (best[t] < 0 || ms_min < best_ms)) { best[t] = v; best_ms = ms_min; }
       }
     }
+    // then the whole decode stage with those variants, a launch a tier on forked streams against one persistent launch
+    // across the tiers; the faster kept
+    float stage_ms[2] = {0, 0};
+    for (int mixed = 0; mixed < 2 && !rc && e == cudaSuccess; mixed++) {
+      for (int t = 0; t < 4; t++) r->variant[t] = t < f.tiers ? best[t] : -1;
+      r->mixed = mixed;
+      const lizg_rx_out out{blocks, ok, its, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+      for (int rep = 0; rep < 4 && !rc && e == cudaSuccess; rep++) {
+        if ((e = cudaEventRecord(e0, st)) != cudaSuccess) break;
+        if ((rc = rx_ldpc(r, fd, frames, r->llrf, &out, st, sms))) break;
+        if ((e = cudaEventRecord(e1, st)) != cudaSuccess || (e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep == 1 || (rep > 1 && ms < stage_ms[mixed])) stage_ms[mixed] = ms;
+      }
+    }
+    r->mixed = stage_ms[1] < stage_ms[0] ? 1 : 0;
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   }
+  if (rc || e != cudaSuccess) r->mixed = 0;
   cudaFree(blocks); cudaFree(ok); cudaFree(its);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

@@ -58,3 +58,22 @@ def test_finish_coef_matches_oracle(n, subch, frames, shift, sigma):
         ok = out["ok"][f].astype(bool)
         assert np.array_equal(out["blocks"][f][ok], blocks[f][ok])
     assert rx.launches == 3 + fmt.tiers
+
+
+@pytest.mark.parametrize("n,subch,frames,sigma", [(384, 64, 3, 3.0), (768, 320, 4, 60.0), (1536, 1024, 2, 3.0)])
+def test_mixed_decode_matches_per_tier(n, subch, frames, sigma):
+    """The decode stage in one persistent launch across the tiers (lizg_rx_set_ldpc_mixed) against a launch a tier:
+    the same blocks, verdicts and iterations (declined, stalled and capped blocks included at the noisy size)."""
+    fmt = lz.Format(n, subch, 128)
+    grids, _ = synth.grids(fmt, frames, seed=n + 7, sigma=sigma)
+    rx = lz.Receiver(n, subch, 128, max_frames=frames)
+    assert rx.set_ldpc_mixed(0) == 0
+    a = rx.finish_grid(grids)
+    assert rx.launches == 4 + 3 + fmt.tiers
+    assert rx.set_ldpc_mixed(1) == 0
+    b = rx.finish_grid(grids)
+    assert rx.launches == 4 + 3 + 1
+    for k in ("blocks", "ok", "its", "llrf", "est"):
+        assert np.array_equal(a[k], b[k]), k
+    if sigma > 10:
+        assert (a["its"] < 0).any() and (a["ok"] == 1).any()
