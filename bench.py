@@ -324,7 +324,10 @@ def bench_receiver(args, stream):
     ok_global = [b[2]["ok"].clone() for b in bufs]
     choices = {}
     for rx, (d_l, d_r, o, s, n) in zip(rxs, bufs):
-        choices[str(n)] = rx.autotune_dev(d_l.data_ptr(), n, n, n, n * n, d_r.data_ptr(), per, sp)[:rx.fmt.tiers]
+        v = rx.autotune_dev(d_l.data_ptr(), n, n, n, n * n, d_r.data_ptr(), per, sp)[:rx.fmt.tiers]
+        mixed = rx.set_ldpc_mixed(0)
+        rx.set_ldpc_mixed(mixed)
+        choices[str(n)] = {"variants": v, "one_launch_across_tiers": bool(mixed)}
     ms = timed()
     ok = sum(int(b[2]["ok"].sum().item()) for b in bufs)
     same = all(bool(torch.equal(a, b[2]["ok"])) for a, b in zip(ok_global, bufs))
@@ -333,7 +336,7 @@ def bench_receiver(args, stream):
                               "frames_per_s": round(256 / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
                               "ms_per_step": round(ms, 3), "blocks_verified": ok, "blocks": blocks_total,
                               "gpu_launches_per_step": sum(rx.launches for rx in rxs),
-                              "ldpc_per_n_and_rate": {"variants_per_tier": choices, "frames_per_s_device_choice": round(256 / (ms_global / 1e3), 1),
+                              "ldpc_per_n_and_rate": {"per_n": choices, "frames_per_s_device_choice": round(256 / (ms_global / 1e3), 1),
                                                       "identical_verdicts": same}}
     peak, peak_src = peaks()
     res["fft_demod_batch"]["error_per_n"] = fft_error_table()
