@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--fmt-only", action="store_true", help="time only the format word and the border nodes (profiling)")
     ap.add_argument("--encode-only", action="store_true", help="time only the sender on the GPU (profiling)")
     ap.add_argument("--refine-only", action="store_true", help="time only the distorted captures' registration comparison")
+    ap.add_argument("--multistream-only", action="store_true", help="time only the multi-stream tick (profiling)")
     ap.add_argument("--refine-frames", type=int, default=0, help="with --refine-only: the first K frames of the spread set alone "
                     "(profiling; 0: the configuration's three sets)")
     ap.add_argument("--ldpc-variants", action="store_true", help="time every decoder kernel variant of every code on the "
@@ -1224,6 +1225,9 @@ def main():
         tune = {"variant": {name: {"index": v, "warps_a_codeword": lz.ldpc_variant(r)[1], "loop_form": lz.ldpc_variant(r)[2], "pair_form": lz.ldpc_variant(r)[3]}
                             for name, r, v in zip(("7/8", "3/4", "2/3", "1/2"), (6, 4, 3, 2), chosen)},
                 "seconds": round(time.perf_counter() - t_tune, 2), "calibration": "8192 codewords a code, all-zero codeword, BPSK/AWGN over the workload's Eb/N0 sweep"}
+    if args.multistream_only:
+        print(json.dumps({"receiver": {"multistream": bench_multistream(args, torch.cuda.current_stream())}}))
+        return
     if args.receiver_only:
         st = torch.cuda.current_stream()
         rec = bench_receiver(args, st)

@@ -84,114 +84,130 @@ __device__ bool warp_gj(double (*A)[kLP + 1], int p, double thresh, double *s_f,
   return true;
 }
 
-// lensm_fit's models over the points (liblizard/src/acquire.c:1651-1668) on a warp, from its summed normal equations
-// sA (upper triangle and right side; n of the np points not dropped): for K = 0..3 radial terms the system of 8 + K
-// unknowns solved (warp_gj), each point's model value on its own lane, the residuals' sum over the points in order on
-// lane 0, AICc; the least kept. Out (shared): tb the coefficients, K (-1 where none solved).
-__device__ void warp_models(int np, int n, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const uint8_t *drop, double (*sA)[kLP + 1],
-                            double (*A)[kLP + 1], double *s_f, double *s_t, double *s_tb, double (*s_pt)[2], int *s_piv, int *s_K) {
-  const int lane = threadIdx.x & 31;
-  if (lane == 0) {
-    for (int p = 1; p < kLP; p++) for (int q = 0; q < p; q++) sA[p][q] = sA[q][p];
-    *s_K = -1;
-    for (int c = 0; c < kLP; c++) s_tb[c] = 0;
+// A fitting block: 4 warps, one a model of K = 0..3 radial terms.
+constexpr int kFitThreads = 128;
+struct FitScratch {
+  double A[4][kLP][kLP + 1];
+  double f[4][kLP], t[4][kLP], term[4][kMaxPts], aicc[4], tb[kLP];
+  int ok[4], piv[4][2], K;
+};
+
+// lensm_fit's models over the points (liblizard/src/acquire.c:1651-1668) from its summed normal equations sA (upper
+// triangle and right side; n of the np points not dropped), on a block of kFitThreads: warp k solves the system of
+// 8 + k unknowns (warp_gj), its lanes each point's residual term, its lane 0 their sum over the points in order and
+// AICc; thread 0 keeps the least in the order k = 0..3. Out: F.tb, F.K (-1 where none solved).
+__device__ void block_models(int np, int n, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const uint8_t *drop, double (*sA)[kLP + 1],
+                             FitScratch &F) {
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < kLP * kLP; e += blockDim.x) {
+    const int p = e / kLP, q = e - p * kLP;
+    if (p > q) sA[p][q] = sA[q][p];
   }
-  __syncwarp();
-  double best = INFINITY;   // lane 0's
-  for (int k = 0; k <= 3; k++) {
-    const int p = 8 + k;
+  __syncthreads();
+  if (w < 4) {
+    const int k = w, p = 8 + k;
+    double (*A)[kLP + 1] = F.A[k];
     for (int e = lane; e < kLP * (kLP + 1); e += 32) {
       const int r = e / (kLP + 1), c = e - r * (kLP + 1);
       A[r][c] = sA[r][c] + (r == c && c < p ? 1e-12 : 0.0);
     }
     __syncwarp();
-    if (2 * n - p - 1 <= 0) continue;
-    if (!warp_gj(A, p, 1e-14, s_f, s_piv)) continue;
-    for (int c = lane; c < kLP; c += 32) s_t[c] = c < p ? A[c][kLP] / A[c][c] : 0.0;
-    __syncwarp();
-    for (int i = lane; i < np; i += 32) {
-      if (drop && drop[i]) continue;
-      double fx = 0, fy = 0;
-      for (int c = 0; c < p; c++) { fx += s_t[c] * rx[i][c]; fy += s_t[c] * ry[i][c]; }
-      s_pt[i][0] = fx; s_pt[i][1] = fy;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      double rss = 0;
-      for (int i = 0; i < np; i++) {
+    const bool ok = 2 * n - p - 1 > 0 && warp_gj(A, p, 1e-14, F.f[k], F.piv[k]);
+    if (ok) {
+      for (int c = lane; c < kLP; c += 32) F.t[k][c] = c < p ? A[c][kLP] / A[c][c] : 0.0;
+      __syncwarp();
+      for (int i = lane; i < np; i += 32) {
         if (drop && drop[i]) continue;
-        const double fx = s_pt[i][0], fy = s_pt[i][1];
-        rss += (d[i][0] - fx) * (d[i][0] - fx) + (d[i][1] - fy) * (d[i][1] - fy);
+        double fx = 0, fy = 0;
+        for (int c = 0; c < p; c++) { fx += F.t[k][c] * rx[i][c]; fy += F.t[k][c] * ry[i][c]; }
+        F.term[k][i] = (d[i][0] - fx) * (d[i][0] - fx) + (d[i][1] - fy) * (d[i][1] - fy);
       }
-      const double n2 = 2.0 * n, aicc = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
-      if (aicc < best) { best = aicc; *s_K = k; for (int c = 0; c < kLP; c++) s_tb[c] = s_t[c]; }
+      __syncwarp();
+      if (lane == 0) {
+        double rss = 0;
+        for (int i = 0; i < np; i++)
+          if (!(drop && drop[i])) rss += F.term[k][i];
+        const double n2 = 2.0 * n;
+        F.aicc[k] = n2 * log(rss / n2 + 1e-30) + 2.0 * p + 2.0 * p * (p + 1) / (n2 - p - 1);
+      }
     }
-    __syncwarp();
+    if (lane == 0) F.ok[k] = ok;
   }
+  __syncthreads();
+  if (tid == 0) {
+    double best = INFINITY;
+    F.K = -1;
+    for (int c = 0; c < kLP; c++) F.tb[c] = 0;
+    for (int k = 0; k <= 3; k++)
+      if (F.ok[k] && F.aicc[k] < best) { best = F.aicc[k]; F.K = k; for (int c = 0; c < kLP; c++) F.tb[c] = F.t[k][c]; }
+  }
+  __syncthreads();
 }
 
-__global__ void __launch_bounds__(32) lens_fit_kernel(FitArgs a) {
-  const int f = blockIdx.x, lane = threadIdx.x;
-  if (a.gate && !a.gate[f]) {
-    if (lane == 0) a.have[f] = 0;
-    return;
-  }
-  __shared__ double s_rx[kMaxPts][kLP], s_ry[kMaxPts][kLP], s_d[kMaxPts][2], s_A[kLP][kLP + 1], A[kLP][kLP + 1];
-  __shared__ int s_np;
-  __shared__ float s_h[9];
-  if (lane < 9) s_h[lane] = a.reg[(int64_t)f * a.hstride + lane];
-  __syncwarp();
-  const double ax = a.ax, ay = a.ay, R = a.R;
-  if (lane == 0) {
-    // the points in the reference's order: the four corner nodes, then the anchors found in row-major order
-    int np = 0;
-    for (int c = 0; c < 4; c++) {
-      float u, v;
-      project_f(s_h, (c == 1 || c == 2) ? a.node_hi : a.node_lo, c >= 2 ? a.node_hi : a.node_lo, &u, &v);
-      rows_of((u - ax) / R, (v - ay) / R, s_rx[np], s_ry[np]);
-      s_d[np][0] = 0; s_d[np][1] = 0; np++;
-    }
-    const float ah = a.a * 0.5f;
-    for (int k = 0; k < kNA; k++) {
-      const int64_t o = (int64_t)f * kNA + k;
-      if (!a.ok[o]) continue;
-      const float X = (float)a.m0[k % 7] + ah, Y = (float)a.m0[k / 7] + ah;
-      float u, v;
-      project_f(s_h, X, Y, &u, &v);
-      rows_of((u - ax) / R, (v - ay) / R, s_rx[np], s_ry[np]);
-      s_d[np][0] = a.dx[o]; s_d[np][1] = a.dy[o]; np++;
-    }
-    s_np = np;
-  }
-  __syncwarp();
-  const int np = s_np;
-  // the normal equations' upper triangle and right side, each entry summed over the points in order
-  for (int e = lane; e < 77; e += 32) {
+// The normal equations' upper triangle and right side over the points not dropped (drop NULL: all), an entry a thread,
+// each summed over the points in their order.
+__device__ void block_normal(int np, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const uint8_t *drop, double (*sA)[kLP + 1]) {
+  for (int e = threadIdx.x; e < 77; e += blockDim.x) {
     int p, q;
     if (e < 66) { p = 0; int r = e; while (r >= kLP - p) { r -= kLP - p; p++; } q = p + r; }
     else { p = e - 66; q = kLP; }
     double acc = 0;
     for (int i = 0; i < np; i++)
-      acc += q < kLP ? s_rx[i][p] * s_rx[i][q] + s_ry[i][p] * s_ry[i][q] : s_rx[i][p] * s_d[i][0] + s_ry[i][p] * s_d[i][1];
-    s_A[p][q] = acc;
+      if (!(drop && drop[i])) acc += q < kLP ? rx[i][p] * rx[i][q] + ry[i][p] * ry[i][q] : rx[i][p] * d[i][0] + ry[i][p] * d[i][1];
+    sA[p][q] = acc;
   }
-  __syncwarp();
-  __shared__ double s_f[kLP], s_t[kLP], s_tb[kLP], s_pt[kMaxPts][2];
-  __shared__ int s_piv[2], s_K;
-  warp_models(np, np, s_rx, s_ry, s_d, nullptr, s_A, A, s_f, s_t, s_tb, s_pt, s_piv, &s_K);
-  if (lane != 0) return;
-  const int K = s_K;
-  double tb[kLP];
-  for (int c = 0; c < kLP; c++) tb[c] = s_tb[c];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kFitThreads) lens_fit_kernel(FitArgs a) {
+  const int f = blockIdx.x, tid = threadIdx.x;
+  if (a.gate && !a.gate[f]) {
+    if (tid == 0) a.have[f] = 0;
+    return;
+  }
+  __shared__ double s_rx[kMaxPts][kLP], s_ry[kMaxPts][kLP], s_d[kMaxPts][2], s_A[kLP][kLP + 1];
+  __shared__ FitScratch F;
+  __shared__ int s_np, s_at[kNA];
+  __shared__ float s_h[9];
+  if (tid < 9) s_h[tid] = a.reg[(int64_t)f * a.hstride + tid];
+  if (tid == 0) {
+    // the points in the reference's order: the four corner nodes, then the anchors found in row-major order
+    int np = 4;
+    for (int k = 0; k < kNA; k++) s_at[k] = a.ok[(int64_t)f * kNA + k] ? np++ : -1;
+    s_np = np;
+  }
+  __syncthreads();
+  const double ax = a.ax, ay = a.ay, R = a.R;
+  const float ah = a.a * 0.5f;
+  for (int t = tid; t < 4 + kNA; t += blockDim.x) {
+    float u, v;
+    if (t < 4) {
+      project_f(s_h, (t == 1 || t == 2) ? a.node_hi : a.node_lo, t >= 2 ? a.node_hi : a.node_lo, &u, &v);
+      rows_of((u - ax) / R, (v - ay) / R, s_rx[t], s_ry[t]);
+      s_d[t][0] = 0; s_d[t][1] = 0;
+    } else {
+      const int k = t - 4, i = s_at[k];
+      if (i < 0) continue;
+      const int64_t o = (int64_t)f * kNA + k;
+      project_f(s_h, (float)a.m0[k % 7] + ah, (float)a.m0[k / 7] + ah, &u, &v);
+      rows_of((u - ax) / R, (v - ay) / R, s_rx[i], s_ry[i]);
+      s_d[i][0] = a.dx[o]; s_d[i][1] = a.dy[o];
+    }
+  }
+  __syncthreads();
+  const int np = s_np;
+  block_normal(np, s_rx, s_ry, s_d, nullptr, s_A);
+  block_models(np, np, s_rx, s_ry, s_d, nullptr, s_A, F);
+  if (tid != 0) return;
   double *L = a.lens + (int64_t)f * kLStride;
-  if (K < 0) {   // no model: no displacement
+  if (F.K < 0) {   // no model: no displacement
     L[0] = 0; L[1] = ax; L[2] = ay; L[3] = R;
     for (int c = 0; c < kLP; c++) L[4 + c] = 0;
     a.have[f] = 0;
     return;
   }
-  L[0] = K; L[1] = ax; L[2] = ay; L[3] = R;
-  for (int c = 0; c < kLP; c++) L[4 + c] = tb[c];
+  L[0] = F.K; L[1] = ax; L[2] = ay; L[3] = R;
+  for (int c = 0; c < kLP; c++) L[4 + c] = F.tb[c];
   a.have[f] = 1;
 }
 
@@ -267,56 +283,44 @@ struct RegArgs {
 };
 
 // lensm_fit (liblizard/src/acquire.c:1630-1694) over np points whose rows (lens_rows at K = 3) are rx, ry, residuals
-// d, places qx, qy, on one warp: every lane takes entries of the normal equations (upper triangle and right side),
-// each summed over the points not dropped in their order; the models as warp_models fits them; with robust, every
-// point's distance from the model on its own lane, their median by ranks (each lane places its distances in the sorted
-// order), the verdicts on lane 0, and round again while a verdict changes (at most four rounds). lens (shared, 15)
-// receives the model (K, ax, ay, R, coefficients). Returns (on every lane) 1 where a model fitted.
-__device__ int warp_lensm_fit(int np, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const double *qx, const double *qy, uint8_t *drop,
-                              bool robust, double tau_floor, double ax, double ay, double R, double *lens, double (*sA)[kLP + 1],
-                              double (*A)[kLP + 1], double *res, int *s_flag) {
-  const int lane = threadIdx.x & 31;
-  __shared__ double s_f[kLP], s_t[kLP], s_tb[kLP], s_pt[kMaxPts][2], s_srt[kMaxPts];
-  __shared__ int s_piv[2], s_K;
+// d, places qx, qy, on a block of kFitThreads: the normal equations over the points not dropped (block_normal), the
+// models (block_models); with robust, every point's distance from the model on its own thread, their median by
+// ranks (each thread places its distances in the sorted order), the verdicts on thread 0, and round again while a
+// verdict changes (at most four rounds). lens (shared, 15) receives the model (K, ax, ay, R, coefficients). Returns
+// (on every thread) 1 where a model fitted.
+__device__ int block_lensm_fit(int np, double (*rx)[kLP], double (*ry)[kLP], double (*d)[2], const double *qx, const double *qy, uint8_t *drop,
+                               bool robust, double tau_floor, double ax, double ay, double R, double *lens, double (*sA)[kLP + 1],
+                               FitScratch &F, double *res, double *srt, int *s_flag) {
+  const int tid = threadIdx.x;
   int ok = 0;
   for (int round = 0; round < 4; round++) {
     int n = 0;
     for (int i = 0; i < np; i++) n += !drop[i];
-    for (int e = lane; e < 77; e += 32) {
-      int p, q;
-      if (e < 66) { p = 0; int r = e; while (r >= kLP - p) { r -= kLP - p; p++; } q = p + r; }
-      else { p = e - 66; q = kLP; }
-      double acc = 0;
-      for (int i = 0; i < np; i++)
-        if (!drop[i]) acc += q < kLP ? rx[i][p] * rx[i][q] + ry[i][p] * ry[i][q] : rx[i][p] * d[i][0] + ry[i][p] * d[i][1];
-      sA[p][q] = acc;
-    }
-    __syncwarp();
-    warp_models(np, n, rx, ry, d, drop, sA, A, s_f, s_t, s_tb, s_pt, s_piv, &s_K);
-    const int K = s_K;
-    if (K < 0) break;
-    if (lane == 0) {
-      lens[0] = K; lens[1] = ax; lens[2] = ay; lens[3] = R;
-      for (int c = 0; c < kLP; c++) lens[4 + c] = s_tb[c];
+    block_normal(np, rx, ry, d, drop, sA);
+    block_models(np, n, rx, ry, d, drop, sA, F);
+    if (F.K < 0) break;
+    if (tid == 0) {
+      lens[0] = F.K; lens[1] = ax; lens[2] = ay; lens[3] = R;
+      for (int c = 0; c < kLP; c++) lens[4 + c] = F.tb[c];
     }
     ok = 1;
-    __syncwarp();
+    __syncthreads();
     if (!robust || round == 3) break;
     // the robust rule: every point's distance from the model, tau from their median, the verdicts again
-    for (int i = lane; i < np; i += 32) {
+    for (int i = tid; i < np; i += blockDim.x) {
       float fx, fy;
       lens_at(lens, qx[i] * R + ax, qy[i] * R + ay, &fx, &fy);
       res[i] = hypot(d[i][0] - fx, d[i][1] - fy);
     }
-    __syncwarp();
-    for (int i = lane; i < np; i += 32) {   // the ascending order, ties by index: the sort's array
+    __syncthreads();
+    for (int i = tid; i < np; i += blockDim.x) {   // the ascending order, ties by index: the sort's array
       int rank = 0;
       for (int j = 0; j < np; j++) rank += res[j] < res[i] || (res[j] == res[i] && j < i);
-      s_srt[rank] = res[i];
+      srt[rank] = res[i];
     }
-    __syncwarp();
-    if (lane == 0) {
-      const double tau = fmax(tau_floor, 3 * 1.4826 * s_srt[np / 2]);
+    __syncthreads();
+    if (tid == 0) {
+      const double tau = fmax(tau_floor, 3 * 1.4826 * srt[np / 2]);
       int changed = 0;
       for (int i = 0; i < np; i++) {
         const uint8_t bad = res[i] > tau;
@@ -324,7 +328,7 @@ __device__ int warp_lensm_fit(int np, double (*rx)[kLP], double (*ry)[kLP], doub
       }
       s_flag[1] = changed > 0;
     }
-    __syncwarp();
+    __syncthreads();
     if (!s_flag[1]) break;
   }
   return ok;
@@ -355,24 +359,25 @@ __global__ void reg_init_kernel(RegArgs a, int frames) {
 }
 
 // One round's bookkeeping after the search: the anchors found, the homography they say, the robust model about it,
-// the anchors it drops no longer found (acquire.c:2133-2143). A warp a frame.
-__global__ void __launch_bounds__(32) reg_round_kernel(RegArgs a, uint8_t *active) {
-  const int f = blockIdx.x, lane = threadIdx.x;
+// the anchors it drops no longer found (acquire.c:2133-2143). A block of kFitThreads a frame.
+__global__ void __launch_bounds__(kFitThreads) reg_round_kernel(RegArgs a, uint8_t *active) {
+  const int f = blockIdx.x, tid = threadIdx.x;
   RegState &S = a.st[f];
   if (!S.active) return;
-  __shared__ double s_rx[kNA][kLP], s_ry[kNA][kLP], s_d[kNA][2], s_qx[kNA], s_qy[kNA], s_A[kLP][kLP + 1], A[kLP][kLP + 1], s_res[kNA];
-  __shared__ double s_M[kLP][kLP + 1], s_mean[6], s_lens[kLensStride];
+  __shared__ double s_rx[kNA][kLP], s_ry[kNA][kLP], s_d[kNA][2], s_qx[kNA], s_qy[kNA], s_A[kLP][kLP + 1], s_res[kNA], s_srt[kNA];
+  __shared__ double s_M[kLP][kLP + 1], s_mean[6], s_lens[kLensStride], s_gf[kLP];
+  __shared__ FitScratch F;
   __shared__ float s_X[kNA], s_Y[kNA], s_u[kNA], s_v[kNA];
   __shared__ uint8_t s_ok[kNA], s_drop[kNA];
-  __shared__ int s_at[kNA], s_np, s_flag[2], s_go;
+  __shared__ int s_at[kNA], s_pos[kNA], s_np, s_flag[2], s_go, s_piv[2];
   const float ah = a.a * 0.5f;
-  for (int k = lane; k < kNA; k += 32) {
+  for (int k = tid; k < kNA; k += blockDim.x) {
     const int64_t o = (int64_t)f * kNA + k;
     s_ok[k] = a.ok[o]; s_u[k] = a.u[o]; s_v[k] = a.v[o];
     s_X[k] = (float)a.m0[k % 7] + ah; s_Y[k] = (float)a.m0[k / 7] + ah;
   }
-  __syncwarp();
-  if (lane == 0) {
+  __syncthreads();
+  if (tid == 0) {
     int now = 0;
     for (int k = 0; k < kNA; k++) now += s_ok[k];
     s_go = 1;
@@ -396,13 +401,14 @@ __global__ void __launch_bounds__(32) reg_round_kernel(RegArgs a, uint8_t *activ
       s_flag[0] = fit;
     }
   }
-  __syncwarp();
+  __syncthreads();
   if (!s_go) return;
   if (s_flag[0]) {
     const double mx = s_mean[0], my = s_mean[1], mu = s_mean[2], mv = s_mean[3], sx = s_mean[4], su = s_mean[5];
-    // the 8 x 8 normal equations and right side, each entry over the anchors in order
-    for (int e = lane; e < 72; e += 32) {
-      const int p = e < 64 ? e / 8 : e - 64, q = e < 64 ? e % 8 : kLP;
+    // the 8 x 8 normal equations and right side, an entry a thread, each over the anchors in order; the rest zero
+    for (int e = tid; e < kLP * (kLP + 1); e += blockDim.x) {
+      const int p = e / (kLP + 1), q = e - p * (kLP + 1);
+      if (p >= 8 || (q >= 8 && q < kLP)) { s_M[p][q] = 0; continue; }
       double acc = 0;
       for (int k = 0; k < kNA; k++) {
         if (!s_ok[k]) continue;
@@ -412,22 +418,10 @@ __global__ void __launch_bounds__(32) reg_round_kernel(RegArgs a, uint8_t *activ
       }
       s_M[p][q] = acc;
     }
-    __syncwarp();
-    if (lane == 0) {
-      for (int p = 0; p < kLP; p++) for (int q = 0; q <= kLP; q++) if (p >= 8 || (q >= 8 && q < kLP)) s_M[p][q] = 0;
-      bool solved = true;
-      for (int c = 0; c < 8 && solved; c++) {
-        int pv = c;
-        for (int r = c + 1; r < 8; r++) if (fabs(s_M[r][c]) > fabs(s_M[pv][c])) pv = r;
-        if (fabs(s_M[pv][c]) < 1e-14) { solved = false; break; }
-        for (int kk = 0; kk <= kLP; kk++) { const double t = s_M[c][kk]; s_M[c][kk] = s_M[pv][kk]; s_M[pv][kk] = t; }
-        for (int r = 0; r < 8; r++) {
-          if (r == c) continue;
-          const double fr = s_M[r][c] / s_M[c][c];
-          for (int kk = c; kk <= kLP; kk++) s_M[r][kk] -= fr * s_M[c][kk];
-        }
-      }
-      if (solved) {
+    __syncthreads();
+    if (tid < 32) {   // solve_lens(M, 8) on warp 0, then H through the centring
+      const bool solved = warp_gj(s_M, 8, 1e-14, s_gf, s_piv);
+      if (solved && tid == 0) {
         double g[9];
         for (int p = 0; p < 8; p++) g[p] = s_M[p][kLP] / s_M[p][p];
         g[8] = 1;
@@ -438,28 +432,31 @@ __global__ void __launch_bounds__(32) reg_round_kernel(RegArgs a, uint8_t *activ
         if (fabs(h[8]) > 1e-12) for (int k = 0; k < 9; k++) S.Ha[k] = (float)(h[k] / h[8]);
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
   // anchor_model_free (acquire.c:2101-2118): the anchors' displacements about Ha, the robust rule at half a module
-  if (lane == 0) {
+  if (tid == 0) {
     int np = 0;
-    for (int k = 0; k < kNA; k++) {
-      if (!s_ok[k]) continue;
-      float hu, hv;
-      project_f(S.Ha, s_X[k], s_Y[k], &hu, &hv);
-      const float ddx = s_u[k] - hu, ddy = s_v[k] - hv;
-      a.dx[(int64_t)f * kNA + k] = ddx; a.dy[(int64_t)f * kNA + k] = ddy;
-      s_qx[np] = (hu - a.ax) / a.R; s_qy[np] = (hv - a.ay) / a.R;
-      rows_of(s_qx[np], s_qy[np], s_rx[np], s_ry[np]);
-      s_d[np][0] = ddx; s_d[np][1] = ddy; s_drop[np] = 0; s_at[np] = k; np++;
-    }
+    for (int k = 0; k < kNA; k++) s_pos[k] = s_ok[k] ? np++ : -1;
     s_np = np;
   }
-  __syncwarp();
+  __syncthreads();
+  for (int k = tid; k < kNA; k += blockDim.x) {
+    const int i = s_pos[k];
+    if (i < 0) continue;
+    float hu, hv;
+    project_f(S.Ha, s_X[k], s_Y[k], &hu, &hv);
+    const float ddx = s_u[k] - hu, ddy = s_v[k] - hv;
+    a.dx[(int64_t)f * kNA + k] = ddx; a.dy[(int64_t)f * kNA + k] = ddy;
+    s_qx[i] = (hu - a.ax) / a.R; s_qy[i] = (hv - a.ay) / a.R;
+    rows_of(s_qx[i], s_qy[i], s_rx[i], s_ry[i]);
+    s_d[i][0] = ddx; s_d[i][1] = ddy; s_drop[i] = 0; s_at[i] = k;
+  }
+  __syncthreads();
   const int np = s_np;
-  const int have = np >= 4 && warp_lensm_fit(np, s_rx, s_ry, s_d, s_qx, s_qy, s_drop, true, 0.5 * (double)S.mpx, a.ax, a.ay, a.R, s_lens,
-                                             s_A, A, s_res, s_flag);
-  if (lane == 0) {
+  const int have = np >= 4 && block_lensm_fit(np, s_rx, s_ry, s_d, s_qx, s_qy, s_drop, true, 0.5 * (double)S.mpx, a.ax, a.ay, a.R, s_lens,
+                                              s_A, F, s_res, s_srt, s_flag);
+  if (tid == 0) {
     S.have = have;
     a.have_mf[f] = have;
     if (have) {
@@ -475,54 +472,53 @@ __global__ void __launch_bounds__(32) reg_round_kernel(RegArgs a, uint8_t *activ
 }
 
 // After the rounds: each corner judged by the anchors' own map (Ha, mf), the joint model of the anchors and the kept
-// corners about the corners' H (acquire.c:2144-2173); the corners to search again. A warp a frame.
-__global__ void __launch_bounds__(32) reg_corners_kernel(RegArgs a) {
-  const int f = blockIdx.x, lane = threadIdx.x;
+// corners about the corners' H (acquire.c:2144-2173); the corners to search again. A block of kFitThreads a frame.
+__global__ void __launch_bounds__(kFitThreads) reg_corners_kernel(RegArgs a) {
+  const int f = blockIdx.x, tid = threadIdx.x;
   RegState &S = a.st[f];
-  __shared__ double s_rx[kMaxPts][kLP], s_ry[kMaxPts][kLP], s_d[kMaxPts][2], s_qx[kMaxPts], s_qy[kMaxPts], s_A[kLP][kLP + 1], A[kLP][kLP + 1];
-  __shared__ double s_res[kMaxPts], s_lens[kLensStride];
+  __shared__ double s_rx[kMaxPts][kLP], s_ry[kMaxPts][kLP], s_d[kMaxPts][2], s_qx[kMaxPts], s_qy[kMaxPts], s_A[kLP][kLP + 1];
+  __shared__ double s_res[kMaxPts], s_srt[kMaxPts], s_lens[kLensStride];
+  __shared__ FitScratch F;
   __shared__ uint8_t s_drop[kMaxPts];
-  __shared__ int s_np, s_flag[2], s_go;
-  if (lane == 0) {
+  __shared__ int s_pos[kNA], s_np, s_flag[2], s_go;
+  if (tid == 0) {
     s_go = S.have && S.nf >= kAnchMin;
     S.held = s_go;
-    if (s_go) {
-      const float ah = a.a * 0.5f, lo = a.node_lo, hi = a.node_hi;
-      int np = 0;
-      for (int c = 0; c < 4; c++) {
-        float u, v;
-        project_f(S.H0, (c == 1 || c == 2) ? hi : lo, c >= 2 ? hi : lo, &u, &v);
-        S.hu[c] = u; S.hv[c] = v;
-        s_qx[np] = (u - a.ax) / a.R; s_qy[np] = (v - a.ay) / a.R;
-        rows_of(s_qx[np], s_qy[np], s_rx[np], s_ry[np]);
-        s_d[np][0] = 0; s_d[np][1] = 0; np++;
-      }
-      for (int k = 0; k < kNA; k++) {
-        const int64_t o = (int64_t)f * kNA + k;
-        if (!a.ok[o]) continue;
-        float hu, hv;
-        project_f(S.H0, (float)a.m0[k % 7] + ah, (float)a.m0[k / 7] + ah, &hu, &hv);
-        s_qx[np] = (hu - a.ax) / a.R; s_qy[np] = (hv - a.ay) / a.R;
-        rows_of(s_qx[np], s_qy[np], s_rx[np], s_ry[np]);
-        s_d[np][0] = a.u[o] - hu; s_d[np][1] = a.v[o] - hv; s_drop[np] = 0; np++;
-      }
-      const double *mf = a.mf + (int64_t)f * kLensStride;
-      for (int c = 0; c < 4; c++) {
-        float pu, pv, mu, mv;
-        project_f(S.Ha, (c == 1 || c == 2) ? hi : lo, c >= 2 ? hi : lo, &pu, &pv);
-        lens_at(mf, pu, pv, &mu, &mv);
-        s_drop[c] = hypotf(pu + mu - S.quad[2 * c], pv + mv - S.quad[2 * c + 1]) > kCornerMod * S.mpx;
-      }
-      s_np = np;
-    }
+    int np = 4;
+    for (int k = 0; k < kNA; k++) s_pos[k] = a.ok[(int64_t)f * kNA + k] ? np++ : -1;
+    s_np = np;
   }
-  __syncwarp();
+  __syncthreads();
   if (!s_go) {
-    if (lane == 0) { a.on_mc[f] = 0; for (int c = 0; c < 4; c++) S.redo[c] = 0; }
+    if (tid == 0) { a.on_mc[f] = 0; for (int c = 0; c < 4; c++) S.redo[c] = 0; }
     return;
   }
-  const int fit = warp_lensm_fit(s_np, s_rx, s_ry, s_d, s_qx, s_qy, s_drop, false, 0, a.ax, a.ay, a.R, s_lens, s_A, A, s_res, s_flag);
-  if (lane == 0) {
+  const float ah = a.a * 0.5f, lo = a.node_lo, hi = a.node_hi;
+  for (int t = tid; t < 4 + kNA; t += blockDim.x) {
+    if (t < 4) {   // the corner nodes about H (no displacement), and each judged by the anchors' own map
+      float u, v, pu, pv, mu, mv;
+      project_f(S.H0, (t == 1 || t == 2) ? hi : lo, t >= 2 ? hi : lo, &u, &v);
+      S.hu[t] = u; S.hv[t] = v;
+      s_qx[t] = (u - a.ax) / a.R; s_qy[t] = (v - a.ay) / a.R;
+      rows_of(s_qx[t], s_qy[t], s_rx[t], s_ry[t]);
+      s_d[t][0] = 0; s_d[t][1] = 0;
+      project_f(S.Ha, (t == 1 || t == 2) ? hi : lo, t >= 2 ? hi : lo, &pu, &pv);
+      lens_at(a.mf + (int64_t)f * kLensStride, pu, pv, &mu, &mv);
+      s_drop[t] = hypotf(pu + mu - S.quad[2 * t], pv + mv - S.quad[2 * t + 1]) > kCornerMod * S.mpx;
+    } else {
+      const int k = t - 4, i = s_pos[k];
+      if (i < 0) continue;
+      const int64_t o = (int64_t)f * kNA + k;
+      float hu, hv;
+      project_f(S.H0, (float)a.m0[k % 7] + ah, (float)a.m0[k / 7] + ah, &hu, &hv);
+      s_qx[i] = (hu - a.ax) / a.R; s_qy[i] = (hv - a.ay) / a.R;
+      rows_of(s_qx[i], s_qy[i], s_rx[i], s_ry[i]);
+      s_d[i][0] = a.u[o] - hu; s_d[i][1] = a.v[o] - hv; s_drop[i] = 0;
+    }
+  }
+  __syncthreads();
+  const int fit = block_lensm_fit(s_np, s_rx, s_ry, s_d, s_qx, s_qy, s_drop, false, 0, a.ax, a.ay, a.R, s_lens, s_A, F, s_res, s_srt, s_flag);
+  if (tid == 0) {
     S.mc_on = fit;
     a.on_mc[f] = fit;
     for (int c = 0; c < kLensStride; c++) a.mc[(int64_t)f * kLensStride + c] = s_lens[c];
@@ -687,7 +683,7 @@ int lizg_refine_dev(lizg_refiner *r, const uint8_t *d_luma, int w, int h, int64_
   for (int round = 0; round < rounds && e == cudaSuccess; round++) {
     // anchors not yet found, through H and (from the second round) the lens model so far; then the model again
     if ((e = anchor_find_launch(r->span, d_luma, w, h, frame_stride, d_reg, hstride, round ? r->lens : nullptr, r->ok, frames, out, st)) != cudaSuccess) break;
-    lens_fit_kernel<<<frames, 32, 0, st>>>(fa);
+    lens_fit_kernel<<<frames, kFitThreads, 0, st>>>(fa);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
@@ -738,10 +734,10 @@ int lizg_anchor_register_dev(lizg_refiner *r, const uint8_t *d_luma, const uint8
   if (e == cudaSuccess) { reg_init_kernel<<<(frames + 127) / 128, 128, 0, st>>>(a, frames); e = cudaGetLastError(); }
   for (int round = 0; round < kRounds && e == cudaSuccess; round++) {
     if ((e = anchor_find_launch(r->span, d_luma, w, h, frame_stride, d_Ha, st_stride, r->mf, r->ok, frames, out, st, r->have_mf, r->active)) != cudaSuccess) break;
-    reg_round_kernel<<<frames, 32, 0, st>>>(a, r->active);
+    reg_round_kernel<<<frames, kFitThreads, 0, st>>>(a, r->active);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) { reg_corners_kernel<<<frames, 32, 0, st>>>(a); e = cudaGetLastError(); }
+  if (e == cudaSuccess) { reg_corners_kernel<<<frames, kFitThreads, 0, st>>>(a); e = cudaGetLastError(); }
   if (e == cudaSuccess) { reg_redo_kernel<<<(4 * frames + 255) / 256, 256, 0, st>>>(r->st, frames, r->redo); e = cudaGetLastError(); }
   if (e == cudaSuccess) {
     const float *d_H0 = reinterpret_cast<const float *>(reinterpret_cast<const char *>(r->st) + offsetof(RegState, H0));
@@ -756,7 +752,7 @@ int lizg_anchor_register_dev(lizg_refiner *r, const uint8_t *d_luma, const uint8
     fa.ax = a.ax; fa.ay = a.ay; fa.R = a.R; fa.node_lo = a.node_lo; fa.node_hi = a.node_hi;
     for (int i = 0; i < 7; i++) fa.m0[i] = a.m0[i];
     fa.reg = d_reg; fa.ok = r->ok; fa.dx = r->dx; fa.dy = r->dy; fa.lens = r->lens; fa.have = r->have; fa.gate = r->held;
-    lens_fit_kernel<<<frames, 32, 0, st>>>(fa);
+    lens_fit_kernel<<<frames, kFitThreads, 0, st>>>(fa);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) { mesh_kernel<<<frames, 256, 0, st>>>(r->lens, r->have, r->node, r->nn, d_reg, hstride); e = cudaGetLastError(); }
