@@ -622,6 +622,19 @@ def bench_multistream(args, stream):
             stream.wait_event(join)
         eng.run_dev(batches, sp)
 
+    def tick_pipelined():
+        # each format's registration, then at once its decode (the engine on that format's batch alone, a graph a
+        # format), on the format's own stream: a format's decode overlaps the other formats' registrations
+        fork.record(stream)
+        for (d_l, d_r, o, d_p, refiner, count), side, join, b in zip(keep, sides, joins, batches):
+            side.wait_event(fork)
+            with torch.cuda.stream(side):
+                d_r.copy_(d_p)
+            refiner.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_r.data_ptr(), count, 3, None, None, side.cuda_stream)
+            eng.run_dev([b], side.cuda_stream)
+            join.record(side)
+            stream.wait_event(join)
+
     def tick_single():
         for rx1, ref1, d_l, d_p, d_r1, o1 in singles:
             d_r1.copy_(d_p)
@@ -642,22 +655,62 @@ def bench_multistream(args, stream):
         e1.record(stream)
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / K
+    def registration():
+        fork.record(stream)
+        for (d_l, d_r, o, d_p, refiner, count), side, join in zip(keep, sides, joins):
+            side.wait_event(fork)
+            with torch.cuda.stream(side):
+                d_r.copy_(d_p)
+            refiner.refine_dev(d_l.data_ptr(), W, Hh, W * Hh, d_r.data_ptr(), count, 3, None, None, side.cuda_stream)
+            join.record(side)
+            stream.wait_event(join)
+
+    def oks():
+        return [o["ok"].cpu().numpy().copy() for _, _, o, _, _, _ in keep]
     K = max(5, args.steps // 3)
+    # the engine both ways on the tick's registered frames: a graph a format on its own stream, and stage-wise across
+    # the formats (one column pass, row pass and decode grid over every format's items); the tuner keeps the faster
+    tick()
+    torch.cuda.synchronize()
+    ms_reg = timed(registration, K)
+    ms_eng, ms_tick, ok_mode = {}, {}, {}
+    for mode in (0, 1):
+        eng.set_mixed(mode)
+        ms_eng[mode] = timed(lambda: eng.run_dev(batches, sp), K)
+        ms_tick[mode] = timed(tick, K)
+        ok_mode[mode] = (oks(), eng.launches)
+    eng.set_mixed(0)
+    ms_pipe = timed(tick_pipelined, K)
+    ok_pipe = oks()
+    tuned, _ = eng.autotune(batches, sp)
     ms = timed(tick, K)
+    arrangement = "registration, then the engine"
+    if ms_pipe < ms:
+        eng.set_mixed(0)
+        ms, arrangement = timed(tick_pipelined, K), "each format's registration then its decode"
     ms1 = timed(tick_single, max(3, K // 2))
     ok = sum(int(o["ok"].sum().item()) for _, _, o, _, _, _ in keep)
     blocks = sum(f[3] * eng.formats[i].blocks for i, f in enumerate(formats))
     same = all(np.array_equal(o["ok"][k].cpu().numpy(), o1[k][0]["ok"][0].cpu().numpy())
                for (_, _, o, _, _, _), (_, _, _, _, _, o1) in zip(keep, singles) for k in range(len(o1)))
+    same_modes = all(np.array_equal(a, b) and np.array_equal(a, c) for a, b, c in zip(ok_mode[0][0], ok_mode[1][0], ok_pipe))
     res = {"workload": "32 streams of 3840x2160 luma at nominal 60 fps; formats n/subch/span 384/64/128 x10, 768/320/128 x8, "
                        "1152/720/256 x6, 1536/1024/256 x5, 1536/1024/512 x3; painted by the sender; rotation 15 deg, tilt 20 deg, "
                        "scale 0.8-1.1 x 1700 px, radial k1 U(+-0.05), blur U(0.5, 2.0) px, AWGN 3 DN; registered on the device "
                        "from a finder's corners (3 rounds of anchors and lens model) inside the tick",
            "streams": streams, "frames_per_s": round(streams / (ms / 1e3), 1), "payload_MBps": round(ok * 472 / (ms / 1e3) / 1e6, 2),
            "ms_per_tick": round(ms, 4), "realtime_60fps_streams": round(streams / (ms / 1e3) / 60, 1),
-           "blocks_verified": ok, "blocks": blocks, "block_pass_rate": round(ok / blocks, 4), "gpu_launches_per_tick": eng.launches,
+           "blocks_verified": ok, "blocks": blocks, "block_pass_rate": round(ok / blocks, 4), "gpu_launches_per_tick": ok_mode[tuned if arrangement.startswith("registration") else 0][1],
            "one_frame_a_launch": {"frames_per_s": round(streams / (ms1 / 1e3), 1), "ms_per_tick": round(ms1, 4)},
-           "batched_vs_one_frame": round(ms1 / ms, 2), "identical_crc_sets": bool(same)}
+           "batched_vs_one_frame": round(ms1 / ms, 2), "identical_crc_sets": bool(same),
+           "engine_mode": ["a graph a format", "stage-wise across formats"][tuned],
+           "registration_ms": round(ms_reg, 4),
+           "engine_ms": {"a_graph_a_format": round(ms_eng[0], 4), "stage_wise": round(ms_eng[1], 4)},
+           "tick_ms": {"a_graph_a_format": round(ms_tick[0], 4), "stage_wise": round(ms_tick[1], 4),
+                       "each_format_registered_then_decoded": round(ms_pipe, 4)},
+           "tick_arrangement": arrangement,
+           "engine_launches": {"a_graph_a_format": ok_mode[0][1], "stage_wise": ok_mode[1][1]},
+           "arrangements_identical_crc_sets": bool(same_modes)}
     peak, peak_src = peaks()
     res["hbm"] = {"algorithmic_bytes_per_tick": tick_bytes, "GBps": round(tick_bytes / (ms / 1e3) / 1e9, 1),
                   "frac": round(tick_bytes / (ms / 1e3) / 1e9 / peak, 4),

@@ -246,9 +246,19 @@ int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int 
 // decoded together. An engine holds one receiver handle per picture format (lizg_engine_add_format returns its
 // index; lizg_engine_rx the handle, for lizg_rx_info and the like). lizg_engine_run_dev takes one batch per format
 // (each format at most once a run): the format's frames, registrations and outputs as lizg_rx_finish_luma_dev
-// takes them; every batch runs on its format's own stream, replayed from that format's CUDA graph (captured on the
-// first run with those buffers), forked from `stream` and joined back to it, so the formats' work overlaps on the
-// GPU. Queued; returns once launched. lizg_engine_launches: the kernels the last run launched.
+// takes them. By default every batch runs on its format's own stream, replayed from that format's CUDA graph
+// (captured on the first run with those buffers), forked from `stream` and joined back to it, so the formats' work
+// overlaps on the GPU. Queued; returns once launched. lizg_engine_launches: the kernels the last run launched.
+//
+// lizg_engine_set_mixed(e, 1) runs the batches stage-wise across formats instead, as persistent work queues: the
+// column pass one grid over every format's (frame, column tile) items whatever their picture sizes, the row pass one
+// grid over every format's (frame, row tile) items, the decode one grid over every format's (tier, block) items of all
+// four codes (the 1/2 code's first), and the light per-frame stages (the shading sums and sampler tables, the surface
+// factors, the pilots' fit, soft values and block stage) a launch a format on the formats' streams; the whole run is
+// one CUDA graph, captured on the first run with those batches. The outputs are the same bit for bit either way.
+// Returns the previous setting. lizg_engine_autotune runs the batches both ways (each four times, the first not
+// timed), keeps the faster and returns it (0 or 1); ms (may be NULL) gets the two best times, per format first.
+// Both write the batches' outputs as a run does.
 typedef struct lizg_engine lizg_engine;
 typedef struct {
   int format;
@@ -265,6 +275,8 @@ int lizg_engine_add_format(lizg_engine *e, int n, int subch, int span, int max_f
 lizg_rx *lizg_engine_rx(lizg_engine *e, int format);
 int lizg_engine_run_dev(lizg_engine *e, const lizg_engine_batch *b, int nb, void *stream);
 int lizg_engine_launches(const lizg_engine *e);
+int lizg_engine_set_mixed(lizg_engine *e, int mixed);
+int lizg_engine_autotune(lizg_engine *e, const lizg_engine_batch *b, int nb, void *stream, float *ms);
 
 // ---------------------------------------------------------------- the batching front (camera frames in, blocks out)
 //

@@ -235,6 +235,8 @@ def _rx_sigs(L):
     L.lizg_engine_rx.restype = P
     L.lizg_engine_run_dev.argtypes = [P, P, I, P]
     L.lizg_engine_launches.argtypes = [P]
+    L.lizg_engine_set_mixed.argtypes = [P, I]
+    L.lizg_engine_autotune.argtypes = [P, P, I, P, ctypes.POINTER(ctypes.c_float)]
     L.lizg_ingest_pixels_dev.argtypes = [P, I, I, I, ctypes.c_int64, I, I, P, P]
     L.lizg_develop_dev.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, I, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, P, P]
     L.lizg_refiner_new.argtypes = [I, I]
@@ -748,6 +750,19 @@ class Engine:
         """batches: list of (format, d_luma ptr, w, h, pitch, frame_stride, d_reg ptr, frames, RxOut)."""
         arr = (EngineBatch * len(batches))(*[EngineBatch(*b) for b in batches])
         _check(lib().lizg_engine_run_dev(self._h, ctypes.cast(arr, ctypes.c_void_p), len(batches), ctypes.c_void_p(stream)), "lizg_engine_run_dev")
+
+    def set_mixed(self, mixed):
+        """1: stage-wise across formats (one column pass, row pass and decode grid over every format's items, the
+        whole run one graph); 0: a graph a format on its own stream. Returns the previous setting."""
+        return _check(lib().lizg_engine_set_mixed(self._h, int(mixed)), "lizg_engine_set_mixed")
+
+    def autotune(self, batches, stream):
+        """Runs the batches both ways, keeps the faster: (mode, [ms a graph a format, ms stage-wise])."""
+        arr = (EngineBatch * len(batches))(*[EngineBatch(*b) for b in batches])
+        ms = (ctypes.c_float * 2)()
+        mode = _check(lib().lizg_engine_autotune(self._h, ctypes.cast(arr, ctypes.c_void_p), len(batches), ctypes.c_void_p(stream), ms),
+                      "lizg_engine_autotune")
+        return mode, [ms[0], ms[1]]
 
     @property
     def launches(self):

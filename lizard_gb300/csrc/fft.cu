@@ -293,6 +293,39 @@ __device__ __forceinline__ SmemMap smem_map(unsigned char *raw) {
   return m;
 }
 
+__host__ __device__ constexpr int cmax_i(int x, int y) { return x > y ? x : y; }
+
+// The mixed-size grids' kernel arguments: each format's tables and buffers, and its first CTA (first[nseg] CTAs in all).
+struct FftColsSeg {
+  FftDev xd;
+  SrcDev src;
+  const float4 *ctab;
+  const double *hole;
+  double *part;
+  float2 *Y;
+  int bands;
+};
+struct FftColsMix {
+  FftColsSeg seg[kFftMixSegs];
+  int first[kFftMixSegs + 1];
+  int nseg;
+};
+struct FftRowsSeg {
+  CUtensorMap ymap;
+  FftDev xd;
+  const float2 *fac;
+  const int32_t *tpos;
+  float2 *C;
+  int *err;
+  int need;
+};
+struct FftRowsMix {
+  FftRowsSeg seg[kFftMixSegs];
+  int first[kFftMixSegs + 1];
+  int nseg;
+};
+static_assert(sizeof(FftColsMix) <= 32000 && sizeof(FftRowsMix) <= 32000, "the mixed grids' arguments fit a launch");
+
 // The surface's value at (x, y) inside an anchor's square (liblizard/src/lizard_phy.c:341-346).
 __device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta, int x, int y) {
   double bb[6], h = 0;
@@ -402,62 +435,93 @@ __device__ __forceinline__ void load_tile(const FftDev &xd, const SrcDev &src, c
   }
 }
 
-// The column pass: a CTA takes a column tile (frame f, columns x0 .. x0 + 2L - 1): the shading surface beta from the
+// The column pass's per-CTA scalars in shared memory.
+struct ColsShared {
+  double rhs[6], beta[6];
+  float part[kThreads / 32][5];
+};
+
+// The column pass on one tile (frame f, columns x0 = 2 L tile .. x0 + 2L - 1): the shading surface beta from the
 // frame's bands, the tile's samples (erased, projections summed: part[f][tile][0..4]), the L lines' transforms along
 // y, and the two real columns of each line separated: A(v) = (Z(v) + conj Z(n - v)) / 2, B(v) = -i (Z(v) - conj
-// Z(n - v)) / 2, written to Y[f][v][x] for the kept rows v.
+// Z(n - v)) / 2, written to Y[f][v][x] for the kept rows v. Every thread of the CTA takes part.
+template <int N>
+__device__ __forceinline__ void cols_tile(const FftDev &xd, const SrcDev &src, const float4 *ctab, int bands, const double *hole,
+                                          double *part, float2 *Y, int f, int tile, unsigned char *smraw, ColsShared &s) {
+  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
+  const SmemMap sm = smem_map<N>(smraw);
+  const int tid = threadIdx.x, l = tid % L, warp = tid >> 5, lane = tid & 31, x0 = tile * 2 * L;
+  for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
+  float2 *line = sm.buf + l * LSTR;
+  if (tid < 6) {
+    double acc = 0;
+    for (int b = 0; b < bands; b++) acc += hole[((int64_t)f * bands + b) * 6 + tid];
+    s.rhs[tid] = acc;
+  }
+  __syncthreads();
+  if (tid == 0) {
+#pragma unroll
+    for (int r = 0; r < 6; r++) {
+      double acc = 0;
+#pragma unroll
+      for (int k = 0; k < 6; k++) acc += xd.hole_inv[r * 6 + k] * s.rhs[k];
+      s.beta[r] = acc;
+    }
+  }
+  __syncthreads();
+  float p[5] = {0, 0, 0, 0, 0};
+  if (src.grid) load_tile<N, kSrcGrid>(xd, src, ctab, f, x0, s.beta, line, p);
+  else if (src.sd.read == LIZG_READ_DECODE) load_tile<N, kSrcDecode>(xd, src, ctab, f, x0, s.beta, line, p);
+  else load_tile<N, kSrcExact>(xd, src, ctab, f, x0, s.beta, line, p);
+#pragma unroll
+  for (int q = 0; q < 5; q++)
+    for (int o = 16; o > 0; o >>= 1) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
+  if (lane == 0)
+    for (int q = 0; q < 5; q++) s.part[warp][q] = p[q];
+  __syncthreads();
+  if (tid < 5) {
+    double acc = 0;
+    for (int w = 0; w < kThreads / 32; w++) acc += s.part[w][tid];
+    part[((int64_t)f * tiles + tile) * 5 + tid] = acc;
+  }
+  fft_lines<N>(sm.buf, sm.tw, L);
+  float2 *Yf = Y + (int64_t)f * xd.vrows * n;
+  const int xa = x0 + l, xb = x0 + L + l;
+  for (int v = tid / L; v < xd.vrows; v += ystep) {
+    const float2 zv = line[pad(v)], zm = line[pad(v ? n - v : 0)];
+    Yf[(int64_t)v * n + xa] = make_float2(0.5f * (zv.x + zm.x), 0.5f * (zv.y - zm.y));
+    Yf[(int64_t)v * n + xb] = make_float2(0.5f * (zv.y + zm.y), -0.5f * (zv.x - zm.x));
+  }
+}
+
+// The column pass of one picture size: CTA b takes tile b mod tiles of frame b / tiles.
 template <int N>
 __global__ void __launch_bounds__(kThreads, 3) fft_cols_kernel(FftDev xd, SrcDev src, const float4 *ctab, int bands, const double *hole, double *part,
                                                                 float2 *Y) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), tiles = n / (2 * L), ystep = kThreads / L;
-  const SmemMap sm = smem_map<N>(smraw);
-  const int tid = threadIdx.x, l = tid % L, warp = tid >> 5, lane = tid & 31;
-  for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
-  __shared__ double s_rhs[6], s_beta[6];
-  __shared__ float s_part[kThreads / 32][5];
-  float2 *line = sm.buf + l * LSTR;
-  {
-    const int f = blockIdx.x / tiles, tile = blockIdx.x % tiles, x0 = tile * 2 * L;
-    if (tid < 6) {
-      double acc = 0;
-      for (int b = 0; b < bands; b++) acc += hole[((int64_t)f * bands + b) * 6 + tid];
-      s_rhs[tid] = acc;
-    }
-    __syncthreads();
-    if (tid == 0) {
-#pragma unroll
-      for (int r = 0; r < 6; r++) {
-        double acc = 0;
-#pragma unroll
-        for (int k = 0; k < 6; k++) acc += xd.hole_inv[r * 6 + k] * s_rhs[k];
-        s_beta[r] = acc;
-      }
-    }
-    __syncthreads();
-    float p[5] = {0, 0, 0, 0, 0};
-    if (src.grid) load_tile<N, kSrcGrid>(xd, src, ctab, f, x0, s_beta, line, p);
-    else if (src.sd.read == LIZG_READ_DECODE) load_tile<N, kSrcDecode>(xd, src, ctab, f, x0, s_beta, line, p);
-    else load_tile<N, kSrcExact>(xd, src, ctab, f, x0, s_beta, line, p);
-#pragma unroll
-    for (int q = 0; q < 5; q++)
-      for (int o = 16; o > 0; o >>= 1) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
-    if (lane == 0)
-      for (int q = 0; q < 5; q++) s_part[warp][q] = p[q];
-    __syncthreads();
-    if (tid < 5) {
-      double acc = 0;
-      for (int w = 0; w < kThreads / 32; w++) acc += s_part[w][tid];
-      part[((int64_t)f * tiles + tile) * 5 + tid] = acc;
-    }
-    fft_lines<N>(sm.buf, sm.tw, L);
-    float2 *Yf = Y + (int64_t)f * xd.vrows * n;
-    const int xa = x0 + l, xb = x0 + L + l;
-    for (int v = tid / L; v < xd.vrows; v += ystep) {
-      const float2 zv = line[pad(v)], zm = line[pad(v ? n - v : 0)];
-      Yf[(int64_t)v * n + xa] = make_float2(0.5f * (zv.x + zm.x), 0.5f * (zv.y - zm.y));
-      Yf[(int64_t)v * n + xb] = make_float2(0.5f * (zv.y + zm.y), -0.5f * (zv.x - zm.x));
-    }
+  __shared__ ColsShared s;
+  constexpr int tiles = N / (2 * plan_of(N).lines);
+  cols_tile<N>(xd, src, ctab, bands, hole, part, Y, blockIdx.x / tiles, blockIdx.x % tiles, smraw, s);
+}
+
+// The column pass over several picture sizes in one grid: a queue of (format, frame, tile) items, format k's at CTAs
+// [first[k], first[k + 1]), each taken by its size's body (every size's tile holds about the same 48 KB of samples,
+// so one CTA shape serves them all; the dynamic shared memory is the largest size's).
+__global__ void __launch_bounds__(kThreads, 3) fft_cols_mixed_kernel(const __grid_constant__ FftColsMix m) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ ColsShared s;
+  int k = 0;
+  while (k < m.nseg - 1 && (int)blockIdx.x >= m.first[k + 1]) k++;
+  const FftColsSeg &g = m.seg[k];
+  const int b = (int)blockIdx.x - m.first[k], tiles = g.xd.n / (2 * plan_of(g.xd.n).lines), f = b / tiles, tile = b - f * tiles;
+  switch (g.xd.n) {
+    case 384: cols_tile<384>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
+    case 512: cols_tile<512>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
+    case 768: cols_tile<768>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
+    case 1024: cols_tile<1024>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
+    case 1152: cols_tile<1152>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
+    case 1280: cols_tile<1280>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
+    default: cols_tile<1536>(g.xd, g.src, g.ctab, g.bands, g.hole, g.part, g.Y, f, tile, smraw, s); break;
   }
 }
 
@@ -500,23 +564,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int lim
   return false;
 }
 
-// The row pass: a CTA takes (frame f, rows v0 .. v0 + L - 1), transforms them along x and takes the surface's
+// The row pass on one tile (frame f, rows v0 = L rtile .. v0 + L - 1): transforms them along x and takes the surface's
 // spectrum off: the xy term pxy X1[u] X1[v] everywhere, the x terms on v = 0, the y terms on u = 0. The used
 // coefficients go straight to their place in pos order: C[f][tpos[v][u]] (tpos -1 where (u, v) is not used).
 // The tile's rows come in by the tensor memory accelerator: bulk tensor copies of 128 complex points of a row each,
 // issued by one thread, landing densely at the start of each line's slots (at a 128-byte boundary) and counted on an
 // mbarrier; then every thread moves its points from the dense rows to the padded lines (all read, then all written).
 template <int N>
-__global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const float2 *fac, const __grid_constant__ CUtensorMap ymap,
-                                                               const int32_t *tpos, int need, float2 *C, int *err) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+__device__ __forceinline__ void rows_tile(const FftDev &xd, const float2 *fac, const CUtensorMap *ymap, const int32_t *tpos, int need, float2 *C,
+                                          int *err, int f, int rtile, unsigned char *smraw, uint64_t *s_bar) {
   constexpr int n = N, L = plan_of(N).lines, LSTR = lstride_of(N), SEGS = N / 128, PER = (L * N + kThreads - 1) / kThreads;
   static_assert(LSTR >= N + 16, "a line's slots hold its dense row at a 128-byte boundary");
-  __shared__ __align__(8) uint64_t s_bar;
   const SmemMap sm = smem_map<N>(smraw);
-  const int tid = threadIdx.x, tiles = (xd.vrows + L - 1) / L;
-  const int f = blockIdx.x / tiles, v0 = (blockIdx.x % tiles) * L, Lr = min(L, xd.vrows - v0);
-  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+  const int tid = threadIdx.x;
+  const int v0 = rtile * L, Lr = min(L, xd.vrows - v0);
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
   // line l's dense row: at the first 128-byte boundary of its slots (room: a line's slots exceed n by 16 or more)
   auto dense = [&](int l) { return (uint32_t)(((uint32_t)__cvta_generic_to_shared(sm.buf + l * LSTR) + 127u) & ~127u); };
   if (tid == 0) {
@@ -530,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const 
     for (int l = 0; l < Lr; l++)
       for (int s = 0; s < SEGS; s++)
         asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n"
-                     ::"r"(dense(l) + 1024u * s), "l"(&ymap), "r"(256 * s), "r"(y0 + l), "r"(bar) : "memory");
+                     ::"r"(dense(l) + 1024u * s), "l"(ymap), "r"(256 * s), "r"(y0 + l), "r"(bar) : "memory");
   }
   for (int i = tid; i < n; i += kThreads) sm.tw[i] = xd.tws[i];
   if (!mbar_wait(bar, 0, 1 << 22)) {   // never expected: record it, wait for the copies once more, leave the tile
@@ -581,6 +643,36 @@ __global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const 
   }
 }
 
+// The row pass of one picture size: CTA b takes row tile b mod tiles of frame b / tiles.
+template <int N>
+__global__ void __launch_bounds__(kThreads, 3) fft_rows_kernel(FftDev xd, const float2 *fac, const __grid_constant__ CUtensorMap ymap,
+                                                               const int32_t *tpos, int need, float2 *C, int *err) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t s_bar;
+  const int tiles = (xd.vrows + plan_of(N).lines - 1) / plan_of(N).lines;
+  rows_tile<N>(xd, fac, &ymap, tpos, need, C, err, blockIdx.x / tiles, blockIdx.x % tiles, smraw, &s_bar);
+}
+
+// The row pass over several picture sizes in one grid: format k's (frame, row tile) items at CTAs
+// [first[k], first[k + 1]), each with its own tensor map over its Y.
+__global__ void __launch_bounds__(kThreads, 3) fft_rows_mixed_kernel(const __grid_constant__ FftRowsMix m) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t s_bar;
+  int k = 0;
+  while (k < m.nseg - 1 && (int)blockIdx.x >= m.first[k + 1]) k++;
+  const FftRowsSeg &g = m.seg[k];
+  const int L = plan_of(g.xd.n).lines, tiles = (g.xd.vrows + L - 1) / L, b = (int)blockIdx.x - m.first[k], f = b / tiles, rt = b - f * tiles;
+  switch (g.xd.n) {
+    case 384: rows_tile<384>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+    case 512: rows_tile<512>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+    case 768: rows_tile<768>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+    case 1024: rows_tile<1024>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+    case 1152: rows_tile<1152>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+    case 1280: rows_tile<1280>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+    default: rows_tile<1536>(g.xd, g.fac, &g.ymap, g.tpos, g.need, g.C, g.err, f, rt, smraw, &s_bar); break;
+  }
+}
+
 int fft_plan(int n, int radix[3], int *lines) {
   const Plan p = plan_of(n);
   if (!p.lines) return -1;
@@ -606,6 +698,23 @@ int fft_y_map(CUtensorMap *map, float2 *Y, int n, int64_t rows) {
                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
+// The shading fit's partial sums, then (captured frames only) the sampler's row and cell table.
+cudaError_t fft_pre_launch(const FftSegArgs &a, cudaStream_t st) {
+  const int bands = fft_hole_bands(a.xd.n);
+  hole_rhs_kernel<<<a.frames * bands, 256, 0, st>>>(a.xd, a.src, bands, a.b.hole);
+  if (!a.src.grid) {
+    if (!a.b.ctab || a.src.sd.nx != a.src.sd.ny) return cudaErrorInvalidValue;
+    const int per_frame = a.xd.n * a.src.sd.nx;
+    cell_table_kernel<<<dim3((per_frame + 255) / 256, a.frames), 256, 0, st>>>(a.src, per_frame, a.b.ctab);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t fft_fac_launch(const FftSegArgs &a, cudaStream_t st) {
+  fac_kernel<<<a.frames, 256, 0, st>>>(a.xd, a.xd.n / (2 * plan_of(a.xd.n).lines), a.b.part, a.b.fac);
+  return cudaGetLastError();
+}
+
 template <int N>
 static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st) {
   constexpr int L = plan_of(N).lines, smem = smem_bytes_of(N), tiles = N / (2 * L);
@@ -617,17 +726,60 @@ static cudaError_t fft_launch_n(const FftDev &xd, int frames, const SrcDev &src,
       (e = opt_rows.set(reinterpret_cast<const void *>(fft_rows_kernel<N>), smem)) != cudaSuccess)
     return e;
   (void)sms;
-  const int bands = fft_hole_bands(N), rtiles = (xd.vrows + L - 1) / L;
-  hole_rhs_kernel<<<frames * bands, 256, 0, st>>>(xd, src, bands, b.hole);
-  if (!src.grid) {
-    if (!b.ctab || src.sd.nx != src.sd.ny) return cudaErrorInvalidValue;
-    const int per_frame = N * src.sd.nx;
-    cell_table_kernel<<<dim3((per_frame + 255) / 256, frames), 256, 0, st>>>(src, per_frame, b.ctab);
-  }
-  fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, b.ctab, bands, b.hole, b.part, b.Y);
-  fac_kernel<<<frames, 256, 0, st>>>(xd, tiles, b.part, b.fac);
+  const FftSegArgs a{xd, src, b, frames};
+  if ((e = fft_pre_launch(a, st)) != cudaSuccess) return e;
+  fft_cols_kernel<N><<<frames * tiles, kThreads, smem, st>>>(xd, src, b.ctab, fft_hole_bands(N), b.hole, b.part, b.Y);
+  if ((e = fft_fac_launch(a, st)) != cudaSuccess) return e;
   if (!b.ymap || !b.err) return cudaErrorInvalidValue;
-  fft_rows_kernel<N><<<frames * rtiles, kThreads, smem, st>>>(xd, b.fac, *b.ymap, b.tpos, b.need, b.C, b.err);
+  fft_rows_kernel<N><<<frames * ((xd.vrows + L - 1) / L), kThreads, smem, st>>>(xd, b.fac, *b.ymap, b.tpos, b.need, b.C, b.err);
+  return cudaGetLastError();
+}
+
+// The largest transform CTA's shared memory over the ladder: the mixed grids' dynamic size.
+constexpr int kFftSmemLadder = cmax_i(cmax_i(cmax_i(smem_bytes_of(384), smem_bytes_of(512)), cmax_i(smem_bytes_of(768), smem_bytes_of(1024))),
+                                      cmax_i(cmax_i(smem_bytes_of(1152), smem_bytes_of(1280)), smem_bytes_of(1536)));
+static_assert(kFftSmemLadder <= kFftSmemMax, "transform CTA's shared memory");
+
+static int ladder_size(int n) { return plan_of(n).lines != 0; }
+
+cudaError_t fft_cols_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st) {
+  if (count < 1 || count > kFftMixSegs) return cudaErrorInvalidValue;
+  static SmemOptIn opt;
+  cudaError_t e;
+  if ((e = opt.set(reinterpret_cast<const void *>(fft_cols_mixed_kernel), kFftSmemLadder)) != cudaSuccess) return e;
+  FftColsMix m{};
+  m.nseg = count;
+  int smem = 0;
+  for (int k = 0; k < count; k++) {
+    const FftSegArgs &s = a[k];
+    if (!ladder_size(s.xd.n) || s.frames < 1) return cudaErrorInvalidValue;
+    FftColsSeg &g = m.seg[k];
+    g.xd = s.xd; g.src = s.src; g.ctab = s.b.ctab; g.hole = s.b.hole; g.part = s.b.part; g.Y = s.b.Y; g.bands = fft_hole_bands(s.xd.n);
+    m.first[k + 1] = m.first[k] + s.frames * (s.xd.n / (2 * plan_of(s.xd.n).lines));
+    smem = cmax_i(smem, smem_bytes_of(s.xd.n));
+  }
+  fft_cols_mixed_kernel<<<m.first[count], kThreads, smem, st>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t fft_rows_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st) {
+  if (count < 1 || count > kFftMixSegs) return cudaErrorInvalidValue;
+  static SmemOptIn opt;
+  cudaError_t e;
+  if ((e = opt.set(reinterpret_cast<const void *>(fft_rows_mixed_kernel), kFftSmemLadder)) != cudaSuccess) return e;
+  FftRowsMix m{};
+  m.nseg = count;
+  int smem = 0;
+  for (int k = 0; k < count; k++) {
+    const FftSegArgs &s = a[k];
+    if (!ladder_size(s.xd.n) || s.frames < 1 || !s.b.ymap || !s.b.err) return cudaErrorInvalidValue;
+    FftRowsSeg &g = m.seg[k];
+    const int L = plan_of(s.xd.n).lines;
+    g.xd = s.xd; g.ymap = *s.b.ymap; g.fac = s.b.fac; g.tpos = s.b.tpos; g.C = s.b.C; g.err = s.b.err; g.need = s.b.need;
+    m.first[k + 1] = m.first[k] + s.frames * ((s.xd.vrows + L - 1) / L);
+    smem = cmax_i(smem, smem_bytes_of(s.xd.n));
+  }
+  fft_rows_mixed_kernel<<<m.first[count], kThreads, smem, st>>>(m);
   return cudaGetLastError();
 }
 

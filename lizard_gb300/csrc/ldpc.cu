@@ -690,15 +690,17 @@ __global__ void __launch_bounds__(cta_threads<C, WPC>(), 1) ldpc_decode_kernel(L
   }
 }
 
-// The receiver's decode in one persistent launch across its tiers (every code): a queue of (tier, block) items, the
-// tiers of the longer codes first, pulled by groups of two warps, each item decoded by its code's form (the pair form
-// with the loop for 7/8, messages in registers for the others) in a slice sized for the longest code. One launch in
-// place of a launch a tier on forked streams: for the small batches where the launches and their tails are the cost.
+// The receivers' decode in one persistent launch across their tiers (every code): a queue of (receiver, tier, block)
+// items, the tiers of the longer codes first, pulled by groups of two warps, each item decoded by its code's form (the
+// pair form with the loop for 7/8, messages in registers for the others) in a slice sized for the longest code. One
+// launch in place of a launch a tier on forked streams: for the small batches where the launches and their tails are
+// the cost, and for an engine's formats together.
 constexpr int cmax(int x, int y) { return x > y ? x : y; }
 constexpr int kMixSlice = cmax(cmax(warp_bytes<0>(), warp_bytes<1>()), cmax(warp_bytes<2>(), warp_bytes<3>()));
 constexpr int kMixWpc = 2, kMixGroups = (227 * 1024 - kCrcBytes) / kMixSlice, kMixThreads = kMixGroups * kMixWpc * 32;
 static_assert(kMixGroups >= 1 && kMixGroups <= 15, "groups of the mixed launch");
-__global__ void __launch_bounds__(kMixThreads, 1) ldpc_mixed_kernel(LdpcMix m) {
+static_assert(sizeof(LdpcMix) <= 32000, "the mixed launch's arguments fit a launch");
+__global__ void __launch_bounds__(kMixThreads, 1) ldpc_mixed_kernel(const __grid_constant__ LdpcMix m) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int s_item[kMixGroups], s_red[kMixGroups][kMixWpc];
   uint32_t *crc_tab = reinterpret_cast<uint32_t *>(smem);
@@ -713,7 +715,7 @@ __global__ void __launch_bounds__(kMixThreads, 1) ldpc_mixed_kernel(LdpcMix m) {
   for (int t = threadIdx.x; t < 33; t += blockDim.x) crc_k[t] = c_crc_shift[t];
   __syncthreads();
   (void)lane;
-  const int total = m.first[4];
+  const int total = m.first[m.nseg];
   for (;;) {
     if (tg == 0) s_item[g] = atomicAdd(m.counter, 1);
     group_sync<kMixWpc>(g);
@@ -721,13 +723,14 @@ __global__ void __launch_bounds__(kMixThreads, 1) ldpc_mixed_kernel(LdpcMix m) {
     group_sync<kMixWpc>(g);
     if (item >= total) break;
     int seg = 0;
-    while (seg < 3 && item >= m.first[seg + 1]) seg++;
-    const int tier = m.tier[seg], local = item - m.first[seg];
+    while (seg < m.nseg - 1 && item >= m.first[seg + 1]) seg++;
+    const LdpcLaunch &a = m.a[seg];
+    const int local = item - m.first[seg];
     switch (m.code[seg]) {
-      case 0: decode_item<0, kMixWpc, true, true>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
-      case 1: decode_item<1, kMixWpc, false, false>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
-      case 2: decode_item<2, kMixWpc, false, false>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
-      default: decode_item<3, kMixWpc, false, false>(m.a, tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      case 0: decode_item<0, kMixWpc, true, true>(a, a.tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      case 1: decode_item<1, kMixWpc, false, false>(a, a.tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      case 2: decode_item<2, kMixWpc, false, false>(a, a.tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
+      default: decode_item<3, kMixWpc, false, false>(a, a.tier, local, slice, crc_tab, crc_k, s_red[g], g); break;
     }
   }
 }
@@ -841,12 +844,13 @@ cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st)
 int ldpc_variant_count(int code) { return code >= 0 && code <= 3 ? variant_count(code) : 0; }
 
 cudaError_t ldpc_mixed_launch(const LdpcMix &m, int sms, cudaStream_t st) {
-  if (m.first[4] <= 0) return cudaSuccess;
+  if (m.nseg < 1 || m.nseg > kMixSegs) return m.nseg == 0 ? cudaSuccess : cudaErrorInvalidValue;
+  if (m.first[m.nseg] <= 0) return cudaSuccess;
   static SmemOptIn opt;
   constexpr int smem = kCrcBytes + kMixGroups * kMixSlice;
   static_assert(smem <= 227 * 1024, "the mixed launch's slices fit");
   if (cudaError_t e = opt.set(reinterpret_cast<const void *>(ldpc_mixed_kernel), smem)) return e;
-  const int need = (m.first[4] + kMixGroups - 1) / kMixGroups;
+  const int need = (m.first[m.nseg] + kMixGroups - 1) / kMixGroups;
   ldpc_mixed_kernel<<<need < sms ? need : sms, kMixThreads, smem, st>>>(m);
   return cudaGetLastError();
 }

@@ -144,6 +144,20 @@ int record_error(int code, const char *what);
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
 cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st);
+// One format's share of a transform stage run across formats (the engine's stage-wise run): its tables, source,
+// buffers and frames. fft_pre_launch: the shading fit's sums and the sampler's table; fft_fac_launch: the surface
+// factors; the mixed launches: one column (row) pass grid over count <= kFftMixSegs formats' tiles.
+constexpr int kFftMixSegs = 8;
+struct FftSegArgs {
+  FftDev xd;
+  SrcDev src;
+  FftBufs b;
+  int frames;
+};
+cudaError_t fft_pre_launch(const FftSegArgs &a, cudaStream_t st);
+cudaError_t fft_fac_launch(const FftSegArgs &a, cudaStream_t st);
+cudaError_t fft_cols_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st);
+cudaError_t fft_rows_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st);
 // The transform plan of picture size n (three passes' radices, lines a CTA): 0, or -1 for a size off the ladder.
 // The sender's inverse transform: the half-plane spectrum S (frames x vrows x n, rows along u, overwritten) to the
 // clipped picture pic (frames x n x n, 0.5 + clamp(P, +-lim) sc). tws: the transform's twiddles.
@@ -177,12 +191,15 @@ cudaError_t anchor_find_launch(int span, const uint8_t *d_luma, int w, int h, in
                                const int *d_lens_on = nullptr, const uint8_t *d_active = nullptr);
 // code: 0 = 7/8, 1 = 3/4, 2 = 2/3, 3 = 1/2. sms: the device's SM count (the persistent grid's bound).
 cudaError_t ldpc_launch(int code, const LdpcLaunch &a, int sms, cudaStream_t st);
-// The receiver's decode of every tier in one persistent launch: a queue of segments, segment s items
-// [first[s], first[s + 1]) of tier tier[s] (code code[s]); a's receiver fields (its, ok, rx, fd, the stop rule) as a
-// tier's launch takes them (its count, counter and tier unused); counter zero at launch.
+// The receivers' decode of every tier in one persistent launch: a queue of segments, segment s items
+// [first[s], first[s + 1]) of tier a[s].tier (code code[s]) of the receiver whose fields a[s] holds (its, ok, rx, fd,
+// the stop rule, as a tier's launch takes them; count and counter unused): one receiver's tiers, or every format's
+// of an engine; counter zero at launch.
+constexpr int kMixSegs = 32;
 struct LdpcMix {
-  LdpcLaunch a;
-  int first[5], tier[4], code[4];
+  LdpcLaunch a[kMixSegs];
+  int first[kMixSegs + 1], code[kMixSegs];
+  int nseg;
   int *counter;
 };
 cudaError_t ldpc_mixed_launch(const LdpcMix &m, int sms, cudaStream_t st);
@@ -195,6 +212,26 @@ cudaError_t ldpc_launch_variant(int code, int v, const LdpcLaunch &a, int sms, c
 // stage. For the registration's refinements, which measure their mismatch where the receiver measures it.
 int rx_spectrum_luma(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
                      float *d_coef, cudaStream_t st);
+// One receiver call split into its stages, for the engine's stage-wise run across formats: the transform's share
+// (fft), the soft stage's arguments and buffers, and the tiers' decode launches. rx_call checks the call as
+// lizg_rx_finish_luma_dev does; rx_call_demap launches the pilots' fit, the soft values and the block stage;
+// rx_call_tier the decode of tier t (count set, counter left to the caller), returning its code.
+struct RxCall {
+  lizg_rx *r;
+  FftSegArgs fft;
+  FmtDev fd;
+  int tiers;
+  const lizg_rx_out *out;
+  int8_t *llrf;
+  double *sub_est;
+  float *sub_rms, *est, *pilot, *align;
+  uint8_t *decl;
+};
+int rx_call(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
+            const lizg_rx_out *out, RxCall &c);
+cudaError_t rx_call_demap(const RxCall &c, cudaStream_t st);
+int rx_call_tier(const RxCall &c, int t, LdpcLaunch &a);
+int rx_read(const lizg_rx *r);   // the handle's read (LIZG_READ_DECODE or LIZG_READ_EXACT)
 
 }  // namespace lizg
 

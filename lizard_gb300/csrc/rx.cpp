@@ -294,30 +294,35 @@ int lizg_rx_set_read(lizg_rx *r, int read) {
   return was;
 }
 
+// Tier t's decode launch of a batch's soft values (count and counter left to the caller).
+static lizg::LdpcLaunch tier_launch(const lizg_rx *r, const lizg::FmtDev &fd, int frames, const int8_t *llrf, const lizg_rx_out *out, int t) {
+  lizg::LdpcLaunch a{};
+  a.its = out->its; a.ok = out->ok;
+  a.count = frames * r->f.tier[t].blocks;
+  a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // the receiver's (liblizard/src/lizard_phy.c:80-82, 1824)
+  a.rx.llrf = llrf; a.rx.decl = r->decl; a.rx.blocks = out->blocks; a.rx.llr_stride = 2 * (int64_t)r->f.subch * lizg::kSub;
+  a.fd = fd; a.tier = t;
+  return a;
+}
+
 // Row (d) and (e) on a batch's soft values: the LDPC decode and CRC of every block not declined, a launch a tier on
 // the tiers' own streams (forked from st, joined back), or every tier in one persistent launch (r->mixed).
 static int rx_ldpc(lizg_rx *r, const lizg::FmtDev &fd, int frames, int8_t *llrf, const lizg_rx_out *out, cudaStream_t st, int sms) {
   const lizg::Format &f = r->f;
-  const int64_t need = (int64_t)f.subch * lizg::kSub;
   cudaError_t e;
   if ((e = cudaMemsetAsync(r->counters, 0, 4 * sizeof(int), st)) != cudaSuccess || (e = cudaEventRecord(r->fork, st)) != cudaSuccess)
     return lizg::record_error(LIZG_E_CUDA, (std::string("rx fork: ") + cudaGetErrorString(e)).c_str());
   if (r->mixed) {
     // every tier in one launch on the caller's stream, the longer codes' tiers first
     lizg::LdpcMix m{};
-    m.a.its = out->its; m.a.ok = out->ok;
-    m.a.max_iter = 30; m.a.stall_it = 9; m.a.stall_ratio = 0.95f;
-    m.a.rx.llrf = llrf; m.a.rx.decl = r->decl; m.a.rx.blocks = out->blocks; m.a.rx.llr_stride = 2 * need;
-    m.a.fd = fd;
-    int order[4], no = 0;
     for (int c = 3; c >= 0; c--)
-      for (int t = 0; t < f.tiers; t++) if (f.tier[t].code == c) order[no++] = t;
-    m.first[0] = 0;
-    for (int sgm = 0; sgm < 4; sgm++) {
-      const int t = sgm < no ? order[sgm] : -1;
-      m.tier[sgm] = t < 0 ? 0 : t; m.code[sgm] = t < 0 ? 0 : f.tier[t].code;
-      m.first[sgm + 1] = m.first[sgm] + (t < 0 ? 0 : frames * f.tier[t].blocks);
-    }
+      for (int t = 0; t < f.tiers; t++)
+        if (f.tier[t].code == c) {
+          m.a[m.nseg] = tier_launch(r, fd, frames, llrf, out, t);
+          m.code[m.nseg] = c;
+          m.first[m.nseg + 1] = m.first[m.nseg] + m.a[m.nseg].count;
+          m.nseg++;
+        }
     m.counter = r->counters;
     if ((e = lizg::ldpc_mixed_launch(m, sms, st)) != cudaSuccess)
       return lizg::record_error(LIZG_E_CUDA, (std::string("rx LDPC: ") + cudaGetErrorString(e)).c_str());
@@ -325,12 +330,8 @@ static int rx_ldpc(lizg_rx *r, const lizg::FmtDev &fd, int frames, int8_t *llrf,
     return 0;
   }
   for (int t = 0; t < f.tiers; t++) {
-    lizg::LdpcLaunch a{};
-    a.its = out->its; a.ok = out->ok;
-    a.count = frames * f.tier[t].blocks; a.counter = r->counters + t;
-    a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // the receiver's (liblizard/src/lizard_phy.c:80-82, 1824)
-    a.rx.llrf = llrf; a.rx.decl = r->decl; a.rx.blocks = out->blocks; a.rx.llr_stride = 2 * need;
-    a.fd = fd; a.tier = t;
+    lizg::LdpcLaunch a = tier_launch(r, fd, frames, llrf, out, t);
+    a.counter = r->counters + t;
     if ((e = cudaStreamWaitEvent(r->side[t], r->fork, 0)) != cudaSuccess ||
         (e = (r->variant[t] >= 0 ? lizg::ldpc_launch_variant(f.tier[t].code, r->variant[t], a, sms, r->side[t])
                                  : lizg::ldpc_launch(f.tier[t].code, a, sms, r->side[t]))) != cudaSuccess ||
@@ -449,6 +450,45 @@ int lizg::rx_spectrum_luma(lizg_rx *r, const uint8_t *d_luma, int w, int h, int 
   const lizg::FftBufs b{r->hole, r->part, r->fac, r->Y, r->tpos, r->f.subch * lizg::kSub, reinterpret_cast<float2 *>(d_coef), r->ctab, &r->ymap, r->dev_err};
   const cudaError_t e = lizg::fft_launch(r->xd, frames, src, b, sms, st);
   return e == cudaSuccess ? 0 : lizg::record_error(LIZG_E_CUDA, (std::string("spectrum from frames: ") + cudaGetErrorString(e)).c_str());
+}
+
+int lizg::rx_call(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
+                  const lizg_rx_out *out, RxCall &c) {
+  int sms = 0;
+  if (int rc = check_call(r, d_luma, frames, out, "lizg_engine_run_dev", &sms)) return rc;
+  if (!d_reg || w < 2 || h < 2 || pitch < w || frame_stride < (int64_t)pitch * h)
+    return lizg::record_error(LIZG_E_ARG, "lizg_engine_run_dev: bad frame geometry or NULL registration");
+  c = RxCall{};
+  c.r = r;
+  c.fft.xd = r->xd;
+  c.fft.frames = frames;
+  SrcDev &src = c.fft.src;
+  src.sd = r->sd;
+  src.luma = d_luma; src.w = w; src.h = h; src.pitch = pitch; src.fstride = frame_stride; src.reg = d_reg;
+  src.regstride = 9 + 2 * r->sd.nx * r->sd.ny;
+  c.fft.b = FftBufs{r->hole, r->part, r->fac, r->Y, r->tpos, r->f.subch * lizg::kSub, r->C, r->ctab, &r->ymap, r->dev_err};
+  c.fd = fmt_dev(r, frames);
+  c.tiers = r->f.tiers;
+  c.out = out;
+  c.llrf = out->llrf ? out->llrf : r->llrf;
+  c.sub_est = out->sub_est ? out->sub_est : r->sub_est;
+  c.sub_rms = out->sub_rms ? out->sub_rms : r->sub_rms;
+  c.est = out->est ? out->est : r->est;
+  c.pilot = out->pilot ? out->pilot : r->pilot;
+  c.align = out->align ? out->align : r->align;
+  c.decl = r->decl;
+  return 0;
+}
+
+cudaError_t lizg::rx_call_demap(const RxCall &c, cudaStream_t st) {
+  return lizg::demap_launch(c.fd, c.fft.b.C, c.fft.b.need, c.align, c.llrf, c.sub_est, c.sub_rms, c.est, c.pilot, c.decl, st);
+}
+
+int lizg::rx_read(const lizg_rx *r) { return r->sd.read; }
+
+int lizg::rx_call_tier(const RxCall &c, int t, LdpcLaunch &a) {
+  a = tier_launch(c.r, c.fd, c.fft.frames, c.llrf, c.out, t);
+  return c.r->f.tier[t].code;
 }
 
 extern "C" {
@@ -575,12 +615,8 @@ int lizg_rx_autotune(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch,
     rc = lizg_rx_finish_luma_dev(r, d_luma, w, h, pitch, frame_stride, d_reg, frames, &out, nullptr, nullptr, stream);
     const lizg::FmtDev fd = fmt_dev(r, frames);
     for (int t = 0; t < f.tiers && !rc && e == cudaSuccess; t++) {
-      lizg::LdpcLaunch a{};
-      a.its = its; a.ok = ok;
-      a.count = frames * f.tier[t].blocks; a.counter = r->counters + t;
-      a.max_iter = 30; a.stall_it = 9; a.stall_ratio = 0.95f;   // as finish_spec launches it
-      a.rx.llrf = r->llrf; a.rx.decl = r->decl; a.rx.blocks = blocks; a.rx.llr_stride = 2 * (int64_t)f.subch * lizg::kSub;
-      a.fd = fd; a.tier = t;
+      lizg::LdpcLaunch a = tier_launch(r, fd, frames, r->llrf, &out, t);   // as finish_spec launches it
+      a.counter = r->counters + t;
       float best_ms = 0;
       for (int v = 0; v < lizg::ldpc_variant_count(f.tier[t].code) && e == cudaSuccess; v++) {
         float ms_min = 0;

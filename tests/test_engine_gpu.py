@@ -1,6 +1,7 @@
-"""The multi-stream engine (lizg_engine_*): batches of three formats decoded together, each on its own stream from
-its own CUDA graph, give exactly what each format's receiver gives alone (blocks, CRC flags, iterations); replays of
-the captured graphs give it again; bad runs are refused."""
+"""The multi-stream engine (lizg_engine_*): batches of several formats decoded together, each on its own stream from
+its own CUDA graph, or stage-wise across formats (one column pass, row pass and decode grid over every format's
+items), give exactly what each format's receiver gives alone (blocks, CRC flags, iterations, soft values); replays of
+the captured graphs give it again; the tuner keeps one of the two; bad runs are refused."""
 import numpy as np
 import pytest
 import torch
@@ -13,14 +14,14 @@ pytestmark = pytest.mark.gpu
 FORMATS = [(384, 64, 128, 1280, 720), (768, 320, 128, 1100, 1000), (1152, 720, 256, 1400, 1400)]
 
 
-def captures(n, subch, span, W, H, frames, seed):
+def captures(n, subch, span, W, H, frames, seed, sigma=2.0):
     fmt = lz.Format(n, subch, span)
     rng = np.random.default_rng(seed)
     lumas, regs = [], []
     for k in range(frames):
         grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, seed + k), parity=k & 3)
         Hw = synth.warp(fmt, W, H, rng, rot_deg=10, scale=(0.95, 1.0))
-        luma, reg = synth.capture(fmt, grey, W, H, H=Hw, sigma=2.0, rng=rng)
+        luma, reg = synth.capture(fmt, grey, W, H, H=Hw, sigma=sigma, rng=rng)
         lumas.append(luma)
         regs.append(reg)
     return np.stack(lumas), np.stack(regs)
@@ -50,6 +51,57 @@ def test_engine_matches_each_receiver():
                 assert np.array_equal(o[k].cpu().numpy(), want[i][k]), (rep, i, k)
             assert want[i]["ok"].all()
     assert eng.launches == sum(5 + 3 + f.tiers for f in eng.formats)
+    eng.close()
+
+
+# two picture sizes of one ring, a size with two rings, noise enough at 768 for stalled and capped blocks
+MIXED = [(384, 64, 128, 1280, 720, 3, 2.0), (768, 320, 128, 1100, 1000, 2, 45.0), (1152, 720, 256, 1400, 1400, 2, 2.0),
+         (1536, 1024, 256, 1800, 1800, 1, 2.0), (1536, 1024, 512, 2400, 2400, 1, 2.0)]
+
+
+def test_stage_wise_engine_matches_each_receiver():
+    eng = lz.Engine()
+    st = torch.cuda.current_stream().cuda_stream
+    batches, keep, want = [], [], []
+    for i, (n, subch, span, W, H, frames, sigma) in enumerate(MIXED):
+        assert eng.add_format(n, subch, span, frames) == i
+        luma, reg = captures(n, subch, span, W, H, frames, 300 + 100 * i, sigma)
+        want.append(lz.Receiver(n, subch, span, max_frames=frames).finish_luma(luma, reg, keep=True, grid=False))
+        d_l, d_r = torch.from_numpy(luma).cuda(), torch.from_numpy(reg).cuda()
+        o, s = lz.rx_outputs(eng.formats[i], frames, keep=True)
+        keep.append((d_l, d_r, o))
+        batches.append((i, d_l.data_ptr(), W, H, W, W * H, d_r.data_ptr(), frames, s))
+    assert (want[1]["its"] < 0).any() and (want[1]["ok"] == 0).any() and (want[1]["ok"] == 1).any()
+    assert eng.set_mixed(1) == 0
+
+    def check(tag):
+        for i, (_, _, o) in enumerate(keep):
+            for k in ("blocks", "ok", "its", "llrf", "est", "pilot", "align", "sub_rms"):
+                a = o[k].cpu().numpy()
+                assert np.array_equal(a, want[i][k], equal_nan=a.dtype.kind == "f"), (tag, i, k)   # a tier without pilots: NaN
+
+    for rep in range(3):   # the first run captures the stage-wise graph, the others replay it
+        for _, _, o in keep:
+            for t in o.values():
+                t.zero_()
+        eng.run_dev(batches, st)
+        torch.cuda.synchronize()
+        check(rep)
+    nb = len(MIXED)
+    assert eng.launches == 2 * nb + 1 + nb + 1 + 3 * nb + 1
+    # new contents in the same buffers: the replay reads them
+    luma, reg = captures(*MIXED[0][:5], MIXED[0][5], 999)
+    keep[0][0].copy_(torch.from_numpy(luma))
+    keep[0][1].copy_(torch.from_numpy(reg))
+    want[0] = lz.Receiver(*MIXED[0][:3], max_frames=MIXED[0][5]).finish_luma(luma, reg, keep=True, grid=False)
+    eng.run_dev(batches, st)
+    torch.cuda.synchronize()
+    check("new frames")
+    # the tuner runs both ways and keeps one; the outputs stay the same
+    mode, ms = eng.autotune(batches, st)
+    torch.cuda.synchronize()
+    assert mode in (0, 1) and ms[0] > 0 and ms[1] > 0 and eng.set_mixed(mode) == mode
+    check("tuned")
     eng.close()
 
 
