@@ -410,9 +410,11 @@ __global__ void __launch_bounds__(256, 1) field_solve_kernel(FieldArgs a, const 
   const float *reg = regs + (int64_t)f * a.reg_stride;
   const uint8_t *px = a.luma + f * a.fstride;
   FieldState &S = st[f];
+  // the last evaluation of a refinement only weighs its point against the best so far: no gradient, no system
+  const bool only_loss = last && !terms;
   // the adjoint pass's partial sums, in block order within each of 8 interleaved sums (8 loads in flight a thread),
   // the 8 then added pairwise (blocks is a multiple of 8 for every picture size; any rest is summed after)
-  for (int q = tid; q < kFPart; q += blockDim.x) {
+  for (int q = tid; q < (only_loss ? 0 : kFPart); q += blockDim.x) {
     const float *p = part + (int64_t)f * blocks * kFPart + q;
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int b = 0;
@@ -424,8 +426,8 @@ __global__ void __launch_bounds__(256, 1) field_solve_kernel(FieldArgs a, const 
     for (; b < blocks; b++) tail += p[(int64_t)b * kFPart];
     s_sum[q] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])) + tail;
   }
-  for (int q = tid; q < 3 * kFP; q += blockDim.x) bv[q / kFP][q % kFP] = 0;
-  for (int q = tid; q < kFP * kFP; q += blockDim.x) smA[q] = 0;
+  for (int q = tid; q < (only_loss ? 0 : 3 * kFP); q += blockDim.x) bv[q / kFP][q % kFP] = 0;
+  for (int q = tid; q < (only_loss ? 0 : kFP * kFP); q += blockDim.x) smA[q] = 0;
   __syncthreads();
   // the track's levels: the dark cells' and the light cells' mean sample
   double ld = 0, ll = 0, nd = 0, nl = 0;
@@ -469,6 +471,22 @@ __global__ void __launch_bounds__(256, 1) field_solve_kernel(FieldArgs a, const 
     }
   }
   __syncthreads();
+  if (only_loss) {
+    // the loss as below, then the better of this point and the best so far kept as the result
+    double fprior = 0;
+    for (int q = 8 + tid; q < kFP; q += blockDim.x) fprior += (double)S.theta[q] * S.theta[q];
+    fprior = fblock_sum(fprior, red) / (kFieldSigma * kFieldSigma);
+    if (tid != 0) return;
+    const double loss = S.wp * s_loss[0] + S.wt * s_loss[1] + S.wa * s_loss[2] + fprior;
+    if (S.evals == 0 || loss < S.loss_best) {
+      if (S.evals > 0) S.improved = 1;
+      S.loss_best = loss;
+      for (int q = 0; q < kFP; q++) S.best[q] = S.theta[q];
+    }
+    S.evals++;
+    for (int q = 0; q < kFP; q++) S.theta[q] = S.best[q];
+    return;
+  }
   const double wt = terms ? 0.0 : S.wt, wa = terms ? 0.0 : S.wa;
   const bool need_a = wt != 0 || wa != 0;
   // the track's rows (term 1), then the anchors' two rows each (term 2)
@@ -886,10 +904,14 @@ int field_eval(lizg_field *g, const lizg::FieldArgs &a, const float *base, int f
   using namespace lizg;
   field_mesh_kernel<<<fc, 256, 0, st>>>(a, g->state, 0, base, g->eff);
   if (int rc = rx_spectrum_luma(g->rx, a.luma, a.w, a.h, a.w, a.fstride, g->eff, fc, reinterpret_cast<float *>(g->coef), st)) return rc;
-  cudaMemsetAsync(g->R, 0, sizeof(float2) * (size_t)fc * a.vrows * a.n, st);
+  // the last evaluation of a refinement (last, no terms asked for) needs the pilots' loss alone: no adjoint
+  const bool adjoint = !last || terms;
+  if (adjoint) cudaMemsetAsync(g->R, 0, sizeof(float2) * (size_t)fc * a.vrows * a.n, st);
   field_pilot_kernel<<<fc, kFThreads, 0, st>>>(a, g->coef, g->skip, g->R, g->pt);
-  if (enc_fft_launch(g->enc, fc, g->R, g->G, st) != cudaSuccess) return record_error(LIZG_E_CUDA, "lizg_field: adjoint transform launch");
-  field_grad_kernel<<<fc * (a.n / kFRows), kFThreads, 0, st>>>(a, g->eff, g->G, g->pt, g->skip, g->part);
+  if (adjoint) {
+    if (enc_fft_launch(g->enc, fc, g->R, g->G, st) != cudaSuccess) return record_error(LIZG_E_CUDA, "lizg_field: adjoint transform launch");
+    field_grad_kernel<<<fc * (a.n / kFRows), kFThreads, 0, st>>>(a, g->eff, g->G, g->pt, g->skip, g->part);
+  }
   const float *au = anchors ? anchors->u + (int64_t)f0 * 49 : nullptr, *av = anchors ? anchors->v + (int64_t)f0 * 49 : nullptr;
   const uint8_t *ao = anchors ? anchors->ok + (int64_t)f0 * 49 : nullptr;
   field_solve_kernel<<<fc, 256, kSolveSmem, st>>>(a, g->eff, g->part, g->pt, au, av, ao, g->skip, g->state, last, terms);
