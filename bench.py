@@ -682,7 +682,9 @@ def bench_multistream(args, stream):
     eng.set_mixed(0)
     ms_pipe = timed(tick_pipelined, K)
     ok_pipe = oks()
-    tuned, _ = eng.autotune(batches, sp)
+    tuned, _ = eng.autotune(batches, sp)   # each format's decode tuned on its batch, then the engine's mode
+    ms_eng_tuned = timed(lambda: eng.run_dev(batches, sp), K)
+    tuned_variants = [[eng.rx_variant(i, t) for t in range(eng.formats[i].tiers)] for i in range(len(formats))]
     ms = timed(tick, K)
     arrangement = "registration, then the engine"
     if ms_pipe < ms:
@@ -705,7 +707,8 @@ def bench_multistream(args, stream):
            "batched_vs_one_frame": round(ms1 / ms, 2), "identical_crc_sets": bool(same),
            "engine_mode": ["a graph a format", "stage-wise across formats"][tuned],
            "registration_ms": round(ms_reg, 4),
-           "engine_ms": {"a_graph_a_format": round(ms_eng[0], 4), "stage_wise": round(ms_eng[1], 4)},
+           "engine_ms": {"a_graph_a_format": round(ms_eng[0], 4), "stage_wise": round(ms_eng[1], 4),
+                         "tuned": round(ms_eng_tuned, 4), "tuned_decode_variants_per_format": tuned_variants},
            "tick_ms": {"a_graph_a_format": round(ms_tick[0], 4), "stage_wise": round(ms_tick[1], 4),
                        "each_format_registered_then_decoded": round(ms_pipe, 4)},
            "tick_arrangement": arrangement,

@@ -256,8 +256,9 @@ int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int 
 // four codes (the 1/2 code's first), and the light per-frame stages (the shading sums and sampler tables, the surface
 // factors, the pilots' fit, soft values and block stage) a launch a format on the formats' streams; the whole run is
 // one CUDA graph, captured on the first run with those batches. The outputs are the same bit for bit either way.
-// Returns the previous setting. lizg_engine_autotune runs the batches both ways (each four times, the first not
-// timed), keeps the faster and returns it (0 or 1); ms (may be NULL) gets the two best times, per format first.
+// Returns the previous setting. lizg_engine_autotune first tunes each format's decode on its batch
+// (lizg_rx_autotune on the format's handle), then runs the batches both ways (each four times, the first not timed),
+// keeps the faster and returns it (0 or 1); ms (may be NULL) gets the two best times, per format first.
 // Both write the batches' outputs as a run does.
 typedef struct lizg_engine lizg_engine;
 typedef struct {

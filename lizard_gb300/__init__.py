@@ -768,6 +768,10 @@ class Engine:
     def launches(self):
         return lib().lizg_engine_launches(self._h)
 
+    def rx_variant(self, format, tier):
+        """Tier `tier`'s LDPC kernel variant in format `format`'s receiver (lizg_rx_variant)."""
+        return _check(lib().lizg_rx_variant(ctypes.c_void_p(lib().lizg_engine_rx(self._h, format)), tier), "lizg_rx_variant")
+
     def close(self):
         if self._h:
             lib().lizg_engine_free(self._h)

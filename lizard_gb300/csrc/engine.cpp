@@ -4,7 +4,8 @@
 // across formats: each heavy stage one persistent grid over every format's work items (the column pass's and the row
 // pass's (frame, tile) items of every picture size, the decode's (tier, block) items of every format's codes), the
 // light per-frame stages a launch a format on the formats' streams, the whole run captured as one CUDA graph.
-// lizg_engine_autotune times both on the caller's batches and keeps the faster. Host C++.
+// lizg_engine_autotune tunes each format's decode on its batch (lizg_rx_autotune), then times both ways on the
+// caller's batches and keeps the faster. Host C++.
 #include "lizard_gb300.h"
 #include "lizg_internal.h"
 #include <cuda_runtime.h>
@@ -265,6 +266,13 @@ int lizg_engine_set_mixed(lizg_engine *e, int mixed) {
 int lizg_engine_autotune(lizg_engine *e, const lizg_engine_batch *b, int nb, void *stream, float *ms_out) {
   if (int rc = check_batches(e, b, nb, "lizg_engine_autotune")) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // each format's decode tuned on its own batch first (each tier's kernel variant, one launch across the tiers or a
+  // launch a tier): timed on the batch, a tier's launch lasts as long as its slowest codeword, so the choice follows
+  // the batch's failing codewords as well as its throughput
+  for (int i = 0; i < nb; i++)
+    if (int rc = lizg_rx_autotune(e->fmts[b[i].format].rx, b[i].d_luma, b[i].w, b[i].h, b[i].pitch, b[i].frame_stride, b[i].d_reg,
+                                  b[i].frames, nullptr, stream))
+      return rc;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t c = cudaEventCreate(&e0);
   if (c == cudaSuccess) c = cudaEventCreate(&e1);

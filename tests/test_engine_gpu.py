@@ -105,6 +105,36 @@ def test_stage_wise_engine_matches_each_receiver():
     eng.close()
 
 
+def test_stage_wise_engine_chunks_many_formats():
+    """More formats than one grid takes (8) and more tiers than one decode launch takes (32): the column and row
+    passes and the decode split into several grids, the outputs still each receiver's own."""
+    eng = lz.Engine()
+    st = torch.cuda.current_stream().cuda_stream
+    specs = [(384, 64, 128, 1280, 720)] * 6 + [(768, 320, 128, 1100, 1000)] * 4
+    batches, keep, want = [], [], []
+    for i, (n, subch, span, W, H) in enumerate(specs):
+        assert eng.add_format(n, subch, span, 1) == i
+        luma, reg = captures(n, subch, span, W, H, 1, 900 + i, 2.0 if i % 3 else 30.0)
+        want.append(lz.Receiver(n, subch, span, max_frames=1).finish_luma(luma, reg, keep=True, grid=False))
+        d_l, d_r = torch.from_numpy(luma).cuda(), torch.from_numpy(reg).cuda()
+        o, s = lz.rx_outputs(eng.formats[i], 1, keep=True)
+        keep.append((d_l, d_r, o))
+        batches.append((i, d_l.data_ptr(), W, H, W, W * H, d_r.data_ptr(), 1, s))
+    tiers = sum(f.tiers for f in eng.formats)
+    assert len(specs) > 8 and tiers > 32
+    eng.set_mixed(1)
+    for rep in range(2):
+        eng.run_dev(batches, st)
+        torch.cuda.synchronize()
+        for i, (_, _, o) in enumerate(keep):
+            for k in ("blocks", "ok", "its", "llrf", "est"):
+                a = o[k].cpu().numpy()
+                assert np.array_equal(a, want[i][k], equal_nan=a.dtype.kind == "f"), (rep, i, k)
+    nb = len(specs)
+    assert eng.launches == 2 * nb + 2 + nb + 2 + 3 * nb + (tiers + 31) // 32
+    eng.close()
+
+
 def test_engine_refuses_bad_runs():
     eng = lz.Engine()
     eng.add_format(384, 64, 128, 1)
