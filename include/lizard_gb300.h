@@ -250,12 +250,12 @@ int lizg_rx_finish_luma_host(lizg_rx *r, const uint8_t *luma, int w, int h, int 
 // (captured on the first run with those buffers), forked from `stream` and joined back to it, so the formats' work
 // overlaps on the GPU. Queued; returns once launched. lizg_engine_launches: the kernels the last run launched.
 //
-// lizg_engine_set_mixed(e, 1) runs the batches stage-wise across formats instead, as persistent work queues: the
-// column pass one grid over every format's (frame, column tile) items whatever their picture sizes, the row pass one
-// grid over every format's (frame, row tile) items, the decode one grid over every format's (tier, block) items of all
-// four codes (the 1/2 code's first), and the light per-frame stages (the shading sums and sampler tables, the surface
-// factors, the pilots' fit, soft values and block stage) a launch a format on the formats' streams; the whole run is
-// one CUDA graph, captured on the first run with those batches. The outputs are the same bit for bit either way.
+// lizg_engine_set_mixed(e, 1) runs the batches stage-wise across formats instead, as work queues: every stage one
+// launch over every format's items whatever their picture sizes and codes: the shading sums with the sampler's tables,
+// the column pass's (frame, column tile) items, the surface factors, the row pass's (frame, row tile) items, the
+// pilots' fit, the soft values, the block stage, and the decode as one persistent grid over every format's (tier,
+// block) items of all four codes (the 1/2 code's first); 8 launches for up to 8 formats. The whole run is one CUDA
+// graph, captured on the first run with those batches. The outputs are the same bit for bit either way.
 // Returns the previous setting. lizg_engine_autotune first tunes each format's decode on its batch
 // (lizg_rx_autotune on the format's handle), then runs the batches both ways (each four times, the first not timed),
 // keeps the faster and returns it (0 or 1); ms (may be NULL) gets the two best times, per format first.

@@ -31,13 +31,12 @@ __device__ __forceinline__ float2 turned(const FmtDev &fd, const float2 *spec, i
 // back. (The products are spread over the cluster's SMs because double arithmetic is slow on one SM.)
 constexpr int kPilotCtas = 8;
 
-__global__ void __cluster_dims__(kPilotCtas, 1, 1) __launch_bounds__(128) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride,
-                                                                                           float *align) {
-  extern __shared__ double tm[];              // chunk x 6: this CTA's pilots' products
+// Frame f's fit by the calling cluster. tm: this CTA's dynamic shared memory (chunk x 6 doubles at least).
+__device__ __forceinline__ void pilot_align_frame(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int f, double *tm) {
   __shared__ double sums[6], dxy[2];
   __shared__ int give_up;
   cg::cluster_group cl = cg::this_cluster();
-  const int rank = (int)cl.block_rank(), f = blockIdx.x / kPilotCtas, used = fd.npilot;
+  const int rank = (int)cl.block_rank(), used = fd.npilot;
   const int chunk = (used + kPilotCtas - 1) / kPilotCtas, p0 = rank * chunk, p1 = min(used, p0 + chunk);
   const float2 *sp = spec + f * spec_stride;
   const double k = 2.0 * 3.14159265358979323846 / fd.n;
@@ -105,6 +104,12 @@ __global__ void __cluster_dims__(kPilotCtas, 1, 1) __launch_bounds__(128) pilot_
   align[3 * f + 2] = (used > 0 && (d0 != 0 || d1 != 0)) ? 1.0f : 0.0f;
 }
 
+__global__ void __cluster_dims__(kPilotCtas, 1, 1) __launch_bounds__(128) pilot_align_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride,
+                                                                                           float *align) {
+  extern __shared__ double tm[];              // chunk x 6: this CTA's pilots' products
+  pilot_align_frame(fd, spec, spec_stride, align, blockIdx.x / kPilotCtas, tm);
+}
+
 // ten Brink's J (liblizard/src/lizard_phy.c:73-75)
 __device__ __forceinline__ double axis_info(double g) { return g > 0 ? pow(1 - pow(2.0, -0.3073 * pow(2 * sqrt(g), 1.7870)), 1.1064) : 0; }
 
@@ -115,10 +120,10 @@ __device__ __forceinline__ double axis_info(double g) { return g > 0 ? pow(1 - p
 constexpr int kDemapBatch = 8;   // 320 / 4 = 80 coefficients a lane, 10 batches
 static_assert(kSubDev % (4 * kDemapBatch) == 0, "whole batches");
 
-__global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
-                                                    int8_t *llrf, double *sub_est, float *sub_rms) {
+__device__ __forceinline__ void demap_block(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const float *align, int8_t *llrf,
+                                            double *sub_est, float *sub_rms, int blk) {
   __shared__ float s_m[64][2], s_k8[64];
-  const int grp = threadIdx.x >> 2, qd = threadIdx.x & 3, gid = blockIdx.x * 64 + grp;
+  const int grp = threadIdx.x >> 2, qd = threadIdx.x & 3, gid = blk * 64 + grp;
   const int f = gid / fd.subch, j = gid - f * fd.subch;
   const bool live = f < fd.frames;
   const float2 *sp = spec + (live ? f : 0) * spec_stride;
@@ -148,7 +153,7 @@ __global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spe
   if (qd == 0) { s_m[grp][0] = p2 + r2; s_m[grp][1] = p4 + r4; }
   __syncthreads();
   if (threadIdx.x < 64) {
-    const int g2 = blockIdx.x * 64 + threadIdx.x, f2 = g2 / fd.subch, j2 = g2 - f2 * fd.subch;
+    const int g2 = blk * 64 + threadIdx.x, f2 = g2 / fd.subch, j2 = g2 - f2 * fd.subch;
     float k8 = 0;
     if (f2 < fd.frames) {
       const double M2 = (double)s_m[threadIdx.x][0] / kSubDev, M4 = (double)s_m[threadIdx.x][1] / kSubDev;
@@ -187,12 +192,18 @@ __global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spe
   }
 }
 
+__global__ void __launch_bounds__(256) demap_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
+                                                    int8_t *llrf, double *sub_est, float *sub_rms) {
+  demap_block(fd, spec, spec_stride, align, llrf, sub_est, sub_rms, blockIdx.x);
+}
+
 // One thread a block: its estimate (its sub-channels' information weighted by the slots it holds there, in double, in
 // order), its pilot reading (the tail's axis values against the whitening in units of their sub-channel's rms, in
 // double, in order; NaN where none was read) and the decline gate (est < 0.2 k / nt in float): decl[f blocks + b] = 1.
-__global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
-                              const double *sub_est, const float *sub_rms, float *est, float *pilot, uint8_t *decl) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+constexpr int kBlocksThreads = 128;
+__device__ __forceinline__ void blocks_block(const FmtDev &fd, const float2 *spec, int64_t spec_stride, const float *align,
+                                             const double *sub_est, const float *sub_rms, float *est, float *pilot, uint8_t *decl, int blk) {
+  const int g = blk * kBlocksThreads + threadIdx.x;
   if (g >= fd.frames * fd.blocks) return;
   const int f = g / fd.blocks, b = g - f * fd.blocks;
   const int t = fd.block_tier[b], nb = fd.tier_slots[t], s0 = fd.block_slot[b], nt = fd.tier_nt[t];
@@ -227,6 +238,66 @@ __global__ void blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride
   decl[g] = e < 0.2f * (float)fd.tier_k[t] / (float)nt;
 }
 
+__global__ void __launch_bounds__(kBlocksThreads) blocks_kernel(FmtDev fd, const float2 *spec, int64_t spec_stride, const float *align,
+                                                                const double *sub_est, const float *sub_rms, float *est, float *pilot,
+                                                                uint8_t *decl) {
+  blocks_block(fd, spec, spec_stride, align, sub_est, sub_rms, est, pilot, decl, blockIdx.x);
+}
+
+// The three stages over several formats' batches, one launch each: format k's frames (clusters), demap CTAs and block
+// CTAs at [pf[k], pf[k + 1]), [df[k], df[k + 1]) and [bf[k], bf[k + 1]).
+struct DemapMix {
+  DemapSeg seg[kDemapMixSegs];
+  int pf[kDemapMixSegs + 1], df[kDemapMixSegs + 1], bf[kDemapMixSegs + 1];
+  int nseg;
+};
+static_assert(sizeof(DemapMix) <= 32000, "the mixed launches' arguments fit a launch");
+__device__ __forceinline__ int seg_at(const int *first, int nseg, int b) {
+  int k = 0;
+  while (k < nseg - 1 && b >= first[k + 1]) k++;
+  return k;
+}
+
+__global__ void __cluster_dims__(kPilotCtas, 1, 1) __launch_bounds__(128) pilot_align_mixed_kernel(const __grid_constant__ DemapMix m) {
+  extern __shared__ double tm[];
+  const int c = blockIdx.x / kPilotCtas, k = seg_at(m.pf, m.nseg, c);
+  const DemapSeg &g = m.seg[k];
+  pilot_align_frame(g.fd, g.spec, g.stride, g.align, c - m.pf[k], tm);
+}
+
+__global__ void __launch_bounds__(256) demap_mixed_kernel(const __grid_constant__ DemapMix m) {
+  const int k = seg_at(m.df, m.nseg, blockIdx.x);
+  const DemapSeg &g = m.seg[k];
+  demap_block(g.fd, g.spec, g.stride, g.align, g.llrf, g.sub_est, g.sub_rms, blockIdx.x - m.df[k]);
+}
+
+__global__ void __launch_bounds__(kBlocksThreads) blocks_mixed_kernel(const __grid_constant__ DemapMix m) {
+  const int k = seg_at(m.bf, m.nseg, blockIdx.x);
+  const DemapSeg &g = m.seg[k];
+  blocks_block(g.fd, g.spec, g.stride, g.align, g.sub_est, g.sub_rms, g.est, g.pilot, g.decl, blockIdx.x - m.bf[k]);
+}
+
+cudaError_t demap_mixed_launch(const DemapSeg *a, int count, cudaStream_t st) {
+  if (count < 1 || count > kDemapMixSegs) return cudaErrorInvalidValue;
+  DemapMix m{};
+  m.nseg = count;
+  int psm = 8;
+  for (int k = 0; k < count; k++) {
+    const FmtDev &fd = a[k].fd;
+    m.seg[k] = a[k];
+    const int chunk = (fd.npilot + kPilotCtas - 1) / kPilotCtas, bytes = 6 * (chunk > 0 ? chunk : 1) * (int)sizeof(double);
+    psm = bytes > psm ? bytes : psm;
+    m.pf[k + 1] = m.pf[k] + fd.frames;
+    m.df[k + 1] = m.df[k] + (fd.frames * fd.subch + 63) / 64;
+    m.bf[k + 1] = m.bf[k] + (fd.frames * fd.blocks + kBlocksThreads - 1) / kBlocksThreads;
+  }
+  if (psm > 48 * 1024) return cudaErrorInvalidValue;
+  pilot_align_mixed_kernel<<<m.pf[count] * kPilotCtas, 128, psm, st>>>(m);
+  demap_mixed_kernel<<<m.df[count], 256, 0, st>>>(m);
+  blocks_mixed_kernel<<<m.bf[count], kBlocksThreads, 0, st>>>(m);
+  return cudaGetLastError();
+}
+
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st) {
   const int chunk = (fd.npilot + kPilotCtas - 1) / kPilotCtas;
@@ -236,7 +307,8 @@ cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stri
   const int groups = fd.frames * fd.subch;
   demap_kernel<<<(groups + 63) / 64, 256, 0, st>>>(fd, spec, spec_stride, align, llrf, sub_est, sub_rms);
   const int nbk = fd.frames * fd.blocks;
-  blocks_kernel<<<(nbk + 127) / 128, 128, 0, st>>>(fd, spec, spec_stride, align, sub_est, sub_rms, est, pilot, decl);
+  blocks_kernel<<<(nbk + kBlocksThreads - 1) / kBlocksThreads, kBlocksThreads, 0, st>>>(fd, spec, spec_stride, align, sub_est, sub_rms, est,
+                                                                                       pilot, decl);
   return cudaGetLastError();
 }
 

@@ -1,9 +1,9 @@
 // The multi-stream engine (include/lizard_gb300.h lizg_engine_*): one receiver handle per picture format, run in one
 // of two ways. A graph a format: each format's batch of frames replayed from its own CUDA graph on its own stream, all
 // forked from the caller's stream and joined back to it, so frames of every format in flight run at once. Stage-wise
-// across formats: each heavy stage one persistent grid over every format's work items (the column pass's and the row
-// pass's (frame, tile) items of every picture size, the decode's (tier, block) items of every format's codes), the
-// light per-frame stages a launch a format on the formats' streams, the whole run captured as one CUDA graph.
+// across formats: every stage one launch over every format's work items (the column pass's and the row pass's
+// (frame, tile) items of every picture size, the decode's (tier, block) items of every format's codes, the light
+// per-frame stages' frames, bands and blocks), the whole run captured as one CUDA graph.
 // lizg_engine_autotune tunes each format's decode on its batch (lizg_rx_autotune), then times both ways on the
 // caller's batches and keeps the faster. Host C++.
 #include "lizard_gb300.h"
@@ -53,9 +53,10 @@ int fork_each(lizg_engine *e, const lizg_engine_batch *b, int nb, cudaStream_t s
   return 0;
 }
 
-// The stage-wise run, queued on st: the shading sums and sampler tables (a format a stream), one column pass grid
-// over every format's tiles, the surface factors (a format a stream), one row pass grid, the soft stage (a format a
-// stream), then one decode grid over every format's tiers, the 1/2 code's first, then 2/3, 3/4, 7/8.
+// The stage-wise run, queued on st, every stage one launch over every format's work items (kFftMixSegs formats a
+// launch; more formats take more launches): the shading sums with the sampler's tables, the column pass, the surface
+// factors, the row pass, the pilots' fit, the soft values, the block stage, then the decode over every format's tiers,
+// the 1/2 code's first, then 2/3, 3/4, 7/8.
 int run_mixed(lizg_engine *e, const lizg_engine_batch *b, int nb, cudaStream_t st) {
   int sms = 0;
   if (int rc = lizg::device_ready(&sms)) return rc;
@@ -66,13 +67,6 @@ int run_mixed(lizg_engine *e, const lizg_engine_batch *b, int nb, cudaStream_t s
       return rc;
   int launches = 0;
   cudaError_t c;
-  auto stage = [&](cudaError_t (*fn)(const lizg::FftSegArgs &, cudaStream_t), int per) {
-    return fork_each(e, b, nb, st, [&](int i, cudaStream_t s) {
-      const cudaError_t x = fn(calls[i].fft, s);
-      launches += per;
-      return x == cudaSuccess ? 0 : cuda_fail("lizg_engine_run_dev", x);
-    });
-  };
   auto grids = [&](cudaError_t (*fn)(const lizg::FftSegArgs *, int, cudaStream_t)) {
     std::vector<lizg::FftSegArgs> segs;
     for (int i0 = 0; i0 < nb; i0 += lizg::kFftMixSegs) {
@@ -84,16 +78,22 @@ int run_mixed(lizg_engine *e, const lizg_engine_batch *b, int nb, cudaStream_t s
     }
     return 0;
   };
-  if (int rc = stage(lizg::fft_pre_launch, 2)) return rc;
+  if (int rc = grids(lizg::fft_pre_mixed_launch)) return rc;
   if (int rc = grids(lizg::fft_cols_mixed_launch)) return rc;
-  if (int rc = stage(lizg::fft_fac_launch, 1)) return rc;
+  if (int rc = grids(lizg::fft_fac_mixed_launch)) return rc;
   if (int rc = grids(lizg::fft_rows_mixed_launch)) return rc;
-  if (int rc = fork_each(e, b, nb, st, [&](int i, cudaStream_t s) {
-        const cudaError_t x = lizg::rx_call_demap(calls[i], s);
-        launches += 3;
-        return x == cudaSuccess ? 0 : cuda_fail("lizg_engine_run_dev", x);
-      }))
-    return rc;
+  {
+    std::vector<lizg::DemapSeg> segs;
+    for (int i0 = 0; i0 < nb; i0 += lizg::kDemapMixSegs) {
+      segs.clear();
+      for (int i = i0; i < nb && i < i0 + lizg::kDemapMixSegs; i++) {
+        const lizg::RxCall &x = calls[i];
+        segs.push_back(lizg::DemapSeg{x.fd, x.fft.b.C, x.fft.b.need, x.align, x.llrf, x.sub_est, x.sub_rms, x.est, x.pilot, x.decl});
+      }
+      if ((c = lizg::demap_mixed_launch(segs.data(), (int)segs.size(), st)) != cudaSuccess) return cuda_fail("lizg_engine_run_dev", c);
+      launches += 3;
+    }
+  }
   // the decode's segments, the longer codes first, kMixSegs a launch
   std::vector<lizg::LdpcLaunch> seg;
   std::vector<int> code;

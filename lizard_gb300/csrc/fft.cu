@@ -243,8 +243,8 @@ __device__ __forceinline__ void hole_basis(const FftDev &xd, int x, int y, doubl
 // every-eighth rows: hole[f][band][0..5]. A warp takes a row: its samples outside the squares summed in float as
 // z, z c(x), z q(x) (the basis is separable: 1, c(x), q(x), c(y), q(y), c(x) c(y)), then the row's six terms added
 // in double; the warps' sums added in warp order.
-__global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, int bands, double *hole) {
-  const int f = blockIdx.x / bands, band = blockIdx.x % bands, n = xd.n, c = n / 8;
+__device__ __forceinline__ void hole_rhs_band(const FftDev &xd, const SrcDev &src, int bands, double *hole, int f, int band) {
+  const int n = xd.n, c = n / 8;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, ky1 = min(c, (band + 1) * kHoleBand);
   double rhs[6] = {0, 0, 0, 0, 0, 0};
   for (int ky = band * kHoleBand + warp; ky < ky1; ky += 8) {
@@ -274,6 +274,9 @@ __global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, in
     for (int w = 0; w < 8; w++) acc += red[w][threadIdx.x];
     hole[((int64_t)f * bands + band) * 6 + threadIdx.x] = acc;
   }
+}
+__global__ void __launch_bounds__(256) hole_rhs_kernel(FftDev xd, SrcDev src, int bands, double *hole) {
+  hole_rhs_band(xd, src, bands, hole, blockIdx.x / bands, blockIdx.x % bands);
 }
 
 // The transform CTA's shared memory: the lines, the twiddles, the moments' reduction.
@@ -340,8 +343,7 @@ __device__ __forceinline__ float hole_value(const FftDev &xd, const double *beta
 // y and mesh cell i < nx - 1 the displacement line cell_terms gives, and at i = nx - 1 the homography's row terms
 // (kw, ku, kv). The decode's read: the row terms of row y at y < n, then each column x's displacement terms at mesh
 // row j (lin_cell) at n + j n + x.
-__global__ void __launch_bounds__(256) cell_table_kernel(SrcDev src, int per_frame, float4 *ctab) {
-  const int f = blockIdx.y, t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void cell_table_entry(const SrcDev &src, int per_frame, float4 *ctab, int f, int t) {
   if (t >= per_frame) return;
   const SampleDev &sd = src.sd;
   const float *H = src.reg + (int64_t)f * src.regstride;
@@ -366,6 +368,9 @@ __global__ void __launch_bounds__(256) cell_table_kernel(SrcDev src, int per_fra
     }
   }
   ctab[(int64_t)f * per_frame + t] = o;
+}
+__global__ void __launch_bounds__(256) cell_table_kernel(SrcDev src, int per_frame, float4 *ctab) {
+  cell_table_entry(src, per_frame, ctab, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // One column tile's samples: thread t takes line l = t mod L (columns xa = x0 + l as the real part, xb = x0 + L + l as
@@ -529,8 +534,8 @@ __global__ void __launch_bounds__(kThreads, 3) fft_cols_mixed_kernel(const __gri
 // (liblizard/src/lizard_phy.c:1697), then the surface spectrum's factors (liblizard/src/lizard_phy.c:1702-1716),
 // rounded to float as there: fac[f] = xy[u] (pxy X1[u]) for u < n, x0[u] (n (px X1[u] + pxx X2[u])) for u < n,
 // y0[v] (n (py X1[v] + pyy X2[v])) for v < vrows.
-__global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const double *part, float2 *fac) {
-  const int f = blockIdx.x, n = xd.n;
+__device__ __forceinline__ void fac_frame(const FftDev &xd, int tiles, const double *part, float2 *fac, int f) {
+  const int n = xd.n;
   __shared__ double s_p[5];
   if (threadIdx.x < 5) {
     double acc = 0;
@@ -550,6 +555,51 @@ __global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const do
     const float2 x1 = xd.x1[v], x2 = xd.x2[v];
     o[2 * n + v] = make_float2((float)(n * (py * x1.x + pyy * x2.x)), (float)(n * (py * x1.y + pyy * x2.y)));
   }
+}
+__global__ void __launch_bounds__(256) fac_kernel(FftDev xd, int tiles, const double *part, float2 *fac) {
+  fac_frame(xd, tiles, part, fac, blockIdx.x);
+}
+
+// The shading sums, the sampler's tables and the surface factors over several formats' batches, one launch a stage:
+// format k's shading-band CTAs at [hf[k], hf[k + 1]), then its table CTAs at [tf[k], tf[k + 1]) (one launch takes
+// both), its frames' factor CTAs at [ff[k], ff[k + 1]).
+struct FftLightSeg {
+  FftDev xd;
+  SrcDev src;
+  double *hole, *part;
+  float4 *ctab;
+  float2 *fac;
+  int bands, per_frame, tblocks, tiles;
+};
+struct FftLightMix {
+  FftLightSeg seg[kFftMixSegs];
+  int hf[kFftMixSegs + 1], tf[kFftMixSegs + 1], ff[kFftMixSegs + 1];
+  int nseg;
+};
+static_assert(sizeof(FftLightMix) <= 32000, "the light stages' arguments fit a launch");
+__device__ __forceinline__ int seg_at(const int *first, int nseg, int b) {
+  int k = 0;
+  while (k < nseg - 1 && b >= first[k + 1]) k++;
+  return k;
+}
+__global__ void __launch_bounds__(256) fft_pre_mixed_kernel(const __grid_constant__ FftLightMix m) {
+  const int b = blockIdx.x;
+  if (b < m.hf[m.nseg]) {
+    const int k = seg_at(m.hf, m.nseg, b);
+    const FftLightSeg &g = m.seg[k];
+    const int lb = b - m.hf[k];
+    hole_rhs_band(g.xd, g.src, g.bands, g.hole, lb / g.bands, lb % g.bands);
+  } else {
+    const int k = seg_at(m.tf, m.nseg, b);
+    const FftLightSeg &g = m.seg[k];
+    const int lb = b - m.tf[k], f = lb / g.tblocks;
+    cell_table_entry(g.src, g.per_frame, g.ctab, f, (lb - f * g.tblocks) * 256 + threadIdx.x);
+  }
+}
+__global__ void __launch_bounds__(256) fac_mixed_kernel(const __grid_constant__ FftLightMix m) {
+  const int k = seg_at(m.ff, m.nseg, blockIdx.x);
+  const FftLightSeg &g = m.seg[k];
+  fac_frame(g.xd, g.tiles, g.part, g.fac, blockIdx.x - m.ff[k]);
 }
 
 // A bounded wait on an mbarrier's phase (try_wait blocks a while in hardware before it answers): false when the
@@ -741,6 +791,39 @@ constexpr int kFftSmemLadder = cmax_i(cmax_i(cmax_i(smem_bytes_of(384), smem_byt
 static_assert(kFftSmemLadder <= kFftSmemMax, "transform CTA's shared memory");
 
 static int ladder_size(int n) { return plan_of(n).lines != 0; }
+
+static cudaError_t light_mix(const FftSegArgs *a, int count, FftLightMix &m) {
+  if (count < 1 || count > kFftMixSegs) return cudaErrorInvalidValue;
+  m = FftLightMix{};
+  m.nseg = count;
+  for (int k = 0; k < count; k++) {
+    const FftSegArgs &s = a[k];
+    if (!ladder_size(s.xd.n) || s.frames < 1 || s.src.grid || !s.b.ctab || s.src.sd.nx != s.src.sd.ny) return cudaErrorInvalidValue;
+    FftLightSeg &g = m.seg[k];
+    g.xd = s.xd; g.src = s.src; g.hole = s.b.hole; g.part = s.b.part; g.ctab = s.b.ctab; g.fac = s.b.fac;
+    g.bands = fft_hole_bands(s.xd.n); g.per_frame = s.xd.n * s.src.sd.nx; g.tblocks = (g.per_frame + 255) / 256;
+    g.tiles = s.xd.n / (2 * plan_of(s.xd.n).lines);
+    m.hf[k + 1] = m.hf[k] + s.frames * g.bands;
+    m.ff[k + 1] = m.ff[k] + s.frames;
+  }
+  m.tf[0] = m.hf[count];
+  for (int k = 0; k < count; k++) m.tf[k + 1] = m.tf[k] + a[k].frames * m.seg[k].tblocks;
+  return cudaSuccess;
+}
+
+cudaError_t fft_pre_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st) {
+  FftLightMix m;
+  if (cudaError_t e = light_mix(a, count, m)) return e;
+  fft_pre_mixed_kernel<<<m.tf[count], 256, 0, st>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t fft_fac_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st) {
+  FftLightMix m;
+  if (cudaError_t e = light_mix(a, count, m)) return e;
+  fac_mixed_kernel<<<m.ff[count], 256, 0, st>>>(m);
+  return cudaGetLastError();
+}
 
 cudaError_t fft_cols_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st) {
   if (count < 1 || count > kFftMixSegs) return cudaErrorInvalidValue;

@@ -143,6 +143,21 @@ int record_error(int code, const char *what);
 // spec: frames x spec_stride complex coefficients in pos order.
 cudaError_t demap_launch(const FmtDev &fd, const float2 *spec, int64_t spec_stride, float *align, int8_t *llrf,
                          double *sub_est, float *sub_rms, float *est, float *pilot, uint8_t *decl, cudaStream_t st);
+// One format's share of the soft stage run across formats: its tables and frames, its spectra and outputs as
+// demap_launch takes them. demap_mixed_launch: the pilots' fit, the soft values and the block stage, each one launch
+// over count <= kDemapMixSegs formats.
+constexpr int kDemapMixSegs = 8;
+struct DemapSeg {
+  FmtDev fd;
+  const float2 *spec;
+  int64_t stride;
+  float *align;
+  int8_t *llrf;
+  double *sub_est;
+  float *sub_rms, *est, *pilot;
+  uint8_t *decl;
+};
+cudaError_t demap_mixed_launch(const DemapSeg *a, int count, cudaStream_t st);
 cudaError_t fft_launch(const FftDev &xd, int frames, const SrcDev &src, const FftBufs &b, int sms, cudaStream_t st);
 // One format's share of a transform stage run across formats (the engine's stage-wise run): its tables, source,
 // buffers and frames. fft_pre_launch: the shading fit's sums and the sampler's table; fft_fac_launch: the surface
@@ -157,6 +172,10 @@ struct FftSegArgs {
 cudaError_t fft_pre_launch(const FftSegArgs &a, cudaStream_t st);
 cudaError_t fft_fac_launch(const FftSegArgs &a, cudaStream_t st);
 cudaError_t fft_cols_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st);
+// The light stages across formats (captured frames only): the shading sums and the sampler's tables in one launch,
+// the surface factors in one launch.
+cudaError_t fft_pre_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st);
+cudaError_t fft_fac_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st);
 cudaError_t fft_rows_mixed_launch(const FftSegArgs *a, int count, cudaStream_t st);
 // The transform plan of picture size n (three passes' radices, lines a CTA): 0, or -1 for a size off the ladder.
 // The sender's inverse transform: the half-plane spectrum S (frames x vrows x n, rows along u, overwritten) to the
@@ -214,8 +233,8 @@ int rx_spectrum_luma(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch,
                      float *d_coef, cudaStream_t st);
 // One receiver call split into its stages, for the engine's stage-wise run across formats: the transform's share
 // (fft), the soft stage's arguments and buffers, and the tiers' decode launches. rx_call checks the call as
-// lizg_rx_finish_luma_dev does; rx_call_demap launches the pilots' fit, the soft values and the block stage;
-// rx_call_tier the decode of tier t (count set, counter left to the caller), returning its code.
+// lizg_rx_finish_luma_dev does; rx_call_tier gives the decode of tier t (count set, counter left to the caller),
+// returning its code.
 struct RxCall {
   lizg_rx *r;
   FftSegArgs fft;
@@ -229,7 +248,6 @@ struct RxCall {
 };
 int rx_call(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, int64_t frame_stride, const float *d_reg, int frames,
             const lizg_rx_out *out, RxCall &c);
-cudaError_t rx_call_demap(const RxCall &c, cudaStream_t st);
 int rx_call_tier(const RxCall &c, int t, LdpcLaunch &a);
 int rx_read(const lizg_rx *r);   // the handle's read (LIZG_READ_DECODE or LIZG_READ_EXACT)
 

@@ -480,10 +480,6 @@ int lizg::rx_call(lizg_rx *r, const uint8_t *d_luma, int w, int h, int pitch, in
   return 0;
 }
 
-cudaError_t lizg::rx_call_demap(const RxCall &c, cudaStream_t st) {
-  return lizg::demap_launch(c.fd, c.fft.b.C, c.fft.b.need, c.align, c.llrf, c.sub_est, c.sub_rms, c.est, c.pilot, c.decl, st);
-}
-
 int lizg::rx_read(const lizg_rx *r) { return r->sd.read; }
 
 int lizg::rx_call_tier(const RxCall &c, int t, LdpcLaunch &a) {
