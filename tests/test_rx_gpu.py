@@ -77,3 +77,33 @@ def test_mixed_decode_matches_per_tier(n, subch, frames, sigma):
         assert np.array_equal(a[k], b[k]), k
     if sigma > 10:
         assert (a["its"] < 0).any() and (a["ok"] == 1).any()
+
+
+def test_receiver_refuses_bad_calls():
+    """Every receiver entry point checks its arguments before it queues anything: a zero or oversized batch, a frame
+    under 2 x 2 or a pitch or frame stride too short for it, a NULL frame, registration or output, an unknown read,
+    decode stage or tier; each is refused with LIZG_E_ARG and the handle stays usable."""
+    import ctypes
+    import torch
+    n, subch, span, W, H = 384, 64, 128, 1280, 720
+    fmt = lz.Format(n, subch, span)
+    grey = synth.picture(fmt, synth.random_blocks(fmt.blocks, 5))
+    luma, reg = synth.capture(fmt, grey, W, H, sigma=2.0, rng=np.random.default_rng(5))
+    rx = lz.Receiver(n, subch, span, max_frames=2)
+    o, s = lz.rx_outputs(rx.fmt, 2)
+    d = torch.zeros((2, H, W), dtype=torch.uint8, device="cuda")
+    r = torch.zeros((2, reg.size), dtype=torch.float32, device="cuda")
+    L, P = lz.lib(), ctypes.c_void_p
+
+    def call(luma=d.data_ptr(), w=W, h=H, pitch=W, stride=W * H, reg=r.data_ptr(), frames=1, out=s):
+        return L.lizg_rx_finish_luma_dev(rx._h, P(luma), w, h, pitch, stride, P(reg), frames, ctypes.byref(out) if out else None,
+                                         None, None, None)
+
+    for kw in ({"frames": 0}, {"frames": 3}, {"w": 1}, {"pitch": W - 1}, {"stride": W * H - 1}, {"luma": 0}, {"reg": 0}, {"out": None}):
+        assert call(**kw) == -1, kw
+    assert call(out=lz.RxOut(None, s.ok, s.its, None, None, None, None, None, None)) == -1
+    assert L.lizg_rx_set_read(rx._h, 7) == -1 and L.lizg_rx_set_ldpc_mixed(rx._h, 3) == -1 and L.lizg_rx_variant(rx._h, 9) == -1
+    assert L.lizg_rx_finish_coef_dev(rx._h, None, 1, ctypes.byref(s), None) == -1
+    # still usable: the clean frame decodes every block
+    out = rx.finish_luma(luma[None], reg[None], grid=False)
+    assert out["ok"].all()
