@@ -261,11 +261,19 @@ __global__ void __launch_bounds__(kFThreads) field_pilot_kernel(FieldArgs a, con
   }
 }
 
-// The adjoint pass over the samples. A CTA takes kFRows picture rows of a frame, a warp a row, lanes along x. G: the
-// inverse transform of the residuals (0.5 + g from the sender's transform). Out, a CTA's partial sums (floats, in a
-// fixed order): H's g t (8), the H tangents' Gram (36, upper triangle), sum z, sum z^2, then per knot pair (b, a)
-// and component the field's g t (kFK^2 x 2) and t^2 (kFK^2 x 2).
-__global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, const float *regs, const float *G, const PilotTerms *pt,
+// The adjoint pass over the samples. A CTA takes kFRows picture rows of a frame, a warp a row, each lane a run of n / 32
+// consecutive columns. G: the mismatch's gradient at every sample (the residuals' inverse transform); g = G - 0.5 - the
+// detrend's adjoint terms; t = the image gradient times the warp's derivative. Out: per CTA, in part[f][blk], the H
+// sums g t (8), the tangents' Gram (36, upper triangle row by row), sum z and sum z^2 of the samples read, then for
+// each knot pair (b, a) and component the field's g t (kFK^2 x 2) and t^2 (kFK^2 x 2).
+// The row's my is fixed, so every H tangent is one of a = Iu / w, b = Iv / w, c = -(Iu U + Iv V) / w times 1, mx or
+// my: the lane sums g a, g b, g c and g times each against mx, and each product of two of a, b, c against 1, mx and
+// mx^2 (24 sums), and the 44 H sums are made from them at the row's end. A sample's weight on knot k along x is the
+// blend (1 - uu) W_i[k] + uu W_{i+1}[k] of its cell's two nodes, so the lane sums g Iu, g Iv and the squares' terms
+// against (1 - uu), uu and their products over the samples of one cell (10 sums), and adds them into its knot sums (in
+// shared memory, a slot a lane) each time its run leaves a cell.
+constexpr int kCellSums = 10;
+__global__ void __launch_bounds__(kFThreads, 2) field_grad_kernel(FieldArgs a, const float *regs, const float *G, const PilotTerms *pt,
                                                                const uint8_t *skip, float *part) {
   const int blocks = a.n / kFRows, f = blockIdx.x / blocks, blk = blockIdx.x - f * blocks;
   if (skip && skip[f]) return;
@@ -275,67 +283,102 @@ __global__ void __launch_bounds__(kFThreads) field_grad_kernel(FieldArgs a, cons
   const float *Gf = G + (int64_t)f * n * n + (int64_t)y * n;
   __shared__ FieldShared fs;
   stage_shared(a, fs);
-  __shared__ float s_pq[kFRows][kFK][4];   // a row's field sums: g t x, g t y, t x^2, t y^2 at each knot a
+  __shared__ float s_kn[kFRows][kFK * 4][32];   // each lane's knot sums: g tx, g ty, tx^2, ty^2 at each knot a
+  __shared__ float s_pq[kFRows][kFK][4];        // a row's field sums over its lanes
   __shared__ float s_wy[kFRows][kFK];
   __shared__ float s_h[kFThreads / 32][kFHs];
+  float (*kn)[32] = s_kn[warp];
+  for (int e = 0; e < kFK * 4; e++) kn[e][lane] = 0;
   // the detrend's adjoint constants in float: the gradient's share of them needs no more (FP64 is a narrow pipe here)
   const float K0 = (float)pt[f].k[0], K1 = (float)pt[f].k[1], K2 = (float)pt[f].k[2], K3 = (float)pt[f].k[3], K4 = (float)pt[f].k[4];
   const float my = a.g0 + (float)y * a.step;
   const float cy = a.cx[y], qy = a.qx[y];
   const bool ysq = in_sq(a, y);
-  float hs[kFHs];
+  // the lane's sums: g a, g a mx, g b, g b mx, g c, g c mx; aa, ab, ac, bb, bc, cc against 1, mx, mx^2; z, z^2
+  float ga[6] = {0, 0, 0, 0, 0, 0}, gm[18], zs = 0, zz = 0;
 #pragma unroll
-  for (int q = 0; q < kFHs; q++) hs[q] = 0;
-  float pq[kFK][4];
+  for (int q = 0; q < 18; q++) gm[q] = 0;
+  float cs[kCellSums];
 #pragma unroll
-  for (int k = 0; k < kFK; k++) pq[k][0] = pq[k][1] = pq[k][2] = pq[k][3] = 0;
-  // the row's mesh row once; each lane's cell found onwards from its last (x rises along the row)
+  for (int q = 0; q < kCellSums; q++) cs[q] = 0;
   const int jrow = cell_of(fs.pos, a.nn, my);
   const float vrow = (my - fs.pos[jrow]) * fs.inv[jrow];
-  int icell = 0;
-  for (int x = lane; x < n; x += 32) {
+  const int per = n / 32, x0 = lane * per;
+  int icell = cell_of(fs.pos, a.nn, a.g0 + (float)x0 * a.step), ccell = icell;
+  // the cell sums of cell ic into the lane's knot sums
+  auto flush = [&](int ic) {
+#pragma unroll
+    for (int k = 0; k < kFK; k++) {
+      const float w0 = fs.wk[ic * kFK + k], w1 = fs.wk[(ic + 1) * kFK + k];
+      if (w0 == 0.0f && w1 == 0.0f) continue;
+      kn[4 * k + 0][lane] += w0 * cs[0] + w1 * cs[1];
+      kn[4 * k + 1][lane] += w0 * cs[2] + w1 * cs[3];
+      kn[4 * k + 2][lane] += w0 * w0 * cs[4] + 2.0f * w0 * w1 * cs[5] + w1 * w1 * cs[6];
+      kn[4 * k + 3][lane] += w0 * w0 * cs[7] + 2.0f * w0 * w1 * cs[8] + w1 * w1 * cs[9];
+    }
+#pragma unroll
+    for (int q = 0; q < kCellSums; q++) cs[q] = 0;
+  };
+  for (int x = x0; x < x0 + per; x++) {
     const float mx = a.g0 + (float)x * a.step;
     while (icell < a.nn - 2 && mx >= fs.pos[icell + 1]) icell++;
-    const WarpAt o = warp_in(a, reg, mx, my, icell, jrow, (mx - fs.pos[icell]) * fs.inv[icell], vrow);
+    if (icell != ccell) { flush(ccell); ccell = icell; }
+    const float uu = (mx - fs.pos[icell]) * fs.inv[icell];
+    const WarpAt o = warp_in(a, reg, mx, my, icell, jrow, uu, vrow);
     float Iu, Iv;
     const float z = read_grad(px, a.w, a.h, o.u, o.v, &Iu, &Iv);
-    hs[44] += z; hs[45] += z * z;
+    zs += z; zz += z * z;
     if (ysq && in_sq(a, x)) continue;   // erased: the shading surface, held constant
     const float cxx = a.cx[x], qxx = a.qx[x];
     const float g = Gf[x] - 0.5f - (K0 * cxx * cy + K1 * cxx + K2 * qxx + K3 * cy + K4 * qy);
-    float du[8], dv[8];
-    dwarp_dh(o, mx, my, du, dv);
-    float t[8];
+    const float ta = o.iw * Iu, tb = o.iw * Iv, tc = -o.iw * (Iu * o.U + Iv * o.V), m2 = mx * mx;
+    const float gta = g * ta, gtb = g * tb, gtc = g * tc;
+    ga[0] += gta; ga[1] += gta * mx; ga[2] += gtb; ga[3] += gtb * mx; ga[4] += gtc; ga[5] += gtc * mx;
+    const float pr[6] = {ta * ta, ta * tb, ta * tc, tb * tb, tb * tc, tc * tc};
 #pragma unroll
-    for (int q = 0; q < 8; q++) { t[q] = Iu * du[q] + Iv * dv[q]; hs[q] += g * t[q]; }
+    for (int q = 0; q < 6; q++) { gm[3 * q] += pr[q]; gm[3 * q + 1] += pr[q] * mx; gm[3 * q + 2] += pr[q] * m2; }
+    const float v1 = uu, v0 = 1.0f - uu, gu = g * Iu, gv = g * Iv, uu2 = Iu * Iu, vv2 = Iv * Iv;
+    cs[0] += gu * v0; cs[1] += gu * v1; cs[2] += gv * v0; cs[3] += gv * v1;
+    cs[4] += uu2 * v0 * v0; cs[5] += uu2 * v0 * v1; cs[6] += uu2 * v1 * v1;
+    cs[7] += vv2 * v0 * v0; cs[8] += vv2 * v0 * v1; cs[9] += vv2 * v1 * v1;
+  }
+  flush(ccell);
+  // the 44 H sums from the lane's 24: t = (a mx, a my, a, b mx, b my, b, c mx, c my), each a (abc) x (mx, my, 1) term
+  float hs[kFHs];
+  {
+    const int which[8] = {0, 0, 0, 1, 1, 1, 2, 2}, mono[8] = {1, 2, 0, 1, 2, 0, 1, 2};   // mono: 0 = 1, 1 = mx, 2 = my
+    const float my2 = my * my;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const float s0 = ga[2 * which[q]], s1 = ga[2 * which[q] + 1];
+      hs[q] = mono[q] == 1 ? s1 : mono[q] == 2 ? my * s0 : s0;
+    }
     int e = 8;
 #pragma unroll
     for (int p = 0; p < 8; p++)
 #pragma unroll
-      for (int q = p; q < 8; q++) hs[e++] += t[p] * t[q];
-#pragma unroll
-    for (int k = 0; k < kFK; k++) {
-      const float wx = knot_w(fs.wk, o.i, o.uu, k);
-      const float tx = Iu * wx, ty = Iv * wx;
-      pq[k][0] += g * tx; pq[k][1] += g * ty; pq[k][2] += tx * tx; pq[k][3] += ty * ty;
-    }
+      for (int q = p; q < 8; q++) {
+        const int u = min(which[p], which[q]), v = max(which[p], which[q]);
+        const int pi = u == 0 ? v : u == 1 ? 2 + v : 5;   // the pair's index in aa, ab, ac, bb, bc, cc
+        const int nx = (mono[p] == 1) + (mono[q] == 1), ny = (mono[p] == 2) + (mono[q] == 2);
+        const float fy = ny == 0 ? 1.0f : ny == 1 ? my : my2;
+        hs[e++] = fy * gm[3 * pi + nx];
+      }
+    hs[44] = zs; hs[45] = zz;
   }
-  // the row's field sums over the warp, then weighted by the row's knot weights across the CTA's rows in order
-#pragma unroll
-  for (int k = 0; k < kFK; k++)
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      float v = pq[k][c];
-#pragma unroll
-      for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-      if (lane == 0) s_pq[warp][k][c] = v;
-    }
+  // the row's field sums over the warp's lanes, then weighted by the row's knot weights across the CTA's rows in order
+  __syncwarp();
+  for (int e = lane; e < kFK * 4; e += 32) {
+    float v = 0;
+    for (int l = 0; l < 32; l++) v += kn[e][l];
+    s_pq[warp][e >> 2][e & 3] = v;
+  }
   if (lane < kFK) s_wy[warp][lane] = knot_w(fs.wk, jrow, vrow, lane);
 #pragma unroll
   for (int q = 0; q < kFHs; q++) {
     float v = hs[q];
 #pragma unroll
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+    for (int s2 = 16; s2 > 0; s2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s2);
     if (lane == 0) s_h[warp][q] = v;
   }
   __syncthreads();
