@@ -1041,7 +1041,7 @@ def bench_refinement(args, stream):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     rx = lz.Receiver(n, subch, span, max_frames=1024)
     ref = lz.Refiner(span, 1024)
-    fld = lz.FieldRefiner(n, subch, span, chunk=32)
+    fld = lz.FieldRefiner(n, subch, span, chunk=152)   # a frame an SM for the step's solve
     for name, js in sets:
         frames = len(js)
         seeds = [j[0] for j in js]

@@ -487,7 +487,8 @@ int lizg_anchor_register_dev(lizg_refiner *r, const uint8_t *d_luma, const uint8
 // to every picture sample, the warp recomputed at each sample); the step's normal equations take the pilots' J^T J
 // from the tangents' own Gram scaled by the pilots' share of the picture's energy, the track's and the anchors'
 // exactly. Each step is kept where the weighted mismatch falls, halved from the best registration otherwise; the
-// registration given is the baseline and the fallback. chunk: frames a pass (1..64).
+// registration given is the baseline and the fallback. chunk: frames a pass (1..256; at n = 1536 about 28 MB of
+// device memory a frame; a chunk of 152, a frame an SM for the step's solve, suits a GB300).
 // d_reg: frames x (9 + 2 nx ny), refined in place (H and the mesh). anchors (may be NULL: no anchor term): the anchor
 // search's outputs through the same registration (lizg_anchor_find_dev, frames x 49 each). d_gate (frames bytes, may
 // be NULL): 0 leaves a frame's registration as it is and spends nothing on it (for instance the frames whose plain

@@ -788,7 +788,7 @@ extern "C" {
 
 lizg_field *lizg_field_new(int n, int subch, int span, int chunk) {
   using namespace lizg;
-  if (chunk < 1 || chunk > 64) { record_error(LIZG_E_ARG, "lizg_field_new: chunk must be 1..64"); return nullptr; }
+  if (chunk < 1 || chunk > 256) { record_error(LIZG_E_ARG, "lizg_field_new: chunk must be 1..256"); return nullptr; }
   int sms = 0;
   if (device_ready(&sms)) return nullptr;
   lizg_field *g = new (std::nothrow) lizg_field();
